@@ -1,0 +1,408 @@
+"""Benchmark of the batched Lennard-Jones MD hot path (atom-steps/s).
+
+Workload (default): 4096 independent cubic argon systems, atom counts
+~U{64..2048} (about 4.36 M atoms), reduced densities ~U[0.7, 0.9], per-system
+temperatures ~U[80, 140] K, cutoff 2.5 sigma (+0.3 sigma Verlet skin),
+BAOAB Langevin (dt 2 fs, friction 1/ps), float32 pair arithmetic with float64
+per-system reductions.  Seeded synthetic positions (a jittered lattice subset
+with a 0.9 sigma minimum separation).
+
+One bench step = one MD step of every system.  `value` times the fused
+persistent kernel on device-resident inputs; `e2e` times the public
+propagator API (``FusedLennardJonesMD.__call__``) fed from pinned host
+buffers, host<->device copies included; the CPU baseline is the float64
+NumPy restatement of the reference's algorithm (dense neighbour list rebuilt
+every step, as the reference's MD app does) on a bounded sample of systems.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_STATE = 64  # float4 position+species and float4 momentum+mass, read and written
+BYTES_PER_HALF_NEIGHBOUR = 4  # uint16 index, stored for both directions
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--systems", type=int, default=4096)
+    ap.add_argument("--chunk", type=int, default=500, help="MD steps per persistent launch")
+    ap.add_argument("--e2e-chunk", type=int, default=50, help="MD steps per public-API call in the e2e leg")
+    ap.add_argument("--e2e-calls", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(n_systems, seed):
+    from kups_gb300 import workloads
+
+    return workloads.batched_uneven_lj(n_systems=n_systems, seed=seed)
+
+
+def algorithmic_bytes_per_step(W) -> float:
+    """64 B of state per atom-step plus 4 B per half-list neighbour within rc + skin."""
+    counts = np.bincount(W.system, minlength=W.n_systems).astype(np.float64)
+    vol = W.tril[:, 0] * W.tril[:, 2] * W.tril[:, 5]
+    rl = W.cutoff + W.skin
+    n_half = 2.0 / 3.0 * math.pi * rl**3 * counts / vol
+    return float(np.sum(counts * (BYTES_STATE + BYTES_PER_HALF_NEIGHBOUR * n_half)))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nme, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nme)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def read_traffic():
+    """DRAM bytes per atom-step of the MD kernel from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "md_lj_batched_uneven_ncu.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_atom_step:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def _cpu_sample_worker(args):
+    """Runs BAOAB steps of the float64 oracle on a few systems until the budget is spent."""
+    sys_ids, seconds, n_systems = args
+    sys.path.insert(0, ROOT)
+    from oracle import md as omd
+
+    W = workload(n_systems, 1)
+    rng = np.random.default_rng(0)
+    done = 0
+    t0 = time.perf_counter()
+    for s in sys_ids:
+        m = W.system == s
+        pos = W.positions[m]
+        n = pos.shape[0]
+        args_ = (W.masses[m], np.zeros(n, int), W.species[m], W.tril[s:s + 1], W.sigma, W.epsilon, [W.cutoff])
+        e, f, _ = omd.lj_forces(pos, np.zeros(n, int), W.species[m], W.tril[s:s + 1], W.sigma, W.epsilon, [W.cutoff])
+        mom = W.momenta[m]
+        while time.perf_counter() - t0 < seconds:
+            noise = rng.standard_normal((1, n, 3))
+            pos, mom, f, _ = omd.baoab(pos, mom, f, W.masses[m], np.zeros(n, int), W.species[m], W.tril[s:s + 1],
+                                       W.sigma, W.epsilon, [W.cutoff], W.time_step[s:s + 1], W.temperature[s:s + 1],
+                                       W.friction[s:s + 1], noise)
+            done += n
+            if done >= 3 * n * 4:  # a few steps per system, then the next system
+                break
+        if time.perf_counter() - t0 >= seconds:
+            break
+    return done, time.perf_counter() - t0
+
+
+def cpu_baseline(n_systems, seconds, processes):
+    """Atom-steps/s of the oracle on a sample of the workload's systems."""
+    rng = np.random.default_rng(123)
+    pick = rng.choice(n_systems, size=64, replace=False).tolist()
+    if processes <= 1:
+        done, el = _cpu_sample_worker((pick, seconds, n_systems))
+        return done / el, 1, f"{done} atom-steps of BAOAB over sampled systems in {el:.1f} s"
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    chunks = [pick[i::processes] for i in range(processes)]
+    t0 = time.perf_counter()
+    with ctx.Pool(processes) as pool:
+        res = pool.map(_cpu_sample_worker, [(c, seconds, n_systems) for c in chunks])
+    el = time.perf_counter() - t0
+    done = sum(r[0] for r in res)
+    rate = sum(r[0] / r[1] for r in res)
+    return rate, processes, f"{done} atom-steps of BAOAB over sampled systems on {processes} processes in {el:.1f} s"
+
+
+# ----------------------------------------------------------------------------- GPU leg
+def run_ours(a):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    from kups_gb300 import md
+
+    W = workload(a.systems, 1 + rank)
+    state = state_from_workload(W, torch)
+    prop = md.make_baoab_langevin_step()
+    packed = md.pack(state)
+    # warm-up (includes the first list build and force evaluation)
+    prop.run_packed(packed, max(a.warmup, 3), seed=11, step0=0)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    chunks = []
+    k = a.steps
+    while k > 0:
+        chunks.append(min(a.chunk, k))
+        k -= chunks[-1]
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in chunks]
+    status = torch.zeros(3, device="cuda", dtype=torch.int64)
+    status[2] = -1
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    step0 = max(a.warmup, 3)
+    for (e0, e1), c in zip(events, chunks):
+        e0.record(stream)
+        prop.launch(packed, c, seed=11, step0=step0, status=status, virial=False)
+        e1.record(stream)
+        step0 += c
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    from kups_gb300.neighborlist import read_status
+    from kups_gb300 import _lib
+
+    _lib.raise_status(read_status(status))
+    ms = t_start.elapsed_time(t_end)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    atom_steps = W.n_atoms * a.steps * world
+    value = atom_steps / (ms / 1e3)
+    launch_ms = [e0.elapsed_time(e1) for e0, e1 in events]
+    bytes_step = algorithmic_bytes_per_step(W)
+    achieved = sum(bytes_step * c for c in chunks) / (sum(launch_ms) / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic_per_atom_step = read_traffic()
+    line = {
+        "metric": "batched LJ MD atom-steps/s",
+        "value": value,
+        "unit": "atom-steps/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": max(a.warmup, 3),
+        "ms_per_step": ms / a.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 pair / fp64 sums",
+        "data": "synthetic (seeded)",
+        "config": {
+            "workload": f"batched uneven LJ MD: {W.n_systems} systems, N~U[64,2048] ({W.n_atoms} atoms), "
+                        f"rho*~U[0.7,0.9], T~U[80,140] K, rc 2.5 sigma + 0.3 sigma skin, BAOAB dt 2 fs",
+            "systems_per_gpu": W.n_systems,
+            "atoms_per_gpu": W.n_atoms,
+            "steps_per_launch": chunks[0],
+            "l2": "inputs larger than L2 (state 4.4M atoms x 48 B + Verlet lists)",
+            "parallelism": f"replicas x{world} (independent systems, no collective)",
+        },
+        "gpu_launches": len(chunks),
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": (traffic_per_atom_step * W.n_atoms * chunks[0]) if traffic_per_atom_step else None,
+            "peak_source": peak_kind,
+            "algorithmic_bytes_per_atom_step": bytes_step / W.n_atoms,
+        },
+        "clocks": clk,
+    }
+    if not a.no_e2e:
+        line["e2e"] = run_e2e(a, W, torch)
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        rate, cores, sample = cpu_baseline(a.systems, a.cpu_seconds, 1)
+        line["cpu_baseline"] = {"value": rate, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                                "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def state_from_workload(W, torch, device="cuda", pin=False):
+    from kups_gb300 import md, potential
+
+    def t(x, dt):
+        v = torch.as_tensor(np.ascontiguousarray(x), dtype=dt)
+        if device == "cpu":
+            return v.pin_memory() if pin else v
+        return v.to(device)
+
+    prm = potential.LennardJonesParameters(("Ar",), torch.as_tensor(W.sigma), torch.as_tensor(W.epsilon),
+                                           torch.tensor([W.cutoff], dtype=torch.float64))
+    parts = md.MDParticles(t(W.positions, torch.float64), t(W.momenta, torch.float64), t(W.masses, torch.float64),
+                           t(W.species, torch.int32), t(W.system, torch.int32), None)
+    systems = md.MDSystems(t(W.tril, torch.float64), t(W.time_step, torch.float64), t(W.temperature, torch.float64),
+                           t(W.friction, torch.float64))
+    return md.MDState(parts, systems, prm, skin=W.skin)
+
+
+def run_e2e(a, W, torch):
+    """Public propagator API with host buffers; H2D inputs and D2H outputs every call."""
+    from kups_gb300 import md
+
+    host = state_from_workload(W, torch, device="cpu", pin=True)
+    n = W.n_atoms
+    out_pos = torch.empty((n, 3), dtype=torch.float64).pin_memory()
+    out_mom = torch.empty_like(out_pos).pin_memory()
+    out_frc = torch.empty_like(out_pos).pin_memory()
+    out_e = torch.empty(W.n_systems, dtype=torch.float64).pin_memory()
+    prop = md.make_baoab_langevin_step(steps_per_call=a.e2e_chunk)
+
+    def one_call(i):
+        p = host.particles
+        dev = md.MDState(
+            md.MDParticles(p.positions.to("cuda", non_blocking=True), p.momenta.to("cuda", non_blocking=True),
+                           p.masses.to("cuda", non_blocking=True), p.species.to("cuda", non_blocking=True),
+                           p.system.to("cuda", non_blocking=True), None),
+            md.MDSystems(*(x.to("cuda", non_blocking=True) for x in (host.systems.tril, host.systems.time_step,
+                                                                      host.systems.temperature,
+                                                                      host.systems.friction_coefficient))),
+            host.lj_parameters, skin=host.skin, step=i * a.e2e_chunk)
+        out = prop([i, 1], dev)
+        out_pos.copy_(out.particles.positions, non_blocking=True)
+        out_mom.copy_(out.particles.momenta, non_blocking=True)
+        out_frc.copy_(out.particles.forces, non_blocking=True)
+        out_e.copy_(out.systems.potential_energy, non_blocking=True)
+
+    one_call(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(a.e2e_calls):
+        one_call(i + 1)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    steps = a.e2e_calls * a.e2e_chunk
+    h2d = n * (3 * 8 * 2 + 8 + 4 + 4) + W.n_systems * 8 * 9
+    d2h = n * 3 * 8 * 3 + W.n_systems * 8
+    return {"value": n * steps / el, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / a.e2e_chunk,
+            "d2h_bytes_per_step": d2h / a.e2e_chunk, "md_steps_per_call": a.e2e_chunk,
+            "api": "kups_gb300.md.FusedLennardJonesMD.__call__ (host state in pinned memory)"}
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    rate, cores, sample = cpu_baseline(a.systems, a.cpu_seconds, procs)
+    line = {
+        "impl": "reference",
+        "metric": "batched LJ MD atom-steps/s",
+        "value": rate,
+        "unit": "atom-steps/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "batched uneven LJ MD (sampled systems of the 4096-system batch)",
+                   "implementation": "float64 NumPy restatement of the reference algorithm (reference JAX "
+                                     "package not installable here: jax/jaxlib absent)"},
+        "cpu_baseline": {"value": rate, "unit": "atom-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,200 @@
+/*
+ * kups_gb300 — C ABI of the GB300 (sm_103a) particle-interaction kernels.
+ *
+ * Conventions shared by every entry point:
+ *   - all array pointers are DEVICE pointers owned by the caller; nothing is
+ *     allocated or freed by the library (scratch space is passed in as
+ *     `workspace`, sized by the matching *_workspace_bytes query);
+ *   - `stream` is a cudaStream_t passed as void*; every call is stream-ordered,
+ *     never synchronises the device and is safe to capture in a CUDA graph
+ *     (it issues only kernel launches and cudaMemsetAsync);
+ *   - the return value reports host-side validation and launch errors
+ *     (KUPS_OK, KUPS_ERR_INVALID, KUPS_ERR_CUDA); device-side conditions
+ *     (capacity overflow, non-finite input) are written to the caller's
+ *     device `kups_status`, which the caller reads back with its outputs.
+ *     Kernels never trap and never write past a capacity: on overflow they
+ *     record the capacity that would have sufficed in `required`, which is
+ *     how kUPS's Capacity / propagate_and_fix grow-and-retry loop
+ *     (src/kups/core/capacity.py:48-133, src/kups/core/propagator.py:137-172)
+ *     maps onto this library.
+ *   - unit cells are lower-triangular, given by `tril` = [L00, L10, L11, L20,
+ *     L21, L22] per system, row convention r = f @ L
+ *     (src/kups/core/unitcell.py:251-300).
+ */
+#ifndef KUPS_GB300_H
+#define KUPS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct kups_status {
+  int32_t code;      /* KUPS_OK or a KUPS_ERR_* code */
+  int32_t detail;    /* KUPS_CAP_* for capacity errors */
+  int64_t required;  /* capacity that would have sufficed */
+  int64_t first_bad; /* first offending particle / system index, -1 if none */
+} kups_status;
+
+enum {
+  KUPS_OK = 0,
+  KUPS_ERR_CAPACITY = 1,
+  KUPS_ERR_NONFINITE = 2,
+  KUPS_ERR_INVALID = 3,
+  KUPS_ERR_CUDA = 4,
+  KUPS_ERR_UNSUPPORTED = 5
+};
+
+enum {
+  KUPS_CAP_EDGES = 1,     /* edge buffer of the neighbour list */
+  KUPS_CAP_NEIGHBORS = 2, /* per-atom Verlet-list slots of the fused MD kernel */
+  KUPS_CAP_GHOSTS = 3,    /* periodic-image copies held in shared memory */
+  KUPS_CAP_CELLS = 4,     /* cells of the per-system cell grid */
+  KUPS_CAP_ATOMS = 5      /* atoms of one system held in shared memory */
+};
+
+const char *kups_version(void);
+const char *kups_error_string(int32_t code);
+
+/* ------------------------------------------------------------------------
+ * Neighbour list — replaces CellListNeighborList.__call__ and
+ * DenseNearestNeighborList.__call__ (src/kups/core/neighborlist.py:985-1077,
+ * 902-982; protocol NearestNeighborList.__call__ :226-255, rh = None).
+ *
+ * Produces the directed edge set of basic_neighborlist (:743-786): pairs of
+ * the same system and valid inclusion segment with |x_j - x_i + s @ L| < rc
+ * (strict, float64), the periodic-image path of
+ * _apply_distance_cutoff_w_images (:595-624) when 2 rc exceeds a cell width,
+ * and the minimum-image-only exclusion rule (:731-735).  Edges are grouped by
+ * i (lh) in increasing order; entries [n_edges, edge_capacity) are padded
+ * with i = j = n_particles and a zero shift, as _compact_edges pads (:651-689).
+ *
+ *   positions  f64 [n_particles, 3]   Cartesian
+ *   system     i32 [n_particles]      values outside [0, n_systems) = empty slot
+ *   inclusion  i32 [n_particles]      valid iff in [0, n_inclusion)
+ *   exclusion  i32 [n_particles]
+ *   tril       f64 [n_systems, 6],  cutoffs f64 [n_systems]
+ *   edges      i32 [edge_capacity, 2],  shifts i32 [edge_capacity, 3]
+ *   n_edges    i64 [1]  (device) number of edges found (may exceed capacity)
+ * ------------------------------------------------------------------------ */
+size_t kups_neighborlist_workspace_bytes(int64_t n_particles, int32_t n_systems);
+int32_t kups_neighborlist_build(const double *positions, const int32_t *system,
+                                const int32_t *inclusion, const int32_t *exclusion,
+                                int64_t n_particles, int32_t n_inclusion,
+                                const double *tril, const double *cutoffs,
+                                int32_t n_systems, int32_t *edges, int32_t *shifts,
+                                int64_t edge_capacity, int64_t *n_edges,
+                                void *workspace, size_t workspace_bytes,
+                                kups_status *status, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Lennard-Jones over an edge list — replaces lennard_jones_energy
+ * (src/kups/potential/classical/lennard_jones.py:149-178) together with the
+ * gradient PotentialFromEnergy obtains by jax.vjp with respect to
+ * PositionAndUnitCell (src/kups/potential/common/energy.py:264-355).
+ *
+ *   species    i32 [n_particles]  index into the n_species x n_species tables
+ *   sigma, epsilon f64 [n_species * n_species] (row-major, symmetric)
+ *   energy     f64 [n_systems]        out: sum_edges E_e / 2
+ *   grad       f64 [n_particles, 3]   out: dE/dx (zeroed by the call)
+ *   grad_tril  f64 [n_systems, 6]     out: dE/dtril at fixed Cartesian x
+ *   pair_fp32  non-zero: pair arithmetic in float32 (sums stay float64)
+ * ------------------------------------------------------------------------ */
+int32_t kups_lj_edges(const double *positions, const int32_t *system,
+                      const int32_t *species, int64_t n_particles,
+                      const double *tril, const double *cutoffs, int32_t n_systems,
+                      const double *sigma, const double *epsilon, int32_t n_species,
+                      const int32_t *edges, const int32_t *shifts, int64_t n_edges,
+                      double *energy, double *grad, double *grad_tril,
+                      int32_t pair_fp32, kups_status *status, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Fused Lennard-Jones MD — replaces one or more calls of the propagator built
+ * by make_velocity_verlet_step / make_baoab_langevin_step
+ * (src/kups/md/integrators.py:273-318, 405-455) with the LJ potential and
+ * neighbour list as derivative_computation
+ * (src/kups/application/md/simulation.py:74-119).
+ *
+ * One persistent launch runs n_steps for every system.  Each CTA takes whole
+ * systems from a work queue and keeps a system's atoms, periodic-image
+ * copies and cell grid in shared memory for all its steps; the Verlet list
+ * (cutoff + skin, uint16 indices) lives in per-CTA workspace.  Pair
+ * arithmetic is float32, per-system energy and virial sums float64.
+ *
+ * Atoms are stored sorted by system: system s owns [sys_offset[s],
+ * sys_offset[s+1]).
+ *   pos        float4 [n_atoms]  (x, y, z, species as int bits) in/out, Cartesian;
+ *              returned wrapped into fractional [-0.5, 0.5) like
+ *              MinimumImageConventionFlow (integrators.py:104-141)
+ *   mom        float4 [n_atoms]  (px, py, pz, mass) in/out
+ *   force      float4 [n_atoms]  (fx, fy, fz, -) in/out: F(t) on entry if
+ *              forces_valid, else computed first; F(t + n dt) on exit
+ *   sys_offset i32 [n_systems + 1]
+ *   order      i32 [n_systems]   processing order (largest first balances load)
+ *   tril       f32 [n_systems, 6]
+ *   cutoff, skin, dt, kT, friction   f32 [n_systems]  (kT in eV, dt internal units)
+ *   lj_table   f32 [n_species * n_species * 2]  (sigma^2, 4 epsilon)
+ *   energy     f64 [n_systems]  out: potential energy at the last step
+ *   kinetic    f64 [n_systems]  out: kinetic energy at the last step
+ *   virial     f64 [n_systems, 6] out (may be NULL): dE/dtril at the last step
+ *   trace_pe, trace_ke  f64 [n_steps, n_systems] out (may be NULL)
+ *   integrator 0 = velocity Verlet (NVE), 1 = BAOAB Langevin (NVT)
+ *   seed, step0  counter-based (Philox4x32-10) noise: stream (seed, atom), counter step
+ * ------------------------------------------------------------------------ */
+typedef struct kups_md_args {
+  void *pos;
+  void *mom;
+  void *force;
+  const int32_t *sys_offset;
+  const int32_t *order;
+  const float *tril;
+  const float *cutoff;
+  const float *skin;
+  const float *dt;
+  const float *kT;
+  const float *friction;
+  const float *lj_table;
+  double *energy;
+  double *kinetic;
+  double *virial;
+  double *trace_pe;
+  double *trace_ke;
+  int64_t n_atoms;
+  int32_t n_systems;
+  int32_t n_species;
+  int32_t n_steps;
+  int32_t integrator;
+  int32_t forces_valid;
+  int32_t neighbor_capacity; /* Verlet-list slots per atom */
+  uint64_t seed;
+  uint64_t step0;
+  int32_t n_ctas;            /* 0 = one per SM */
+  int32_t block_threads;     /* 0 = library default */
+} kups_md_args;
+
+size_t kups_lj_md_workspace_bytes(const kups_md_args *args);
+int32_t kups_lj_md_run(const kups_md_args *args, void *workspace, size_t workspace_bytes,
+                       kups_status *status, void *stream);
+/* Atoms of one system the fused kernel keeps in shared memory. */
+int32_t kups_lj_md_max_atoms(void);
+
+/* Layout conversion between the reference's particle table (float64 [N, 3]
+ * positions / momenta / forces, float64 masses, int32 species; any order —
+ * MDParticles, src/kups/application/md/data.py:31-65) and the packed float4
+ * arrays of kups_lj_md_run.  perm[k] (may be NULL = identity) is the particle
+ * index stored at packed slot k; force may be NULL (packed as zero / not
+ * written back). */
+int32_t kups_md_pack(const double *pos, const double *mom, const double *force,
+                     const double *mass, const int32_t *species, const int32_t *perm,
+                     int64_t n, void *pos4, void *mom4, void *force4, void *stream);
+int32_t kups_md_unpack(const void *pos4, const void *mom4, const void *force4,
+                       const int32_t *perm, int64_t n, double *pos, double *mom, double *force,
+                       void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KUPS_GB300_H */

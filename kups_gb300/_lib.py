@@ -1,0 +1,114 @@
+"""ctypes binding of the kups_gb300 C ABI (``include/kups_gb300.h``).
+
+The library is the only compute path of this package: if it cannot be loaded
+the calls raise instead of falling back to anything else.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libkups_gb300.so")
+
+KUPS_OK = 0
+KUPS_ERR_CAPACITY = 1
+KUPS_ERR_NONFINITE = 2
+KUPS_ERR_INVALID = 3
+KUPS_ERR_CUDA = 4
+KUPS_ERR_UNSUPPORTED = 5
+
+KUPS_CAP_EDGES = 1
+KUPS_CAP_NEIGHBORS = 2
+KUPS_CAP_GHOSTS = 3
+KUPS_CAP_CELLS = 4
+KUPS_CAP_ATOMS = 5
+
+CAPACITY_NAMES = {1: "edges", 2: "neighbors", 3: "ghosts", 4: "cells", 5: "atoms"}
+
+
+class Status(C.Structure):
+    _fields_ = [("code", C.c_int32), ("detail", C.c_int32), ("required", C.c_int64), ("first_bad", C.c_int64)]
+
+
+class MdArgs(C.Structure):
+    _fields_ = [
+        ("pos", C.c_void_p), ("mom", C.c_void_p), ("force", C.c_void_p),
+        ("sys_offset", C.c_void_p), ("order", C.c_void_p), ("tril", C.c_void_p),
+        ("cutoff", C.c_void_p), ("skin", C.c_void_p), ("dt", C.c_void_p), ("kT", C.c_void_p),
+        ("friction", C.c_void_p), ("lj_table", C.c_void_p),
+        ("energy", C.c_void_p), ("kinetic", C.c_void_p), ("virial", C.c_void_p),
+        ("trace_pe", C.c_void_p), ("trace_ke", C.c_void_p),
+        ("n_atoms", C.c_int64), ("n_systems", C.c_int32), ("n_species", C.c_int32),
+        ("n_steps", C.c_int32), ("integrator", C.c_int32), ("forces_valid", C.c_int32),
+        ("neighbor_capacity", C.c_int32), ("seed", C.c_uint64), ("step0", C.c_uint64),
+        ("n_ctas", C.c_int32), ("block_threads", C.c_int32),
+    ]
+
+
+# Every symbol declared in include/kups_gb300.h: name -> (restype, argtypes)
+_P, _I32, _I64, _SZ = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t
+SIGNATURES = {
+    "kups_version": (C.c_char_p, []),
+    "kups_error_string": (C.c_char_p, [_I32]),
+    "kups_neighborlist_workspace_bytes": (_SZ, [_I64, _I32]),
+    "kups_neighborlist_build": (_I32, [_P, _P, _P, _P, _I64, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _SZ, _P, _P]),
+    "kups_lj_edges": (_I32, [_P, _P, _P, _I64, _P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _I32, _P, _P]),
+    "kups_lj_md_workspace_bytes": (_SZ, [C.POINTER(MdArgs)]),
+    "kups_lj_md_run": (_I32, [C.POINTER(MdArgs), _P, _SZ, _P, _P]),
+    "kups_lj_md_max_atoms": (_I32, []),
+    "kups_md_pack": (_I32, [_P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
+    "kups_md_unpack": (_I32, [_P, _P, _P, _P, _I64, _P, _P, _P, _P]),
+}
+
+_lib = None
+
+
+class KupsError(RuntimeError):
+    pass
+
+
+class CapacityError(KupsError):
+    """A device buffer was too small; ``required`` is the size that suffices."""
+
+    def __init__(self, which: str, required: int, first_bad: int):
+        super().__init__(f"capacity '{which}' exceeded: {required} required (first offender {first_bad})")
+        self.which = which
+        self.required = int(required)
+        self.first_bad = int(first_bad)
+
+
+def load(path: str | None = None):
+    """Load (building first if needed) the shared library; raises if impossible."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from . import build as _build
+
+        _build.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != KUPS_OK:
+        msg = load().kups_error_string(rc).decode()
+        raise KupsError(f"{what}: {msg} (code {rc})")
+
+
+def raise_status(st: Status) -> None:
+    """Turn a device status word (already copied to the host) into an exception."""
+    if st.code == KUPS_OK:
+        return
+    if st.code == KUPS_ERR_CAPACITY:
+        raise CapacityError(CAPACITY_NAMES.get(st.detail, str(st.detail)), st.required, st.first_bad)
+    msg = load().kups_error_string(st.code).decode()
+    raise KupsError(f"device error: {msg} (code {st.code}, first offender {st.first_bad})")

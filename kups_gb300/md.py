@@ -1,0 +1,281 @@
+"""Fused Lennard-Jones molecular dynamics behind kUPS's ``Propagator`` interface.
+
+Mirrors ``Propagator.__call__(key, state) -> state`` (src/kups/core/propagator.py:84-121)
+for the propagators built by ``make_velocity_verlet_step`` and
+``make_baoab_langevin_step`` (src/kups/md/integrators.py:273-318, 405-455)
+around the Lennard-Jones potential, as ``make_md_propagator`` wires them
+(src/kups/application/md/simulation.py:74-119).  One call runs
+``steps_per_call`` steps of every system in one persistent CUDA launch
+(``kups_lj_md_run``).
+
+State layout: the reference's particle table (float64 positions, momenta,
+masses, species, system index; ``MDParticles``, application/md/data.py:31-65)
+and system table (lattice ``tril``, time step, temperature, friction;
+``MDSystems``, :68-106).  Inside, atoms are packed once into float4 arrays
+grouped by system (``PackedMD``); repeated calls on a ``PackedMD`` keep the
+state on the device.  Capacity overflows restore the state from a backup and
+retry with the size the kernel reported, as ``ResetOnErrorPropagator``
+(propagator.py:534-566) with ``propagate_and_fix`` (:137-172) do.
+
+Randomness: Philox4x32-10 keyed by (seed, atom) with the step as counter; the
+JAX PRNG key is folded into the 64-bit seed (JAX's threefry stream cannot be
+reproduced bit for bit, so stochastic parity is statistical).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field, replace
+
+import torch
+
+from . import _lib
+from .neighborlist import _stream, new_status, read_status
+from .potential import LennardJonesParameters
+from .units import BOLTZMANN_CONSTANT
+
+INTEGRATORS = {"velocity_verlet": 0, "vv": 0, "nve": 0, "baoab": 1, "baoab_langevin": 1, "nvt": 1}
+
+
+@dataclass
+class MDParticles:
+    positions: torch.Tensor  # f64 [N, 3]
+    momenta: torch.Tensor  # f64 [N, 3]
+    masses: torch.Tensor  # f64 [N]
+    species: torch.Tensor  # int [N]
+    system: torch.Tensor  # int [N]
+    forces: torch.Tensor | None = None  # f64 [N, 3]; None = not yet computed
+
+
+@dataclass
+class MDSystems:
+    tril: torch.Tensor  # f64 [S, 6]
+    time_step: torch.Tensor  # [S] internal units (fs * FEMTO_SECOND)
+    temperature: torch.Tensor  # [S] K
+    friction_coefficient: torch.Tensor  # [S] 1 / internal time
+    potential_energy: torch.Tensor | None = None
+    kinetic_energy: torch.Tensor | None = None
+    unitcell_gradients: torch.Tensor | None = None  # dE/dtril [S, 6]
+
+
+@dataclass
+class MDState:
+    particles: MDParticles
+    systems: MDSystems
+    lj_parameters: LennardJonesParameters
+    skin: float = 1.0
+    step: int = 0
+
+
+@dataclass
+class PackedMD:
+    """Device-resident packed state of a batch of systems."""
+
+    pos4: torch.Tensor  # float32 [N, 4]
+    mom4: torch.Tensor
+    frc4: torch.Tensor
+    perm: torch.Tensor  # int32 [N]: reference index of packed slot k
+    sys_offset: torch.Tensor  # int32 [S + 1]
+    order: torch.Tensor  # int32 [S], largest systems first
+    tril32: torch.Tensor  # float32 [S, 6]
+    cutoff: torch.Tensor  # float32 [S]
+    skin: torch.Tensor
+    dt: torch.Tensor
+    kT: torch.Tensor
+    friction: torch.Tensor
+    lj_table: torch.Tensor  # float32 [T * T * 2]
+    n_species: int
+    max_atoms: int
+    max_density: float
+    forces_valid: bool = False
+    energy: torch.Tensor | None = None
+    kinetic: torch.Tensor | None = None
+    virial: torch.Tensor | None = None
+
+    @property
+    def n_atoms(self) -> int:
+        return self.pos4.shape[0]
+
+    @property
+    def n_systems(self) -> int:
+        return self.sys_offset.shape[0] - 1
+
+    def clone_dynamic(self) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+        return self.pos4.clone(), self.mom4.clone(), self.frc4.clone()
+
+
+def lj_table(params: LennardJonesParameters) -> torch.Tensor:
+    s = params.sigma.to(torch.float64)
+    e = params.epsilon.to(torch.float64)
+    return torch.stack([s * s, 4.0 * e], -1).reshape(-1).to(device="cuda", dtype=torch.float32)
+
+
+def pack(state: MDState) -> PackedMD:
+    """Reference layout -> packed device arrays (the kups_md_pack kernel)."""
+    lib = _lib.load()
+    p, sy = state.particles, state.systems
+    dev = "cuda"
+    system = p.system.to(dev, torch.int64)
+    n = system.shape[0]
+    s = sy.tril.shape[0]
+    perm = torch.argsort(system, stable=True)
+    counts = torch.bincount(system, minlength=s)
+    sys_offset = torch.zeros(s + 1, dtype=torch.int64, device=dev)
+    sys_offset[1:] = torch.cumsum(counts, 0)
+    order = torch.argsort(counts, descending=True, stable=True)
+    pos = p.positions.to(dev, torch.float64).contiguous()
+    mom = p.momenta.to(dev, torch.float64).contiguous()
+    frc = p.forces.to(dev, torch.float64).contiguous() if p.forces is not None else None
+    mass = p.masses.to(dev, torch.float64).contiguous()
+    species = p.species.to(dev, torch.int32).contiguous()
+    perm32 = perm.to(torch.int32).contiguous()
+    pos4 = torch.empty((n, 4), device=dev, dtype=torch.float32)
+    mom4 = torch.empty_like(pos4)
+    frc4 = torch.empty_like(pos4)
+    rc = lib.kups_md_pack(pos.data_ptr(), mom.data_ptr(), frc.data_ptr() if frc is not None else None,
+                          mass.data_ptr(), species.data_ptr(), perm32.data_ptr(), n, pos4.data_ptr(),
+                          mom4.data_ptr(), frc4.data_ptr(), _stream())
+    _lib.check(rc, "kups_md_pack")
+    f32 = lambda x: torch.as_tensor(x, dtype=torch.float64).to(dev).reshape(-1).expand(s).to(torch.float32).contiguous()
+    tril = sy.tril.to(dev, torch.float64)
+    vol = (tril[:, 0] * tril[:, 2] * tril[:, 5]).abs()
+    dens = float((counts.to(torch.float64) / vol).max()) if s > 0 else 0.0
+    kT = torch.as_tensor(sy.temperature, dtype=torch.float64).to(dev) * BOLTZMANN_CONSTANT
+    return PackedMD(
+        pos4=pos4, mom4=mom4, frc4=frc4, perm=perm32, sys_offset=sys_offset.to(torch.int32).contiguous(),
+        order=order.to(torch.int32).contiguous(), tril32=tril.to(torch.float32).contiguous(),
+        cutoff=f32(state.lj_parameters.cutoff), skin=f32(state.skin), dt=f32(sy.time_step), kT=f32(kT),
+        friction=f32(sy.friction_coefficient), lj_table=lj_table(state.lj_parameters),
+        n_species=int(state.lj_parameters.sigma.shape[0]), max_atoms=int(counts.max()) if s > 0 else 0,
+        max_density=dens, forces_valid=p.forces is not None,
+    )
+
+
+def unpack(packed: PackedMD, state: MDState) -> MDState:
+    """Packed device arrays -> a new reference-layout state (kups_md_unpack)."""
+    lib = _lib.load()
+    n = packed.n_atoms
+    pos = torch.empty((n, 3), device="cuda", dtype=torch.float64)
+    mom = torch.empty_like(pos)
+    frc = torch.empty_like(pos)
+    rc = lib.kups_md_unpack(packed.pos4.data_ptr(), packed.mom4.data_ptr(), packed.frc4.data_ptr(),
+                            packed.perm.data_ptr(), n, pos.data_ptr(), mom.data_ptr(), frc.data_ptr(), _stream())
+    _lib.check(rc, "kups_md_unpack")
+    parts = replace(state.particles, positions=pos, momenta=mom, forces=frc)
+    systems = replace(state.systems, potential_energy=packed.energy, kinetic_energy=packed.kinetic,
+                      unitcell_gradients=packed.virial)
+    return replace(state, particles=parts, systems=systems)
+
+
+def key_to_seed(key) -> int:
+    if key is None:
+        return 0
+    if isinstance(key, int):
+        return key & (2**64 - 1)
+    t = torch.as_tensor(key).reshape(-1).to(torch.int64).cpu()
+    h = 0x9E3779B97F4A7C15
+    for v in t.tolist():
+        h = ((h ^ (v & 0xFFFFFFFF)) * 0x100000001B3) & (2**64 - 1)
+    return h
+
+
+@dataclass
+class FusedLennardJonesMD:
+    """Propagator: ``steps_per_call`` VV or BAOAB steps of LJ dynamics per call."""
+
+    integrator: str = "baoab"
+    steps_per_call: int = 1
+    neighbor_capacity: int | None = None
+    n_ctas: int = 0
+    block_threads: int = 0
+    _ws: torch.Tensor | None = field(default=None, repr=False)
+
+    def __call__(self, key, state: MDState) -> MDState:
+        packed = pack(state)
+        self.run_packed(packed, self.steps_per_call, key_to_seed(key), state.step)
+        out = unpack(packed, state)
+        return replace(out, step=state.step + self.steps_per_call)
+
+    def capacity_for(self, packed: PackedMD) -> int:
+        if self.neighbor_capacity is not None:
+            return self.neighbor_capacity
+        rl = float((packed.cutoff + packed.skin).max())
+        est = 4.0 / 3.0 * math.pi * rl**3 * packed.max_density * 1.35 + 16
+        return int(math.ceil(est / 16.0) * 16)
+
+    def args(self, packed: PackedMD, n_steps: int, seed: int, step0: int, trace_pe=None, trace_ke=None,
+             virial: bool = True) -> _lib.MdArgs:
+        s = packed.n_systems
+        if packed.energy is None:
+            packed.energy = torch.zeros(s, device="cuda", dtype=torch.float64)
+            packed.kinetic = torch.zeros(s, device="cuda", dtype=torch.float64)
+            packed.virial = torch.zeros((s, 6), device="cuda", dtype=torch.float64)
+        a = _lib.MdArgs()
+        a.pos, a.mom, a.force = packed.pos4.data_ptr(), packed.mom4.data_ptr(), packed.frc4.data_ptr()
+        a.sys_offset, a.order, a.tril = packed.sys_offset.data_ptr(), packed.order.data_ptr(), packed.tril32.data_ptr()
+        a.cutoff, a.skin, a.dt = packed.cutoff.data_ptr(), packed.skin.data_ptr(), packed.dt.data_ptr()
+        a.kT, a.friction, a.lj_table = packed.kT.data_ptr(), packed.friction.data_ptr(), packed.lj_table.data_ptr()
+        a.energy, a.kinetic = packed.energy.data_ptr(), packed.kinetic.data_ptr()
+        a.virial = packed.virial.data_ptr() if virial else None
+        a.trace_pe = trace_pe.data_ptr() if trace_pe is not None else None
+        a.trace_ke = trace_ke.data_ptr() if trace_ke is not None else None
+        a.n_atoms, a.n_systems, a.n_species = packed.n_atoms, s, packed.n_species
+        a.n_steps = int(n_steps)
+        a.integrator = INTEGRATORS[self.integrator]
+        a.forces_valid = int(packed.forces_valid)
+        a.neighbor_capacity = self.capacity_for(packed)
+        a.seed, a.step0 = int(seed) & (2**64 - 1), int(step0)
+        a.n_ctas, a.block_threads = self.n_ctas, self.block_threads
+        return a
+
+    def workspace(self, a: _lib.MdArgs) -> torch.Tensor:
+        nbytes = _lib.load().kups_lj_md_workspace_bytes(C.byref(a))
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(nbytes, device="cuda", dtype=torch.uint8)
+        return self._ws
+
+    def launch(self, packed: PackedMD, n_steps: int, seed: int = 0, step0: int = 0, status=None, trace_pe=None,
+               trace_ke=None, virial: bool = True) -> torch.Tensor:
+        """Enqueue one persistent launch (no host synchronisation)."""
+        a = self.args(packed, n_steps, seed, step0, trace_pe, trace_ke, virial)
+        ws = self.workspace(a)
+        status = status if status is not None else new_status()
+        rc = _lib.load().kups_lj_md_run(C.byref(a), ws.data_ptr(), ws.numel(), status.data_ptr(), _stream())
+        _lib.check(rc, "kups_lj_md_run")
+        packed.forces_valid = True
+        return status
+
+    def run_packed(self, packed: PackedMD, n_steps: int, seed: int = 0, step0: int = 0, trace: bool = False,
+                   max_tries: int = 6):
+        """Run and check the status; on a capacity overflow restore and retry."""
+        backup = packed.clone_dynamic()
+        valid0 = packed.forces_valid
+        for _ in range(max_tries):
+            tpe = tke = None
+            if trace:
+                tpe = torch.zeros((n_steps, packed.n_systems), device="cuda", dtype=torch.float64)
+                tke = torch.zeros_like(tpe)
+            st = self.launch(packed, n_steps, seed, step0, None, tpe, tke)
+            status = read_status(st)
+            if status.code == _lib.KUPS_OK:
+                return (tpe, tke) if trace else None
+            if status.code == _lib.KUPS_ERR_CAPACITY and status.detail == _lib.KUPS_CAP_NEIGHBORS:
+                packed.pos4.copy_(backup[0])
+                packed.mom4.copy_(backup[1])
+                packed.frc4.copy_(backup[2])
+                packed.forces_valid = valid0
+                self.neighbor_capacity = int(math.ceil(status.required * 1.25 / 16.0) * 16)
+                continue
+            _lib.raise_status(status)
+        raise _lib.KupsError("fused MD capacity did not converge")
+
+
+def make_velocity_verlet_step(steps_per_call: int = 1, **kw) -> FusedLennardJonesMD:
+    """Velocity Verlet (NVE) with the LJ force as derivative computation (integrators.py:273-318)."""
+    return FusedLennardJonesMD("velocity_verlet", steps_per_call, **kw)
+
+
+def make_baoab_langevin_step(steps_per_call: int = 1, **kw) -> FusedLennardJonesMD:
+    """BAOAB Langevin (NVT) with the LJ force as derivative computation (integrators.py:405-455)."""
+    return FusedLennardJonesMD("baoab", steps_per_call, **kw)

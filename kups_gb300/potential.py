@@ -1,0 +1,126 @@
+"""Lennard-Jones potential on the GPU behind kUPS's ``Potential`` interface.
+
+Mirrors src/kups/core/potential.py (``PotentialOut`` :78-139, ``Potential``
+:142-198) and src/kups/potential/classical/lennard_jones.py
+(``LennardJonesParameters`` :82-141, ``make_lennard_jones_potential``
+:355-392).  The energy and both gradients (positions and cell ``tril``, the
+``PositionAndUnitCell`` pair of src/kups/potential/common/energy.py:57-59)
+come from the ``kups_lj_edges`` CUDA kernel over the GPU neighbour list.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Any, NamedTuple
+
+import torch
+
+from . import _lib
+from .neighborlist import CellListNeighborList, NeighborListPoints, _f64, _i32, _stream, new_status, read_status
+from .unitcell import as_tril
+
+
+class PositionAndUnitCell(NamedTuple):
+    positions: torch.Tensor  # dE/dx [N, 3]
+    unitcell: torch.Tensor  # dE/dtril [S, 6]
+
+
+@dataclass
+class PotentialOut:
+    total_energies: torch.Tensor  # [S]
+    gradients: Any = None
+    hessians: Any = None
+
+
+@dataclass
+class LennardJonesParameters:
+    labels: tuple
+    sigma: torch.Tensor  # [T, T]
+    epsilon: torch.Tensor  # [T, T]
+    cutoff: torch.Tensor  # [S]
+
+    @classmethod
+    def from_lorentz_berthelot_mixing(cls, labels, sigma, epsilon, cutoff) -> "LennardJonesParameters":
+        """sigma_ij = (sigma_i + sigma_j) / 2, eps_ij = sqrt(eps_i eps_j) (lennard_jones.py:125-141)."""
+        s = torch.as_tensor(sigma, dtype=torch.float64)
+        e = torch.as_tensor(epsilon, dtype=torch.float64)
+        return cls(tuple(labels), (s[:, None] + s) / 2, torch.sqrt(e[:, None] * e),
+                   torch.as_tensor(cutoff, dtype=torch.float64).reshape(-1))
+
+    @classmethod
+    def from_dict(cls, cutoff, parameters: dict, mixing_rule: str = "lorentz_berthelot"):
+        """Missing sigma defaults to 1.0 and epsilon to 0.0 (lennard_jones.py:98-123)."""
+        if mixing_rule != "lorentz_berthelot":
+            raise ValueError(f"unknown mixing rule {mixing_rule}")
+        labels = tuple(parameters.keys())
+        raw = [(s or 1.0, e or 0.0) for s, e in parameters.values()]
+        return cls.from_lorentz_berthelot_mixing(labels, [r[0] for r in raw], [r[1] for r in raw], [cutoff])
+
+
+@dataclass
+class LJParticles:
+    positions: torch.Tensor  # f64 [N, 3]
+    species: torch.Tensor  # int [N] index into the parameter tables
+    system: torch.Tensor  # int [N]
+    inclusion: torch.Tensor | None = None
+    exclusion: torch.Tensor | None = None
+
+
+@dataclass
+class LJState:
+    particles: LJParticles
+    systems: Any  # tril [S, 6] or an object with .unitcell
+    parameters: LennardJonesParameters
+
+
+class LennardJonesPotential:
+    """``Potential.__call__(state, patch=None) -> PotentialOut`` on the GPU."""
+
+    def __init__(self, neighborlist: CellListNeighborList | None = None, pair_fp32: bool = True):
+        self.neighborlist = neighborlist or CellListNeighborList()
+        self.pair_fp32 = pair_fp32
+
+    def __call__(self, state: LJState, patch=None) -> PotentialOut:
+        if patch is not None:
+            raise NotImplementedError("incremental LJ updates are served by the Monte Carlo kernels")
+        p = state.particles
+        tril = _f64(as_tril(state.systems))
+        s = tril.shape[0]
+        prm = state.parameters
+        cut = _f64(prm.cutoff.reshape(-1).expand(s))
+        pts = NeighborListPoints(p.positions, p.system, p.inclusion, p.exclusion)
+        edges, self.neighborlist = self.neighborlist.call_and_fix(pts, None, tril, cut)
+        return lj_from_edges(p.positions, p.system, p.species, tril, prm.sigma, prm.epsilon, cut, edges.indices,
+                             edges.shifts, edges.n_edges, self.pair_fp32)
+
+
+def lj_from_edges(positions, system, species, tril, sigma, epsilon, cutoffs, edges, shifts, n_edges,
+                  pair_fp32: bool = True) -> PotentialOut:
+    lib = _lib.load()
+    pos = _f64(positions)
+    n = pos.shape[0]
+    sysi = _i32(system)
+    sp = _i32(species)
+    tril = _f64(tril)
+    s = tril.shape[0]
+    cut = _f64(torch.as_tensor(cutoffs).reshape(-1).expand(s))
+    sig = _f64(torch.as_tensor(sigma))
+    eps = _f64(torch.as_tensor(epsilon))
+    t = sig.shape[0]
+    e_idx = _i32(edges).reshape(-1, 2)
+    e_sh = _i32(shifts).reshape(-1, 3)
+    energy = torch.empty(s, device="cuda", dtype=torch.float64)
+    grad = torch.empty((n, 3), device="cuda", dtype=torch.float64)
+    gtril = torch.empty((s, 6), device="cuda", dtype=torch.float64)
+    status = new_status()
+    rc = lib.kups_lj_edges(pos.data_ptr(), sysi.data_ptr(), sp.data_ptr(), n, tril.data_ptr(), cut.data_ptr(), s,
+                           sig.data_ptr(), eps.data_ptr(), t, e_idx.data_ptr(), e_sh.data_ptr(), int(n_edges),
+                           energy.data_ptr(), grad.data_ptr(), gtril.data_ptr(), int(bool(pair_fp32)),
+                           status.data_ptr(), _stream())
+    _lib.check(rc, "kups_lj_edges")
+    _lib.raise_status(read_status(status))
+    return PotentialOut(energy, PositionAndUnitCell(grad, gtril))
+
+
+def make_lennard_jones_potential(neighborlist=None, pair_fp32: bool = True) -> LennardJonesPotential:
+    return LennardJonesPotential(neighborlist, pair_fp32)

@@ -1,0 +1,130 @@
+"""Seeded synthetic inputs with the shapes of the benchmark configurations.
+
+* ``argon_fcc``: LJ argon on an FCC lattice (864 atoms = 6x6x6 cells, a = 5.74 A).
+* ``batched_uneven_lj``: many independent cubic LJ systems with atom counts
+  drawn uniformly from [n_min, n_max], reduced densities from U[rho_min,
+  rho_max] sigma^-3 and temperatures from U[t_min, t_max] K.  Positions are a
+  random subset of the sites of a simple-cubic lattice of spacing a >= the
+  minimum separation d, each displaced by at most (a - d)/2 per axis, which
+  guarantees every pair is at least d apart while staying seeded and fast.
+* ``ionic_melt``: +1/-1 point ions with per-species LJ in a cubic box, same
+  non-overlap construction.
+
+Maxwell-Boltzmann momenta with the centre-of-mass drift removed follow
+src/kups/application/md/data.py:170-176.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from .units import BOLTZMANN_CONSTANT, FEMTO_SECOND
+
+ARGON_SIGMA = 3.405
+ARGON_EPS = 119.8 * BOLTZMANN_CONSTANT
+ARGON_MASS = 39.948
+
+
+@dataclass
+class MDWorkload:
+    positions: np.ndarray  # f64 [N, 3]
+    momenta: np.ndarray  # f64 [N, 3]
+    masses: np.ndarray  # f64 [N]
+    species: np.ndarray  # int32 [N]
+    system: np.ndarray  # int32 [N]
+    tril: np.ndarray  # f64 [S, 6]
+    temperature: np.ndarray  # K [S]
+    time_step: np.ndarray  # internal units [S]
+    friction: np.ndarray  # 1/internal time [S]
+    sigma: np.ndarray  # [T, T]
+    epsilon: np.ndarray  # [T, T]
+    cutoff: float
+    skin: float
+    charges: np.ndarray | None = None
+
+    @property
+    def n_atoms(self) -> int:
+        return int(self.positions.shape[0])
+
+    @property
+    def n_systems(self) -> int:
+        return int(self.tril.shape[0])
+
+
+def _mb_momenta(rng, masses, kT, system, n_sys):
+    std = np.sqrt(masses * kT[system])
+    p = rng.standard_normal((masses.size, 3)) * std[:, None]
+    cnt = np.bincount(system, minlength=n_sys).astype(np.float64)
+    drift = np.stack([np.bincount(system, weights=p[:, a], minlength=n_sys) for a in range(3)], -1)
+    return p - (drift / np.maximum(cnt, 1)[:, None])[system]
+
+
+_BASES = {
+    "sc": (np.zeros((1, 3)), 1.0),
+    "bcc": (np.array([[0, 0, 0], [0.5, 0.5, 0.5]]), math.sqrt(3) / 2),
+    "fcc": (np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]]), 1 / math.sqrt(2)),
+}
+
+
+def lattice_positions(rng, n, box, dmin):
+    """n points in a cubic box (centred at 0), pairwise >= dmin apart under PBC.
+
+    Sites of whichever of the sc / bcc / fcc lattices (with the fewest cells
+    holding n sites) has the largest nearest-neighbour spacing; a random subset
+    of n sites, each jittered by at most (spacing - dmin) / 2 per axis.
+    """
+    best = None
+    for base, nn_factor in _BASES.values():
+        k = max(1, int(math.ceil((n / len(base)) ** (1 / 3))))
+        while len(base) * k**3 < n:
+            k += 1
+        nn = box / k * nn_factor
+        if best is None or nn > best[0]:
+            best = (nn, k, base)
+    nn, k, base = best
+    if nn < dmin:
+        raise ValueError("box too small for the minimum separation")
+    cells = np.stack(np.meshgrid(*[np.arange(k)] * 3, indexing="ij"), -1).reshape(-1, 1, 3)
+    sites = (cells + base[None]).reshape(-1, 3) / k * box
+    pick = rng.choice(sites.shape[0], size=n, replace=False)
+    jitter = (nn - dmin) / 2.0 / math.sqrt(3)
+    return sites[pick] + rng.uniform(-jitter, jitter, (n, 3)) - box / 2
+
+
+def argon_fcc(n_side=6, a=5.74, temperature=94.4, dt_fs=2.0, friction_per_ps=1.0, cutoff=8.5, skin=1.0, seed=0):
+    rng = np.random.default_rng(seed)
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.array([(i, j, k) for i in range(n_side) for j in range(n_side) for k in range(n_side)])
+    frac = ((g[:, None, :] + base[None]) / n_side).reshape(-1, 3) - 0.5
+    L = n_side * a
+    pos = frac * L
+    n = pos.shape[0]
+    masses = np.full(n, ARGON_MASS)
+    system = np.zeros(n, np.int32)
+    T = np.array([temperature])
+    mom = _mb_momenta(rng, masses, T * BOLTZMANN_CONSTANT, system, 1)
+    return MDWorkload(pos, mom, masses, np.zeros(n, np.int32), system, np.array([[L, 0, L, 0, 0, L]], float), T,
+                      np.array([dt_fs * FEMTO_SECOND]), np.array([friction_per_ps / 1000.0 / FEMTO_SECOND]),
+                      np.array([[ARGON_SIGMA]]), np.array([[ARGON_EPS]]), cutoff, skin)
+
+
+def batched_uneven_lj(n_systems=4096, n_min=64, n_max=2048, rho_min=0.7, rho_max=0.9, t_min=80.0, t_max=140.0,
+                      rc_sigma=2.5, skin_sigma=0.3, dt_fs=2.0, friction_per_ps=1.0, min_sep_sigma=0.9, seed=1):
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(n_min, n_max + 1, n_systems)
+    rho = rng.uniform(rho_min, rho_max, n_systems)
+    temps = rng.uniform(t_min, t_max, n_systems)
+    boxes = (counts / rho) ** (1 / 3) * ARGON_SIGMA
+    pos = np.concatenate([lattice_positions(rng, int(c), float(b), min_sep_sigma * ARGON_SIGMA)
+                          for c, b in zip(counts, boxes)])
+    system = np.repeat(np.arange(n_systems, dtype=np.int32), counts)
+    masses = np.full(pos.shape[0], ARGON_MASS)
+    mom = _mb_momenta(rng, masses, temps * BOLTZMANN_CONSTANT, system, n_systems)
+    tril = np.zeros((n_systems, 6))
+    tril[:, 0] = tril[:, 2] = tril[:, 5] = boxes
+    return MDWorkload(pos, mom, masses, np.zeros(pos.shape[0], np.int32), system, tril, temps,
+                      np.full(n_systems, dt_fs * FEMTO_SECOND), np.full(n_systems, friction_per_ps / 1000.0 / FEMTO_SECOND),
+                      np.array([[ARGON_SIGMA]]), np.array([[ARGON_EPS]]), rc_sigma * ARGON_SIGMA, skin_sigma * ARGON_SIGMA)

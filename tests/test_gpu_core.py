@@ -1,0 +1,278 @@
+"""GPU parity of the neighbour list, LJ and fused-MD kernels against the CPU oracle.
+
+Bars: neighbour-list edge sets bit-exact as sorted (i, j, shift) rows;
+float64 pair arithmetic within rtol 1e-10 of the oracle; float32 pair
+arithmetic within force RMS relative error 1e-5 and energy relative error
+1e-5 of the float64 oracle evaluated at the same (float32-representable)
+positions.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import lennard_jones as olj
+from oracle import md as omd
+from oracle import neighborlist as onl
+from oracle import unitcell as ouc
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RMS_TOL = 1e-5
+ENERGY_REL_TOL = 1e-5
+
+
+def cuda(x, dtype=None):
+    return torch.as_tensor(np.asarray(x), dtype=dtype).cuda()
+
+
+def gpu_edges(pos, system, tril, cutoffs, inclusion=None, exclusion=None, n_inclusion=None, avg_edges=64):
+    from kups_gb300.neighborlist import CellListNeighborList, NeighborListPoints
+
+    pts = NeighborListPoints(cuda(pos, torch.float64), cuda(system, torch.int32),
+                             None if inclusion is None else cuda(inclusion, torch.int32),
+                             None if exclusion is None else cuda(exclusion, torch.int32), n_inclusion)
+    edges, _ = CellListNeighborList(avg_edges).call_and_fix(pts, None, cuda(tril, torch.float64),
+                                                             cuda(cutoffs, torch.float64))
+    idx, sh = edges.valid()
+    return onl.sort_edges(idx.cpu().numpy(), sh.cpu().numpy()), edges
+
+
+def assert_same_edges(got, exp):
+    ge, gs = got
+    ee, es = exp
+    assert ge.shape == ee.shape, (ge.shape, ee.shape)
+    np.testing.assert_array_equal(ge, ee)
+    np.testing.assert_array_equal(gs, es)
+
+
+def _cube(L, n=1):
+    return np.repeat(ouc.tril_from_lattice(np.eye(3) * L)[None], n, axis=0)
+
+
+# ------------------------------------------------------------------ neighbour list
+GOLDEN_NL = [
+    # (positions, system, lattice-or-tril, cutoffs, exclusion) from test/core/test_neighborlist.py
+    (np.array([[0.0, 0, 0], [0.4, 0, 0]]), [0, 0], ouc.tril_from_lattice(np.diag([1.0, 10, 10]))[None], [0.8], None),
+    (np.array([[0.0, 0, 0], [0.3, 0.3, 0.3]]), [0, 0], _cube(1.0), [0.8], None),
+    (np.random.default_rng(42).uniform(0, 1, (5, 3)), [0] * 5, _cube(1.5), [1.2], None),
+    (np.array([[0.0, 0, 0], [0.4, 0, 0], [0.0, 0, 0], [1.0, 0, 0]]), [0, 0, 1, 1],
+     ouc.tril_from_lattice(np.stack([np.diag([1.0, 10.0, 10.0]), np.eye(3) * 10])), [0.8, 1.5], None),
+    (np.array([[0.0, 0, 0], [0.3, 0.2, 0.1]]), [0, 0],
+     ouc.tril_from_lattice(np.array([[1.0, 0, 0], [0.5, 0.866, 0], [0, 0, 10.0]]))[None], [0.8], None),
+    (np.zeros((1, 3)), [0], _cube(0.5), [0.55], None),
+    (np.array([[0.0, 0, 0], [0.3, 0, 0]]), [0, 0], _cube(1.0), [np.inf], None),
+    (np.array([[0.1, 0.1, 0.1], [0.4, 0.1, 0.1]]), [0, 0], _cube(0.5), [0.4], [0, 0]),
+    (np.random.default_rng(0).uniform(0, 10, (15, 3)), [0] * 15, _cube(10.0), [3.0], None),
+]
+
+
+@pytest.mark.parametrize("case", range(len(GOLDEN_NL)))
+def test_nl_golden_cases_bit_exact(case):
+    pos, sysi, tril, cut, excl = GOLDEN_NL[case]
+    exp = onl.neighbor_list(pos, sysi, tril, cut, exclusion=excl)
+    got, _ = gpu_edges(pos, sysi, tril, cut, exclusion=excl)
+    assert_same_edges(got, exp)
+
+
+def random_triclinic_batch(seed=0, n_sys=8):
+    rng = np.random.default_rng(seed)
+    pos, sysi, trils, cuts, excl, incl = [], [], [], [], [], []
+    off = 0
+    for s in range(n_sys):
+        lengths = rng.uniform(6, 16, 3)
+        angles = rng.uniform(70, 110, 3)
+        L = ouc.lattice_from_lengths_angles(lengths, angles)
+        t = ouc.tril_from_lattice(L)
+        n = int(rng.integers(3, 60)) * 3
+        f = rng.uniform(-0.7, 0.7, (n, 3))  # some outside the primary cell on purpose
+        pos.append(f @ L)
+        sysi += [s] * n
+        trils.append(t)
+        cuts.append(rng.uniform(2.0, 9.0))  # some need periodic images
+        excl += list(off + np.arange(n) // 3)  # molecules of three
+        inc = np.full(n, s)
+        inc[rng.uniform(size=n) < 0.05] = n_sys  # a few invalid inclusion labels
+        incl += list(inc)
+        off += n
+    return np.concatenate(pos), np.array(sysi), np.stack(trils), np.array(cuts), np.array(excl), np.array(incl)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_nl_random_triclinic_batches_bit_exact(seed):
+    pos, sysi, tril, cut, excl, incl = random_triclinic_batch(seed)
+    exp = onl.neighbor_list(pos, sysi, tril, cut, inclusion=incl, exclusion=excl, n_inclusion=len(tril))
+    got, _ = gpu_edges(pos, sysi, tril, cut, inclusion=incl, exclusion=excl, n_inclusion=len(tril))
+    assert_same_edges(got, exp)
+
+
+def test_nl_batched_uneven_subset_bit_exact():
+    from kups_gb300 import workloads
+
+    W = workloads.batched_uneven_lj(n_systems=24, n_max=600, seed=3)
+    cut = np.full(W.n_systems, W.cutoff)
+    exp = onl.neighbor_list(W.positions, W.system, W.tril, cut)
+    got, _ = gpu_edges(W.positions, W.system, W.tril, cut)
+    assert_same_edges(got, exp)
+
+
+def test_nl_capacity_overflow_reports_required_and_pads():
+    from kups_gb300 import _lib
+    from kups_gb300.neighborlist import CellListNeighborList, NeighborListPoints
+
+    pos, sysi, tril, cut, excl, incl = random_triclinic_batch(5, 3)
+    exp = onl.neighbor_list(pos, sysi, tril, cut, exclusion=excl)
+    pts = NeighborListPoints(cuda(pos, torch.float64), cuda(sysi, torch.int32), None, cuda(excl, torch.int32))
+    with pytest.raises(_lib.CapacityError) as err:
+        CellListNeighborList(avg_edges=1)(pts, None, cuda(tril, torch.float64), cuda(cut, torch.float64))
+    assert err.value.required == len(exp[0])
+    got, edges = gpu_edges(pos, sysi, tril, cut, exclusion=excl, avg_edges=1)
+    assert_same_edges(got, exp)
+    tail = edges.indices[edges.n_edges:]
+    assert bool((tail == len(pos)).all()) and bool((edges.shifts[edges.n_edges:] == 0).all())
+
+
+# ------------------------------------------------------------------ LJ over edges
+SIG = np.array([[1.0, 1.2], [1.2, 1.0]])
+EPS = np.array([[1.0, 0.8], [0.8, 1.0]])
+
+
+def test_lj_golden_pairs_on_gpu():
+    from kups_gb300.potential import lj_from_edges
+
+    cases = [
+        (np.array([[0.0, 0, 0], [1.0, 0, 0]]), [0, 1], [[0, 1]], 4 * 0.8 * (1.2**12 - 1.2**6)),
+        (np.array([[0.0, 0, 0], [1.5, 0, 0]]), [0, 0], [[0, 1]], 4 * ((1 / 1.5) ** 12 - (1 / 1.5) ** 6)),
+    ]
+    for pos, sp, e, expected in cases:
+        for fp32 in (False, True):
+            out = lj_from_edges(cuda(pos), cuda([0, 0]), cuda(sp), cuda(_cube(10.0)), cuda(SIG), cuda(EPS), cuda([12.0]),
+                                cuda(e, torch.int32), cuda(np.zeros((1, 3)), torch.int32), 1, fp32)
+            assert np.isclose(out.total_energies.cpu().numpy()[0] * 2, expected, rtol=1e-6)
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_lj_edges_match_oracle(fp32):
+    from kups_gb300.potential import lj_from_edges
+
+    rng = np.random.default_rng(7)
+    pos, sysi, tril, cut, excl, incl = random_triclinic_batch(7, 4)
+    # spread atoms so LJ stays moderate: sigma small relative to spacing
+    sp = rng.integers(0, 2, len(pos))
+    sig = SIG * 1.1
+    e, s = onl.neighbor_list(pos, sysi, tril, cut)
+    en, g, dt = olj.lj_from_edges(pos, sysi, sp, tril, sig, EPS, cut, e, s)
+    out = lj_from_edges(cuda(pos), cuda(sysi), cuda(sp), cuda(tril), cuda(sig), cuda(EPS), cuda(cut), cuda(e, torch.int32),
+                        cuda(s, torch.int32), len(e), fp32)
+    ge = out.total_energies.cpu().numpy()
+    gg = out.gradients.positions.cpu().numpy()
+    gt = out.gradients.unitcell.cpu().numpy()
+    if not fp32:
+        np.testing.assert_allclose(ge, en, rtol=1e-10)
+        np.testing.assert_allclose(gg, g, rtol=1e-9, atol=1e-9 * np.abs(g).max())
+        np.testing.assert_allclose(gt, dt, rtol=1e-9, atol=1e-9 * np.abs(dt).max())
+    else:
+        assert np.all(np.abs(ge - en) <= ENERGY_REL_TOL * np.abs(en) + 1e-12)
+        rms = np.sqrt(np.mean((gg - g) ** 2)) / np.sqrt(np.mean(g**2))
+        assert rms <= FORCE_RMS_TOL, rms
+        np.testing.assert_allclose(gt, dt, rtol=1e-4, atol=1e-5 * np.abs(dt).max())
+
+
+# ------------------------------------------------------------------ fused MD
+def md_state(W, forces=None):
+    from kups_gb300 import md, potential
+
+    prm = potential.LennardJonesParameters("Ar", torch.as_tensor(W.sigma), torch.as_tensor(W.epsilon),
+                                           torch.tensor([W.cutoff], dtype=torch.float64))
+    parts = md.MDParticles(cuda(W.positions, torch.float64), cuda(W.momenta, torch.float64), cuda(W.masses, torch.float64),
+                           cuda(W.species, torch.int32), cuda(W.system, torch.int32), forces)
+    systems = md.MDSystems(cuda(W.tril, torch.float64), cuda(W.time_step), cuda(W.temperature), cuda(W.friction))
+    return md.MDState(parts, systems, prm, skin=W.skin)
+
+
+def small_batch():
+    from kups_gb300 import workloads
+
+    return workloads.batched_uneven_lj(n_systems=12, n_min=64, n_max=700, seed=11)
+
+
+def oracle_forces(W, pos):
+    cut = np.full(W.n_systems, W.cutoff)
+    return omd.lj_forces(pos, W.system, W.species, W.tril, W.sigma, W.epsilon, cut)
+
+
+@pytest.mark.parametrize("which", ["batch", "argon"])
+def test_fused_md_forces_energy_virial_match_oracle(which):
+    from kups_gb300 import md, workloads
+
+    W = small_batch() if which == "batch" else workloads.argon_fcc()
+    W.positions = W.positions + np.random.default_rng(1).normal(0, 0.1, W.positions.shape)
+    state = md_state(W)
+    prop = md.make_velocity_verlet_step(steps_per_call=0)
+    out = prop(None, state)
+    pos = out.particles.positions.cpu().numpy()
+    e, f, dt = oracle_forces(W, pos)
+    gf = out.particles.forces.cpu().numpy()
+    ge = out.systems.potential_energy.cpu().numpy()
+    gv = out.systems.unitcell_gradients.cpu().numpy()
+    rms = np.sqrt(np.mean((gf - f) ** 2)) / np.sqrt(np.mean(f**2))
+    assert rms <= FORCE_RMS_TOL, rms
+    assert np.all(np.abs(ge - e) <= ENERGY_REL_TOL * np.abs(e)), (ge, e)
+    np.testing.assert_allclose(gv, dt, rtol=1e-4, atol=1e-4 * np.abs(dt).max())
+
+
+def test_fused_md_velocity_verlet_tracks_oracle():
+    from kups_gb300 import md
+
+    W = small_batch()
+    state = md_state(W)
+    prop = md.make_velocity_verlet_step(steps_per_call=10)
+    # start both from the same float32-rounded state with forces at t = 0
+    s0 = md.make_velocity_verlet_step(steps_per_call=0)(None, state)
+    pos0 = s0.particles.positions.cpu().numpy()
+    mom0 = s0.particles.momenta.cpu().numpy()
+    _, f0, _ = oracle_forces(W, pos0)
+    out = prop(None, s0)
+    cut = np.full(W.n_systems, W.cutoff)
+    pos, mom, _, _ = omd.velocity_verlet(pos0, mom0, f0, W.masses, W.system, W.species, W.tril, W.sigma, W.epsilon, cut,
+                                         W.time_step, 10)
+    gp = out.particles.positions.cpu().numpy()
+    d = ouc.wrap(gp - pos, W.tril[W.system])
+    assert np.abs(d).max() < 1e-3, np.abs(d).max()
+    np.testing.assert_allclose(out.particles.momenta.cpu().numpy(), mom, atol=2e-3 * np.abs(mom).max())
+
+
+def test_fused_md_is_deterministic():
+    from kups_gb300 import md
+
+    W = small_batch()
+    outs = []
+    for _ in range(2):
+        prop = md.make_baoab_langevin_step(steps_per_call=25)
+        o = prop([7, 9], md_state(W))
+        outs.append((o.particles.positions.cpu().numpy(), o.systems.potential_energy.cpu().numpy()))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+def test_fused_md_capacity_retry_matches_large_capacity():
+    from kups_gb300 import md
+
+    W = small_batch()
+    a = md.FusedLennardJonesMD("velocity_verlet", 5, neighbor_capacity=16)(None, md_state(W))
+    b = md.FusedLennardJonesMD("velocity_verlet", 5, neighbor_capacity=256)(None, md_state(W))
+    np.testing.assert_array_equal(a.particles.positions.cpu().numpy(), b.particles.positions.cpu().numpy())
+
+
+def test_fused_md_baoab_thermostat_temperature():
+    from kups_gb300 import md, workloads
+    from kups_gb300.units import BOLTZMANN_CONSTANT
+
+    W = workloads.batched_uneven_lj(n_systems=8, n_min=400, n_max=500, seed=4, friction_per_ps=20.0)
+    prop = md.make_baoab_langevin_step()
+    packed = md.pack(md_state(W))
+    _, tke = prop.run_packed(packed, 1500, seed=3, trace=True)
+    ke = tke.cpu().numpy()[500:].mean(axis=0)
+    n = np.bincount(W.system)
+    T = 2 * ke / (3 * n * BOLTZMANN_CONSTANT)
+    np.testing.assert_allclose(T, W.temperature, rtol=0.06)
