@@ -434,12 +434,19 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
       cart_of(p, f, x, y, z);
       sm.shift_vec[c] = make_float4(x, y, z, 0.f);
     }
+    int bad_species = 0;
     for (int i = tid; i < n; i += nt) {
-      sm.pos[i] = gpos[a0 + i];
+      const float4 q = gpos[a0 + i];
+      const int t = __float_as_int(q.w);
+      bad_species |= (t < 0) | (t >= nsp);
+      sm.pos[i] = q;
       sm.mom[i] = gmom[a0 + i];
       sm.frc[i] = gfrc[a0 + i];
     }
-    __syncthreads();
+    if (__syncthreads_or(bad_species)) {
+      if (tid == 0) status_error(status, KUPS_ERR_INVALID, s);
+      continue;
+    }
     const int tpa = choose_tpa(n, nt);
     bool ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s);
     if (!ok) continue;

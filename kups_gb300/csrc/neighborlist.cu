@@ -363,11 +363,11 @@ extern "C" int32_t kups_neighborlist_build(const double *positions, const int32_
   scatter_kernel<<<gb, 256, 0, stream>>>(w.cell_of, n, w.cell_start, w.cell_fill, w.cell_items);
   sort_cells_kernel<<<(unsigned)((w.n_cells_cap + 255) / 256), 256, 0, stream>>>(
       w.cell_start, w.n_cells, w.cell_items);
-  pairs_kernel<false><<<gb, 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys,
+  pairs_kernel<false><<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys,
                                               w.frac, w.cell_of, w.cell_start, w.cell_items,
                                               w.edge_off, edges, shifts, cap);
   KUPS_CUDA_TRY(exclusive_scan<int64_t>(w.edge_off, n, w.scan_tmp, n_edges, stream));
-  pairs_kernel<true><<<gb, 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys,
+  pairs_kernel<true><<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys,
                                              w.frac, w.cell_of, w.cell_start, w.cell_items,
                                              w.edge_off, edges, shifts, cap);
   check_capacity_kernel<<<1, 1, 0, stream>>>(n_edges, cap, status);
