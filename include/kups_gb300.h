@@ -140,6 +140,7 @@ int32_t kups_lj_edges(const double *positions, const int32_t *system,
  *   kinetic    f64 [n_systems]  out: kinetic energy at the last step
  *   virial     f64 [n_systems, 6] out (may be NULL): dE/dtril at the last step
  *   trace_pe, trace_ke  f64 [n_steps, n_systems] out (may be NULL)
+ *   rebuilds   i32 [n_systems] out (may be NULL): list builds during the call
  *   integrator 0 = velocity Verlet (NVE), 1 = BAOAB Langevin (NVT)
  *   seed, step0  counter-based (Philox4x32-10) noise: stream (seed, atom), counter step
  * ------------------------------------------------------------------------ */
@@ -161,6 +162,7 @@ typedef struct kups_md_args {
   double *virial;
   double *trace_pe;
   double *trace_ke;
+  int32_t *rebuilds;         /* [n_systems] out (may be NULL): Verlet-list builds per system */
   int64_t n_atoms;
   int32_t n_systems;
   int32_t n_species;

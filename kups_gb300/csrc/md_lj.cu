@@ -500,6 +500,7 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
       }
       const int need = __syncthreads_or(moved_far);
       if (need) {
+        if (tid == 0 && a.rebuilds != nullptr) a.rebuilds[s] += 1;
         ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s);
         if (!ok) break;
       } else {
