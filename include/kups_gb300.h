@@ -141,6 +141,10 @@ int32_t kups_lj_edges(const double *positions, const int32_t *system,
  *   virial     f64 [n_systems, 6] out (may be NULL): dE/dtril at the last step
  *   trace_pe, trace_ke  f64 [n_steps, n_systems] out (may be NULL)
  *   rebuilds   i32 [n_systems] out (may be NULL): list builds during the call
+ *   profile    u64 [10] out (may be NULL): clock64 cycles spent per phase (setup
+ *              + first build, integrate, list/ghost update, forces, kick +
+ *              reductions, write-back, and inside list builds: ghosts, binning,
+ *              in-cell ordering, Verlet list), accumulated by each CTA's thread 0
  *   integrator 0 = velocity Verlet (NVE), 1 = BAOAB Langevin (NVT)
  *   seed, step0  counter-based (Philox4x32-10) noise: stream (seed, atom), counter step
  * ------------------------------------------------------------------------ */
@@ -163,6 +167,7 @@ typedef struct kups_md_args {
   double *trace_pe;
   double *trace_ke;
   int32_t *rebuilds;         /* [n_systems] out (may be NULL): Verlet-list builds per system */
+  uint64_t *profile;         /* [10] out (may be NULL): SM cycles per phase, summed over CTAs */
   int64_t n_atoms;
   int32_t n_systems;
   int32_t n_species;

@@ -42,25 +42,7 @@ constexpr int kMaxSpecies = 8;
 constexpr int kShiftSide = 5;  // image offsets in [-2, 2]^3
 constexpr int kShiftCount = kShiftSide * kShiftSide * kShiftSide;
 constexpr int kThreads = 1024;
-
-struct Smem {
-  float4 pos[kMaxItems];
-  float4 mom[kMaxAtoms];
-  float4 frc[kMaxAtoms];
-  uint32_t ghost_meta[kMaxGhosts];  // source atom | shift code << 16
-  uint16_t cell_of[kMaxItems];
-  uint16_t cell_items[kMaxItems];
-  int cell_start[kMaxCells + 1];
-  int cell_fill[kMaxCells];
-  uint16_t nbr_count[kMaxAtoms];
-  float4 shift_vec[kShiftCount];
-  float2 lj[kMaxSpecies * kMaxSpecies];  // (sigma^2, 4 eps)
-  double red[72];
-  int iscan[40];
-  int n_ghosts;
-  int flag;
-  int next_sys;
-};
+constexpr int kScratchPerCta = 3 * kMaxAtoms > 2 * kMaxGhosts ? 3 * kMaxAtoms : 2 * kMaxGhosts;  // float4s
 
 struct SysParams {
   float L[6];     // L00 L10 L11 L20 L21 L22
@@ -70,8 +52,34 @@ struct SysParams {
   int K[3];       // image layers per side
   int nc[3];
   float ext[3];   // 1 + 2 m
+  float coff[3];  // 0.5 + m
+  float cscale[3];  // cells per fractional unit
   float dt, c1, c2;
 };
+
+struct Smem {
+  SysParams p;
+  float4 pos[kMaxItems];
+  float4 mom[kMaxAtoms];
+  float4 frc[kMaxAtoms];
+  uint32_t ghost_meta[kMaxGhosts];  // source atom | shift code << 16
+  uint16_t bin_a[kMaxItems];  // scratch of the counting sorts (cell, then new slot, of an item)
+  uint16_t bin_b[kMaxItems];  // scratch of the counting sorts (items grouped by cell)
+  int cell_start[kMaxCells + 1];   // atoms of cell c: [cell_start[c], cell_start[c + 1])
+  int ghost_start[kMaxCells + 1];  // ghosts of cell c: n + [ghost_start[c], ghost_start[c + 1])
+  int cell_fill[kMaxCells];
+  uint16_t gid[kMaxAtoms];  // index of each (cell-sorted) atom inside its system's input order
+  uint16_t nbr_count[kMaxAtoms];
+  float4 shift_vec[kShiftCount];
+  float2 lj[kMaxSpecies * kMaxSpecies];  // (sigma^2, 4 eps)
+  double red[72];
+  int iscan[40];
+  int n_ghosts;
+  int flag;
+  int next_sys;
+  int work;
+};
+
 
 __device__ inline void frac_of(const SysParams &p, float x, float y, float z, float f[3]) {
   f[0] = (x * p.inv[0] + y * p.inv[1]) + z * p.inv[3];
@@ -107,166 +115,272 @@ __device__ inline int shift_code(int ox, int oy, int oz) {
   return ((ox + 2) * kShiftSide + (oy + 2)) * kShiftSide + (oz + 2);
 }
 
-__device__ inline int cell_coord(float pf, float m, float ext, int nc) {
-  int c = (int)floorf((pf + 0.5f + m) / ext * (float)nc);
+__device__ inline int cell_coord(float pf, float off, float scale, int nc) {
+  int c = (int)floorf((pf + off) * scale);
   return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
-// Cost model for the number of lanes serving one atom in the force loop.
-__device__ inline int choose_tpa(int n, int threads) {
-  int best = 1;
-  float best_cost = 1e30f;
-  for (int t = 1; t <= 16; t <<= 1) {
-    const int rounds = (n * t + threads - 1) / threads;
-    const float cost = rounds * (72.0f / t + 6.0f * __log2f((float)t) + 4.0f);
-    if (cost < best_cost) {
-      best_cost = cost;
-      best = t;
-    }
-  }
-  return best;
+__device__ inline int cell_of_point(const SysParams &p, float x, float y, float z, int &cx, int &cy,
+                                    int &cz) {
+  float f[3];
+  frac_of(p, x, y, z, f);
+  cx = cell_coord(f[0], p.coff[0], p.cscale[0], p.nc[0]);
+  cy = cell_coord(f[1], p.coff[1], p.cscale[1], p.nc[1]);
+  cz = cell_coord(f[2], p.coff[2], p.cscale[2], p.nc[2]);
+  return (cz * p.nc[1] + cy) * p.nc[0] + cx;
 }
 
-// Wrap atoms, build the ghost copies, the cell grid and the Verlet list.
-// Returns false (and records the requirement) if a capacity is exceeded.
-__device__ bool rebuild(Smem &sm, const SysParams &p, int n, int tpa, uint16_t *nl, int nb_cap,
-                        kups_status *status, int sys_index) {
+// Lanes serving one atom: the smallest power of two (<= 16) that still gives
+// every thread of the block an atom-lane to work on.
+__device__ inline int choose_tpa(int n, int threads) {
+  int t = 1;
+  while (t < 16 && n * t < threads) t <<= 1;
+  return t;
+}
+
+__device__ __forceinline__ void prof_add(unsigned long long *prof, int k, long long &t0) {
+  if (prof != nullptr && threadIdx.x == 0) {
+    const long long t = clock64();
+    atomicAdd(&prof[k], (unsigned long long)(t - t0));
+    t0 = t;
+  }
+}
+
+// Counting sort of `count` items by cell into cell-contiguous order: on entry
+// sm.bin_a[k] holds the cell of item k; on exit sm.bin_a[k] holds the item's
+// new slot and `start` the exclusive prefix of the per-cell counts.  The order
+// inside a cell follows the item index, so the result is deterministic.
+__device__ void sort_by_cell(Smem &sm, int count, int ncell, int *start) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  // 1. wrap atoms into [-0.5, 0.5), reset travelled distance, count ghosts
-  int my_total = 0;
-  {
-    for (int i = tid; i < n; i += nt) {
-      float4 q = sm.pos[i];
-      float f[3];
-      wrap_position(p, q, f);
-      sm.pos[i] = q;
-      sm.frc[i].w = 0.0f;
-      int c = 0;
-      for (int ox = -p.K[0]; ox <= p.K[0]; ++ox)
-        for (int oy = -p.K[1]; oy <= p.K[1]; ++oy)
-          for (int oz = -p.K[2]; oz <= p.K[2]; ++oz) {
-            if (ox == 0 && oy == 0 && oz == 0) continue;
-            const float g0 = f[0] + ox, g1 = f[1] + oy, g2 = f[2] + oz;
-            c += (g0 >= -0.5f - p.m[0]) & (g0 < 0.5f + p.m[0]) & (g1 >= -0.5f - p.m[1]) &
-                 (g1 < 0.5f + p.m[1]) & (g2 >= -0.5f - p.m[2]) & (g2 < 0.5f + p.m[2]);
-          }
-      my_total += c;
+  for (int c = tid; c <= ncell; c += nt) start[c] = 0;
+  __syncthreads();
+  for (int k = tid; k < count; k += nt) atomicAdd(&start[sm.bin_a[k]], 1);
+  __syncthreads();
+  int carry = 0;
+  for (int b0 = 0; b0 < ncell; b0 += nt) {
+    const int c = b0 + tid;
+    const int v = c < ncell ? start[c] : 0;
+    int tot;
+    const int ex = block_exclusive_scan<int>(v, sm.iscan, &tot);
+    __syncthreads();
+    if (c < ncell) {
+      start[c] = carry + ex;
+      sm.cell_fill[c] = carry + ex;
     }
+    carry += tot;
+  }
+  if (tid == 0) start[ncell] = carry;
+  __syncthreads();
+  for (int k = tid; k < count; k += nt) {
+    const int slot = atomicAdd(&sm.cell_fill[sm.bin_a[k]], 1);
+    sm.bin_b[slot] = (uint16_t)k;
+  }
+  __syncthreads();
+  for (int k = tid; k < count; k += nt) {
+    int lo = 0, hi = ncell - 1;  // cell with start[c] <= k < start[c + 1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (start[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    const int b = start[lo], e = start[lo + 1];
+    const uint16_t v = sm.bin_b[k];
+    int r = 0;
+    for (int m = b; m < e; ++m) r += sm.bin_b[m] < v;
+    sm.bin_a[v] = (uint16_t)(b + r);
+  }
+  __syncthreads();
+}
+
+// Wrap and cell-sort the atoms, build the cell-sorted ghost copies and the
+// Verlet list.  Returns false (and records the requirement) if a capacity is
+// exceeded.  `scratch` is this CTA's slice of global workspace (permutation
+// staging, 48 bytes per atom).
+// Verlet-list layout: 8-byte units of four uint16 item indices (entries
+// 4u .. 4u + 3 of atom i); unit u of atom i sits at ((u / tpa) * n + i) * tpa
+// + u % tpa, so the tpa lanes serving atom i, and the atoms of a warp, read
+// consecutive units.  The last unit is padded with the far-away sentinel item.
+__device__ __noinline__ bool rebuild(Smem &sm, const SysParams &p, int n, int tpa, uint2 *nl,
+                                     int nb_cap, kups_status *status, int sys_index,
+                                     unsigned long long *prof, float4 *scratch) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  long long tp = clock64();
+  const int ncell = p.nc[0] * p.nc[1] * p.nc[2];
+  // 1. wrap atoms into [-0.5, 0.5), reset travelled distance, sort atoms by cell
+  for (int i = tid; i < n; i += nt) {
+    float4 q = sm.pos[i];
+    float f[3];
+    wrap_position(p, q, f);
+    sm.pos[i] = q;
+    sm.frc[i].w = 0.0f;
+    int cx, cy, cz;
+    sm.bin_a[i] = (uint16_t)cell_of_point(p, q.x, q.y, q.z, cx, cy, cz);
+  }
+  __syncthreads();
+  sort_by_cell(sm, n, ncell, sm.cell_start);
+  for (int i = tid; i < n; i += nt) {
+    const int d = sm.bin_a[i];
+    float4 m = sm.mom[i];
+    scratch[3 * d] = sm.pos[i];
+    scratch[3 * d + 1] = m;
+    scratch[3 * d + 2] = make_float4(sm.frc[i].x, sm.frc[i].y, sm.frc[i].z, __int_as_float((int)sm.gid[i]));
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += nt) {
+    sm.pos[i] = scratch[3 * i];
+    sm.mom[i] = scratch[3 * i + 1];
+    const float4 f = scratch[3 * i + 2];
+    sm.frc[i] = make_float4(f.x, f.y, f.z, 0.0f);
+    sm.gid[i] = (uint16_t)__float_as_int(f.w);
+  }
+  __syncthreads();
+  prof_add(prof, 6, tp);
+  // 2. ghosts: count, write in atom-major order, then sort by cell
+  int my_total = 0;
+  for (int i = tid; i < n; i += nt) {
+    const float4 q = sm.pos[i];
+    float f[3];
+    frac_of(p, q.x, q.y, q.z, f);
+    int c = 0;
+    for (int ox = -p.K[0]; ox <= p.K[0]; ++ox)
+      for (int oy = -p.K[1]; oy <= p.K[1]; ++oy)
+        for (int oz = -p.K[2]; oz <= p.K[2]; ++oz) {
+          if (ox == 0 && oy == 0 && oz == 0) continue;
+          const float g0 = f[0] + ox, g1 = f[1] + oy, g2 = f[2] + oz;
+          c += (g0 >= -0.5f - p.m[0]) & (g0 < 0.5f + p.m[0]) & (g1 >= -0.5f - p.m[1]) &
+               (g1 < 0.5f + p.m[1]) & (g2 >= -0.5f - p.m[2]) & (g2 < 0.5f + p.m[2]);
+        }
+    my_total += c;
   }
   int total;
   int base = block_exclusive_scan<int>(my_total, sm.iscan, &total);
   __syncthreads();
-  if (total > kMaxGhosts) {
-    if (tid == 0) status_capacity(status, KUPS_CAP_GHOSTS, total, sys_index);
+  if (total > kMaxGhosts - 1) {  // one slot stays free for the sentinel item
+    if (tid == 0) status_capacity(status, KUPS_CAP_GHOSTS, total + 1, sys_index);
     return false;
   }
-  // 2. write ghosts (deterministic order: atom-major, offset order)
-  {
-    for (int i = tid; i < n; i += nt) {
-      const float4 q = sm.pos[i];
-      float f[3];
-      frac_of(p, q.x, q.y, q.z, f);
-      for (int ox = -p.K[0]; ox <= p.K[0]; ++ox)
-        for (int oy = -p.K[1]; oy <= p.K[1]; ++oy)
-          for (int oz = -p.K[2]; oz <= p.K[2]; ++oz) {
-            if (ox == 0 && oy == 0 && oz == 0) continue;
-            const float g0 = f[0] + ox, g1 = f[1] + oy, g2 = f[2] + oz;
-            if ((g0 >= -0.5f - p.m[0]) & (g0 < 0.5f + p.m[0]) & (g1 >= -0.5f - p.m[1]) &
-                (g1 < 0.5f + p.m[1]) & (g2 >= -0.5f - p.m[2]) & (g2 < 0.5f + p.m[2])) {
-              const int code = shift_code(ox, oy, oz);
-              const float4 sv = sm.shift_vec[code];
-              sm.pos[n + base] = make_float4(q.x + sv.x, q.y + sv.y, q.z + sv.z, q.w);
-              sm.ghost_meta[base] = (uint32_t)i | ((uint32_t)code << 16);
-              ++base;
-            }
-          }
-    }
-  }
-  const int n_items = n + total;
-  const int ncell = p.nc[0] * p.nc[1] * p.nc[2];
-  for (int c = tid; c < ncell; c += nt) {
-    sm.cell_start[c] = 0;
-    sm.cell_fill[c] = 0;
-  }
-  __syncthreads();
-  // 3. bin items into the extended grid
-  for (int it = tid; it < n_items; it += nt) {
-    const float4 q = sm.pos[it];
-    float f[3];
-    frac_of(p, q.x, q.y, q.z, f);
-    const int cx = cell_coord(f[0], p.m[0], p.ext[0], p.nc[0]);
-    const int cy = cell_coord(f[1], p.m[1], p.ext[1], p.nc[1]);
-    const int cz = cell_coord(f[2], p.m[2], p.ext[2], p.nc[2]);
-    const int c = (cz * p.nc[1] + cy) * p.nc[0] + cx;
-    sm.cell_of[it] = (uint16_t)c;
-    atomicAdd(&sm.cell_start[c], 1);
-  }
-  __syncthreads();
-  {
-    int carry = 0;
-    for (int b0 = 0; b0 < ncell; b0 += nt) {
-      const int c = b0 + tid;
-      const int v = c < ncell ? sm.cell_start[c] : 0;
-      int tot;
-      const int ex = block_exclusive_scan<int>(v, sm.iscan, &tot);
-      __syncthreads();
-      if (c < ncell) sm.cell_start[c] = carry + ex;
-      carry += tot;
-    }
-    if (tid == 0) sm.cell_start[ncell] = carry;
-  }
-  __syncthreads();
-  for (int it = tid; it < n_items; it += nt) {
-    const int c = sm.cell_of[it];
-    const int slot = atomicAdd(&sm.cell_fill[c], 1);
-    sm.cell_items[sm.cell_start[c] + slot] = (uint16_t)it;
-  }
-  __syncthreads();
-  for (int c = tid; c < ncell; c += nt) {  // deterministic order inside each cell
-    const int b = sm.cell_start[c], e = sm.cell_start[c + 1];
-    for (int k = b + 1; k < e; ++k) {
-      const uint16_t v = sm.cell_items[k];
-      int m = k - 1;
-      while (m >= b && sm.cell_items[m] > v) {
-        sm.cell_items[m + 1] = sm.cell_items[m];
-        --m;
-      }
-      sm.cell_items[m + 1] = v;
-    }
-  }
-  if (tid == 0) sm.flag = 0;
-  __syncthreads();
-  // 4. Verlet list: entry k of atom i at ((k / tpa) * n + i) * tpa + k % tpa
-  int my_max = 0;
   for (int i = tid; i < n; i += nt) {
     const float4 q = sm.pos[i];
-    const int c = sm.cell_of[i];
-    const int cx = c % p.nc[0], cy = (c / p.nc[0]) % p.nc[1], cz = c / (p.nc[0] * p.nc[1]);
-    int cnt = 0;
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, p.nc[2] - 1); ++z)
-      for (int y = max(cy - 1, 0); y <= min(cy + 1, p.nc[1] - 1); ++y)
-        for (int x = max(cx - 1, 0); x <= min(cx + 1, p.nc[0] - 1); ++x) {
-          const int cc = (z * p.nc[1] + y) * p.nc[0] + x;
-          const int b = sm.cell_start[cc], e = sm.cell_start[cc + 1];
-          for (int k = b; k < e; ++k) {
-            const int j = sm.cell_items[k];
-            if (j == i) continue;
-            const float4 o = sm.pos[j];
-            const float dx = o.x - q.x, dy = o.y - q.y, dz = o.z - q.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < p.rl2) {
-              if (cnt < nb_cap) nl[((size_t)(cnt / tpa) * n + i) * tpa + (cnt % tpa)] = (uint16_t)j;
-              ++cnt;
-            }
+    float f[3];
+    frac_of(p, q.x, q.y, q.z, f);
+    for (int ox = -p.K[0]; ox <= p.K[0]; ++ox)
+      for (int oy = -p.K[1]; oy <= p.K[1]; ++oy)
+        for (int oz = -p.K[2]; oz <= p.K[2]; ++oz) {
+          if (ox == 0 && oy == 0 && oz == 0) continue;
+          const float g0 = f[0] + ox, g1 = f[1] + oy, g2 = f[2] + oz;
+          if ((g0 >= -0.5f - p.m[0]) & (g0 < 0.5f + p.m[0]) & (g1 >= -0.5f - p.m[1]) &
+              (g1 < 0.5f + p.m[1]) & (g2 >= -0.5f - p.m[2]) & (g2 < 0.5f + p.m[2])) {
+            const int code = shift_code(ox, oy, oz);
+            const float4 sv = sm.shift_vec[code];
+            const float4 gq = make_float4(q.x + sv.x, q.y + sv.y, q.z + sv.z, q.w);
+            int cx, cy, cz;
+            sm.bin_a[base] = (uint16_t)cell_of_point(p, gq.x, gq.y, gq.z, cx, cy, cz);
+            scratch[2 * base] = gq;
+            scratch[2 * base + 1] = make_float4(__int_as_float((int)((uint32_t)i | ((uint32_t)code << 16))), 0.f, 0.f, 0.f);
+            ++base;
           }
         }
-    sm.nbr_count[i] = (uint16_t)min(cnt, nb_cap);
-    my_max = max(my_max, cnt);
-  }
-  if (my_max > nb_cap) {
-    atomicMax(&sm.flag, my_max);
   }
   __syncthreads();
+  sort_by_cell(sm, total, ncell, sm.ghost_start);
+  for (int g = tid; g < total; g += nt) {
+    const int d = sm.bin_a[g];
+    sm.pos[n + d] = scratch[2 * g];
+    sm.ghost_meta[d] = (uint32_t)__float_as_int(scratch[2 * g + 1].x);
+  }
+  const int n_items = n + total;
+  if (tid == 0) {
+    sm.pos[n_items] = make_float4(1e15f, 1e15f, 1e15f, __int_as_float(0));  // sentinel item
+    sm.flag = 0;
+    sm.work = 0;
+  }
+  __syncthreads();
+  prof_add(prof, 7, tp);
+  prof_add(prof, 8, tp);
+  // 3. Verlet list, row-major: a warp takes one x-row of cells and walks its
+  //    (cell-sorted, hence contiguous) atoms 32 at a time, one lane per atom;
+  //    the candidates of a chunk are the contiguous atom and ghost ranges of
+  //    the 3 x 3 neighbour rows over the x-range of the chunk's cells plus one
+  //    cell either side, read once per warp (shared-memory broadcast).  Hits
+  //    of 32 candidates are gathered in a per-lane bit mask, then appended in
+  //    candidate order (deterministic), four per 8-byte store.
+  const int lane = threadIdx.x & 31;
+  const int ltpa = __ffs(tpa) - 1;
+  const uint32_t sent = (uint32_t)n_items;
+  const int n_rows = p.nc[1] * p.nc[2];
+  int my_max = 0;
+  while (true) {
+    int unit = 0;
+    if (lane == 0) unit = atomicAdd(&sm.work, 1);
+    unit = __shfl_sync(0xffffffffu, unit, 0);
+    if (unit >= n_rows) break;
+    const int cy = unit % p.nc[1], cz = unit / p.nc[1];
+    const int rowc = unit * p.nc[0];
+    const int ab = sm.cell_start[rowc], ae = sm.cell_start[rowc + p.nc[0]];
+    if (ae == ab) continue;
+    const int z0 = max(cz - 1, 0), z1 = min(cz + 1, p.nc[2] - 1);
+    const int y0 = max(cy - 1, 0), y1 = min(cy + 1, p.nc[1] - 1);
+    const float rl2 = p.rl2;
+    for (int a0 = ab; a0 < ae; a0 += 32) {
+      // x-range of the chunk's cells (cells of a row are consecutive)
+      const int last = min(a0 + 32, ae) - 1;
+      int cfirst = 0, clast = 0;
+      for (int c = 0; c < p.nc[0]; ++c) {
+        if (sm.cell_start[rowc + c] <= a0) cfirst = c;
+        if (sm.cell_start[rowc + c] <= last) clast = c;
+      }
+      const int x0 = max(cfirst - 1, 0), x1 = min(clast + 1, p.nc[0] - 1);
+      const bool mine = a0 + lane < ae;
+      const int i = mine ? a0 + lane : ab;
+      const float4 q = sm.pos[i];
+      int cnt = 0;
+      uint32_t buf0 = 0, buf1 = 0;
+      auto push = [&](uint32_t j) {
+        const uint32_t sh = (cnt & 1) << 4;
+        if (cnt & 2) buf1 |= j << sh; else buf0 |= j << sh;
+        if ((cnt & 3) == 3) {
+          const int u = cnt >> 2;
+          if (cnt < nb_cap) nl[(((size_t)(u >> ltpa) * n + i) << ltpa) + (u & (tpa - 1))] = make_uint2(buf0, buf1);
+          buf0 = buf1 = 0;
+        }
+        ++cnt;
+      };
+      auto scan_range = [&](int kb, int ke) {
+        for (int k0 = kb; k0 < ke; k0 += 32) {
+          const int kn = min(32, ke - k0);
+          uint32_t hits = 0;
+#pragma unroll 4
+          for (int t = 0; t < kn; ++t) {
+            const float4 o = sm.pos[k0 + t];
+            const float dx = o.x - q.x, dy = o.y - q.y, dz = o.z - q.z;
+            const bool h = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < rl2;
+            hits |= (uint32_t)h << t;
+          }
+          if (k0 <= i && i < k0 + kn) hits &= ~(1u << (i - k0));  // not the atom itself
+          if (!mine) hits = 0;
+          while (hits) {
+            const int t = __ffs(hits) - 1;
+            hits &= hits - 1;
+            push((uint32_t)(k0 + t));
+          }
+        }
+      };
+      for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y) {
+          const int row = (z * p.nc[1] + y) * p.nc[0];
+          scan_range(sm.cell_start[row + x0], sm.cell_start[row + x1 + 1]);
+          scan_range(n + sm.ghost_start[row + x0], n + sm.ghost_start[row + x1 + 1]);
+        }
+      if (mine) {
+        const int total_cnt = cnt;
+        while (cnt & 3) push(sent);  // pad the last unit with the sentinel item
+        sm.nbr_count[i] = (uint16_t)min(total_cnt, nb_cap);
+        my_max = max(my_max, total_cnt);
+      }
+    }
+  }
+  if (my_max > nb_cap) atomicMax(&sm.flag, my_max);
+  __syncthreads();
+  prof_add(prof, 9, tp);
   const int need = sm.flag;
   if (need > nb_cap) {
     if (tid == 0) status_capacity(status, KUPS_CAP_NEIGHBORS, need, sys_index);
@@ -277,7 +391,7 @@ __device__ bool rebuild(Smem &sm, const SysParams &p, int n, int tpa, uint16_t *
   return true;
 }
 
-__device__ inline void update_ghosts(Smem &sm, int n) {
+__device__ __forceinline__ void update_ghosts(Smem &sm, int n) {
   const int ng = sm.n_ghosts;
   for (int g = threadIdx.x; g < ng; g += blockDim.x) {
     const uint32_t m = sm.ghost_meta[g];
@@ -287,89 +401,147 @@ __device__ inline void update_ghosts(Smem &sm, int n) {
   }
 }
 
-// Forces into sm.frc[i].xyz; returns this thread's share of the potential
-// energy (float64) and adds the Cartesian pair virial W_cb = 1/2 sum d_c g_b
-// (symmetric, [xx, yx, yy, zx, zy, zz]) into wv when VIRIAL.
-template <bool VIRIAL>
-__device__ double compute_forces(Smem &sm, const SysParams &p, int n, int nsp, int tpa,
-                                 const uint16_t *nl, float wv[6]) {
-  const int lane_g = threadIdx.x & (tpa - 1);
-  const int grp = threadIdx.x / tpa;
-  const int ngrp = blockDim.x / tpa;
-  double e_acc = 0.0;
-  for (int base = 0; base < n; base += ngrp) {
-    const int i = base + grp;
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Accumulators of one lane for one atom.
+struct PairAcc {
+  float fx, fy, fz, e;
+  float w[6];
+};
+
+template <bool ENERGY, bool VIRIAL, bool SINGLE>
+__device__ __forceinline__ void lj_pair(const Smem &sm, const float4 &xi, int ti, int nsp, uint32_t j,
+                                        float rc2, float sig2, float a4, PairAcc &acc) {
+  const float4 xj = sm.pos[j];
+  const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  float s2c = sig2, ac = a4;
+  if (!SINGLE) {
+    const float2 c = sm.lj[ti * nsp + __float_as_int(xj.w)];
+    s2c = c.x;
+    ac = c.y;
+  }
+  const float inv = rcp_approx(r2);
+  const float s2 = s2c * inv;
+  const float c6 = s2 * s2 * s2;
+  // g = dE/dd = -6 (4 eps) c6 (2 c6 - 1) / r2 * d ; F_i = sum_j g
+  float fs = c6 * fmaf(12.0f * ac, c6, -6.0f * ac) * inv;
+  const bool in = r2 < rc2;
+  fs = in ? fs : 0.0f;
+  acc.fx = fmaf(-fs, dx, acc.fx);
+  acc.fy = fmaf(-fs, dy, acc.fy);
+  acc.fz = fmaf(-fs, dz, acc.fz);
+  if (ENERGY) acc.e += in ? ac * fmaf(c6, c6, -c6) : 0.0f;
+  if (VIRIAL) {
+    const float h = -0.5f * fs;  // (1/2) d_c g_b = -(1/2) fs d_c d_b
+    acc.w[0] = fmaf(h * dx, dx, acc.w[0]);
+    acc.w[1] = fmaf(h * dy, dx, acc.w[1]);
+    acc.w[2] = fmaf(h * dy, dy, acc.w[2]);
+    acc.w[3] = fmaf(h * dz, dx, acc.w[3]);
+    acc.w[4] = fmaf(h * dz, dy, acc.w[4]);
+    acc.w[5] = fmaf(h * dz, dz, acc.w[5]);
+  }
+}
+
+// Forces into sm.frc[i].xyz.  With ENERGY, adds this thread's share of the
+// potential energy (sum over its pairs / 2) to *pe; with VIRIAL, adds the
+// Cartesian pair virial W_cb = 1/2 sum d_c g_b ([xx, yx, yy, zx, zy, zz]) to wv.
+// Warps take 32 / tpa atoms at a time from a shared counter (sm.work, zeroed
+// by the caller before the preceding barrier), so uneven neighbour counts do
+// not leave warps idle at the barrier; each lane loads a 4-entry list unit
+// (8 bytes) per iteration, fetched one iteration ahead.
+template <bool ENERGY, bool VIRIAL, bool SINGLE>
+__device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa, const uint2 *nl,
+                                               float rc2, float sig2, float a4, double *pe,
+                                               float wv[6]) {
+  const int lane = threadIdx.x & 31;
+  const int lane_g = lane & (tpa - 1);
+  const int per_warp = 32 / tpa;
+  const size_t stride = (size_t)n * tpa;
+  while (true) {
+    int wb = 0;
+    if (lane == 0) wb = atomicAdd(&sm.work, per_warp);
+    wb = __shfl_sync(0xffffffffu, wb, 0);
+    if (wb >= n) break;
+    const int i = wb + lane / tpa;
     const bool active = i < n;
-    float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-    float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
+    PairAcc acc;
+    acc.fx = acc.fy = acc.fz = acc.e = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc.w[k] = 0.f;
     if (active) {
       const float4 xi = sm.pos[i];
       const int ti = __float_as_int(xi.w);
-      const int cnt = sm.nbr_count[i];
-      const uint16_t *row = nl + (size_t)i * tpa + lane_g;
-      const size_t stride = (size_t)n * tpa;
-      int r = 0;
-      for (int k = lane_g; k < cnt; k += tpa, ++r) {
-        const int j = row[(size_t)r * stride];
-        const float4 xj = sm.pos[j];
-        const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < p.rc2) {
-          const float2 c = sm.lj[ti * nsp + __float_as_int(xj.w)];
-          const float inv = __fdividef(1.0f, r2);
-          const float s2 = c.x * inv;
-          const float c6 = s2 * s2 * s2;
-          // g = dE/dd = -6 (4 eps) c6 (2 c6 - 1) / r2 * d ; F_i = sum_j g
-          const float fs = 6.0f * c.y * c6 * (2.0f * c6 - 1.0f) * inv;
-          fx -= fs * dx;
-          fy -= fs * dy;
-          fz -= fs * dz;
-          e += c.y * (c6 * c6 - c6);
-          if (VIRIAL) {
-            const float h = -0.5f * fs;  // (1/2) d_c g_b = -(1/2) fs d_c d_b
-            w0 += h * dx * dx;
-            w1 += h * dy * dx;
-            w2 += h * dy * dy;
-            w3 += h * dz * dx;
-            w4 += h * dz * dy;
-            w5 += h * dz * dz;
-          }
-        }
+      const int nu = (sm.nbr_count[i] + 3) >> 2;  // 4-entry units
+      const uint2 *row = nl + (size_t)i * tpa + lane_g;
+      int u = lane_g;
+      uint2 v0 = make_uint2(0u, 0u), v1 = make_uint2(0u, 0u);
+      if (u < nu) v0 = row[0];
+      if (u + tpa < nu) v1 = row[stride];
+      while (u < nu) {
+        const uint2 cur = v0;
+        v0 = v1;
+        row += stride;
+        u += tpa;
+        if (u + tpa < nu) v1 = row[stride];
+        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.x & 0xffffu, rc2, sig2, a4, acc);
+        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.x >> 16, rc2, sig2, a4, acc);
+        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.y & 0xffffu, rc2, sig2, a4, acc);
+        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.y >> 16, rc2, sig2, a4, acc);
       }
     }
     for (int o = tpa >> 1; o > 0; o >>= 1) {
-      fx += __shfl_xor_sync(0xffffffffu, fx, o);
-      fy += __shfl_xor_sync(0xffffffffu, fy, o);
-      fz += __shfl_xor_sync(0xffffffffu, fz, o);
+      acc.fx += __shfl_xor_sync(0xffffffffu, acc.fx, o);
+      acc.fy += __shfl_xor_sync(0xffffffffu, acc.fy, o);
+      acc.fz += __shfl_xor_sync(0xffffffffu, acc.fz, o);
     }
     if (active && lane_g == 0) {
       float4 f = sm.frc[i];
-      f.x = fx;
-      f.y = fy;
-      f.z = fz;
+      f.x = acc.fx;
+      f.y = acc.fy;
+      f.z = acc.fz;
       sm.frc[i] = f;
     }
-    e_acc += 0.5 * (double)e;
+    if (ENERGY) *pe += 0.5 * (double)acc.e;
     if (VIRIAL) {
-      wv[0] += w0; wv[1] += w1; wv[2] += w2; wv[3] += w3; wv[4] += w4; wv[5] += w5;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) wv[k] += acc.w[k];
     }
   }
-  return e_acc;
+}
+
+template <bool ENERGY, bool VIRIAL>
+__device__ __forceinline__ void forces_dispatch(Smem &sm, int n, int nsp, int tpa, const uint2 *nl,
+                                                float rc2, float sig2, float a4, double *pe,
+                                                float wv[6]) {
+  if (nsp == 1)
+    compute_forces<ENERGY, VIRIAL, true>(sm, n, nsp, tpa, nl, rc2, sig2, a4, pe, wv);
+  else
+    compute_forces<ENERGY, VIRIAL, false>(sm, n, nsp, tpa, nl, rc2, sig2, a4, pe, wv);
 }
 
 template <int INTEGRATOR>
 __global__ void __launch_bounds__(kThreads, 1)
-md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
+md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
   const int tid = threadIdx.x, nt = blockDim.x;
   float4 *gpos = reinterpret_cast<float4 *>(a.pos);
   float4 *gmom = reinterpret_cast<float4 *>(a.mom);
   float4 *gfrc = reinterpret_cast<float4 *>(a.force);
-  uint16_t *nl = nl_ws + (size_t)blockIdx.x * kMaxAtoms * a.neighbor_capacity;
+  uint2 *nl = reinterpret_cast<uint2 *>(nl_ws) + (size_t)blockIdx.x * kMaxAtoms * (a.neighbor_capacity / 4);
+  float4 *scratch = reinterpret_cast<float4 *>(reinterpret_cast<char *>(nl_ws) +
+                                               (size_t)gridDim.x * kMaxAtoms * (a.neighbor_capacity / 4) * sizeof(uint2)) +
+                    (size_t)blockIdx.x * kScratchPerCta;
+  unsigned long long *prof = reinterpret_cast<unsigned long long *>(a.profile);
   const int nsp = a.n_species;
   for (int k = tid; k < nsp * nsp; k += nt)
     sm.lj[k] = make_float2(a.lj_table[2 * k], a.lj_table[2 * k + 1]);
+  const float sig2_0 = a.lj_table[0], a4_0 = a.lj_table[1];
 
   while (true) {
     if (tid == 0) sm.next_sys = atomicAdd(queue, 1);
@@ -385,9 +557,10 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
       if (tid == 0) status_capacity(status, KUPS_CAP_ATOMS, n, s);
       continue;
     }
-    // ---- per-system parameters (uniform across the block)
-    SysParams p;
-    {
+    long long t0 = clock64();
+    // ---- per-system parameters, computed once into shared memory
+    SysParams &p = sm.p;
+    if (tid == 0) {
       for (int k = 0; k < 6; ++k) p.L[k] = a.tril[6 * (int64_t)s + k];
       const float A = p.L[0], B = p.L[1], C = p.L[2], D = p.L[3], E = p.L[4], F = p.L[5];
       p.inv[0] = 1.0f / A;
@@ -419,10 +592,15 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
         p.nc[am] = (p.nc[am] + 1) / 2;
         ncell = p.nc[0] * p.nc[1] * p.nc[2];
       }
+      for (int d = 0; d < 3; ++d) {
+        p.coff[d] = 0.5f + p.m[d];
+        p.cscale[d] = (float)p.nc[d] / p.ext[d];
+      }
       p.dt = a.dt[s];
       p.c1 = expf(-a.friction[s] * p.dt);
       p.c2 = sqrtf(a.kT[s] * (1.0f - p.c1 * p.c1));
     }
+    __syncthreads();
     if (p.K[0] > 2 || p.K[1] > 2 || p.K[2] > 2) {
       if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
       continue;
@@ -436,98 +614,116 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
     }
     int bad_species = 0;
     for (int i = tid; i < n; i += nt) {
-      const float4 q = gpos[a0 + i];
-      const int t = __float_as_int(q.w);
+      const float4 qv = gpos[a0 + i];
+      const int t = __float_as_int(qv.w);
       bad_species |= (t < 0) | (t >= nsp);
-      sm.pos[i] = q;
+      sm.pos[i] = qv;
       sm.mom[i] = gmom[a0 + i];
       sm.frc[i] = gfrc[a0 + i];
+      sm.gid[i] = (uint16_t)i;
     }
     if (__syncthreads_or(bad_species)) {
       if (tid == 0) status_error(status, KUPS_ERR_INVALID, s);
       continue;
     }
     const int tpa = choose_tpa(n, nt);
-    bool ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s);
+    bool ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s, prof, scratch);
+    if (tid == 0) sm.work = 0;
+    __syncthreads();
     if (!ok) continue;
+    if (tid == 0 && a.rebuilds != nullptr) a.rebuilds[s] += 1;
+    prof_add(prof, 0, t0);
+    // hot scalars in registers
+    const float rc2 = p.rc2, dt = p.dt, hdt = 0.5f * p.dt, c1 = p.c1, c2 = p.c2;
+    const float half_skin = p.half_skin;
     float wv[6] = {0, 0, 0, 0, 0, 0};
     double pe = 0.0;
     if (!a.forces_valid) {
       if (a.n_steps == 0 && a.virial != nullptr)
-        pe = compute_forces<true>(sm, p, n, nsp, tpa, nl, wv);
+        forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
       else
-        pe = compute_forces<false>(sm, p, n, nsp, tpa, nl, wv);
+        forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
       __syncthreads();
     }
-    const float hdt = 0.5f * p.dt;
     for (int step = 0; step < a.n_steps && ok; ++step) {
       const bool last = step == a.n_steps - 1;
+      const bool want_e = last || a.trace_pe != nullptr || a.trace_ke != nullptr;
       // ---- B A (O A)
+      if (tid == 0) sm.work = 0;
       int moved_far = 0;
       for (int i = tid; i < n; i += nt) {
         float4 x = sm.pos[i], m = sm.mom[i], f = sm.frc[i];
         const float inv_m = 1.0f / m.w;
-        m.x += f.x * hdt;
-        m.y += f.y * hdt;
-        m.z += f.z * hdt;
+        m.x = fmaf(f.x, hdt, m.x);
+        m.y = fmaf(f.y, hdt, m.y);
+        m.z = fmaf(f.z, hdt, m.z);
         float dx, dy, dz;
         if (INTEGRATOR == 0) {
-          dx = m.x * inv_m * p.dt;
-          dy = m.y * inv_m * p.dt;
-          dz = m.z * inv_m * p.dt;
+          const float sc = inv_m * dt;
+          dx = m.x * sc;
+          dy = m.y * sc;
+          dz = m.z * sc;
         } else {
-          dx = m.x * inv_m * hdt;
-          dy = m.y * inv_m * hdt;
-          dz = m.z * inv_m * hdt;
+          const float sc = inv_m * hdt;
+          dx = m.x * sc;
+          dy = m.y * sc;
+          dz = m.z * sc;
           float eta[4];
-          normal4(a.seed, (uint64_t)(a0 + i), a.step0 + (uint64_t)step, eta);
-          const float amp = p.c2 * sqrtf(m.w);
-          m.x = p.c1 * m.x + amp * eta[0];
-          m.y = p.c1 * m.y + amp * eta[1];
-          m.z = p.c1 * m.z + amp * eta[2];
-          dx += m.x * inv_m * hdt;
-          dy += m.y * inv_m * hdt;
-          dz += m.z * inv_m * hdt;
+          normal4(a.seed, (uint64_t)(a0 + sm.gid[i]), a.step0 + (uint64_t)step, eta);
+          const float amp = c2 * sqrtf(m.w);
+          m.x = fmaf(c1, m.x, amp * eta[0]);
+          m.y = fmaf(c1, m.y, amp * eta[1]);
+          m.z = fmaf(c1, m.z, amp * eta[2]);
+          dx = fmaf(m.x, sc, dx);
+          dy = fmaf(m.y, sc, dy);
+          dz = fmaf(m.z, sc, dz);
         }
         x.x += dx;
         x.y += dy;
         x.z += dz;
-        f.w += sqrtf(dx * dx + dy * dy + dz * dz);
-        moved_far |= f.w > p.half_skin;
+        f.w += sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+        moved_far |= f.w > half_skin;
         sm.pos[i] = x;
         sm.mom[i] = m;
         sm.frc[i] = f;
       }
       const int need = __syncthreads_or(moved_far);
+      prof_add(prof, 1, t0);
       if (need) {
         if (tid == 0 && a.rebuilds != nullptr) a.rebuilds[s] += 1;
-        ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s);
+        ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s, prof, scratch);
         if (!ok) break;
+        if (tid == 0) sm.work = 0;
+        __syncthreads();
       } else {
         update_ghosts(sm, n);
         __syncthreads();
       }
+      prof_add(prof, 2, t0);
       // ---- forces
-      const bool want_e = last || a.trace_pe != nullptr;
+      pe = 0.0;
       if (last && a.virial != nullptr)
-        pe = compute_forces<true>(sm, p, n, nsp, tpa, nl, wv);
+        forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+      else if (want_e)
+        forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
       else
-        pe = compute_forces<false>(sm, p, n, nsp, tpa, nl, wv);
+        forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
       __syncthreads();
-      // ---- B, kinetic energy
-      double ke = 0.0;
+      prof_add(prof, 3, t0);
+      // ---- B (and kinetic energy when recorded)
+      float ke = 0.f;
       for (int i = tid; i < n; i += nt) {
         float4 m = sm.mom[i];
         const float4 f = sm.frc[i];
-        m.x += f.x * hdt;
-        m.y += f.y * hdt;
-        m.z += f.z * hdt;
+        m.x = fmaf(f.x, hdt, m.x);
+        m.y = fmaf(f.y, hdt, m.y);
+        m.z = fmaf(f.z, hdt, m.z);
         sm.mom[i] = m;
-        ke += 0.5 * ((double)m.x * m.x + (double)m.y * m.y + (double)m.z * m.z) / (double)m.w;
+        if (want_e) ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
       }
-      if (want_e || a.trace_ke != nullptr) {
+      if (want_e) {
         const double pe_tot = block_sum(pe, sm.red);
-        const double ke_tot = block_sum(ke, sm.red + 36);
+        const double ke_tot = block_sum((double)ke, sm.red + 36);
         if (tid == 0) {
           if (a.trace_pe) a.trace_pe[(int64_t)step * a.n_systems + s] = pe_tot;
           if (a.trace_ke) a.trace_ke[(int64_t)step * a.n_systems + s] = ke_tot;
@@ -536,19 +732,18 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
             a.kinetic[s] = ke_tot;
           }
         }
-      } else {
-        __syncthreads();
       }
+      prof_add(prof, 4, t0);
     }
     if (!ok) continue;
     if (a.n_steps == 0) {
-      double ke = 0.0;
+      float ke = 0.f;
       for (int i = tid; i < n; i += nt) {
         const float4 m = sm.mom[i];
-        ke += 0.5 * ((double)m.x * m.x + (double)m.y * m.y + (double)m.z * m.z) / (double)m.w;
+        ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
       }
       const double pe_tot = block_sum(pe, sm.red);
-      const double ke_tot = block_sum(ke, sm.red + 36);
+      const double ke_tot = block_sum((double)ke, sm.red + 36);
       if (tid == 0) {
         a.energy[s] = pe_tot;
         a.kinetic[s] = ke_tot;
@@ -556,15 +751,17 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
     }
     // ---- write back (wrapped positions), virial dE/dtril
     float fw[6] = {0, 0, 0, 0, 0, 0};  // sum_i f_i,a F_i,b for (a, b) in tril order
+    __syncthreads();
     for (int i = tid; i < n; i += nt) {
       float4 x = sm.pos[i];
       float f[3];
       wrap_position(p, x, f);
-      gpos[a0 + i] = x;
-      gmom[a0 + i] = sm.mom[i];
+      const int o = a0 + sm.gid[i];
+      gpos[o] = x;
+      gmom[o] = sm.mom[i];
       float4 F = sm.frc[i];
       F.w = 0.f;
-      gfrc[a0 + i] = F;
+      gfrc[o] = F;
       fw[0] += f[0] * F.x;
       fw[1] += f[1] * F.x;
       fw[2] += f[1] * F.y;
@@ -576,7 +773,10 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
       // X_ab = sum_c (L^-1)_{ca} W_cb ; W symmetric from wv = [xx, yx, yy, zx, zy, zz]
       double W[3][3];
       double acc[6];
-      for (int k = 0; k < 6; ++k) acc[k] = block_sum((double)wv[k], sm.red + 0), __syncthreads();
+      for (int k = 0; k < 6; ++k) {
+        acc[k] = block_sum((double)wv[k], sm.red);
+        __syncthreads();
+      }
       W[0][0] = acc[0];
       W[1][0] = W[0][1] = acc[1];
       W[1][1] = acc[2];
@@ -584,8 +784,10 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
       W[2][1] = W[1][2] = acc[4];
       W[2][2] = acc[5];
       double fwt[6];
-      for (int k = 0; k < 6; ++k) fwt[k] = block_sum((double)fw[k], sm.red + 36), __syncthreads();
-      // inverse (float64 from the float32 cell)
+      for (int k = 0; k < 6; ++k) {
+        fwt[k] = block_sum((double)fw[k], sm.red + 36);
+        __syncthreads();
+      }
       const double A = p.L[0], B = p.L[1], C = p.L[2], D = p.L[3], E = p.L[4], F = p.L[5];
       double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
       Li[1][0] = -(B * Li[0][0]) / C;
@@ -600,6 +802,7 @@ md_lj_kernel(kups_md_args a, uint16_t *nl_ws, int *queue, kups_status *status) {
         }
       }
     }
+    prof_add(prof, 5, t0);
     __syncthreads();
   }
 }
@@ -616,7 +819,8 @@ extern "C" size_t kups_lj_md_workspace_bytes(const kups_md_args *a) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int ctas = a->n_ctas > 0 ? a->n_ctas : (sms > 0 ? sms : 1);
-  return 256 + (size_t)ctas * kMaxAtoms * (size_t)a->neighbor_capacity * sizeof(uint16_t) + 256;
+  return 256 + (size_t)ctas * (kMaxAtoms * (size_t)(a->neighbor_capacity / 4) * sizeof(uint2) +
+                              kScratchPerCta * sizeof(float4)) + 256;
 }
 
 extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t ws_bytes,
@@ -636,7 +840,7 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
   const int threads = a->block_threads > 0 ? a->block_threads : kThreads;
   if (threads % 32 != 0 || threads > kThreads || threads < 64) return KUPS_ERR_INVALID;
   int *queue = reinterpret_cast<int *>(((uintptr_t)workspace + 255) & ~uintptr_t(255));
-  uint16_t *nl = reinterpret_cast<uint16_t *>(reinterpret_cast<char *>(queue) + 256);
+  uint32_t *nl = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(queue) + 256);
   KUPS_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(int), stream));
   const size_t smem = sizeof(Smem);
   if (a->integrator == 0) {

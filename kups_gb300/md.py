@@ -93,6 +93,7 @@ class PackedMD:
     kinetic: torch.Tensor | None = None
     virial: torch.Tensor | None = None
     rebuilds: torch.Tensor | None = None  # int32 [S], accumulated list builds (optional)
+    profile: torch.Tensor | None = None  # int64 [10], cycles per kernel phase (optional)
 
     @property
     def n_atoms(self) -> int:
@@ -222,6 +223,7 @@ class FusedLennardJonesMD:
         a.trace_pe = trace_pe.data_ptr() if trace_pe is not None else None
         a.trace_ke = trace_ke.data_ptr() if trace_ke is not None else None
         a.rebuilds = packed.rebuilds.data_ptr() if packed.rebuilds is not None else None
+        a.profile = packed.profile.data_ptr() if packed.profile is not None else None
         a.n_atoms, a.n_systems, a.n_species = packed.n_atoms, s, packed.n_species
         a.n_steps = int(n_steps)
         a.integrator = INTEGRATORS[self.integrator]
