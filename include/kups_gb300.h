@@ -200,6 +200,68 @@ int32_t kups_md_unpack(const void *pos4, const void *mom4, const void *force4,
                        const int32_t *perm, int64_t n, double *pos, double *mom, double *force,
                        void *stream);
 
+/* ------------------------------------------------------------------------
+ * Ewald summation.
+ *
+ * kups_ewald_recip replaces ewald_long_range_energy with _structure_factor_full
+ * (src/kups/potential/classical/ewald.py:394-439, 549-601), prefactor
+ * (:363-391) and EwaldLongRangeInput.kvecs (:265-274), plus the jax.vjp
+ * gradients with respect to positions and tril.  Atoms are grouped by system
+ * (system s owns [sys_offset[s], sys_offset[s+1])).
+ *   kvec_n     i32 [n_systems, n_kvecs, 3]  integer k coefficients (the
+ *              reference's reciprocal_lattice_shifts; zero rows are padding)
+ *   alpha      f64 [n_systems]; coulomb_k = HARTREE * BOHR (eV A / e^2)
+ *   energy     f64 [n_systems] out;  grad f64 [N, 3] out (written, not added)
+ *   grad_tril  f64 [n_systems, 6] out (may be NULL)
+ *   structure_factor f64 [n_systems, n_kvecs, 2] out: S(k) (the EwaldCache
+ *              structure_factor, float64 accumulation)
+ * |n_a| <= 16 per axis.
+ *
+ * kups_ewald_self replaces ewald_self_interaction_energy (:277-302).
+ *
+ * kups_pair_edges evaluates, over a directed edge list, any sum of
+ *   terms & 1: Lennard-Jones (lennard_jones.py:149-178),
+ *   terms & 2: real-space Ewald K q_i q_j erfc(alpha r) / r (ewald.py:305-325),
+ *   terms & 4: minus bare Coulomb K q_i q_j / r, the exclusion correction over
+ *              intramolecular edges (ewald.py:328-346, coulomb.py:64-83),
+ * each summed / 2 per system, with dE/dx (zeroed then accumulated) and
+ * dE/dtril (may be NULL).  Distances and pair arithmetic in float64.
+ * ------------------------------------------------------------------------ */
+size_t kups_ewald_recip_workspace_bytes(int32_t n_systems, int32_t n_kvecs);
+int32_t kups_ewald_recip(const double *positions, const double *charges,
+                         const int32_t *sys_offset, int32_t n_systems,
+                         int32_t max_atoms_per_system, const double *tril,
+                         const int32_t *kvec_n, int32_t n_kvecs, const double *alpha,
+                         double coulomb_k, double *energy, double *grad, double *grad_tril,
+                         double *structure_factor, void *workspace, size_t workspace_bytes,
+                         kups_status *status, void *stream);
+int32_t kups_ewald_self(const double *charges, const int32_t *sys_offset, int32_t n_systems,
+                        const double *alpha, double coulomb_k, double *energy, void *stream);
+int32_t kups_pair_edges(const double *positions, const int32_t *system, const int32_t *species,
+                        const double *charges, int64_t n_particles, const double *tril,
+                        int32_t n_systems, const double *lj_sigma, const double *lj_epsilon,
+                        int32_t n_species, const double *lj_cutoff, const double *alpha,
+                        const double *ewald_cutoff, double coulomb_k, int32_t terms,
+                        const int32_t *edges, const int32_t *shifts, int64_t n_edges,
+                        double *energy, double *grad, double *grad_tril, kups_status *status,
+                        void *stream);
+
+/* ------------------------------------------------------------------------
+ * Integrator building blocks on the float64 particle table (systems larger
+ * than kups_lj_md_max_atoms, Ewald MD): MomentumStep (p -= dE/dx * dt * scale),
+ * PositionStep + MinimumImageConventionFlow (r += p/m * dt * scale, wrapped
+ * into fractional [-0.5, 0.5)) and StochasticStep (Ornstein-Uhlenbeck)
+ * (src/kups/md/integrators.py:104-401).  dt, kT, friction are per system.
+ * ------------------------------------------------------------------------ */
+int32_t kups_md_kick(double *momenta, const double *grad, const int32_t *system,
+                     const double *dt, double scale, int64_t n_particles, void *stream);
+int32_t kups_md_drift(double *positions, const double *momenta, const double *masses,
+                      const int32_t *system, const double *dt, const double *tril, double scale,
+                      int64_t n_particles, void *stream);
+int32_t kups_md_thermostat(double *momenta, const double *masses, const int32_t *system,
+                           const double *dt, const double *kT, const double *friction,
+                           uint64_t seed, uint64_t step, int64_t n_particles, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,13 @@ SIGNATURES = {
     "kups_lj_md_max_atoms": (_I32, []),
     "kups_md_pack": (_I32, [_P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
     "kups_md_unpack": (_I32, [_P, _P, _P, _P, _I64, _P, _P, _P, _P]),
+    "kups_ewald_recip_workspace_bytes": (_SZ, [_I32, _I32]),
+    "kups_ewald_recip": (_I32, [_P, _P, _P, _I32, _I32, _P, _P, _I32, _P, C.c_double, _P, _P, _P, _P, _P, _SZ, _P, _P]),
+    "kups_ewald_self": (_I32, [_P, _P, _I32, _P, C.c_double, _P, _P]),
+    "kups_md_kick": (_I32, [_P, _P, _P, _P, C.c_double, _I64, _P]),
+    "kups_md_drift": (_I32, [_P, _P, _P, _P, _P, _P, C.c_double, _I64, _P]),
+    "kups_md_thermostat": (_I32, [_P, _P, _P, _P, _P, _P, C.c_uint64, C.c_uint64, _I64, _P]),
+    "kups_pair_edges": (_I32, [_P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

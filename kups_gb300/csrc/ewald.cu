@@ -1,0 +1,462 @@
+// Ewald summation: reciprocal-space structure factor, energy, forces and
+// cell gradient; self energy; real-space pair terms over an edge list.
+//
+// Replaces src/kups/potential/classical/ewald.py: EwaldLongRangeInput.kvecs
+// (:265-274, k = 2 pi L^-1 n), prefactor (:363-391), _frequency_response /
+// _structure_factor_full (:394-439), long_range (:349-360),
+// ewald_long_range_energy (:585-601), ewald_self_interaction_energy
+// (:277-302), ewald_short_range_energy (:305-325), exclusion_correction_energy
+// (:328-346) with coulomb_vacuum_energy (coulomb.py:64-83), and the jax.vjp
+// gradients PotentialFromEnergy takes of them (energy.py:264-355).
+//
+// Reciprocal space, per system s with n_k integer vectors n (zero rows are
+// padding, masked like k = 0):
+//   theta_ik = 2 pi n_k . f_i  (f = fractional coordinates),
+//   S(k) = sum_i q_i (cos, sin)(theta_ik)            [float64 accumulation]
+//   P(k) = (2 - [n_x = 0]) 2 pi / V exp(-k^2 / 4 alpha^2) / k^2
+//   E = K sum_k P(k) |S(k)|^2
+//   dE/dr_i = 2 K q_i sum_k P(k) k (S_s cos - S_c sin)(theta_ik)
+//   dE/dL_ab = sum_i f_ia F_ib - sum_k c_k (L^-T k)_a k_b - delta_ab E / L_aa,
+//   c_k = K |S|^2 P (-1 / (2 alpha^2) - 2 / k^2)    (F = -dE/dr)
+// e^{i theta} is built per atom from per-axis tables e^{2 pi i m f_a},
+// m in [-M, M] (the standard Ewald recurrence), so each (atom, k) costs two
+// complex products.
+#include "common.cuh"
+
+namespace kups {
+namespace {
+
+constexpr int kMaxM = 16;            // |n_a| <= 16
+constexpr int kTab = 2 * kMaxM + 1;  // table entries per axis
+constexpr int kAtomsPerChunk = 32;
+constexpr int kKPerBlock = 128;
+
+struct Coef {
+  double ps_c, ps_s, ck, pad;  // P S_c, P S_s, cell-gradient coefficient
+};
+
+struct RecipSys {
+  double inv[6];  // L^-1 (tril)
+  double L[6];
+  double volume;
+  int m[3];       // table half-widths actually used
+};
+
+__device__ inline void frac64(const double *inv, const double r[3], double f[3]) {
+  f[0] = (r[0] * inv[0] + r[1] * inv[1]) + r[2] * inv[3];
+  f[1] = r[1] * inv[2] + r[2] * inv[4];
+  f[2] = r[2] * inv[5];
+}
+
+// k = 2 pi L^-1 n  (column vector), written for the lower-triangular inverse.
+__device__ inline void kvec(const double *inv, const int n[3], double k[3]) {
+  const double tp = 6.283185307179586476925286766559;
+  k[0] = tp * (inv[0] * n[0]);
+  k[1] = tp * (inv[1] * n[0] + inv[2] * n[1]);
+  k[2] = tp * (inv[3] * n[0] + inv[4] * n[1] + inv[5] * n[2]);
+}
+
+__global__ void recip_setup_kernel(const double *tril, const int32_t *kn, int32_t s, int32_t nk,
+                                   RecipSys *sys, kups_status *status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s) return;
+  RecipSys r;
+  const Tril64 L = load_tril64(tril + 6 * (int64_t)i);
+  const Tril64 inv = inverse_tril64(L);
+  for (int k = 0; k < 6; ++k) {
+    r.L[k] = L.t[k];
+    r.inv[k] = inv.t[k];
+  }
+  r.volume = fabs(L.t[0] * L.t[2] * L.t[5]);
+  int m[3] = {0, 0, 0};
+  for (int k = 0; k < nk; ++k)
+    for (int a = 0; a < 3; ++a) m[a] = max(m[a], abs(kn[((int64_t)i * nk + k) * 3 + a]));
+  for (int a = 0; a < 3; ++a) {
+    if (m[a] > kMaxM) {
+      status_error(status, KUPS_ERR_UNSUPPORTED, i);
+      m[a] = kMaxM;
+    }
+    r.m[a] = m[a];
+  }
+  sys[i] = r;
+}
+
+// Per-atom tables e^{2 pi i m f_a}, m in [-M, M], from sincospi of the
+// fundamental and complex products (error grows ~linearly in |m| <= 16).
+__device__ inline void fill_tables(float2 *tab, const double f[3]) {
+  for (int a = 0; a < 3; ++a) {
+    float s1, c1;
+    // reduce f to [-0.5, 0.5) in float64 first so the float32 argument is small
+    const double fr = f[a] - rint(f[a]);
+    sincospif((float)(2.0 * fr), &s1, &c1);
+    float2 *t = tab + a * kTab + kMaxM;
+    t[0] = make_float2(1.f, 0.f);
+    float cr = 1.f, ci = 0.f;
+    for (int m = 1; m <= kMaxM; ++m) {
+      const float nr = cr * c1 - ci * s1;
+      const float ni = cr * s1 + ci * c1;
+      cr = nr;
+      ci = ni;
+      t[m] = make_float2(cr, ci);
+      t[-m] = make_float2(cr, -ci);
+    }
+  }
+}
+
+__device__ inline float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// S(k): grid (k tiles, atom chunks, systems).  Each block stages the tables of
+// 32 atoms in shared memory; each thread owns one k and accumulates the
+// chunk in float32, then adds it to S in float64.
+__global__ void structure_factor_kernel(const double *pos, const double *q, const int32_t *sys_offset,
+                                        const int32_t *kn, int32_t nk, const RecipSys *sysp,
+                                        double *sk) {
+  __shared__ float2 tab[kAtomsPerChunk][3 * kTab];
+  __shared__ float qs[kAtomsPerChunk];
+  const int s = blockIdx.z;
+  const int a0 = sys_offset[s], a1 = sys_offset[s + 1];
+  const int c0 = a0 + blockIdx.y * kAtomsPerChunk;
+  if (c0 >= a1) return;
+  const int na = min(kAtomsPerChunk, a1 - c0);
+  const RecipSys &P = sysp[s];
+  for (int t = threadIdx.x; t < na; t += blockDim.x) {
+    const double r[3] = {pos[3 * (c0 + t)], pos[3 * (c0 + t) + 1], pos[3 * (c0 + t) + 2]};
+    double f[3];
+    frac64(P.inv, r, f);
+    fill_tables(tab[t], f);
+    qs[t] = (float)q[c0 + t];
+  }
+  __syncthreads();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  const int *nv = kn + ((int64_t)s * nk + k) * 3;
+  const int nx = nv[0] + kMaxM, ny = nv[1] + kMaxM, nz = nv[2] + kMaxM;
+  float sc = 0.f, ss = 0.f;
+  for (int t = 0; t < na; ++t) {
+    const float2 e = cmul(cmul(tab[t][nx], tab[t][kTab + ny]), tab[t][2 * kTab + nz]);
+    sc = fmaf(qs[t], e.x, sc);
+    ss = fmaf(qs[t], e.y, ss);
+  }
+  atomicAdd(&sk[((int64_t)s * nk + k) * 2], (double)sc);
+  atomicAdd(&sk[((int64_t)s * nk + k) * 2 + 1], (double)ss);
+}
+
+// Per system: energy and the per-k coefficients; one block per system.
+//   coef[k] = (P S_c, P S_s, c_k)  with c_k for the cell gradient.
+__global__ void recip_energy_kernel(const int32_t *kn, int32_t nk, const double *alpha,
+                                    const RecipSys *sysp, const double *sk, double ke,
+                                    Coef *coef, double *energy, double *dtril) {
+  __shared__ double red[40];
+  const int s = blockIdx.x;
+  const RecipSys &P = sysp[s];
+  const double a = alpha[s];
+  const double tp = 6.283185307179586476925286766559;
+  double e = 0.0, w[6] = {0, 0, 0, 0, 0, 0};
+  // L^-T k: (L^-T)_{ab} = inv_{ba}
+  const double *iv = P.inv;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    const int *nv = kn + ((int64_t)s * nk + k) * 3;
+    const int n3[3] = {nv[0], nv[1], nv[2]};
+    double kv[3];
+    kvec(iv, n3, kv);
+    const double k2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+    double p = 0.0, ck = 0.0;
+    const double sc = sk[((int64_t)s * nk + k) * 2], ss = sk[((int64_t)s * nk + k) * 2 + 1];
+    const double s2 = sc * sc + ss * ss;
+    if (k2 > 0.0) {
+      p = (2.0 - (n3[0] == 0 ? 1.0 : 0.0)) * tp / P.volume * exp(-k2 / (4.0 * a * a)) / k2;
+      ck = ke * s2 * p * (-1.0 / (2.0 * a * a) - 2.0 / k2);
+    }
+    e += ke * p * s2;
+    coef[(int64_t)s * nk + k] = Coef{p * sc, p * ss, ck, 0.0};
+    // u = L^-T k
+    const double u0 = iv[0] * kv[0] + iv[1] * kv[1] + iv[3] * kv[2];
+    const double u1 = iv[2] * kv[1] + iv[4] * kv[2];
+    const double u2 = iv[5] * kv[2];
+    w[0] += ck * u0 * kv[0];
+    w[1] += ck * u1 * kv[0];
+    w[2] += ck * u1 * kv[1];
+    w[3] += ck * u2 * kv[0];
+    w[4] += ck * u2 * kv[1];
+    w[5] += ck * u2 * kv[2];
+  }
+  const double et = block_sum(e, red);
+  __syncthreads();
+  double wt[6];
+  for (int c = 0; c < 6; ++c) {
+    wt[c] = block_sum(w[c], red);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    energy[s] = et;
+    if (dtril) {
+      const int diag[6] = {1, 0, 1, 0, 0, 1};
+      const int dk[6] = {0, -1, 2, -1, -1, 5};
+      for (int c = 0; c < 6; ++c) {
+        double v = -wt[c];
+        if (diag[c]) v -= et / P.L[dk[c]];
+        dtril[6 * (int64_t)s + c] = v;  // the sum_i f F part is added by the force kernel
+      }
+    }
+  }
+}
+
+// dE/dr_i for every atom of every system (thread per atom; k coefficients
+// staged through shared memory), plus the sum_i f_ia F_ib part of dE/dL.
+__global__ void recip_force_kernel(const double *pos, const double *q, const int32_t *sys_offset,
+                                   const int32_t *kn, int32_t nk, const RecipSys *sysp,
+                                   const Coef *coef, double ke, double *grad, double *dtril) {
+  __shared__ float2 tab[kAtomsPerChunk][3 * kTab];
+  __shared__ float4 kc[kKPerBlock];  // (P S_c, P S_s, -, -) as float
+  __shared__ int4 kni[kKPerBlock];
+  __shared__ double red[40];
+  const int s = blockIdx.y;
+  const int a0 = sys_offset[s], a1 = sys_offset[s + 1];
+  const int c0 = a0 + blockIdx.x * kAtomsPerChunk;
+  if (c0 >= a1) return;
+  const int na = min(kAtomsPerChunk, a1 - c0);
+  const RecipSys &P = sysp[s];
+  const int t = threadIdx.x;  // blockDim.x == kAtomsPerChunk * 4: 4 lanes per atom split k
+  const int atom = t >> 2, sub = t & 3;
+  double f[3] = {0, 0, 0};
+  if (t < na) {
+    const double r[3] = {pos[3 * (c0 + t)], pos[3 * (c0 + t) + 1], pos[3 * (c0 + t) + 2]};
+    frac64(P.inv, r, f);
+    fill_tables(tab[t], f);
+  }
+  __syncthreads();
+  // gradient in fractional components: dE/df_a = sum_k 2 K q P 2 pi n_a (Ss c - Sc s)
+  float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+  for (int kb = 0; kb < nk; kb += kKPerBlock) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < kKPerBlock; j += blockDim.x) {
+      if (kb + j < nk) {
+        const Coef cc = coef[(int64_t)s * nk + kb + j];
+        kc[j] = make_float4((float)cc.ps_c, (float)cc.ps_s, 0.f, 0.f);
+        const int *nv = kn + ((int64_t)s * nk + kb + j) * 3;
+        kni[j] = make_int4(nv[0], nv[1], nv[2], 0);
+      } else {
+        kc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        kni[j] = make_int4(0, 0, 0, 0);
+      }
+    }
+    __syncthreads();
+    if (atom < na) {
+      const int kend = min(kKPerBlock, nk - kb);
+      for (int j = sub; j < kend; j += 4) {
+        const int4 n3 = kni[j];
+        const float2 e = cmul(cmul(tab[atom][n3.x + kMaxM], tab[atom][kTab + n3.y + kMaxM]),
+                              tab[atom][2 * kTab + n3.z + kMaxM]);
+        const float4 c = kc[j];
+        const float w = c.y * e.x - c.x * e.y;  // P (S_s cos - S_c sin)
+        g0 = fmaf(w, (float)n3.x, g0);
+        g1 = fmaf(w, (float)n3.y, g1);
+        g2 = fmaf(w, (float)n3.z, g2);
+      }
+    }
+  }
+  // reduce the 4 lanes of an atom
+  for (int o = 1; o < 4; o <<= 1) {
+    g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+    g1 += __shfl_xor_sync(0xffffffffu, g1, o);
+    g2 += __shfl_xor_sync(0xffffffffu, g2, o);
+  }
+  double fw[6] = {0, 0, 0, 0, 0, 0};
+  if (atom < na && sub == 0) {
+    const int i = c0 + atom;
+    const double tp = 6.283185307179586476925286766559;
+    const double scale = 2.0 * ke * q[i] * tp;
+    // dE/df -> dE/dr: r = f L  =>  f = r L^-1, dE/dr_b = sum_a dE/df_a (L^-1)_{ba}
+    const double df[3] = {scale * g0, scale * g1, scale * g2};
+    const double *iv = P.inv;
+    const double gr[3] = {df[0] * iv[0], df[0] * iv[1] + df[1] * iv[2],
+                          df[0] * iv[3] + df[1] * iv[4] + df[2] * iv[5]};
+    grad[3 * (int64_t)i] = gr[0];
+    grad[3 * (int64_t)i + 1] = gr[1];
+    grad[3 * (int64_t)i + 2] = gr[2];
+    // fractional coordinates of atom i (recomputed: the table owner is lane `atom`)
+    const double r[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    double fi[3];
+    frac64(P.inv, r, fi);
+    // sum_i f_ia F_ib, F = -dE/dr
+    fw[0] = -fi[0] * gr[0];
+    fw[1] = -fi[1] * gr[0];
+    fw[2] = -fi[1] * gr[1];
+    fw[3] = -fi[2] * gr[0];
+    fw[4] = -fi[2] * gr[1];
+    fw[5] = -fi[2] * gr[2];
+  }
+  if (dtril) {
+    for (int c = 0; c < 6; ++c) {
+      const double v = block_sum(fw[c], red);
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&dtril[6 * (int64_t)s + c], v);
+    }
+  }
+  (void)f;
+}
+
+__global__ void self_energy_kernel(const double *q, const int32_t *sys_offset, const double *alpha,
+                                   double ke, double *energy) {
+  __shared__ double red[40];
+  const int s = blockIdx.x;
+  double acc = 0.0;
+  for (int i = sys_offset[s] + threadIdx.x; i < sys_offset[s + 1]; i += blockDim.x) acc += q[i] * q[i];
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) energy[s] = -t * alpha[s] / sqrt(3.14159265358979323846) * ke;
+}
+
+// ---------------------------------------------------------------- real space
+// Per directed edge (i, j, shift), d = x_j - x_i + s @ L, r = |d|:
+//   LJ    4 eps (c6^2 - c6) [r^2 < rc_lj^2]
+//   EWALD K q_i q_j erfc(alpha r) / r [r < rc_ew]
+//   VACUUM (exclusion correction, subtracted) K q_i q_j / r, no cutoff
+// Each term is summed / 2 per system (directed edges), gradients as in
+// kups_lj_edges.  Float64 distance; pair arithmetic in float64.
+__global__ void pair_edges_kernel(const double *pos, const int32_t *system, const int32_t *species,
+                                  const double *q, int64_t n, const double *tril, int32_t s,
+                                  const double *lj_sigma, const double *lj_eps, int32_t nsp,
+                                  const double *rc_lj, const double *alpha, const double *rc_ew,
+                                  double ke, int32_t terms, const int32_t *edges,
+                                  const int32_t *shifts, int64_t n_edges, double *energy,
+                                  double *grad, double *dtril) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_edges) return;
+  const int i = edges[2 * e], j = edges[2 * e + 1];
+  if (i < 0 || i >= n || j < 0 || j >= n) return;
+  const int si = system[i];
+  if (si < 0 || si >= s) return;
+  const Tril64 L = load_tril64(tril + 6 * (int64_t)si);
+  const double sh[3] = {(double)shifts[3 * e], (double)shifts[3 * e + 1], (double)shifts[3 * e + 2]};
+  double sL[3];
+  row_times_tril64(sh, L, sL);
+  const double d[3] = {pos[3 * j] - pos[3 * i] + sL[0], pos[3 * j + 1] - pos[3 * i + 1] + sL[1],
+                       pos[3 * j + 2] - pos[3 * i + 2] + sL[2]};
+  const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  double en = 0.0, dedr2 = 0.0;  // dE/d(r^2)
+  if ((terms & 1) && lj_sigma) {
+    const int ti = species[i], tj = species[j];
+    const double sig = lj_sigma[ti * nsp + tj], eps = lj_eps[ti * nsp + tj];
+    const double rc = rc_lj[si];
+    if (r2 < rc * rc) {
+      const double inv = 1.0 / r2, s2 = sig * sig * inv, c6 = s2 * s2 * s2;
+      en += 4.0 * eps * (c6 * c6 - c6);
+      dedr2 += -12.0 * eps * c6 * (2.0 * c6 - 1.0) * inv;
+    }
+  }
+  if (terms & 6) {
+    const double r = sqrt(r2), qq = q[i] * q[j] * ke;
+    if (terms & 2) {
+      const double a = alpha[si];
+      if (r < rc_ew[si]) {
+        const double er = erfc(a * r);
+        en += qq * er / r;
+        const double dedr = qq * (-er / r2 - 2.0 * a * 0.56418958354775628695 * exp(-a * a * r2) / r);
+        dedr2 += dedr / (2.0 * r);
+      }
+    }
+    if (terms & 4) {
+      en -= qq / r;
+      dedr2 -= -qq / (r2 * r) / 2.0;
+    }
+  }
+  const double g[3] = {2.0 * dedr2 * d[0], 2.0 * dedr2 * d[1], 2.0 * dedr2 * d[2]};
+  atomicAdd(&energy[si], 0.5 * en);
+  for (int a = 0; a < 3; ++a) {
+    atomicAdd(&grad[3 * (int64_t)j + a], 0.5 * g[a]);
+    atomicAdd(&grad[3 * (int64_t)i + a], -0.5 * g[a]);
+  }
+  if (dtril) {
+    atomicAdd(&dtril[6 * (int64_t)si + 0], 0.5 * sh[0] * g[0]);
+    atomicAdd(&dtril[6 * (int64_t)si + 1], 0.5 * sh[1] * g[0]);
+    atomicAdd(&dtril[6 * (int64_t)si + 2], 0.5 * sh[1] * g[1]);
+    atomicAdd(&dtril[6 * (int64_t)si + 3], 0.5 * sh[2] * g[0]);
+    atomicAdd(&dtril[6 * (int64_t)si + 4], 0.5 * sh[2] * g[1]);
+    atomicAdd(&dtril[6 * (int64_t)si + 5], 0.5 * sh[2] * g[2]);
+  }
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+}  // namespace kups
+
+using namespace kups;
+
+extern "C" size_t kups_ewald_recip_workspace_bytes(int32_t n_systems, int32_t n_kvecs) {
+  return align256(sizeof(RecipSys) * (size_t)n_systems) +
+         align256(sizeof(Coef) * (size_t)n_systems * (size_t)n_kvecs) + 512;
+}
+
+extern "C" int32_t kups_ewald_recip(const double *positions, const double *charges,
+                                    const int32_t *sys_offset, int32_t n_systems,
+                                    int32_t max_atoms_per_system, const double *tril,
+                                    const int32_t *kvec_n, int32_t n_kvecs, const double *alpha,
+                                    double coulomb_k, double *energy, double *grad,
+                                    double *grad_tril, double *structure_factor,
+                                    void *workspace, size_t workspace_bytes, kups_status *status,
+                                    void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_systems < 0 || n_kvecs < 0 || max_atoms_per_system < 0) return KUPS_ERR_INVALID;
+  if (workspace_bytes < kups_ewald_recip_workspace_bytes(n_systems, n_kvecs)) return KUPS_ERR_INVALID;
+  if (n_systems == 0) return KUPS_OK;
+  char *base = (char *)(((uintptr_t)workspace + 255) & ~uintptr_t(255));
+  RecipSys *sysp = (RecipSys *)base;
+  Coef *coef = (Coef *)(base + align256(sizeof(RecipSys) * (size_t)n_systems));
+  recip_setup_kernel<<<(n_systems + 127) / 128, 128, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
+                                                                   sysp, status);
+  KUPS_CUDA_TRY(cudaMemsetAsync(structure_factor, 0, sizeof(double) * 2 * (size_t)n_systems * n_kvecs, stream));
+  const int chunks = (max_atoms_per_system + kAtomsPerChunk - 1) / kAtomsPerChunk;
+  if (n_kvecs > 0 && chunks > 0) {
+    dim3 g((n_kvecs + kKPerBlock - 1) / kKPerBlock, chunks, n_systems);
+    structure_factor_kernel<<<g, kKPerBlock, 0, stream>>>(positions, charges, sys_offset, kvec_n,
+                                                          n_kvecs, sysp, structure_factor);
+  }
+  recip_energy_kernel<<<n_systems, 256, 0, stream>>>(kvec_n, n_kvecs, alpha, sysp, structure_factor,
+                                                     coulomb_k, coef, energy, grad_tril);
+  if (chunks > 0) {
+    dim3 g(chunks, n_systems);
+    recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
+                                                             n_kvecs, sysp, coef, coulomb_k, grad,
+                                                             grad_tril);
+  }
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_ewald_self(const double *charges, const int32_t *sys_offset,
+                                   int32_t n_systems, const double *alpha, double coulomb_k,
+                                   double *energy, void *stream) {
+  if (n_systems < 0) return KUPS_ERR_INVALID;
+  if (n_systems == 0) return KUPS_OK;
+  self_energy_kernel<<<n_systems, 256, 0, (cudaStream_t)stream>>>(charges, sys_offset, alpha,
+                                                                 coulomb_k, energy);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_pair_edges(const double *positions, const int32_t *system,
+                                   const int32_t *species, const double *charges, int64_t n,
+                                   const double *tril, int32_t n_systems, const double *lj_sigma,
+                                   const double *lj_epsilon, int32_t n_species,
+                                   const double *lj_cutoff, const double *alpha,
+                                   const double *ewald_cutoff, double coulomb_k, int32_t terms,
+                                   const int32_t *edges, const int32_t *shifts, int64_t n_edges,
+                                   double *energy, double *grad, double *grad_tril,
+                                   kups_status *status, void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n < 0 || n_systems < 0 || n_edges < 0 || (terms & ~7) != 0) return KUPS_ERR_INVALID;
+  if ((terms & 1) && (lj_sigma == nullptr || n_species <= 0)) return KUPS_ERR_INVALID;
+  if (n_systems > 0) {
+    KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * n_systems, stream));
+    if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * n_systems, stream));
+  }
+  if (n > 0) KUPS_CUDA_TRY(cudaMemsetAsync(grad, 0, sizeof(double) * 3 * n, stream));
+  if (n_edges == 0) return KUPS_OK;
+  pair_edges_kernel<<<(unsigned)((n_edges + 255) / 256), 256, 0, stream>>>(
+      positions, system, species, charges, n, tril, n_systems, lj_sigma, lj_epsilon, n_species,
+      lj_cutoff, alpha, ewald_cutoff, coulomb_k, terms, edges, shifts, n_edges, energy, grad,
+      grad_tril);
+  (void)status;
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}

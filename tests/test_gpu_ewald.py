@@ -1,0 +1,150 @@
+"""GPU parity of the Ewald kernels against the float64 oracle.
+
+Bars: the NaCl Madelung constant at the reference's rtol 5e-5
+(test/potential/test_ewald.py:272-335); real-space pair terms in float64 within
+rtol 1e-10; reciprocal space (float32 phase tables, float64 structure-factor
+accumulation) within relative 1e-6 in energy and S(k), force RMS relative
+error 1e-5, cell gradient relative 1e-5.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import ewald as oew
+from oracle import lennard_jones as olj
+from oracle import neighborlist as onl
+from oracle import unitcell as ouc
+from oracle.units import TO_STANDARD_UNITS as KE
+
+pytestmark = pytest.mark.gpu
+
+
+def cuda(x, dtype=None):
+    return torch.as_tensor(np.asarray(x), dtype=dtype).cuda()
+
+
+def offsets(system, s):
+    c = np.bincount(system, minlength=s)
+    o = np.zeros(s + 1, np.int32)
+    o[1:] = np.cumsum(c)
+    return cuda(o, torch.int32), int(c.max())
+
+
+def ionic_batch(seed=0):
+    rng = np.random.default_rng(seed)
+    pos, q, sysi, trils = [], [], [], []
+    for s in range(2):
+        L = ouc.lattice_from_lengths_angles(rng.uniform(12, 16, 3), rng.uniform(80, 100, 3))
+        n = 40 + 10 * s
+        f = rng.uniform(-0.5, 0.5, (n, 3))
+        pos.append(f @ L)
+        qq = rng.normal(0, 1, n)
+        q.append(qq - qq.mean())
+        sysi += [s] * n
+        trils.append(ouc.tril_from_lattice(L))
+    return np.concatenate(pos), np.concatenate(q), np.array(sysi), np.stack(trils)
+
+
+def test_recip_matches_oracle():
+    from kups_gb300.ewald import ewald_recip
+
+    pos, q, sysi, tril = ionic_batch(1)
+    kn = np.stack([oew.kvecs_cube(5)] * 2)
+    alpha = np.array([0.3, 0.35])
+    e, g, dt, sk = oew.long_range(pos, q, sysi, tril, kn, alpha)
+    off, mx = offsets(sysi, 2)
+    ge, gg, gdt, gsk, _ = ewald_recip(cuda(pos), cuda(q), off, mx, cuda(tril), cuda(kn, torch.int32), cuda(alpha))
+    ge, gg, gdt, gsk = (x.cpu().numpy() for x in (ge, gg, gdt, gsk))
+    np.testing.assert_allclose(ge, e, rtol=1e-6)
+    np.testing.assert_allclose(gsk, sk, atol=2e-6 * np.abs(sk).max())
+    rms = np.sqrt(np.mean((gg - g) ** 2) / np.mean(g**2))
+    assert rms < 1e-5, rms
+    np.testing.assert_allclose(gdt, dt, rtol=1e-5, atol=1e-5 * np.abs(dt).max())
+
+
+def test_pair_edges_match_oracle():
+    from kups_gb300.ewald import TERM_EWALD_REAL, TERM_LJ, TERM_VACUUM, pair_edges
+
+    pos, q, sysi, tril = ionic_batch(2)
+    rng = np.random.default_rng(3)
+    sp = rng.integers(0, 2, len(q))
+    sig, eps = olj.lorentz_berthelot([1.0, 1.3], [0.01, 0.02])
+    rc = np.array([5.5, 6.0])
+    e, s = onl.neighbor_list(pos, sysi, tril, rc)
+    alpha = np.array([0.3, 0.35])
+    el, gl, tl = olj.lj_from_edges(pos, sysi, sp, tril, sig, eps, rc, e, s)
+    ee, ge, te = oew.short_range_from_edges(pos, q, sysi, tril, alpha, rc, e, s)
+    en, gg, gt = pair_edges(cuda(pos), cuda(sysi), cuda(sp), cuda(q), cuda(tril), cuda(e, torch.int32),
+                            cuda(s, torch.int32), len(e), TERM_LJ | TERM_EWALD_REAL, cuda(sig), cuda(eps), cuda(rc),
+                            cuda(alpha), cuda(rc))
+    np.testing.assert_allclose(en.cpu().numpy(), el + ee, rtol=1e-10)
+    np.testing.assert_allclose(gg.cpu().numpy(), gl + ge, rtol=1e-9, atol=1e-10)
+    np.testing.assert_allclose(gt.cpu().numpy(), tl + te, rtol=1e-9, atol=1e-10)
+    # exclusion correction over explicit edges (ewald.py:328-346)
+    xe = np.array([[0, 1], [1, 0], [2, 3], [3, 2]])
+    xs = np.zeros((4, 3), np.int64)
+    exp = oew.short_range_from_edges(pos, q, sysi, tril, alpha, [np.inf] * 2, xe, xs)[0] - \
+        oew.coulomb_vacuum_from_edges(pos, q, sysi, tril, xe, xs, 2)
+    got, _, _ = pair_edges(cuda(pos), cuda(sysi), None, cuda(q), cuda(tril), cuda(xe, torch.int32), cuda(xs, torch.int32),
+                           4, TERM_EWALD_REAL | TERM_VACUUM, alpha=cuda(alpha), ewald_cutoff=cuda([np.inf, np.inf]))
+    np.testing.assert_allclose(got.cpu().numpy(), exp, rtol=1e-10)
+
+
+def test_madelung_on_gpu():
+    from kups_gb300 import ewald
+
+    cell = np.array([[0, 0, 0], [1, 1, 0], [1, 0, 1], [0, 1, 1], [1, 1, 1], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    tril, pos, q = ouc.make_supercell(ouc.tril_from_lattice(np.eye(3) * 2.0), 5, cell, np.array([-1.0] * 4 + [1.0] * 4))
+    est = ewald.estimate_ewald_parameters(q, tril, epsilon_total=5e-5)
+    prm = ewald.EwaldParameters(torch.tensor([est["alpha"]]), torch.tensor([est["real_cutoff"]]),
+                                torch.as_tensor(ewald.kvecs_from_kmax(tril, est["k_max"]))[None])
+    pot = ewald.LJEwaldPotential(prm)
+    out = pot(ewald.EwaldParticles(cuda(pos), cuda(q), cuda(np.zeros(len(q), np.int32))), cuda(tril[None]))
+    total = out.total_energies.cpu().numpy()[0] / KE
+    assert np.isclose(-1.7475646 * 5**3 * 4, total, rtol=5e-5), total
+
+
+def test_lj_ewald_potential_matches_oracle_sum():
+    from kups_gb300 import ewald
+
+    pos, q, sysi, tril = ionic_batch(4)
+    sig, eps = olj.lorentz_berthelot([1.0, 1.2], [0.005, 0.01])
+    sp = (np.arange(len(q)) % 2).astype(np.int32)
+    kn = np.stack([oew.kvecs_cube(4)] * 2)
+    alpha, rc = np.array([0.32, 0.32]), np.array([5.5, 5.5])
+    prm = ewald.EwaldParameters(torch.tensor(alpha), torch.tensor(rc), torch.as_tensor(kn, dtype=torch.int32))
+    pot = ewald.LJEwaldPotential(prm, sig, eps, rc)
+    out = pot(ewald.EwaldParticles(cuda(pos), cuda(q), cuda(sysi, torch.int32), cuda(sp, torch.int32)), cuda(tril))
+    e, s = onl.neighbor_list(pos, sysi, tril, rc)
+    tot = olj.lj_from_edges(pos, sysi, sp, tril, sig, eps, rc, e, s)[0] + \
+        oew.short_range_from_edges(pos, q, sysi, tril, alpha, rc, e, s)[0] + \
+        oew.long_range(pos, q, sysi, tril, kn, alpha)[0] + oew.self_energy(q, sysi, alpha, 2)
+    np.testing.assert_allclose(out.total_energies.cpu().numpy(), tot, rtol=1e-6)
+
+
+def test_lj_ewald_md_conserves_energy_with_graph_replay():
+    from kups_gb300 import ewald
+    from kups_gb300.units import FEMTO_SECOND, KILO_CALORIE, MOL
+    from kups_gb300.workloads import lattice_positions
+
+    rng = np.random.default_rng(5)
+    n, box = 216, 20.0
+    pos = lattice_positions(rng, n, box, 2.2)
+    q = np.where(np.arange(n) % 2 == 0, 1.0, -1.0)
+    sp = (np.arange(n) % 2).astype(np.int32)
+    kcal = KILO_CALORIE / MOL
+    sig, eps = olj.lorentz_berthelot([2.35, 4.40], [0.1 * kcal, 0.15 * kcal])
+    masses = np.where(sp == 0, 22.99, 35.45)
+    mom = rng.normal(0, 1, (n, 3)) * np.sqrt(masses * 300 * 8.617e-5)[:, None]
+    tril = np.array([[box, 0, box, 0, 0, box]])
+    prm = ewald.EwaldParameters(torch.tensor([0.3]), torch.tensor([9.0]), torch.as_tensor(oew.kvecs_cube(6)[None], dtype=torch.int32))
+    parts = ewald.EwaldParticles(cuda(pos), cuda(q), cuda(np.zeros(n, np.int32)), cuda(sp))
+    md = ewald.LJEwaldMD(parts, cuda(masses), cuda(tril), prm, 0.5 * FEMTO_SECOND, sig, eps, [9.0])
+    md.start(cuda(mom))
+    e0 = float((md.energy + md.kinetic_energy()).item())
+    md.run(200)
+    torch.cuda.synchronize()
+    md.check()
+    e1 = float((md.energy + md.kinetic_energy()).item())
+    assert abs(e1 - e0) / abs(e0) < 2e-3, (e0, e1)
