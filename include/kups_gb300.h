@@ -262,6 +262,89 @@ int32_t kups_md_thermostat(double *momenta, const double *masses, const int32_t 
                            const double *dt, const double *kT, const double *friction,
                            uint64_t seed, uint64_t step, int64_t n_particles, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Batched grand-canonical Monte Carlo of one rigid molecule species in rigid
+ * frameworks (LJ + Ewald + LJ tail correction, muVT ensemble) — replaces
+ * MCMCPropagator.__call__ with the moves of make_gcmc_mcmc_propagator
+ * (src/kups/core/propagator.py:312-345, src/kups/mcmc/moves.py:1078-1230),
+ * the incremental potential (src/kups/potential/common/graph.py:419-453,
+ * src/kups/potential/classical/ewald.py:442-486), MuVTLogProbabilityRatio
+ * (src/kups/mcmc/probability.py:176-225) and acceptance_target_schedule
+ * (src/kups/core/parameter_scheduler.py:161-208).  One launch runs n_steps
+ * MC steps of every system (one CTA per system).
+ *
+ * Guests of system s occupy slots [0, n_mol[s]) of guest_pos
+ * [n_systems, max_mol, atoms_per_mol] (float4 x, y, z, species bits); a
+ * deletion moves the last molecule into the freed slot.  Framework atoms of
+ * system s are fw_pos[fw_start[s] .. + fw_count[s]] (systems may share them).
+ * Move kinds: 0 translate, 1 rotate, 2 reinsert, 3 insert, 4 delete;
+ * move_cum = cumulative probabilities of translate, rotate, reinsert
+ * (the rest is exchange, split evenly between insert and delete).
+ * Schedulers 0..3 = translate, rotate, reinsert, exchange: width[s*4+k],
+ * width_max[s*4+k] (<= 0: unbounded), history (bits) [s*4+k][4 words],
+ * history_index [s*4+k].
+ * With `proposals` non-NULL (one per system) the moves are taken from there
+ * instead of the generator (tests / replays); out_delta[s] = (dE, dE_real,
+ * dE_recip, log acceptance) of the last step.
+ * ------------------------------------------------------------------------ */
+typedef struct kups_gcmc_proposal {
+  int32_t kind;
+  int32_t mol;
+  int32_t force_reject;
+  int32_t pad;
+  float pos[8][4]; /* new positions (x, y, z, species bits) of the molecule */
+} kups_gcmc_proposal;
+
+typedef struct kups_gcmc_args {
+  const void *fw_pos;           /* float4 */
+  const float *fw_charge;
+  const int32_t *fw_start;
+  const int32_t *fw_count;
+  void *guest_pos;              /* float4 [S, max_mol, apm] in/out */
+  int32_t *n_mol;               /* [S] in/out */
+  const void *motif_pos;        /* float4 [apm]: template (x, y, z, species bits) */
+  const float *motif_charge;    /* [apm] */
+  const double *motif_species_count; /* [n_species] */
+  const double *fw_species_count;    /* [S, n_species] */
+  const double *tril;           /* [S, 6] */
+  const double *rc_lj;          /* [S] */
+  const double *rc_ew;          /* [S] */
+  const double *alpha;          /* [S] */
+  const int32_t *kvec_n;        /* [S, n_kvecs, 3] */
+  const double *prefactor;      /* [S, n_kvecs] P(k) */
+  double *structure_factor;     /* [S, n_kvecs, 2] in/out */
+  const float *lj_table;        /* [n_species^2 * 2]: sigma^2, 4 eps */
+  const double *tail_coef;      /* [S, n_species^2] or NULL */
+  const double *self_energy_mol;      /* [S] self energy of one molecule */
+  const double *exclusion_energy_mol; /* [S] intramolecular exclusion correction */
+  const double *kT;             /* [S] */
+  const double *log_activity;   /* [S] ln(f / kT) */
+  double *energy;               /* [S] in/out */
+  float *width;                 /* [S, 4] */
+  const float *width_max;       /* [S, 4] */
+  uint32_t *history;            /* [S, 4, 4] */
+  int32_t *history_index;       /* [S, 4] */
+  int64_t *attempted;           /* [S, 5] */
+  int64_t *accepted;            /* [S, 5] */
+  const kups_gcmc_proposal *proposals; /* [S] or NULL */
+  double *out_delta;            /* [S, 4] or NULL */
+  float move_cum[3];
+  float pad0;
+  double coulomb_k;
+  uint64_t seed;
+  uint64_t step0;
+  int32_t n_systems;
+  int32_t max_mol;
+  int32_t atoms_per_mol;
+  int32_t n_species;
+  int32_t n_kvecs;
+  int32_t n_steps;
+  int32_t history_len;
+  int32_t pad1;
+} kups_gcmc_args;
+
+int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

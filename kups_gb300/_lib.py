@@ -47,6 +47,29 @@ class MdArgs(C.Structure):
     ]
 
 
+class GcmcProposal(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("mol", C.c_int32), ("force_reject", C.c_int32), ("pad", C.c_int32),
+                ("pos", (C.c_float * 4) * 8)]
+
+
+class GcmcArgs(C.Structure):
+    _fields_ = [
+        ("fw_pos", C.c_void_p), ("fw_charge", C.c_void_p), ("fw_start", C.c_void_p), ("fw_count", C.c_void_p),
+        ("guest_pos", C.c_void_p), ("n_mol", C.c_void_p), ("motif_pos", C.c_void_p), ("motif_charge", C.c_void_p),
+        ("motif_species_count", C.c_void_p), ("fw_species_count", C.c_void_p), ("tril", C.c_void_p),
+        ("rc_lj", C.c_void_p), ("rc_ew", C.c_void_p), ("alpha", C.c_void_p), ("kvec_n", C.c_void_p),
+        ("prefactor", C.c_void_p), ("structure_factor", C.c_void_p), ("lj_table", C.c_void_p),
+        ("tail_coef", C.c_void_p), ("self_energy_mol", C.c_void_p), ("exclusion_energy_mol", C.c_void_p),
+        ("kT", C.c_void_p), ("log_activity", C.c_void_p), ("energy", C.c_void_p), ("width", C.c_void_p),
+        ("width_max", C.c_void_p), ("history", C.c_void_p), ("history_index", C.c_void_p),
+        ("attempted", C.c_void_p), ("accepted", C.c_void_p), ("proposals", C.c_void_p), ("out_delta", C.c_void_p),
+        ("move_cum", C.c_float * 3), ("pad0", C.c_float), ("coulomb_k", C.c_double), ("seed", C.c_uint64),
+        ("step0", C.c_uint64), ("n_systems", C.c_int32), ("max_mol", C.c_int32), ("atoms_per_mol", C.c_int32),
+        ("n_species", C.c_int32), ("n_kvecs", C.c_int32), ("n_steps", C.c_int32), ("history_len", C.c_int32),
+        ("pad1", C.c_int32),
+    ]
+
+
 # Every symbol declared in include/kups_gb300.h: name -> (restype, argtypes)
 _P, _I32, _I64, _SZ = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t
 SIGNATURES = {
@@ -66,6 +89,7 @@ SIGNATURES = {
     "kups_md_kick": (_I32, [_P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_drift": (_I32, [_P, _P, _P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_thermostat": (_I32, [_P, _P, _P, _P, _P, _P, C.c_uint64, C.c_uint64, _I64, _P]),
+    "kups_gcmc_run": (_I32, [C.POINTER(GcmcArgs), _P, _P]),
     "kups_pair_edges": (_I32, [_P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
 }
 

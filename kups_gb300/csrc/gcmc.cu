@@ -1,0 +1,583 @@
+// Batched grand-canonical Monte Carlo of rigid molecules in rigid frameworks.
+//
+// Replaces, per MC step and for every system at once, MCMCPropagator.__call__
+// (src/kups/core/propagator.py:312-345) with the moves of
+// make_gcmc_mcmc_propagator (src/kups/mcmc/moves.py:1078-1230: translation
+// :222-244, rotation about the centre of mass :247-265 with :158-197,
+// reinsertion :268-295, insertion :573-675, deletion :678-773), the
+// incremental energy of LocalGraphSumComposer (src/kups/potential/common/graph.py:419-453)
+// over the changed pairs of neighborlist_changes (src/kups/core/neighborlist.py:1425-1515),
+// the incremental structure factor (src/kups/potential/classical/ewald.py:442-486,
+// 604-657), the global LJ tail correction (lennard_jones.py:276-315), the
+// muVT acceptance (src/kups/mcmc/probability.py:98-225) and
+// acceptance_target_schedule (src/kups/core/parameter_scheduler.py:161-208).
+//
+// One CTA owns one system for all n_steps (systems are independent); the
+// move kind of a step is drawn from a counter that every CTA evaluates alike,
+// so all systems make the same kind of move in a step, as propose_mixed does
+// (propagator.py:244-273), and so is the insert/delete coin (moves.py:1217).
+// Randomness: Philox4x32-10 keyed by the seed, stream = system, counter = step.
+//
+// Pair enumeration follows the reference neighbour list exactly
+// (neighborlist.py:453-624): with n_a = odd ceil(2 rc / w_a) images per axis,
+// if prod(n_a) == 1 the shift is round(f_i - f_j); otherwise every offset of
+// the centred n_x x n_y x n_z grid is tried (no minimum image on axes with
+// n_a == 1), and intramolecular pairs are excluded on the minimum image only.
+// Pair arithmetic float32, energy differences and the log acceptance float64.
+#include "common.cuh"
+
+namespace kups {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxApm = 8;       // atoms per molecule
+constexpr int kMaxSpeciesMC = 8;
+constexpr int kMaxKVec = 4096;
+constexpr int kMaxImg = 5;       // odd image count per axis
+
+struct ImgCfg {
+  int n[3];
+  int image_mode;
+  float rc2;
+};
+
+struct StepShared {
+  float4 old_pos[kMaxApm];  // (x, y, z, species bits)
+  float4 new_pos[kMaxApm];
+  float q[kMaxApm];
+  int kind;      // 0 translate, 1 rotate, 2 reinsert, 3 insert, 4 delete
+  int mol;       // molecule slot
+  int has_old, has_new;
+  double de_real;
+  double de_recip;
+  int accept;
+  double log_p;
+  double de_total;
+};
+
+__device__ inline void frac32(const float inv[6], float x, float y, float z, float f[3]) {
+  f[0] = (x * inv[0] + y * inv[1]) + z * inv[3];
+  f[1] = y * inv[2] + z * inv[4];
+  f[2] = z * inv[5];
+}
+
+__device__ inline void cart32(const float L[6], const float f[3], float c[3]) {
+  c[0] = (f[0] * L[0] + f[1] * L[1]) + f[2] * L[3];
+  c[1] = f[1] * L[2] + f[2] * L[4];
+  c[2] = f[2] * L[5];
+}
+
+__device__ inline void wrap32(const float L[6], const float inv[6], float c[3]) {
+  float f[3];
+  frac32(inv, c[0], c[1], c[2], f);
+  for (int a = 0; a < 3; ++a) f[a] = (f[a] + 0.5f) - floorf(f[a] + 0.5f) - 0.5f;
+  cart32(L, f, c);
+}
+
+__device__ inline U4 rng4(uint64_t seed, uint64_t stream, uint64_t ctr) {
+  U4 c{(uint32_t)ctr, (uint32_t)(ctr >> 32), (uint32_t)stream, (uint32_t)(stream >> 32)};
+  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+__device__ inline float u01(uint32_t v) { return (float)(v >> 8) * (1.0f / 16777216.0f); }  // [0, 1)
+
+// Shoemake uniform rotation (quaternion.py:71-98): w, x, y, z
+__device__ inline void shoemake(float u1, float u2, float u3, float q[4]) {
+  float s2, c2, s3, c3;
+  sincospif(2.0f * u2, &s2, &c2);
+  sincospif(2.0f * u3, &s3, &c3);
+  const float a = sqrtf(1.0f - u1), b = sqrtf(u1);
+  q[0] = a * s2;
+  q[1] = a * c2;
+  q[2] = b * s3;
+  q[3] = b * c3;
+}
+
+// q ** e (quaternion.py:241-263): scale the rotation angle by e
+__device__ inline void qpow(const float qin[4], float e, float q[4]) {
+  float w = qin[0], x = qin[1], y = qin[2], z = qin[3];
+  if (w < 0.f) {
+    w = -w; x = -x; y = -y; z = -z;
+  }
+  const float angle = 2.0f * acosf(fminf(fmaxf(w, -1.0f), 1.0f));
+  const float sh = sqrtf(x * x + y * y + z * z);
+  const float inv = sh > 1e-10f ? 1.0f / sh : 1.0f;
+  const float ax = x * inv, ay = y * inv, az = z * inv;
+  float s, c;
+  sincosf(0.5f * angle * e, &s, &c);
+  q[0] = c;
+  q[1] = ax * s;
+  q[2] = ay * s;
+  q[3] = az * s;
+}
+
+// rotate v by the matrix of q (quaternion.py:266-285), v' = R v
+__device__ inline void qrot(const float q[4], const float v[3], float o[3]) {
+  const float w = q[0], x = q[1], y = q[2], z = q[3];
+  const float x2 = x * x, y2 = y * y, z2 = z * z, w2 = w * w;
+  const float xy = x * y, zw = z * w, xz = x * z, yw = y * w, yz = y * z, xw = x * w;
+  o[0] = (x2 - y2 - z2 + w2) * v[0] + 2.f * (xy - zw) * v[1] + 2.f * (xz + yw) * v[2];
+  o[1] = 2.f * (xy + zw) * v[0] + (-x2 + y2 - z2 + w2) * v[1] + 2.f * (yz - xw) * v[2];
+  o[2] = 2.f * (xz - yw) * v[0] + 2.f * (yz + xw) * v[1] + (-x2 - y2 + z2 + w2) * v[2];
+}
+
+__device__ inline float pair_u(float r2, int ti, int tj, float qq, const float2 *lj, int nsp,
+                               const ImgCfg &lj_img, const ImgCfg &ew_img, float alpha, float ke,
+                               bool in_lj, bool in_ew) {
+  float e = 0.f;
+  if (in_lj && r2 < lj_img.rc2) {
+    const float2 c = lj[ti * nsp + tj];
+    const float s2 = c.x / r2;
+    const float c6 = s2 * s2 * s2;
+    e += c.y * (c6 * c6 - c6);
+  }
+  if (in_ew && r2 < ew_img.rc2 && qq != 0.f) {
+    const float r = sqrtf(r2);
+    e += ke * qq * erfcf(alpha * r) / r;
+  }
+  return e;
+}
+
+// Sum over the reference's image set of the pair (a at fa, j at fj) for one
+// term configuration; `excl` drops the minimum image (same molecule).
+__device__ inline float pair_images(const float L[6], const float fa[3], const float fj[3], int ti,
+                                    int tj, float qq, const float2 *lj, int nsp, const ImgCfg &li,
+                                    const ImgCfg &ei, float alpha, float ke, bool excl) {
+  float d0[3] = {fa[0] - fj[0], fa[1] - fj[1], fa[2] - fj[2]};
+  const float ms[3] = {rintf(d0[0]), rintf(d0[1]), rintf(d0[2])};
+  float e = 0.f;
+  // LJ and Ewald may use different image sets; enumerate the union
+  const bool any_img = li.image_mode || ei.image_mode;
+  const bool same = li.image_mode == ei.image_mode && li.n[0] == ei.n[0] && li.n[1] == ei.n[1] &&
+                    li.n[2] == ei.n[2];
+  if (any_img && same) {
+    const int hx = li.n[0] / 2, hy = li.n[1] / 2, hz = li.n[2] / 2;
+    for (int ox = -hx; ox <= hx; ++ox)
+      for (int oy = -hy; oy <= hy; ++oy)
+        for (int oz = -hz; oz <= hz; ++oz) {
+          if (excl && ms[0] == (float)ox && ms[1] == (float)oy && ms[2] == (float)oz) continue;
+          float d[3] = {d0[0] - ox, d0[1] - oy, d0[2] - oz}, c[3];
+          cart32(L, d, c);
+          e += pair_u(c[0] * c[0] + c[1] * c[1] + c[2] * c[2], ti, tj, qq, lj, nsp, li, ei, alpha, ke, true, true);
+        }
+    return e;
+  }
+  if (!any_img) {
+    if (excl) return 0.f;
+    float d[3] = {d0[0] - ms[0], d0[1] - ms[1], d0[2] - ms[2]}, c[3];
+    cart32(L, d, c);
+    const float r2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+    return pair_u(r2, ti, tj, qq, lj, nsp, li, ei, alpha, ke, true, true);
+  }
+  const int hx = max(li.n[0], ei.n[0]) / 2, hy = max(li.n[1], ei.n[1]) / 2, hz = max(li.n[2], ei.n[2]) / 2;
+  for (int ox = -hx; ox <= hx; ++ox)
+    for (int oy = -hy; oy <= hy; ++oy)
+      for (int oz = -hz; oz <= hz; ++oz) {
+        const float o[3] = {(float)ox, (float)oy, (float)oz};
+        // per term: is this offset in its set, and what shift does it imply
+        bool in_l, in_e;
+        float sl[3], se[3];
+        in_l = true;
+        in_e = true;
+        if (li.image_mode) {
+          in_l = abs(ox) <= li.n[0] / 2 && abs(oy) <= li.n[1] / 2 && abs(oz) <= li.n[2] / 2;
+          sl[0] = o[0]; sl[1] = o[1]; sl[2] = o[2];
+        } else {
+          in_l = ox == 0 && oy == 0 && oz == 0;
+          sl[0] = ms[0]; sl[1] = ms[1]; sl[2] = ms[2];
+        }
+        if (ei.image_mode) {
+          in_e = abs(ox) <= ei.n[0] / 2 && abs(oy) <= ei.n[1] / 2 && abs(oz) <= ei.n[2] / 2;
+          se[0] = o[0]; se[1] = o[1]; se[2] = o[2];
+        } else {
+          in_e = ox == 0 && oy == 0 && oz == 0;
+          se[0] = ms[0]; se[1] = ms[1]; se[2] = ms[2];
+        }
+        if (in_l) {
+          const bool is_min = (sl[0] == ms[0]) && (sl[1] == ms[1]) && (sl[2] == ms[2]);
+          if (!(excl && is_min)) {
+            float d[3] = {d0[0] - sl[0], d0[1] - sl[1], d0[2] - sl[2]}, c[3];
+            cart32(L, d, c);
+            e += pair_u(c[0] * c[0] + c[1] * c[1] + c[2] * c[2], ti, tj, qq, lj, nsp, li, ei, alpha, ke,
+                        true, false);
+          }
+        }
+        if (in_e) {
+          const bool is_min = (se[0] == ms[0]) && (se[1] == ms[1]) && (se[2] == ms[2]);
+          if (!(excl && is_min)) {
+            float d[3] = {d0[0] - se[0], d0[1] - se[1], d0[2] - se[2]}, c[3];
+            cart32(L, d, c);
+            e += pair_u(c[0] * c[0] + c[1] * c[1] + c[2] * c[2], ti, tj, qq, lj, nsp, li, ei, alpha, ke,
+                        false, true);
+          }
+        }
+      }
+  return e;
+}
+
+__device__ inline double tail_energy(const double *counts, int nsp, const double *coef) {
+  // sum_ab coef_ab N_a N_b   (coef = (8/3) pi eps sigma^3 [(sigma/rc)^9/3 - (sigma/rc)^3] / V, masked)
+  double e = 0.0;
+  for (int a = 0; a < nsp; ++a)
+    for (int b = 0; b < nsp; ++b) e += coef[a * nsp + b] * counts[a] * counts[b];
+  return e;
+}
+
+__global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_status *status) {
+  __shared__ StepShared sh;
+  __shared__ float2 lj[kMaxSpeciesMC * kMaxSpeciesMC];
+  __shared__ float2 dS[kMaxKVec];
+  __shared__ double red[40];
+  __shared__ float Lf[6], If[6];
+  const int s = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int apm = a.atoms_per_mol;
+  const int nsp = a.n_species;
+  const int nk = a.n_kvecs;
+  for (int k = tid; k < nsp * nsp; k += kThreads)
+    lj[k] = make_float2(a.lj_table[2 * k], a.lj_table[2 * k + 1]);
+  if (tid == 0) {
+    const Tril64 L = load_tril64(a.tril + 6 * (int64_t)s);
+    const Tril64 inv = inverse_tril64(L);
+    for (int k = 0; k < 6; ++k) {
+      Lf[k] = (float)L.t[k];
+      If[k] = (float)inv.t[k];
+    }
+  }
+  __syncthreads();
+  // image configurations of the two terms (neighborlist.py:461-466)
+  ImgCfg li, ei;
+  {
+    const Tril64 L = load_tril64(a.tril + 6 * (int64_t)s);
+    double w[3];
+    perpendicular_widths64(L, w);
+    const double rcs[2] = {a.rc_lj[s], a.rc_ew[s]};
+    for (int t = 0; t < 2; ++t) {
+      ImgCfg &c = t == 0 ? li : ei;
+      int prod = 1;
+      for (int d = 0; d < 3; ++d) {
+        int n = (int)ceil(2.0 * rcs[t] / w[d]);
+        n = n < 1 ? 1 : n;
+        if (n % 2 == 0) n += 1;
+        if (n > kMaxImg) {
+          n = kMaxImg;
+          if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
+        }
+        c.n[d] = n;
+        prod *= n;
+      }
+      c.image_mode = prod > 1;
+      c.rc2 = (float)(rcs[t] * rcs[t]);
+    }
+  }
+  const float alpha = (float)a.alpha[s];
+  const float ke = (float)a.coulomb_k;
+  const double kT = a.kT[s];
+  const double volume = fabs(a.tril[6 * (int64_t)s] * a.tril[6 * (int64_t)s + 2] * a.tril[6 * (int64_t)s + 5]);
+  const int fw0 = a.fw_start[s], fwn = a.fw_count[s];
+  float4 *gpos = reinterpret_cast<float4 *>(a.guest_pos) + (int64_t)s * a.max_mol * apm;
+  const float4 *motif = reinterpret_cast<const float4 *>(a.motif_pos);
+  const float4 *fwp = reinterpret_cast<const float4 *>(a.fw_pos);
+  double *sk = a.structure_factor + (int64_t)s * nk * 2;
+  const double *pk = a.prefactor + (int64_t)s * nk;
+  const int32_t *kn = a.kvec_n + (int64_t)s * nk * 3;
+
+  for (int step = 0; step < a.n_steps; ++step) {
+    const uint64_t ctr = a.step0 + (uint64_t)step;
+    // ---------------------------------------------------------------- proposal (thread 0)
+    if (tid == 0) {
+      const int nmol = a.n_mol[s];
+      int kind;
+      if (a.proposals != nullptr) {
+        kind = a.proposals[s].kind;
+      } else {
+        const U4 g = rng4(a.seed, 0, ctr);  // shared by all systems
+        const float u = u01(g.x);
+        kind = 0;
+        while (kind < 3 && u >= a.move_cum[kind]) ++kind;  // 0..3 (3 = exchange)
+        if (kind == 3) kind = (g.y & 1u) ? 4 : 3;          // shared insert / delete coin
+      }
+      // per-system draws of this step: counters 8 ctr + 0 .. 4 (selection, rotation,
+      // offset, translation normals, acceptance)
+      const U4 r1 = rng4(a.seed, 1 + (uint64_t)s, 8 * ctr);
+      const U4 r2 = rng4(a.seed, 1 + (uint64_t)s, 8 * ctr + 1);
+      const U4 r3 = rng4(a.seed, 1 + (uint64_t)s, 8 * ctr + 2);
+      sh.kind = kind;
+      sh.has_old = 0;
+      sh.has_new = 0;
+      int mol = -1;
+      if (kind == 3) {
+        mol = nmol;  // next free slot
+        if (nmol < a.max_mol) sh.has_new = 1;
+        else status_capacity(status, KUPS_CAP_ATOMS, (int64_t)(nmol + 1) * apm, s);
+      } else if (nmol > 0) {
+        mol = a.proposals != nullptr ? a.proposals[s].mol : (int)(r1.x % (uint32_t)nmol);
+        if (mol >= 0 && mol < nmol) {
+          sh.has_old = 1;
+          sh.has_new = kind != 4;
+        } else {
+          mol = -1;  // an out-of-range replayed proposal changes nothing
+        }
+      }
+      sh.mol = mol;
+      for (int i = 0; i < apm; ++i) sh.q[i] = a.motif_charge[i];
+      if (sh.has_old)
+        for (int i = 0; i < apm; ++i) sh.old_pos[i] = gpos[mol * apm + i];
+      if (sh.has_new) {
+        if (a.proposals != nullptr) {
+          for (int i = 0; i < apm; ++i) sh.new_pos[i] = reinterpret_cast<const float4 *>(a.proposals[s].pos)[i];
+        } else if (kind == 0) {  // translation: N(0, 1) * width per axis, wrap
+          float eta[4];
+          normal4(a.seed, 1 + (uint64_t)s, 8 * ctr + 3, eta);
+          const float w = a.width[s * 4 + 0];
+          for (int i = 0; i < apm; ++i) {
+            const float4 p = sh.old_pos[i];
+            float c[3] = {p.x + eta[0] * w, p.y + eta[1] * w, p.z + eta[2] * w};
+            wrap32(Lf, If, c);
+            sh.new_pos[i] = make_float4(c[0], c[1], c[2], p.w);
+          }
+        } else if (kind == 1 || kind == 2) {  // rotation about the COM (q ** w), reinsertion
+          float com[3] = {0.f, 0.f, 0.f};
+          const float4 r0 = sh.old_pos[0];
+          float rel[kMaxApm][3];
+          for (int i = 0; i < apm; ++i) {
+            const float4 p = sh.old_pos[i];
+            float d[3] = {p.x - r0.x, p.y - r0.y, p.z - r0.z};
+            wrap32(Lf, If, d);
+            for (int c = 0; c < 3; ++c) com[c] += d[c];
+          }
+          for (int c = 0; c < 3; ++c) com[c] = com[c] / apm;
+          float cm[3] = {com[0] + r0.x, com[1] + r0.y, com[2] + r0.z};
+          wrap32(Lf, If, cm);
+          for (int i = 0; i < apm; ++i) {
+            const float4 p = sh.old_pos[i];
+            float d[3] = {p.x - cm[0], p.y - cm[1], p.z - cm[2]};
+            wrap32(Lf, If, d);
+            for (int c = 0; c < 3; ++c) rel[i][c] = d[c];
+          }
+          float q0[4], q[4];
+          shoemake(u01(r2.x), u01(r2.y), u01(r2.z), q0);
+          if (kind == 1) qpow(q0, a.width[s * 4 + 1], q);
+          else for (int c = 0; c < 4; ++c) q[c] = q0[c];
+          float shift[3] = {0.f, 0.f, 0.f};
+          if (kind == 2) {
+            const float fo[3] = {u01(r3.x), u01(r3.y), u01(r3.z)};
+            cart32(Lf, fo, shift);
+          }
+          for (int i = 0; i < apm; ++i) {
+            float o[3];
+            qrot(q, rel[i], o);
+            float c[3] = {o[0] + cm[0], o[1] + cm[1], o[2] + cm[2]};
+            wrap32(Lf, If, c);
+            if (kind == 2) {
+              c[0] += shift[0];
+              c[1] += shift[1];
+              c[2] += shift[2];
+              wrap32(Lf, If, c);
+            }
+            sh.new_pos[i] = make_float4(c[0], c[1], c[2], sh.old_pos[i].w);
+          }
+        } else if (kind == 3) {  // insertion: template @ R + uniform offset, wrap
+          float q[4];
+          shoemake(u01(r2.x), u01(r2.y), u01(r2.z), q);
+          const float fo[3] = {u01(r3.x), u01(r3.y), u01(r3.z)};
+          float shift[3];
+          cart32(Lf, fo, shift);
+          for (int i = 0; i < apm; ++i) {
+            const float4 m = motif[i];
+            const float v[3] = {m.x, m.y, m.z};
+            float o[3];
+            qrot(q, v, o);
+            float c[3] = {o[0] + shift[0], o[1] + shift[1], o[2] + shift[2]};
+            wrap32(Lf, If, c);
+            sh.new_pos[i] = make_float4(c[0], c[1], c[2], m.w);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const int has_old = sh.has_old, has_new = sh.has_new, mol = sh.mol, kind = sh.kind;
+    // ---------------------------------------------------------------- real space: moved vs others
+    float e_acc = 0.f;
+    const int nmol = a.n_mol[s];
+    const int n_other = fwn + nmol * apm;
+    for (int j = tid; j < n_other; j += kThreads) {
+      float4 pj;
+      float qj;
+      if (j < fwn) {
+        pj = fwp[fw0 + j];
+        qj = a.fw_charge[fw0 + j];
+      } else {
+        const int g = j - fwn;
+        if (has_old && g / apm == mol) continue;  // the moved molecule itself
+        pj = gpos[g];
+        qj = a.motif_charge[g % apm];
+      }
+      float fj[3];
+      frac32(If, pj.x, pj.y, pj.z, fj);
+      const int tj = __float_as_int(pj.w);
+      for (int st = 0; st < 2; ++st) {
+        if ((st == 0 && !has_old) || (st == 1 && !has_new)) continue;
+        const float sign = st == 0 ? -1.f : 1.f;
+        for (int i = 0; i < apm; ++i) {
+          const float4 pa = st == 0 ? sh.old_pos[i] : sh.new_pos[i];
+          float fa[3];
+          frac32(If, pa.x, pa.y, pa.z, fa);
+          e_acc += sign * pair_images(Lf, fa, fj, __float_as_int(pa.w), tj, sh.q[i] * qj, lj, nsp, li, ei,
+                                      alpha, ke, false);
+        }
+      }
+    }
+    // moved vs moved (same molecule): 1/2 sum over ordered pairs incl. self images
+    for (int t = tid; t < 2 * apm * apm; t += kThreads) {
+      const int st = t / (apm * apm), ab = t % (apm * apm), ia = ab / apm, ib = ab % apm;
+      if ((st == 0 && !has_old) || (st == 1 && !has_new)) continue;
+      const float4 pa = st == 0 ? sh.old_pos[ia] : sh.new_pos[ia];
+      const float4 pb = st == 0 ? sh.old_pos[ib] : sh.new_pos[ib];
+      float fa[3], fb[3];
+      frac32(If, pa.x, pa.y, pa.z, fa);
+      frac32(If, pb.x, pb.y, pb.z, fb);
+      const float sign = st == 0 ? -0.5f : 0.5f;
+      e_acc += sign * pair_images(Lf, fa, fb, __float_as_int(pa.w), __float_as_int(pb.w), sh.q[ia] * sh.q[ib], lj,
+                                  nsp, li, ei, alpha, ke, true);
+    }
+    const double de_real = block_sum((double)e_acc, red);
+    // ---------------------------------------------------------------- reciprocal space
+    double de_rec = 0.0;
+    for (int k = tid; k < nk; k += kThreads) {
+      const int n0 = kn[3 * k], n1 = kn[3 * k + 1], n2 = kn[3 * k + 2];
+      float dc = 0.f, ds = 0.f;
+      for (int st = 0; st < 2; ++st) {
+        if ((st == 0 && !has_old) || (st == 1 && !has_new)) continue;
+        const float sign = st == 0 ? -1.f : 1.f;
+        for (int i = 0; i < apm; ++i) {
+          const float4 p = st == 0 ? sh.old_pos[i] : sh.new_pos[i];
+          float f[3];
+          frac32(If, p.x, p.y, p.z, f);
+          float t = n0 * f[0] + n1 * f[1] + n2 * f[2];
+          t -= rintf(t);
+          float sn, cs;
+          sincospif(2.0f * t, &sn, &cs);
+          dc += sign * sh.q[i] * cs;
+          ds += sign * sh.q[i] * sn;
+        }
+      }
+      dS[k] = make_float2(dc, ds);
+      const double sc = sk[2 * k], ss = sk[2 * k + 1];
+      de_rec += pk[k] * (2.0 * (sc * dc + ss * ds) + (double)dc * dc + (double)ds * ds);
+    }
+    __syncthreads();
+    de_rec = block_sum(de_rec, red) * a.coulomb_k;
+    // ---------------------------------------------------------------- acceptance (thread 0)
+    if (tid == 0) {
+      double de = de_real + de_rec;
+      const int n_old = nmol;
+      int n_new = n_old;
+      if (kind == 3 && has_new) n_new = n_old + 1;
+      if (kind == 4 && has_old) n_new = n_old - 1;
+      if (n_new != n_old) {
+        const double sgn = n_new > n_old ? 1.0 : -1.0;
+        de += sgn * (a.self_energy_mol[s] + a.exclusion_energy_mol[s]);
+        // tail correction with species counts before / after
+        double c0[kMaxSpeciesMC], c1[kMaxSpeciesMC];
+        for (int t = 0; t < nsp; ++t) {
+          c0[t] = a.fw_species_count[s * nsp + t] + (double)n_old * a.motif_species_count[t];
+          c1[t] = a.fw_species_count[s * nsp + t] + (double)n_new * a.motif_species_count[t];
+        }
+        if (a.tail_coef != nullptr) {
+          const double *tc = a.tail_coef + (int64_t)s * nsp * nsp;
+          de += tail_energy(c1, nsp, tc) - tail_energy(c0, nsp, tc);
+        }
+      }
+      double logp = -de / kT;
+      if (n_new != n_old) {
+        const double lnfv = a.log_activity[s] + log(volume);
+        logp += (n_new - n_old) * lnfv + lgamma((double)n_old + 1.0) - lgamma((double)n_new + 1.0);
+      }
+      const U4 r4 = rng4(a.seed, 1 + (uint64_t)s, 8 * ctr + 4);
+      const double u = ((double)(r4.w >> 8) + 1.0) * (1.0 / 16777216.0);  // (0, 1]
+      int accept = logp > log(u);
+      if (a.proposals != nullptr && a.proposals[s].force_reject) accept = 0;
+      if (kind == 3 && !has_new) accept = 0;  // no free slot: capacity recorded, nothing changes
+      sh.accept = accept;
+      sh.log_p = logp;
+      sh.de_total = de;
+      sh.de_real = de_real;
+      sh.de_recip = de_rec;
+      if (a.out_delta != nullptr) {
+        a.out_delta[4 * (int64_t)s] = de;
+        a.out_delta[4 * (int64_t)s + 1] = de_real;
+        a.out_delta[4 * (int64_t)s + 2] = de_rec;
+        a.out_delta[4 * (int64_t)s + 3] = logp;
+      }
+    }
+    __syncthreads();
+    const int accept = sh.accept;
+    // ---------------------------------------------------------------- commit
+    if (accept) {
+      for (int k = tid; k < nk; k += kThreads) {
+        const float2 d = dS[k];
+        sk[2 * k] += (double)d.x;
+        sk[2 * k + 1] += (double)d.y;
+      }
+      if (tid == 0) {
+        a.energy[s] += sh.de_total;
+        if (kind == 3 && has_new) {
+          for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = sh.new_pos[i];
+          a.n_mol[s] = nmol + 1;
+        } else if (kind == 4 && has_old) {
+          const int last = nmol - 1;
+          for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = gpos[last * apm + i];
+          a.n_mol[s] = last;
+        } else if (has_new) {
+          for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = sh.new_pos[i];
+        }
+      }
+    }
+    // ---------------------------------------------------------------- statistics and step widths
+    if (tid == 0) {
+      a.attempted[5 * (int64_t)s + kind] += 1;
+      a.accepted[5 * (int64_t)s + kind] += accept;
+      const int sched = kind >= 3 ? 3 : kind;  // insert / delete share the exchange scheduler
+      const int hs = a.history_len;
+      uint32_t *hist = a.history + ((int64_t)s * 4 + sched) * 4;
+      int idx = a.history_index[s * 4 + sched];
+      const uint32_t bit = 1u << (idx & 31);
+      hist[idx >> 5] = accept ? (hist[idx >> 5] | bit) : (hist[idx >> 5] & ~bit);
+      idx = (idx + 1) % hs;
+      a.history_index[s * 4 + sched] = idx;
+      if (idx == 0) {
+        int acc = 0;
+        for (int w = 0; w < 4; ++w) {
+          const uint32_t m = w * 32 >= hs ? 0u : (w * 32 + 32 <= hs ? 0xffffffffu : ((1u << (hs - w * 32)) - 1u));
+          acc += __popc(hist[w] & m);
+        }
+        const float avg = (float)acc / hs;
+        const float target = 0.5f, tol = 0.05f, mult = 1.1f;
+        float v = a.width[s * 4 + sched];
+        float nv = avg < target ? v / mult : v * mult;  // step widths correlate negatively
+        nv = fmaxf(nv, 0.0f);
+        const float ub = a.width_max[s * 4 + sched];
+        if (ub > 0.f) nv = fminf(nv, ub);
+        if (fabsf(avg - target) > tol) a.width[s * 4 + sched] = nv;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+}  // namespace kups
+
+using namespace kups;
+
+extern "C" int32_t kups_gcmc_run(const kups_gcmc_args *a, kups_status *status, void *stream) {
+  if (a == nullptr || a->n_systems < 0 || a->n_steps < 0 || a->atoms_per_mol <= 0 ||
+      a->atoms_per_mol > kMaxApm || a->n_species <= 0 || a->n_species > kMaxSpeciesMC ||
+      a->n_kvecs < 0 || a->n_kvecs > kMaxKVec || a->history_len <= 0 || a->history_len > 128 ||
+      a->max_mol < 0)
+    return KUPS_ERR_INVALID;
+  if (a->n_systems == 0 || a->n_steps == 0) return KUPS_OK;
+  gcmc_kernel<<<a->n_systems, kThreads, 0, (cudaStream_t)stream>>>(*a, status);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}

@@ -153,11 +153,16 @@ class RecipWorkspace:
 
 
 def ewald_recip(positions, charges, sys_offset, max_atoms, tril, kvec_n, alpha, grad_tril=True, ws=None,
-                out=None):
-    """Reciprocal energy [S], dE/dx [N,3], dE/dtril [S,6], S(k) [S,nk,2] (atoms grouped by system)."""
+                out=None, status=None):
+    """Reciprocal energy [S], dE/dx [N,3], dE/dtril [S,6], S(k) [S,nk,2] (atoms grouped by system).
+
+    Every converted input is held in a local until the launch is enqueued, so
+    no temporary's memory can be recycled under the kernel.
+    """
     lib = _lib.load()
-    pos, q, tril = _f64(positions), _f64(charges), _f64(tril)
+    pos, q, tril, al = _f64(positions), _f64(charges), _f64(tril), _f64(alpha)
     kn = _i32(kvec_n)
+    off = _i32(sys_offset)
     s, nk = tril.shape[0], kn.shape[1]
     n = pos.shape[0]
     energy, grad, gtril, sk = out if out is not None else (
@@ -165,9 +170,9 @@ def ewald_recip(positions, charges, sys_offset, max_atoms, tril, kvec_n, alpha, 
         torch.empty((s, 6), dtype=torch.float64, device="cuda"), torch.empty((s, nk, 2), dtype=torch.float64, device="cuda"))
     nbytes = lib.kups_ewald_recip_workspace_bytes(s, nk)
     buf = (ws or RecipWorkspace()).get(nbytes)
-    status = new_status()
-    rc = lib.kups_ewald_recip(pos.data_ptr(), q.data_ptr(), sys_offset.data_ptr(), s, int(max_atoms), tril.data_ptr(),
-                              kn.data_ptr(), nk, _f64(alpha).data_ptr(), TO_STANDARD_UNITS, energy.data_ptr(),
+    status = status if status is not None else new_status()
+    rc = lib.kups_ewald_recip(pos.data_ptr(), q.data_ptr(), off.data_ptr(), s, int(max_atoms), tril.data_ptr(),
+                              kn.data_ptr(), nk, al.data_ptr(), TO_STANDARD_UNITS, energy.data_ptr(),
                               grad.data_ptr(), gtril.data_ptr() if grad_tril else None, sk.data_ptr(), buf.data_ptr(),
                               buf.numel(), status.data_ptr(), _stream())
     _lib.check(rc, "kups_ewald_recip")
@@ -176,31 +181,34 @@ def ewald_recip(positions, charges, sys_offset, max_atoms, tril, kvec_n, alpha, 
 
 def ewald_self(charges, sys_offset, alpha, n_systems):
     lib = _lib.load()
+    q, al, off = _f64(charges), _f64(alpha), _i32(sys_offset)
     e = torch.empty(n_systems, dtype=torch.float64, device="cuda")
-    rc = lib.kups_ewald_self(_f64(charges).data_ptr(), sys_offset.data_ptr(), n_systems, _f64(alpha).data_ptr(),
-                             TO_STANDARD_UNITS, e.data_ptr(), _stream())
+    rc = lib.kups_ewald_self(q.data_ptr(), off.data_ptr(), n_systems, al.data_ptr(), TO_STANDARD_UNITS, e.data_ptr(),
+                             _stream())
     _lib.check(rc, "kups_ewald_self")
     return e
 
 
 def pair_edges(positions, system, species, charges, tril, edges, shifts, n_edges, terms, lj_sigma=None,
-               lj_epsilon=None, lj_cutoff=None, alpha=None, ewald_cutoff=None, grad_tril=True, out=None):
+               lj_epsilon=None, lj_cutoff=None, alpha=None, ewald_cutoff=None, grad_tril=True, out=None, status=None):
     lib = _lib.load()
-    pos = _f64(positions)
-    n = pos.shape[0]
-    tril = _f64(tril)
-    s = tril.shape[0]
-    ptr = lambda x, f: f(x).data_ptr() if x is not None else None
+    pos, tril = _f64(positions), _f64(tril)
+    n, s = pos.shape[0], tril.shape[0]
+    keep = dict(system=_i32(system), edges=_i32(edges), shifts=_i32(shifts))
+    for name, x, conv in (("species", species, _i32), ("charges", charges, _f64), ("sig", lj_sigma, _f64),
+                          ("eps", lj_epsilon, _f64), ("rc_lj", lj_cutoff, _f64), ("alpha", alpha, _f64),
+                          ("rc_ew", ewald_cutoff, _f64)):
+        keep[name] = conv(torch.as_tensor(x)) if x is not None else None
+    ptr = lambda k: keep[k].data_ptr() if keep[k] is not None else None
     energy, grad, gtril = out if out is not None else (
         torch.empty(s, dtype=torch.float64, device="cuda"), torch.empty((n, 3), dtype=torch.float64, device="cuda"),
         torch.empty((s, 6), dtype=torch.float64, device="cuda"))
-    nsp = int(torch.as_tensor(lj_sigma).shape[0]) if lj_sigma is not None else 0
-    status = new_status()
-    rc = lib.kups_pair_edges(pos.data_ptr(), _i32(system).data_ptr(), ptr(species, _i32), ptr(charges, _f64), n,
-                             tril.data_ptr(), s, ptr(lj_sigma, _f64), ptr(lj_epsilon, _f64), nsp, ptr(lj_cutoff, _f64),
-                             ptr(alpha, _f64), ptr(ewald_cutoff, _f64), TO_STANDARD_UNITS, int(terms),
-                             _i32(edges).data_ptr(), _i32(shifts).data_ptr(), int(n_edges), energy.data_ptr(),
-                             grad.data_ptr(), gtril.data_ptr() if grad_tril else None, status.data_ptr(), _stream())
+    nsp = int(keep["sig"].shape[0]) if keep["sig"] is not None else 0
+    status = status if status is not None else new_status()
+    rc = lib.kups_pair_edges(pos.data_ptr(), ptr("system"), ptr("species"), ptr("charges"), n, tril.data_ptr(), s,
+                             ptr("sig"), ptr("eps"), nsp, ptr("rc_lj"), ptr("alpha"), ptr("rc_ew"), TO_STANDARD_UNITS,
+                             int(terms), ptr("edges"), ptr("shifts"), int(n_edges), energy.data_ptr(), grad.data_ptr(),
+                             gtril.data_ptr() if grad_tril else None, status.data_ptr(), _stream())
     _lib.check(rc, "kups_pair_edges")
     return energy, grad, gtril
 
@@ -331,9 +339,9 @@ class LJEwaldMD:
         terms = TERM_EWALD_REAL | (TERM_LJ if self.lj else 0)
         pair_edges(pos, self.system, self.species, self.q, self.tril, self.edges, self.shifts, self.cap, terms,
                    self.sig, self.eps, self.rc_lj, self.alpha, self.rc_ew, grad_tril=False,
-                   out=(self.e_pair, self.g_pair, self.t_pair))
+                   out=(self.e_pair, self.g_pair, self.t_pair), status=self.status)
         ewald_recip(pos, self.q, self.off, self.max_atoms, self.tril, self.kn, self.alpha, grad_tril=False,
-                    ws=self.rws, out=(self.e_rec, self.g_rec, self.t_rec, self.sk))
+                    ws=self.rws, out=(self.e_rec, self.g_rec, self.t_rec, self.sk), status=self.status)
         torch.add(self.g_pair, self.g_rec, out=self.grad)
         torch.add(self.e_pair, self.e_rec, out=self.energy)
         self.energy.add_(self.e_self)

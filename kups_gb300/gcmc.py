@@ -1,0 +1,315 @@
+"""Batched GCMC of rigid molecules in rigid frameworks behind kUPS's MCMC propagator.
+
+Mirrors the pieces of src/kups/application/simulations/mcmc_rigid.py the
+GCMC run wires together (``init_state`` :310-382, ``make_propagator``
+:281-307): the LJ + Ewald (with intramolecular exclusion) + LJ tail
+potential, the muVT acceptance with the Peng-Robinson fugacity
+(src/kups/mcmc/fugacity.py:38-193, application/mcmc/data.py:380-392) and
+``make_gcmc_mcmc_propagator`` (src/kups/mcmc/moves.py:1078-1230) with one
+adaptive step-width scheduler per move (``ParameterSchedulerState.create``,
+src/kups/core/parameter_scheduler.py:103-160; translation bounded by half
+the smallest cell width, mcmc_rigid.py:357-372).  Every MC step of every
+system runs on the GPU (``kups_gcmc_run``); host code only sets up.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .neighborlist import _stream, new_status, read_status
+from .units import BOLTZMANN_CONSTANT, PASCAL, TO_STANDARD_UNITS
+
+MOVES = ("translate", "rotate", "reinsert", "insert", "delete")
+
+
+# ----------------------------------------------------------------------------- host-side thermodynamics
+def _cubic_roots(c):
+    r = np.roots(c)
+    return r
+
+
+def peng_robinson_log_fugacity(pressure_pa, temperature, pc_pa, tc, omega):
+    """ln f (f in the pressure's unit) of a pure gas, gas-phase root (fugacity.py:38-127)."""
+    pr, tr = pressure_pa / pc_pa, temperature / tc
+    m = 0.37464 + 1.54226 * omega - 0.26992 * omega**2
+    sa = 1 + m * (1 - tr**0.5)
+    A = 0.45724 * pr / tr**2 * sa**2
+    B = 0.0778 * pr / tr
+    roots = _cubic_roots([1.0, B - 1.0, A - 3.0 * B**2 - 2.0 * B, -(A * B - B**2 - B**3)])
+    best = None
+    for z in roots:
+        if abs(z.imag) > 1e-12 or z.real <= B:
+            continue
+        z = z.real
+        sq2 = math.sqrt(2.0)
+        lnphi = (z - 1) - math.log(z - B) - A / (2 * sq2 * B) * (2.0 - 1.0) * math.log(
+            (z + (1 + sq2) * B) / (z + (1 - sq2) * B))
+        if best is None or lnphi < best:
+            best = lnphi
+    return best + math.log(pressure_pa)
+
+
+def lorentz_berthelot(sigma, epsilon):
+    s, e = np.asarray(sigma, float), np.asarray(epsilon, float)
+    return (s[:, None] + s) / 2, np.sqrt(e[:, None] * e)
+
+
+def prefactor(tril, kvec_n, alpha):
+    """P(k) = (2 - [n_x = 0]) 2 pi / V exp(-k^2 / 4 a^2) / k^2, 0 for k = 0 (ewald.py:363-391)."""
+    t = np.asarray(tril, float)
+    L = np.array([[t[0], 0, 0], [t[1], t[2], 0], [t[3], t[4], t[5]]])
+    inv = np.linalg.inv(L)
+    k = 2 * np.pi * np.asarray(kvec_n, float) @ inv.T
+    k2 = (k * k).sum(-1)
+    vol = abs(t[0] * t[2] * t[5])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        p = (2 - (np.asarray(kvec_n)[:, 0] == 0)) * 2 * np.pi / vol * np.exp(-k2 / (4 * alpha**2)) / k2
+    return np.where(k2 > 0, p, 0.0)
+
+
+# ----------------------------------------------------------------------------- state
+@dataclass
+class GCMCSetup:
+    """Host description of a batch of GCMC systems sharing one molecule species."""
+
+    fw_positions: np.ndarray  # [F, 3] Cartesian, as stored (no wrap applied)
+    fw_species: np.ndarray  # [F]
+    fw_charges: np.ndarray  # [F]
+    fw_start: np.ndarray  # [S]
+    fw_count: np.ndarray  # [S]
+    tril: np.ndarray  # [S, 6]
+    motif_positions: np.ndarray  # [apm, 3] template
+    motif_species: np.ndarray  # [apm]
+    motif_charges: np.ndarray  # [apm]
+    sigma: np.ndarray  # [T, T]
+    epsilon: np.ndarray  # [T, T]
+    rc_lj: np.ndarray  # [S]
+    rc_ew: np.ndarray  # [S]
+    alpha: np.ndarray  # [S]
+    kvec_n: np.ndarray  # [S, nk, 3]
+    temperature: np.ndarray  # [S] K
+    log_activity: np.ndarray  # [S] ln(f / kT), 1 / A^3
+    max_mol: int = 64
+    tail_correction: bool = True
+    move_weights: tuple = (1.0, 1.0, 1.0, 2.0)  # translate, rotate, reinsert, exchange
+
+    @property
+    def n_systems(self) -> int:
+        return int(self.tril.shape[0])
+
+
+def exclusion_energy_of_molecule(pos, q, alpha):
+    """sum over intramolecular pairs of K q_a q_b (erfc(alpha r) - 1) / r (ewald.py:328-346)."""
+    from scipy.special import erfc
+
+    e = 0.0
+    for a in range(len(q)):
+        for b in range(a + 1, len(q)):
+            r = float(np.linalg.norm(pos[a] - pos[b]))
+            e += TO_STANDARD_UNITS * q[a] * q[b] * (erfc(alpha * r) - 1.0) / r
+    return e
+
+
+def tail_coefficients(sigma, epsilon, rc, volume, enabled=True):
+    """(8/3) pi eps sigma^3 [(sigma/rc)^9/3 - (sigma/rc)^3] / V per species pair (lennard_jones.py:276-315)."""
+    t1 = (sigma / rc) ** 3
+    c = (8 / 3) * np.pi * epsilon * sigma**3 * (t1**3 / 3 - t1) / volume
+    return np.where(epsilon > 0, c, 0.0) if enabled else np.zeros_like(c)
+
+
+class GCMC:
+    """Device state + the propagator ``__call__(key, n_steps)``."""
+
+    def __init__(self, setup: GCMCSetup, seed: int = 0):
+        self.setup = setup
+        s = setup.n_systems
+        apm = len(setup.motif_charges)
+        T = setup.sigma.shape[0]
+        if not (1 <= apm <= 8 and 1 <= T <= 8):
+            raise ValueError("GCMC supports 1..8 atoms per molecule and 1..8 species")
+        for name, sp in (("framework", setup.fw_species), ("motif", setup.motif_species)):
+            if len(sp) and (np.min(sp) < 0 or np.max(sp) >= T):
+                raise ValueError(f"{name} species outside the {T} parameter rows")
+        if setup.kvec_n.shape[1] > 4096 or np.abs(setup.kvec_n).max() > 16:
+            raise ValueError("at most 4096 k vectors with |n| <= 16 per axis")
+        dev = "cuda"
+        f32 = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float32, device=dev)
+        f64 = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)
+        i32 = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.int32, device=dev)
+        sp_bits = lambda sp: np.asarray(sp, np.int32).view(np.float32)
+        self.fw_pos = f32(np.concatenate([setup.fw_positions, sp_bits(setup.fw_species)[:, None]], 1))
+        self.fw_q = f32(setup.fw_charges)
+        self.fw_start, self.fw_count = i32(setup.fw_start), i32(setup.fw_count)
+        self.guest = torch.zeros((s, setup.max_mol, apm, 4), dtype=torch.float32, device=dev)
+        self.n_mol = torch.zeros(s, dtype=torch.int32, device=dev)
+        self.motif = f32(np.concatenate([setup.motif_positions, sp_bits(setup.motif_species)[:, None]], 1))
+        self.motif_q = f32(setup.motif_charges)
+        msc = np.bincount(setup.motif_species, minlength=T).astype(float)
+        self.motif_sc = f64(msc)
+        fwsc = np.stack([np.bincount(setup.fw_species[a:a + n], minlength=T) for a, n in
+                         zip(setup.fw_start, setup.fw_count)]).astype(float)
+        self.fw_sc = f64(fwsc)
+        self.tril = f64(setup.tril)
+        self.rc_lj, self.rc_ew, self.alpha = f64(setup.rc_lj), f64(setup.rc_ew), f64(setup.alpha)
+        self.kn = i32(setup.kvec_n)
+        nk = setup.kvec_n.shape[1]
+        self.pk = f64(np.stack([prefactor(setup.tril[i], setup.kvec_n[i], setup.alpha[i]) for i in range(s)]))
+        self.sk = torch.zeros((s, nk, 2), dtype=torch.float64, device=dev)
+        self.lj_table = f32(np.stack([setup.sigma**2, 4 * setup.epsilon], -1).reshape(-1))
+        vol = np.abs(setup.tril[:, 0] * setup.tril[:, 2] * setup.tril[:, 5])
+        self.volume = vol
+        self.tail = f64(np.stack([tail_coefficients(setup.sigma, setup.epsilon, setup.rc_lj[i], vol[i],
+                                                    setup.tail_correction) for i in range(s)]))
+        self.self_mol = f64(-TO_STANDARD_UNITS * setup.alpha / math.sqrt(math.pi) * float(np.sum(setup.motif_charges**2)))
+        self.excl_mol = f64([exclusion_energy_of_molecule(setup.motif_positions, setup.motif_charges, a)
+                             for a in setup.alpha])
+        self.kT = f64(setup.temperature * BOLTZMANN_CONSTANT)
+        self.log_activity = f64(setup.log_activity)
+        self.energy = torch.zeros(s, dtype=torch.float64, device=dev)
+        # framework-only structure factor (guests start empty)
+        self._init_structure_factor()
+        widths = np.tile(np.array([0.1, 0.1, 0.1, 0.1], np.float32), (s, 1))
+        wmax = np.zeros((s, 4), np.float32)
+        wmax[:, 0] = self._min_half_width()
+        self.width, self.width_max = f32(widths), f32(wmax)
+        self.history = torch.zeros((s, 4, 4), dtype=torch.int32, device=dev)
+        self.history_index = torch.zeros((s, 4), dtype=torch.int32, device=dev)
+        self.attempted = torch.zeros((s, 5), dtype=torch.int64, device=dev)
+        self.accepted = torch.zeros((s, 5), dtype=torch.int64, device=dev)
+        w = np.asarray(setup.move_weights, float)
+        self.move_cum = np.cumsum(w[:3]) / w.sum()
+        self.seed = seed
+        self.step = 0
+        self.status = new_status()
+
+    def _min_half_width(self):
+        out = []
+        for t in self.setup.tril:
+            L = np.array([[t[0], 0, 0], [t[1], t[2], 0], [t[3], t[4], t[5]]])
+            v = abs(np.linalg.det(L))
+            w = [v / np.linalg.norm(np.cross(L[1], L[2])), v / np.linalg.norm(np.cross(L[0], L[2])),
+                 v / np.linalg.norm(np.cross(L[0], L[1]))]
+            out.append(min(w) / 2)
+        return np.array(out, np.float32)
+
+    def _init_structure_factor(self):
+        from .ewald import ewald_recip
+
+        st = self.setup
+        pos, q, off = [], [], [0]
+        for a, n in zip(st.fw_start, st.fw_count):
+            pos.append(st.fw_positions[a:a + n])
+            q.append(st.fw_charges[a:a + n])
+            off.append(off[-1] + n)
+        P = torch.as_tensor(np.concatenate(pos), dtype=torch.float64, device="cuda")
+        Q = torch.as_tensor(np.concatenate(q), dtype=torch.float64, device="cuda")
+        O = torch.as_tensor(np.array(off, np.int32), device="cuda")
+        _, _, _, sk, _ = ewald_recip(P, Q, O, int(np.max(st.fw_count)), self.tril, self.kn, self.alpha, grad_tril=False)
+        self.sk.copy_(sk)
+
+    def args(self, n_steps, proposals=None, out_delta=None) -> _lib.GcmcArgs:
+        a = _lib.GcmcArgs()
+        st = self.setup
+        a.fw_pos, a.fw_charge, a.fw_start, a.fw_count = (self.fw_pos.data_ptr(), self.fw_q.data_ptr(),
+                                                         self.fw_start.data_ptr(), self.fw_count.data_ptr())
+        a.guest_pos, a.n_mol = self.guest.data_ptr(), self.n_mol.data_ptr()
+        a.motif_pos, a.motif_charge = self.motif.data_ptr(), self.motif_q.data_ptr()
+        a.motif_species_count, a.fw_species_count = self.motif_sc.data_ptr(), self.fw_sc.data_ptr()
+        a.tril, a.rc_lj, a.rc_ew, a.alpha = (self.tril.data_ptr(), self.rc_lj.data_ptr(), self.rc_ew.data_ptr(),
+                                             self.alpha.data_ptr())
+        a.kvec_n, a.prefactor, a.structure_factor = self.kn.data_ptr(), self.pk.data_ptr(), self.sk.data_ptr()
+        a.lj_table, a.tail_coef = self.lj_table.data_ptr(), self.tail.data_ptr()
+        a.self_energy_mol, a.exclusion_energy_mol = self.self_mol.data_ptr(), self.excl_mol.data_ptr()
+        a.kT, a.log_activity, a.energy = self.kT.data_ptr(), self.log_activity.data_ptr(), self.energy.data_ptr()
+        a.width, a.width_max = self.width.data_ptr(), self.width_max.data_ptr()
+        a.history, a.history_index = self.history.data_ptr(), self.history_index.data_ptr()
+        a.attempted, a.accepted = self.attempted.data_ptr(), self.accepted.data_ptr()
+        a.proposals = proposals.data_ptr() if proposals is not None else None
+        a.out_delta = out_delta.data_ptr() if out_delta is not None else None
+        for i in range(3):
+            a.move_cum[i] = float(self.move_cum[i])
+        a.coulomb_k = TO_STANDARD_UNITS
+        a.seed, a.step0 = int(self.seed) & (2**64 - 1), int(self.step)
+        a.n_systems, a.max_mol, a.atoms_per_mol = st.n_systems, st.max_mol, len(st.motif_charges)
+        a.n_species, a.n_kvecs, a.n_steps, a.history_len = st.sigma.shape[0], st.kvec_n.shape[1], int(n_steps), 100
+        return a
+
+    def launch(self, n_steps, proposals=None, out_delta=None):
+        a = self.args(n_steps, proposals, out_delta)
+        rc = _lib.load().kups_gcmc_run(C.byref(a), self.status.data_ptr(), _stream())
+        _lib.check(rc, "kups_gcmc_run")
+        self.step += n_steps
+
+    def __call__(self, key=None, n_steps: int = 1):
+        """Propagator: n_steps MC steps of every system (one launch)."""
+        if key is not None:
+            from .md import key_to_seed
+
+            self.seed = key_to_seed(key)
+        self.launch(n_steps)
+        return self
+
+    def check(self):
+        _lib.raise_status(read_status(self.status))
+
+    def evaluate(self, kinds, mols, new_positions, force_reject=True):
+        """One step with explicit proposals (no commit when force_reject): (dE, dE_real, dE_recip, log p) [S, 4]."""
+        s = self.setup.n_systems
+        apm = len(self.setup.motif_charges)
+        props = np.zeros(s, dtype=[("kind", np.int32), ("mol", np.int32), ("force_reject", np.int32),
+                                   ("pad", np.int32), ("pos", np.float32, (8, 4))])
+        props["kind"], props["mol"], props["force_reject"] = kinds, mols, int(force_reject)
+        sp = np.asarray(self.setup.motif_species, np.int32).view(np.float32)
+        for i in range(s):
+            if new_positions[i] is not None:
+                props["pos"][i, :apm, :3] = new_positions[i]
+                props["pos"][i, :apm, 3] = sp
+        buf = torch.as_tensor(props.view(np.uint8).copy(), device="cuda")
+        out = torch.zeros((s, 4), dtype=torch.float64, device="cuda")
+        self.launch(1, proposals=buf, out_delta=out)
+        return out.cpu().numpy()
+
+    def guest_positions(self) -> list[np.ndarray]:
+        g = self.guest.cpu().numpy()
+        n = self.n_mol.cpu().numpy()
+        return [g[i, : n[i], :, :3].reshape(-1, 3) for i in range(len(n))]
+
+    def set_guests(self, positions_per_system: list[np.ndarray]):
+        """Place molecules (each [n_mol * apm, 3]) and update S(k) and counts (energy cache not changed)."""
+        apm = len(self.setup.motif_charges)
+        g = np.zeros(self.guest.shape, np.float32)
+        sp = np.asarray(self.setup.motif_species, np.int32).view(np.float32)
+        nm = []
+        for i, p in enumerate(positions_per_system):
+            m = len(p) // apm
+            g[i, :m, :, :3] = np.asarray(p).reshape(m, apm, 3)
+            g[i, :m, :, 3] = sp
+            nm.append(m)
+        self.guest.copy_(torch.as_tensor(g))
+        self.n_mol.copy_(torch.as_tensor(np.array(nm, np.int32)))
+        # structure factor of framework + guests
+        from .ewald import ewald_recip
+
+        st = self.setup
+        pos, q, off = [], [], [0]
+        for i, (a, n) in enumerate(zip(st.fw_start, st.fw_count)):
+            gp = np.asarray(positions_per_system[i]).reshape(-1, 3)
+            pos.append(np.concatenate([st.fw_positions[a:a + n], gp]))
+            q.append(np.concatenate([st.fw_charges[a:a + n], np.tile(st.motif_charges, len(gp) // apm)]))
+            off.append(off[-1] + len(pos[-1]))
+        P = torch.as_tensor(np.concatenate(pos), dtype=torch.float64, device="cuda")
+        Q = torch.as_tensor(np.concatenate(q), dtype=torch.float64, device="cuda")
+        O = torch.as_tensor(np.array(off, np.int32), device="cuda")
+        _, _, _, sk, _ = ewald_recip(P, Q, O, int(np.diff(off).max()), self.tril, self.kn, self.alpha, grad_tril=False)
+        self.sk.copy_(sk)
+
+    def statistics(self):
+        att = self.attempted.cpu().numpy()
+        acc = self.accepted.cpu().numpy()
+        return {m: (int(att[:, i].sum()), int(acc[:, i].sum())) for i, m in enumerate(MOVES)}

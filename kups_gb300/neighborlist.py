@@ -142,7 +142,7 @@ def read_status(status: torch.Tensor) -> _lib.Status:
 def new_status(device="cuda") -> torch.Tensor:
     """Zeroed status word (kups_status is 24 bytes: i32, i32, i64, i64)."""
     st = torch.zeros(3, device=device, dtype=torch.int64)
-    st[2] = -1
+    st[2:].fill_(-1)  # a device fill, safe inside CUDA-graph capture
     return st
 
 

@@ -128,3 +128,43 @@ def batched_uneven_lj(n_systems=4096, n_min=64, n_max=2048, rho_min=0.7, rho_max
     return MDWorkload(pos, mom, masses, np.zeros(pos.shape[0], np.int32), system, tril, temps,
                       np.full(n_systems, dt_fs * FEMTO_SECOND), np.full(n_systems, friction_per_ps / 1000.0 / FEMTO_SECOND),
                       np.array([[ARGON_SIGMA]]), np.array([[ARGON_EPS]]), rc_sigma * ARGON_SIGMA, skin_sigma * ARGON_SIGMA)
+
+
+@dataclass
+class IonicMelt:
+    positions: np.ndarray  # f64 [N, 3]
+    momenta: np.ndarray
+    masses: np.ndarray
+    charges: np.ndarray
+    species: np.ndarray  # 0 = cation, 1 = anion
+    tril: np.ndarray  # [1, 6]
+    sigma: np.ndarray  # [2, 2] Lorentz-Berthelot
+    epsilon: np.ndarray
+    cutoff: float
+    alpha: float
+    kvec_n: np.ndarray  # [1, n_k, 3]
+    time_step: float
+
+
+def ionic_melt(n_ions=4000, box=40.0, min_sep=2.2, temperature=1200.0, dt_fs=1.0, cutoff=12.0, alpha=0.3, kmax=8,
+               seed=2):
+    """+1/-1 point ions with per-species LJ (eps 0.1 / 0.15 kcal/mol, sigma 2.35 / 4.40 A, LB mixing) in
+    a cubic box; k vectors = the half-space integer box |n|_inf <= kmax (n_x >= 0).  Masses (not given by
+    the configuration) are those of Na and Cl, 22.99 and 35.45 u."""
+    from .units import KILO_CALORIE, MOL
+
+    rng = np.random.default_rng(seed)
+    pos = lattice_positions(rng, n_ions, box, min_sep)
+    species = (np.arange(n_ions) % 2).astype(np.int32)
+    charges = np.where(species == 0, 1.0, -1.0)
+    masses = np.where(species == 0, 22.99, 35.45)
+    kcal = KILO_CALORIE / MOL
+    s = np.array([2.35, 4.40])
+    e = np.array([0.1, 0.15]) * kcal
+    sigma, epsilon = (s[:, None] + s) / 2, np.sqrt(e[:, None] * e)
+    system = np.zeros(n_ions, np.int32)
+    mom = _mb_momenta(rng, masses, np.array([temperature * BOLTZMANN_CONSTANT]), system, 1)
+    m = int(kmax)
+    kn = np.stack(np.meshgrid(np.arange(0, m + 1), np.arange(-m, m + 1), np.arange(-m, m + 1)), -1).reshape(-1, 3)
+    return IonicMelt(pos, mom, masses, charges, species, np.array([[box, 0, box, 0, 0, box]], float), sigma, epsilon,
+                     cutoff, alpha, kn[None].astype(np.int32), dt_fs * FEMTO_SECOND)
