@@ -345,6 +345,26 @@ typedef struct kups_gcmc_args {
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Tensor-core GEMM (tcgen05, BF16 inputs, FP32 accumulation in tensor memory)
+ * used by the learned insertion proposal (no counterpart in the reference;
+ * the proposal enters through the ChangesFn log-ratio of the insertion move,
+ * src/kups/mcmc/moves.py:92-98 and src/kups/core/propagator.py:330-334).
+ *   C[m, n] = act(alpha * sum_k A[m, k] B[n, k] + beta * C[m, n] + bias[n]) * gate'
+ * Operands are addressed element-wise as p[r * s_row + c * s_col] (any
+ * transposition); *_bf16 selects bfloat16 (else float32) storage.
+ * act: 0 none, 1 ReLU, 2 softplus.  gate_kind 1 / 2 multiplies by the ReLU /
+ * softplus derivative of gate[m, n] (backward passes).  c2 (may be NULL) is a
+ * second copy of C with its own strides and type.
+ * ------------------------------------------------------------------------ */
+int32_t kups_gemm_bf16(const void *a, int32_t a_bf16, int64_t sa_row, int64_t sa_col,
+                       const void *b, int32_t b_bf16, int64_t sb_row, int64_t sb_col,
+                       void *c, int32_t c_bf16, int64_t sc_row, int64_t sc_col, void *c2,
+                       int32_t c2_bf16, int64_t sc2_row, int64_t sc2_col, const float *bias,
+                       const float *gate, int32_t gate_kind, int64_t sg_row, int64_t sg_col,
+                       int32_t m, int32_t n, int32_t k, float alpha, float beta, int32_t act,
+                       kups_status *status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

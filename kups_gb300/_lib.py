@@ -90,6 +90,8 @@ SIGNATURES = {
     "kups_md_drift": (_I32, [_P, _P, _P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_thermostat": (_I32, [_P, _P, _P, _P, _P, _P, C.c_uint64, C.c_uint64, _I64, _P]),
     "kups_gcmc_run": (_I32, [C.POINTER(GcmcArgs), _P, _P]),
+    "kups_gemm_bf16": (_I32, [_P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64,
+                               _I64, _P, _P, _I32, _I64, _I64, _I32, _I32, _I32, C.c_float, C.c_float, _I32, _P, _P]),
     "kups_pair_edges": (_I32, [_P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
 }
 

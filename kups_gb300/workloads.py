@@ -168,3 +168,64 @@ def ionic_melt(n_ions=4000, box=40.0, min_sep=2.2, temperature=1200.0, dt_fs=1.0
     kn = np.stack(np.meshgrid(np.arange(0, m + 1), np.arange(-m, m + 1), np.arange(-m, m + 1)), -1).reshape(-1, 3)
     return IonicMelt(pos, mom, masses, charges, species, np.array([[box, 0, box, 0, 0, box]], float), sigma, epsilon,
                      cutoff, alpha, kn[None].astype(np.int32), dt_fs * FEMTO_SECOND)
+
+
+def porous_framework(rng, tril, n_atoms, channel_radius=6.0, jitter=0.2):
+    """Rigid host: a random subset of a fractional grid outside a cylindrical channel
+    along c through the cell centre (positions stored in [0, 1) fractional, as a CIF
+    host is).  2000 sites at >= 2.8 A separation do not fit in a 25 A, 120 degree cell
+    (packing fraction above one), so the grid spacing is the densest that leaves the
+    channel empty."""
+    t = np.asarray(tril, float)
+    L = np.array([[t[0], 0, 0], [t[1], t[2], 0], [t[3], t[4], t[5]]])
+    n = 8
+    while True:
+        g = np.stack(np.meshgrid(*[np.arange(n)] * 3, indexing="ij"), -1).reshape(-1, 3)
+        f = (g + 0.5) / n
+        d = f[:, :2] - 0.5
+        d -= np.round(d)
+        cart = np.concatenate([d, np.zeros((len(d), 1))], 1) @ L
+        keep = np.hypot(cart[:, 0], cart[:, 1]) > channel_radius
+        if keep.sum() >= n_atoms:
+            break
+        n += 1
+    f = f[keep]
+    pick = rng.choice(len(f), size=n_atoms, replace=False)
+    f = f[pick] + rng.uniform(-1, 1, (n_atoms, 3)) * (jitter / np.array([t[0], t[2], t[5]]))
+    return (f % 1.0) @ L
+
+
+def gcmc_co2_framework(n_replicas=1024, n_fw=2000, p_min_bar=0.1, p_max_bar=10.0, temperature=298.0, rc=12.0,
+                       alpha=0.25, precision=1e-6, max_mol=64, seed=3):
+    """Rigid 3-site CO2 in a synthetic rigid framework (4 LJ types, Gaussian charges shifted
+    to net zero), replicas at log-spaced pressures; critical constants of CO2 for the
+    Peng-Robinson fugacity: Tc 303.75 K, Pc 7.84 MPa, omega 0.22394."""
+    from . import gcmc
+    from .ewald import kvecs_from_kmax
+    from .units import PASCAL
+
+    rng = np.random.default_rng(seed)
+    L = np.array([[25.0, 0, 0], [25.0 * np.cos(np.radians(120)), 25.0 * np.sin(np.radians(120)), 0],
+                  [0, 0, 25.0]])
+    tril = np.array([L[0, 0], L[1, 0], L[1, 1], L[2, 0], L[2, 1], L[2, 2]])
+    fw = porous_framework(rng, tril, n_fw)
+    fw_sp = rng.integers(0, 4, n_fw)
+    q = rng.normal(0, 0.3, n_fw)
+    q -= q.mean()
+    sig = np.concatenate([rng.uniform(2.5, 3.5, 4), [2.80, 3.05]])
+    eps = np.concatenate([rng.uniform(20, 80, 4), [27.0, 79.0]]) * BOLTZMANN_CONSTANT
+    sigma, epsilon = gcmc.lorentz_berthelot(sig, eps)
+    kmax = 2 * alpha * np.sqrt(-np.log(precision / 2))
+    kn = kvecs_from_kmax(tril, kmax)
+    pressures = np.logspace(np.log10(p_min_bar), np.log10(p_max_bar), n_replicas) * 1e5
+    kT = temperature * BOLTZMANN_CONSTANT
+    la = np.array([gcmc.peng_robinson_log_fugacity(p, temperature, 7.84e6, 303.75, 0.22394) + np.log(PASCAL)
+                   - np.log(kT) for p in pressures])
+    S = n_replicas
+    return gcmc.GCMCSetup(
+        fw_positions=fw, fw_species=fw_sp, fw_charges=q, fw_start=np.zeros(S, int), fw_count=np.full(S, n_fw),
+        tril=np.repeat(tril[None], S, 0),
+        motif_positions=np.array([[0.0, 0, 0], [1.16, 0, 0], [-1.16, 0, 0]]), motif_species=np.array([4, 5, 5]),
+        motif_charges=np.array([0.70, -0.35, -0.35]), sigma=sigma, epsilon=epsilon, rc_lj=np.full(S, rc),
+        rc_ew=np.full(S, rc), alpha=np.full(S, alpha), kvec_n=np.repeat(kn[None], S, 0),
+        temperature=np.full(S, temperature), log_activity=la, max_mol=max_mol, tail_correction=True)
