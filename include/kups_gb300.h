@@ -4,10 +4,12 @@
  * Conventions shared by every entry point:
  *   - all array pointers are DEVICE pointers owned by the caller; nothing is
  *     allocated or freed by the library (scratch space is passed in as
- *     `workspace`, sized by the matching *_workspace_bytes query);
- *   - `stream` is a cudaStream_t passed as void*; every call is stream-ordered,
- *     never synchronises the device and is safe to capture in a CUDA graph
- *     (it issues only kernel launches and cudaMemsetAsync);
+ *     `workspace`, sized by the matching *_workspace_bytes query, except in
+ *     kups_ewald_recip_static, which uses a fixed array of the library);
+ *   - `stream` is a cudaStream_t passed as void*; every call is stream-ordered
+ *     and never synchronises the device; every call except
+ *     kups_ewald_recip_static is safe to capture in a CUDA graph (it issues
+ *     only kernel launches and cudaMemsetAsync);
  *   - the return value reports host-side validation and launch errors
  *     (KUPS_OK, KUPS_ERR_INVALID, KUPS_ERR_CUDA); device-side conditions
  *     (capacity overflow, non-finite input) are written to the caller's
@@ -235,6 +237,30 @@ int32_t kups_ewald_recip(const double *positions, const double *charges,
                          double coulomb_k, double *energy, double *grad, double *grad_tril,
                          double *structure_factor, void *workspace, size_t workspace_bytes,
                          kups_status *status, void *stream);
+/*
+ * kups_ewald_recip_static — no counterpart in the reference.  The same
+ * computation and outputs as kups_ewald_recip, for callers that cannot
+ * allocate device memory and so cannot pass a workspace (e.g. an FFI handler
+ * that receives only its input and output buffers).  Its scratch is one fixed
+ * device array of KUPS_EWALD_RECIP_STATIC_SCRATCH_BYTES inside the library;
+ * nothing is allocated or freed.
+ *   - The scratch is 120 bytes of cell data per system (rounded up to 256
+ *     bytes) plus 32 bytes per (system, k vector); sizes that need more than
+ *     the array are refused with KUPS_ERR_CAPACITY before anything is
+ *     launched (16 MiB holds, e.g., 512 systems x 1000 k vectors).
+ *   - The first call on each device looks up the array's address with that
+ *     device current; make that first call before any stream capture.
+ *   - The array is shared by all calls on a device and keeps the last call's
+ *     contents; nothing in it needs to start at zero.  Calls that overlap in
+ *     time (other streams or host threads) race on it: order them.
+ */
+#define KUPS_EWALD_RECIP_STATIC_SCRATCH_BYTES ((size_t)16 << 20)
+int32_t kups_ewald_recip_static(const double *positions, const double *charges,
+                                const int32_t *sys_offset, int32_t n_systems,
+                                int32_t max_atoms_per_system, const double *tril,
+                                const int32_t *kvec_n, int32_t n_kvecs, const double *alpha,
+                                double coulomb_k, double *energy, double *grad, double *grad_tril,
+                                double *structure_factor, kups_status *status, void *stream);
 int32_t kups_ewald_self(const double *charges, const int32_t *sys_offset, int32_t n_systems,
                         const double *alpha, double coulomb_k, double *energy, void *stream);
 int32_t kups_pair_edges(const double *positions, const int32_t *system, const int32_t *species,

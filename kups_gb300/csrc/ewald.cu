@@ -21,6 +21,8 @@
 // e^{i theta} is built per atom from per-axis tables e^{2 pi i m f_a},
 // m in [-M, M] (the standard Ewald recurrence), so each (atom, k) costs two
 // complex products.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace kups {
@@ -405,6 +407,82 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
   char *base = (char *)(((uintptr_t)workspace + 255) & ~uintptr_t(255));
   RecipSys *sysp = (RecipSys *)base;
   Coef *coef = (Coef *)(base + align256(sizeof(RecipSys) * (size_t)n_systems));
+  recip_setup_kernel<<<(n_systems + 127) / 128, 128, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
+                                                                   sysp, status);
+  KUPS_CUDA_TRY(cudaMemsetAsync(structure_factor, 0, sizeof(double) * 2 * (size_t)n_systems * n_kvecs, stream));
+  const int chunks = (max_atoms_per_system + kAtomsPerChunk - 1) / kAtomsPerChunk;
+  if (n_kvecs > 0 && chunks > 0) {
+    dim3 g((n_kvecs + kKPerBlock - 1) / kKPerBlock, chunks, n_systems);
+    structure_factor_kernel<<<g, kKPerBlock, 0, stream>>>(positions, charges, sys_offset, kvec_n,
+                                                          n_kvecs, sysp, structure_factor);
+  }
+  recip_energy_kernel<<<n_systems, 256, 0, stream>>>(kvec_n, n_kvecs, alpha, sysp, structure_factor,
+                                                     coulomb_k, coef, energy, grad_tril);
+  if (chunks > 0) {
+    dim3 g(chunks, n_systems);
+    recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
+                                                             n_kvecs, sysp, coef, coulomb_k, grad,
+                                                             grad_tril);
+  }
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// kups_ewald_recip_static: the reciprocal-space computation above with its
+// scratch (per-system cell data, then per-(system, k) coefficients) in one
+// fixed device array instead of a caller-supplied workspace.  It serves
+// callers that have no device allocator to draw a workspace from, e.g. an
+// FFI handler that a host framework hands only its input and output buffers.
+//
+// The array is shared by every call on a device and keeps whatever the last
+// call left in it; every byte a call reads is written earlier in the same
+// call, so nothing in it has to start at zero.  Two calls whose launches
+// overlap in time (different streams, or different host threads) race on it.
+namespace kups {
+namespace {
+constexpr size_t kStaticScratchBytes = KUPS_EWALD_RECIP_STATIC_SCRATCH_BYTES;
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_scratch_mutex;
+void *g_static_scratch_ptr[kStaticMaxDevices] = {};
+}  // namespace
+static __device__ __align__(256) unsigned char g_recip_static_scratch[kStaticScratchBytes];
+}  // namespace kups
+
+extern "C" int32_t kups_ewald_recip_static(const double *positions, const double *charges,
+                                           const int32_t *sys_offset, int32_t n_systems,
+                                           int32_t max_atoms_per_system, const double *tril,
+                                           const int32_t *kvec_n, int32_t n_kvecs,
+                                           const double *alpha, double coulomb_k, double *energy,
+                                           double *grad, double *grad_tril,
+                                           double *structure_factor, kups_status *status,
+                                           void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_systems < 0 || n_kvecs < 0 || max_atoms_per_system < 0) return KUPS_ERR_INVALID;
+  // Sizes beyond the array are refused before anything is touched.
+  if ((size_t)n_systems > kStaticScratchBytes / sizeof(RecipSys)) return KUPS_ERR_CAPACITY;
+  if (n_kvecs > 0 && (size_t)n_systems > kStaticScratchBytes / sizeof(Coef) / (size_t)n_kvecs)
+    return KUPS_ERR_CAPACITY;
+  const size_t sys_bytes = align256(sizeof(RecipSys) * (size_t)n_systems);
+  if (sys_bytes + align256(sizeof(Coef) * (size_t)n_systems * (size_t)n_kvecs) > kStaticScratchBytes)
+    return KUPS_ERR_CAPACITY;
+  if (n_systems == 0) return KUPS_OK;
+  // Once per device, with that device current: look up the array's address.
+  int dev = 0;
+  KUPS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kStaticMaxDevices) return KUPS_ERR_UNSUPPORTED;
+  char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_scratch_mutex);
+    if (g_static_scratch_ptr[dev] == nullptr) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_recip_static_scratch) != cudaSuccess || p == nullptr)
+        return KUPS_ERR_CUDA;
+      g_static_scratch_ptr[dev] = p;
+    }
+    base = (char *)g_static_scratch_ptr[dev];
+  }
+  RecipSys *sysp = (RecipSys *)base;
+  Coef *coef = (Coef *)(base + sys_bytes);
   recip_setup_kernel<<<(n_systems + 127) / 128, 128, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
                                                                    sysp, status);
   KUPS_CUDA_TRY(cudaMemsetAsync(structure_factor, 0, sizeof(double) * 2 * (size_t)n_systems * n_kvecs, stream));
