@@ -354,6 +354,8 @@ typedef struct kups_gcmc_args {
   int64_t *accepted;            /* [S, 5] */
   const kups_gcmc_proposal *proposals; /* [S] or NULL */
   double *out_delta;            /* [S, 4] or NULL */
+  const float *proposal_node;   /* [G^3] learned insertion density (kups_mlp_grid_norm) or NULL */
+  const double *proposal_cdf;   /* [G^3 + 1] */
   float move_cum[3];
   float pad0;
   double coulomb_k;
@@ -366,7 +368,9 @@ typedef struct kups_gcmc_args {
   int32_t n_kvecs;
   int32_t n_steps;
   int32_t history_len;
-  int32_t pad1;
+  int32_t proposal_grid;        /* G; with proposal_node set, insertions draw the molecule's
+                                   centre (atom mean) from the grid density q and add
+                                   -ln(V q) to ln acc, deletions add +ln(V q) */
 } kups_gcmc_args;
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);
@@ -380,8 +384,12 @@ int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *str
  * Operands are addressed element-wise as p[r * s_row + c * s_col] (any
  * transposition); *_bf16 selects bfloat16 (else float32) storage.
  * act: 0 none, 1 ReLU, 2 softplus.  gate_kind 1 / 2 multiplies by the ReLU /
- * softplus derivative of gate[m, n] (backward passes).  c2 (may be NULL) is a
- * second copy of C with its own strides and type.
+ * softplus derivative of gate[m, n] (backward passes); 3 by the softplus
+ * derivative written through the layer's output h = gate[m, n]: 1 - exp(-h).
+ * c2 (may be NULL) is a second copy of C with its own strides and type.
+ * split_k > 1 splits K over CTAs that atomically add alpha * partial into a
+ * float32 C (beta must be 1, no act / bias / gate / c2); zero C first to get
+ * the plain product.
  * ------------------------------------------------------------------------ */
 int32_t kups_gemm_bf16(const void *a, int32_t a_bf16, int64_t sa_row, int64_t sa_col,
                        const void *b, int32_t b_bf16, int64_t sb_row, int64_t sb_col,
@@ -389,7 +397,66 @@ int32_t kups_gemm_bf16(const void *a, int32_t a_bf16, int64_t sa_row, int64_t sa
                        int32_t c2_bf16, int64_t sc2_row, int64_t sc2_col, const float *bias,
                        const float *gate, int32_t gate_kind, int64_t sg_row, int64_t sg_col,
                        int32_t m, int32_t n, int32_t k, float alpha, float beta, int32_t act,
-                       kups_status *status, void *stream);
+                       int32_t split_k, kups_status *status, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Learned insertion proposal (no counterpart in the reference; its density
+ * enters the exchange move's log proposal ratio, the ChangesFn hook of
+ * src/kups/mcmc/moves.py:92-98 summed at src/kups/core/propagator.py:330-334).
+ *
+ * Network (fixed): 64 Fourier features (sin, cos)(2 pi m_j . f) of the
+ * fractional position f for 32 integer vectors freq[j] = m_j, three softplus
+ * layers of width 256 on the tensor cores (bfloat16 operands, float32
+ * accumulation), linear output g(f).  Flat float32 parameters, offsets:
+ *   W1 [256, 64] at 0, b1 at 16384, W2 [256, 256] at 16640, b2 at 82176,
+ *   W3 [256, 256] at 82432, b3 at 147968, w4 [256] at 148224, b4 at 148480.
+ * Training minimises the noise-contrastive loss over equal halves of data
+ * and uniform points, L = mean softplus(-g) (data) + mean softplus(g)
+ * (uniform), whose minimiser is g = ln p_data on the unit cube.
+ * ------------------------------------------------------------------------ */
+#define KUPS_MLP_PARAMS 148481
+typedef struct kups_mlp {
+  float *param;        /* [KUPS_MLP_PARAMS] float32 master copy */
+  void *param_bf16;    /* [KUPS_MLP_PARAMS] bfloat16 copy the GEMMs read */
+  float *grad;         /* [KUPS_MLP_PARAMS] accumulated by kups_mlp_bwd, zeroed by kups_mlp_adam */
+  float *adam_m;       /* [KUPS_MLP_PARAMS] */
+  float *adam_v;       /* [KUPS_MLP_PARAMS] */
+  const int32_t *freq; /* [32, 3] integer frequency vectors */
+} kups_mlp;
+
+/* workspace for kups_mlp_fwd / kups_mlp_bwd / kups_mlp_grid_norm over n points
+ * (forward passes run in chunks of at most 65536 points) */
+size_t kups_mlp_workspace_bytes(int64_t n_points);
+/* weights uniform with variance 1 / fan_in from Philox(seed), biases, moments, gradient zero */
+int32_t kups_mlp_init(const kups_mlp *net, uint64_t seed, void *stream);
+/* g [n] (float32) at fractional points x [n, 3] (float64) */
+int32_t kups_mlp_fwd(const kups_mlp *net, const double *x, int64_t n, float *g, void *workspace,
+                     size_t workspace_bytes, kups_status *status, void *stream);
+/* training batch: rows [0, batch/2) drawn with replacement from data [n_data, 3]
+ * (label 1), rows [batch/2, batch) uniform in [0, 1)^3 (label 0); batch even */
+int32_t kups_mlp_nce_batch(const double *data, int64_t n_data, int32_t batch, uint64_t seed,
+                           uint64_t step, double *x, float *label, void *stream);
+/* forward + backward of the loss over n <= 65536 labelled points: adds dL/dparam
+ * to net->grad and L to *loss (loss may be NULL) */
+int32_t kups_mlp_bwd(const kups_mlp *net, const double *x, const float *label, int32_t n, float *loss,
+                     void *workspace, size_t workspace_bytes, kups_status *status, void *stream);
+/* Adam step t >= 1 (Kingma & Ba); refreshes param_bf16 and zeroes grad */
+int32_t kups_mlp_adam(const kups_mlp *net, int64_t t, float lr, float beta1, float beta2, float eps,
+                      void *stream);
+/* Grid density for the sampler: node[(i G + j) G + k] = exp(g(i/G, j/G, k/G) - max g)
+ * + floor_frac * mean (so every cell has positive mass), cdf [G^3 + 1] = running
+ * sums of cell masses (mean of the 8 corners), float64.  2 <= G <= 256. */
+int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float floor_frac, float *node,
+                           double *cdf, void *workspace, size_t workspace_bytes, kups_status *status,
+                           void *stream);
+/* n exact draws f [n, 3] from the piecewise-trilinear grid density (cell by its
+ * mass, corner by its value, per-axis sqrt transform) with ln q_f(f), the
+ * density in fractional measure (the insertion's log ratio is -ln q_f) */
+int32_t kups_proposal_sample(const float *node, const double *cdf, int32_t grid, int64_t n,
+                             uint64_t seed, double *f, double *log_q, void *stream);
+/* ln q_f at fractional points f [n, 3] (any periodic image) */
+int32_t kups_proposal_log_density(const float *node, const double *cdf, int32_t grid, const double *f,
+                                  int64_t n, double *log_q, void *stream);
 
 #ifdef __cplusplus
 }

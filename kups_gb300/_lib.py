@@ -63,11 +63,17 @@ class GcmcArgs(C.Structure):
         ("kT", C.c_void_p), ("log_activity", C.c_void_p), ("energy", C.c_void_p), ("width", C.c_void_p),
         ("width_max", C.c_void_p), ("history", C.c_void_p), ("history_index", C.c_void_p),
         ("attempted", C.c_void_p), ("accepted", C.c_void_p), ("proposals", C.c_void_p), ("out_delta", C.c_void_p),
+        ("proposal_node", C.c_void_p), ("proposal_cdf", C.c_void_p),
         ("move_cum", C.c_float * 3), ("pad0", C.c_float), ("coulomb_k", C.c_double), ("seed", C.c_uint64),
         ("step0", C.c_uint64), ("n_systems", C.c_int32), ("max_mol", C.c_int32), ("atoms_per_mol", C.c_int32),
         ("n_species", C.c_int32), ("n_kvecs", C.c_int32), ("n_steps", C.c_int32), ("history_len", C.c_int32),
-        ("pad1", C.c_int32),
+        ("proposal_grid", C.c_int32),
     ]
+
+
+class Mlp(C.Structure):
+    _fields_ = [("param", C.c_void_p), ("param_bf16", C.c_void_p), ("grad", C.c_void_p), ("adam_m", C.c_void_p),
+                ("adam_v", C.c_void_p), ("freq", C.c_void_p)]
 
 
 # Every symbol declared in include/kups_gb300.h: name -> (restype, argtypes)
@@ -91,8 +97,17 @@ SIGNATURES = {
     "kups_md_drift": (_I32, [_P, _P, _P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_thermostat": (_I32, [_P, _P, _P, _P, _P, _P, C.c_uint64, C.c_uint64, _I64, _P]),
     "kups_gcmc_run": (_I32, [C.POINTER(GcmcArgs), _P, _P]),
+    "kups_mlp_workspace_bytes": (_SZ, [_I64]),
+    "kups_mlp_init": (_I32, [_P, C.c_uint64, _P]),
+    "kups_mlp_fwd": (_I32, [_P, _P, _I64, _P, _P, _SZ, _P, _P]),
+    "kups_mlp_nce_batch": (_I32, [_P, _I64, _I32, C.c_uint64, C.c_uint64, _P, _P, _P]),
+    "kups_mlp_bwd": (_I32, [_P, _P, _P, _I32, _P, _P, _SZ, _P, _P]),
+    "kups_mlp_adam": (_I32, [_P, _I64, C.c_float, C.c_float, C.c_float, C.c_float, _P]),
+    "kups_mlp_grid_norm": (_I32, [_P, _I32, C.c_float, _P, _P, _P, _SZ, _P, _P]),
+    "kups_proposal_sample": (_I32, [_P, _P, _I32, _I64, C.c_uint64, _P, _P, _P]),
+    "kups_proposal_log_density": (_I32, [_P, _P, _I32, _P, _I64, _P, _P]),
     "kups_gemm_bf16": (_I32, [_P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64,
-                               _I64, _P, _P, _I32, _I64, _I64, _I32, _I32, _I32, C.c_float, C.c_float, _I32, _P, _P]),
+                               _I64, _P, _P, _I32, _I64, _I64, _I32, _I32, _I32, C.c_float, C.c_float, _I32, _I32, _P, _P]),
     "kups_pair_edges": (_I32, [_P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
 }
 

@@ -25,6 +25,7 @@
 // n_a == 1), and intramolecular pairs are excluded on the minimum image only.
 // Pair arithmetic float32, energy differences and the log acceptance float64.
 #include "common.cuh"
+#include "proposal.cuh"
 
 namespace kups {
 namespace {
@@ -53,6 +54,7 @@ struct StepShared {
   int accept;
   double log_p;
   double de_total;
+  double ln_ratio;  // log proposal ratio of the learned insertion density (0 when uniform)
 };
 
 __device__ inline void frac32(const float inv[6], float x, float y, float z, float f[3]) {
@@ -72,6 +74,23 @@ __device__ inline void wrap32(const float L[6], const float inv[6], float c[3]) 
   frac32(inv, c[0], c[1], c[2], f);
   for (int a = 0; a < 3; ++a) f[a] = (f[a] + 0.5f) - floorf(f[a] + 0.5f) - 0.5f;
   cart32(L, f, c);
+}
+
+struct F3 {
+  double v[3];
+};
+
+// Fractional coordinates of a molecule's atom mean (atoms unwrapped against atom 0).
+__device__ inline F3 anchor_frac(const float4 *p, int apm, const float L[6], const float inv[6]) {
+  float m[3] = {0.f, 0.f, 0.f};
+  for (int i = 0; i < apm; ++i) {
+    float d[3] = {p[i].x - p[0].x, p[i].y - p[0].y, p[i].z - p[0].z};
+    wrap32(L, inv, d);
+    for (int c = 0; c < 3; ++c) m[c] += d[c];
+  }
+  float f[3];
+  frac32(inv, p[0].x + m[0] / apm, p[0].y + m[1] / apm, p[0].z + m[2] / apm, f);
+  return F3{{(double)f[0], (double)f[1], (double)f[2]}};
 }
 
 __device__ inline U4 rng4(uint64_t seed, uint64_t stream, uint64_t ctr) {
@@ -282,6 +301,7 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
   const double *pk = a.prefactor + (int64_t)s * nk;
   const int32_t *kn = a.kvec_n + (int64_t)s * nk * 3;
 
+  const bool learned = a.proposal_node != nullptr;
   for (int step = 0; step < a.n_steps; ++step) {
     const uint64_t ctr = a.step0 + (uint64_t)step;
     // ---------------------------------------------------------------- proposal (thread 0)
@@ -305,6 +325,7 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
       sh.kind = kind;
       sh.has_old = 0;
       sh.has_new = 0;
+      sh.ln_ratio = 0.0;
       int mol = -1;
       if (kind == 3) {
         mol = nmol;  // next free slot
@@ -380,12 +401,26 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
         } else if (kind == 3) {  // insertion: template @ R + uniform offset, wrap
           float q[4];
           shoemake(u01(r2.x), u01(r2.y), u01(r2.z), q);
-          const float fo[3] = {u01(r3.x), u01(r3.y), u01(r3.z)};
+          float fo[3] = {u01(r3.x), u01(r3.y), u01(r3.z)};
+          float centre[3] = {0.f, 0.f, 0.f};
+          if (learned) {
+            // the template's atom mean goes to a point drawn from the grid density
+            const double ua[3] = {u32_open0(r3.x), u32_open0(r3.y), u32_open0(r3.z)};
+            double fd[3];
+            sh.ln_ratio = -grid_sample(a.proposal_node, a.proposal_cdf, a.proposal_grid, u53(r1.x, r1.y),
+                                       u53(r1.z, r1.w), ua, fd);
+            for (int c = 0; c < 3; ++c) fo[c] = (float)fd[c];
+            for (int i = 0; i < apm; ++i) {
+              centre[0] += motif[i].x / apm;
+              centre[1] += motif[i].y / apm;
+              centre[2] += motif[i].z / apm;
+            }
+          }
           float shift[3];
           cart32(Lf, fo, shift);
           for (int i = 0; i < apm; ++i) {
             const float4 m = motif[i];
-            const float v[3] = {m.x, m.y, m.z};
+            const float v[3] = {m.x - centre[0], m.y - centre[1], m.z - centre[2]};
             float o[3];
             qrot(q, v, o);
             float c[3] = {o[0] + shift[0], o[1] + shift[1], o[2] + shift[2]};
@@ -394,6 +429,12 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
           }
         }
       }
+      if (learned && a.proposals != nullptr && kind == 3 && sh.has_new)
+        sh.ln_ratio = -grid_log_q(a.proposal_node, a.proposal_cdf, a.proposal_grid,
+                                  anchor_frac(sh.new_pos, apm, Lf, If).v);
+      if (learned && kind == 4 && sh.has_old)
+        sh.ln_ratio = grid_log_q(a.proposal_node, a.proposal_cdf, a.proposal_grid,
+                                 anchor_frac(sh.old_pos, apm, Lf, If).v);
     }
     __syncthreads();
     const int has_old = sh.has_old, has_new = sh.has_new, mol = sh.mol, kind = sh.kind;
@@ -489,7 +530,7 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
           de += tail_energy(c1, nsp, tc) - tail_energy(c0, nsp, tc);
         }
       }
-      double logp = -de / kT;
+      double logp = -de / kT + sh.ln_ratio;
       if (n_new != n_old) {
         const double lnfv = a.log_activity[s] + log(volume);
         logp += (n_new - n_old) * lnfv + lgamma((double)n_old + 1.0) - lgamma((double)n_new + 1.0);
@@ -576,6 +617,8 @@ extern "C" int32_t kups_gcmc_run(const kups_gcmc_args *a, kups_status *status, v
       a->atoms_per_mol > kMaxApm || a->n_species <= 0 || a->n_species > kMaxSpeciesMC ||
       a->n_kvecs < 0 || a->n_kvecs > kMaxKVec || a->history_len <= 0 || a->history_len > 128 ||
       a->max_mol < 0)
+    return KUPS_ERR_INVALID;
+  if (a->proposal_node != nullptr && (a->proposal_cdf == nullptr || a->proposal_grid < 2 || a->proposal_grid > 256))
     return KUPS_ERR_INVALID;
   if (a->n_systems == 0 || a->n_steps == 0) return KUPS_OK;
   gcmc_kernel<<<a->n_systems, kThreads, 0, (cudaStream_t)stream>>>(*a, status);

@@ -5,7 +5,8 @@
 // src/kups/core/propagator.py:330-334).
 //
 // GEMM: C[M, N] = act(alpha * A[M, K] . B[N, K]^T + bias[N]) with arbitrary
-// element strides for A, B and C (so transposed operands need no copies).
+// element strides for A, B and C (so transposed operands need no copies);
+// split-K (grid z) for the weight gradients, whose K is the batch.
 // One CTA computes a 128 x BN tile: four warps stage K-chunks of 64 from
 // global memory into shared memory in the canonical no-swizzle K-major
 // layout (8-row x 16-byte core matrices), one thread issues
@@ -16,7 +17,10 @@
 // tensor memory and returns.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "common.cuh"
+#include "proposal.cuh"
 
 namespace kups {
 namespace {
@@ -94,7 +98,9 @@ struct GemmArgs {
   float alpha, beta;  // C = alpha * AB^T (+ beta * C)
   int act;            // 0 none, 1 relu, 2 softplus
   int a_bf16, b_bf16, c_bf16, c2_bf16;
-  int gate_kind;      // 0 none, 1: multiply by relu'(gate) (gate > 0), 2: by softplus'(gate) = sigmoid
+  int gate_kind;      // 0 none, 1: multiply by relu'(gate) (gate > 0), 2: by softplus'(gate) = sigmoid,
+                      // 3: by softplus' expressed through its output h = softplus(z): 1 - exp(-h)
+  int split_k;        // > 1: blockIdx.z takes a slice of K and atomically adds alpha * partial to C
 };
 
 template <int BN>
@@ -120,13 +126,18 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
   const uint32_t idesc = make_idesc(kBM, BN);
   uint32_t phase = 0;
   bool ok = true;
-  const int nk = (g.k + kBK - 1) / kBK;
-  for (int kc = 0; kc < nk && ok; ++kc) {
+  const int nk_all = (g.k + kBK - 1) / kBK;
+  const int per_split = (nk_all + g.split_k - 1) / g.split_k;
+  const int kc_begin = blockIdx.z * per_split;
+  const int kc_end = min(nk_all, kc_begin + per_split);
+  // walk the staging loops along whichever operand index has unit stride
+  const bool a_rows = g.sar == 1 && g.sac != 1, b_rows = g.sbr == 1 && g.sbc != 1;
+  for (int kc = kc_begin; kc < kc_end && ok; ++kc) {
     const int k0 = kc * kBK;
     // stage A (128 x 64) and B (BN x 64) as bf16 core matrices: element (r, kk) at
     // ((r / 8) * 8 + kk / 8) * 64 + (r % 8) * 8 + kk % 8   (elements)
     for (int e = tid; e < kBM * kBK; e += kGemmThreads) {
-      const int r = e / kBK, kk = e % kBK;
+      const int r = a_rows ? e % kBM : e / kBK, kk = a_rows ? e / kBM : e % kBK;
       const int gr = m0 + r, gk = k0 + kk;
       float v = 0.f;
       if (gr < g.m && gk < g.k)
@@ -134,7 +145,7 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
       sa[((r >> 3) * (kBK / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7)] = __float2bfloat16(v);
     }
     for (int e = tid; e < BN * kBK; e += kGemmThreads) {
-      const int r = e / kBK, kk = e % kBK;
+      const int r = b_rows ? e % BN : e / kBK, kk = b_rows ? e / BN : e % kBK;
       const int gr = n0 + r, gk = k0 + kk;
       float v = 0.f;
       if (gr < g.n && gk < g.k)
@@ -149,7 +160,7 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
         // K step of 16 = two core matrices along K = 256 bytes
         const uint64_t ad = make_sdesc(smem_u32(sa) + ks * 256, 128, (kBK / 8) * 128);
         const uint64_t bd = make_sdesc(smem_u32(sb) + ks * 256, 128, (kBK / 8) * 128);
-        const uint32_t accumulate = (kc > 0 || ks > 0) ? 1u : 0u;
+        const uint32_t accumulate = (kc > kc_begin || ks > 0) ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
@@ -166,7 +177,7 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
   }
   if (!ok) {
     if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
-  } else {
+  } else if (kc_begin < kc_end) {  // an empty K slice holds no accumulator
     // epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (rows), 16 columns at a time
     const int row = m0 + warp * 32 + lane;
     for (int c0 = 0; c0 < BN; c0 += 16) {
@@ -184,6 +195,10 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
           const int col = n0 + c0 + i;
           if (col >= g.n) break;
           float v = g.alpha * __uint_as_float(r[i]);
+          if (g.split_k > 1) {
+            atomicAdd((float *)g.c + (int64_t)row * g.scr + (int64_t)col * g.scc, v);
+            continue;
+          }
           if (g.beta != 0.f) {
             const int64_t o = (int64_t)row * g.scr + (int64_t)col * g.scc;
             v += g.beta * (g.c_bf16 ? __bfloat162float(((__nv_bfloat16 *)g.c)[o]) : ((float *)g.c)[o]);
@@ -191,7 +206,9 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
           if (g.bias) v += g.bias[col];
           if (g.gate_kind) {
             const float pre = g.gate[(int64_t)row * g.sgr + (int64_t)col * g.sgc];
-            v *= g.gate_kind == 1 ? (pre > 0.f ? 1.f : 0.f) : 1.f / (1.f + expf(-pre));
+            v *= g.gate_kind == 1 ? (pre > 0.f ? 1.f : 0.f)
+                 : g.gate_kind == 2 ? 1.f / (1.f + expf(-pre))
+                                    : -expm1f(-pre);
           }
           v = act_fn(v, g.act);
           const int64_t o = (int64_t)row * g.scr + (int64_t)col * g.scc;
@@ -218,9 +235,398 @@ template <int BN>
 int32_t launch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t stream) {
   const size_t smem = (size_t)(kBM + BN) * kBK * 2 + 64;
   KUPS_CUDA_TRY(cudaFuncSetAttribute(gemm_tcgen05_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((g.m + kBM - 1) / kBM, (g.n + BN - 1) / BN);
+  dim3 grid((g.m + kBM - 1) / kBM, (g.n + BN - 1) / BN, g.split_k);
   gemm_tcgen05_kernel<BN><<<grid, kGemmThreads, smem, stream>>>(g, status);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+int32_t dispatch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t st) {
+  if (g.n <= 64) return launch_gemm<64>(g, status, st);
+  if (g.n <= 128) return launch_gemm<128>(g, status, st);
+  return launch_gemm<256>(g, status, st);
+}
+
+// Row-major operand helper for the network's own GEMM calls.
+struct Op {
+  const void *p;
+  int bf16;
+  int64_t sr, sc;
+};
+
+int32_t gemm_call(Op a, Op b, void *c, int64_t scr, int64_t scc, void *c2, const float *bias, const float *gate,
+                  int gate_kind, int m, int n, int k, float beta, int act, int split, kups_status *status,
+                  cudaStream_t st) {
+  GemmArgs g;
+  g.a = a.p; g.b = b.p; g.c = c; g.c2 = c2; g.bias = bias; g.gate = gate;
+  g.sar = a.sr; g.sac = a.sc; g.sbr = b.sr; g.sbc = b.sc; g.scr = scr; g.scc = scc;
+  g.sc2r = scr; g.sc2c = scc; g.sgr = scr; g.sgc = scc;
+  g.m = m; g.n = n; g.k = k; g.alpha = 1.f; g.beta = beta; g.act = act;
+  g.a_bf16 = a.bf16; g.b_bf16 = b.bf16; g.c_bf16 = 0; g.c2_bf16 = 1; g.gate_kind = gate_kind;
+  g.split_k = split;
+  return dispatch_gemm(g, status, st);
+}
+
+// ============================================================================
+// Learned insertion proposal: network, training and grid density.
+//
+// Fixed architecture: 64 Fourier features of the fractional position f,
+// (sin, cos)(2 pi m_j . f) for 32 integer vectors m_j, three softplus layers of
+// width 256 (tensor-core GEMMs, bfloat16 operands, float32 accumulation) and
+// a linear output g(f).  Parameters are one flat float32 array at the kOff*
+// offsets plus a bfloat16 copy read by the GEMMs.  Each layer's output h is
+// stored in float32 (the head and the gates read it) and, where it is the
+// next GEMM's operand, in bfloat16.  Training minimises the noise-contrastive
+// loss with equal halves of data and uniform points,
+//   L = (1/n) [sum_data softplus(-g) + sum_uniform softplus(g)],
+// whose minimiser is g(f) = ln p_data(f) for f uniform on the unit cube.
+constexpr int kFreq = 32, kIn = 2 * kFreq, kHid = 256;
+constexpr int64_t kOffW1 = 0, kOffB1 = kOffW1 + kHid * kIn, kOffW2 = kOffB1 + kHid, kOffB2 = kOffW2 + kHid * kHid,
+                  kOffW3 = kOffB2 + kHid, kOffB3 = kOffW3 + kHid * kHid, kOffW4 = kOffB3 + kHid,
+                  kOffB4 = kOffW4 + kHid, kParams = kOffB4 + 1;
+static_assert(kParams == KUPS_MLP_PARAMS, "parameter layout");
+constexpr int64_t kChunk = 65536;  // points per forward pass over the workspace
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct MlpWork {
+  __nv_bfloat16 *feat, *h1b, *h2b;
+  float *h1, *h2, *h3, *dza, *dzb, *g;
+};
+
+MlpWork carve(void *ws, int64_t c) {
+  char *p = (char *)(((uintptr_t)ws + 255) & ~uintptr_t(255));
+  MlpWork w;
+  auto take = [&](size_t bytes) {
+    char *q = p;
+    p += align256(bytes);
+    return (void *)q;
+  };
+  w.feat = (__nv_bfloat16 *)take(2 * (size_t)c * kIn);
+  w.h1b = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.h2b = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.h1 = (float *)take(4 * (size_t)c * kHid);
+  w.h2 = (float *)take(4 * (size_t)c * kHid);
+  w.h3 = (float *)take(4 * (size_t)c * kHid);
+  w.dza = (float *)take(4 * (size_t)c * kHid);
+  w.dzb = (float *)take(4 * (size_t)c * kHid);
+  w.g = (float *)take(4 * (size_t)c);
+  return w;
+}
+
+size_t work_bytes(int64_t c) {
+  return align256(2 * (size_t)c * kIn) + 2 * align256(2 * (size_t)c * kHid) + 5 * align256(4 * (size_t)c * kHid) +
+         align256(4 * (size_t)c) + 256;
+}
+
+__device__ inline float warp_sum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ inline float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+
+// Features of point row0 + r: from x (fractional, f64 [., 3]) or, with x null,
+// of grid node row0 + r of a grid^3 lattice.
+__global__ void features_kernel(const double *x, int64_t row0, int64_t n, int grid, const int32_t *freq,
+                                __nv_bfloat16 *feat) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double f[3];
+  if (x != nullptr) {
+    for (int a = 0; a < 3; ++a) f[a] = x[3 * (row0 + r) + a];
+  } else {
+    const int64_t v = row0 + r, g2 = (int64_t)grid * grid;
+    f[0] = (double)(v / g2) / grid;
+    f[1] = (double)((v / grid) % grid) / grid;
+    f[2] = (double)(v % grid) / grid;
+  }
+  __nv_bfloat162 *o = reinterpret_cast<__nv_bfloat162 *>(feat + r * kIn);
+  for (int j = 0; j < kFreq; ++j) {
+    double t = freq[3 * j] * f[0] + freq[3 * j + 1] * f[1] + freq[3 * j + 2] * f[2];
+    t -= rint(t);
+    float sn, cs;
+    sincospif(2.0f * (float)t, &sn, &cs);
+    o[j] = __floats2bfloat162_rn(sn, cs);
+  }
+}
+
+// Equal halves: rows [0, batch/2) are data points drawn with replacement,
+// rows [batch/2, batch) uniform points; Philox keyed by (seed, step, row).
+__global__ void nce_batch_kernel(const double *data, int64_t n_data, int64_t batch, uint64_t seed, uint64_t step,
+                                 double *x, float *label) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= batch) return;
+  const U4 c{(uint32_t)r, (uint32_t)(r >> 32), (uint32_t)step, (uint32_t)(step >> 32)};
+  const U4 w = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  if (r < batch / 2) {
+    const uint64_t idx = ((((uint64_t)w.x) << 32) | w.y) % (uint64_t)n_data;
+    for (int a = 0; a < 3; ++a) x[3 * r + a] = data[3 * idx + a];
+    label[r] = 1.f;
+  } else {
+    x[3 * r] = w.x * (1.0 / 4294967296.0);
+    x[3 * r + 1] = w.y * (1.0 / 4294967296.0);
+    x[3 * r + 2] = w.z * (1.0 / 4294967296.0);
+    label[r] = 0.f;
+  }
+}
+
+// g = h3 . w4 + b4, one warp per row.
+__global__ void head_kernel(const float *h, int64_t n, const float *w4, const float *b4, float *g) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (row >= n) return;
+  float acc = 0.f;
+  for (int j = lane; j < kHid; j += 32) acc = fmaf(h[row * kHid + j], w4[j], acc);
+  acc = warp_sum(acc);
+  if (lane == 0) g[row] = acc + b4[0];
+}
+
+// Head forward + loss + first backward step, 8 warps per block, a warp per row:
+//   dL/dg = (sigmoid(g) - y) / n,  dz3 = dL/dg * w4 * (1 - exp(-h3)),
+//   grad_w4 += sum_rows dL/dg h3,  grad_b4 += sum_rows dL/dg,  loss += L.
+__global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n, const float *w4, const float *b4,
+                                                       const float *label, float *dz, float *grad_w4,
+                                                       float *grad_b4, float *loss) {
+  __shared__ float red_w[8][kHid];
+  __shared__ float red_b[8], red_l[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float wl[8], dw[8];
+  for (int j = 0; j < 8; ++j) {
+    wl[j] = w4[lane + 32 * j];
+    dw[j] = 0.f;
+  }
+  float db = 0.f, ls = 0.f;
+  const float inv_n = 1.f / (float)n;
+  for (int64_t row = (int64_t)blockIdx.x * 8 + warp; row < n; row += (int64_t)gridDim.x * 8) {
+    const float *hr = h + row * kHid;
+    float hv[8], acc = 0.f;
+    for (int j = 0; j < 8; ++j) {
+      hv[j] = hr[lane + 32 * j];
+      acc = fmaf(hv[j], wl[j], acc);
+    }
+    const float gg = warp_sum(acc) + b4[0];
+    const float y = label[row];
+    const float dg = (1.f / (1.f + expf(-gg)) - y) * inv_n;
+    if (lane == 0) {
+      ls += y > 0.5f ? softplus(-gg) : softplus(gg);
+      db += dg;
+    }
+    for (int j = 0; j < 8; ++j) {
+      dw[j] = fmaf(dg, hv[j], dw[j]);
+      dz[row * kHid + lane + 32 * j] = dg * wl[j] * -expm1f(-hv[j]);
+    }
+  }
+  for (int j = 0; j < 8; ++j) red_w[warp][lane + 32 * j] = dw[j];
+  if (lane == 0) {
+    red_b[warp] = db;
+    red_l[warp] = ls;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < kHid; c += blockDim.x) {
+    float s = 0.f;
+    for (int w = 0; w < 8; ++w) s += red_w[w][c];
+    atomicAdd(&grad_w4[c], s);
+  }
+  if (threadIdx.x == 0) {
+    float s = 0.f, l = 0.f;
+    for (int w = 0; w < 8; ++w) {
+      s += red_b[w];
+      l += red_l[w];
+    }
+    atomicAdd(grad_b4, s);
+    if (loss != nullptr) atomicAdd(loss, l * inv_n);
+  }
+}
+
+// out[c] += sum_r z[r, c] over 256 columns (bias gradients); thread = column.
+__global__ void __launch_bounds__(kHid) colsum_kernel(const float *z, int64_t n, float *out) {
+  const int c = threadIdx.x;
+  const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
+  if (r0 >= r1) return;
+  float s = 0.f;
+  for (int64_t r = r0; r < r1; ++r) s += z[r * kHid + c];
+  atomicAdd(&out[c], s);
+}
+
+// Adam (Kingma & Ba 2015) with bias corrections c1 = 1 / (1 - beta1^t),
+// c2 = 1 / (1 - beta2^t); refreshes the bfloat16 copy and zeroes the gradient.
+__global__ void adam_kernel(float *p, __nv_bfloat16 *pb, float *g, float *m, float *v, int64_t n, float lr,
+                            float b1, float b2, float eps, float c1, float c2) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  p[i] = pi;
+  pb[i] = __float2bfloat16(pi);
+  g[i] = 0.f;
+}
+
+// Weights uniform with variance 1 / fan_in (Philox keyed by (seed, index)),
+// biases zero; optimiser state and gradients zero.
+__global__ void init_kernel(float *p, __nv_bfloat16 *pb, float *g, float *m, float *v, uint64_t seed) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  float fan = 0.f;
+  if (i < kOffB1) fan = kIn;
+  else if ((i >= kOffW2 && i < kOffB2) || (i >= kOffW3 && i < kOffB3) || (i >= kOffW4 && i < kOffB4)) fan = kHid;
+  float val = 0.f;
+  if (fan > 0.f) {
+    const U4 c{(uint32_t)i, (uint32_t)(i >> 32), 0x6d6c70u, 0u};
+    const U4 w = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const float u = (float)(w.x >> 8) * (1.0f / 16777216.0f);
+    val = (2.f * u - 1.f) * sqrtf(3.f / fan);
+  }
+  p[i] = val;
+  pb[i] = __float2bfloat16(val);
+  g[i] = 0.f;
+  m[i] = 0.f;
+  v[i] = 0.f;
+}
+
+__device__ inline float block_max1024(float v, float *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float w = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+    if (threadIdx.x == 0) red[0] = w;
+  }
+  __syncthreads();
+  const float r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ inline double block_sum_d(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double w = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (threadIdx.x == 0) red[0] = w;
+  }
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// node holds g on entry; on exit d = exp(g - max g) + floor_frac * mean(exp(g - max g)).
+// One block of 1024 threads.
+__global__ void __launch_bounds__(1024) grid_normalise_kernel(float *node, int64_t n, float floor_frac,
+                                                              kups_status *status) {
+  __shared__ float redf[32];
+  __shared__ double redd[32];
+  float mx = -INFINITY;
+  int bad = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const float v = node[i];
+    if (!isfinite(v)) bad = 1;
+    mx = fmaxf(mx, v);
+  }
+  if (__syncthreads_or(bad)) {
+    if (threadIdx.x == 0) status_error(status, KUPS_ERR_NONFINITE, -1);
+    return;
+  }
+  mx = block_max1024(mx, redf);
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const float e = expf(node[i] - mx);
+    node[i] = e;
+    s += e;
+  }
+  const double mean = block_sum_d(s, redd) / (double)n;
+  const float fl = (float)(floor_frac * mean);
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) node[i] += fl;
+}
+
+// cdf[c] = sum_{c' < c} mass(c'), mass = mean of the cell's 8 corners (float64);
+// one block of 1024 threads, each owning a contiguous run of cells.
+__global__ void __launch_bounds__(1024) grid_cdf_kernel(const float *node, int g, double *cdf) {
+  __shared__ double part[1024];
+  const int64_t n = (int64_t)g * g * g;
+  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
+  const int64_t c0 = (int64_t)threadIdx.x * per, c1 = min(n, c0 + per);
+  auto mass = [&](int64_t c) {
+    const int i = (int)(c / ((int64_t)g * g)), j = (int)((c / g) % g), k = (int)(c % g);
+    double d[8];
+    grid_corners(node, g, i, j, k, d);
+    double s = 0.0;
+    for (int b = 0; b < 8; ++b) s += d[b];
+    return s * 0.125;
+  };
+  double local = 0.0;
+  for (int64_t c = c0; c < c1; ++c) local += mass(c);
+  part[threadIdx.x] = local;
+  __syncthreads();
+  // inclusive Hillis-Steele scan over the 1024 partial sums
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    const double add = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0.0;
+    __syncthreads();
+    part[threadIdx.x] += add;
+    __syncthreads();
+  }
+  double run = part[threadIdx.x] - local;
+  for (int64_t c = c0; c < c1; ++c) {
+    cdf[c] = run;
+    run += mass(c);
+  }
+  if (c0 < c1 && c1 == n) cdf[n] = run;
+}
+
+__global__ void proposal_sample_kernel(const float *node, const double *cdf, int g, int64_t n, uint64_t seed,
+                                       double *f, double *lnq) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const U4 a = philox4x32_10(U4{(uint32_t)i, (uint32_t)(i >> 32), 1u, 0u}, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const U4 b = philox4x32_10(U4{(uint32_t)i, (uint32_t)(i >> 32), 2u, 0u}, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const double ua[3] = {u32_open0(b.x), u32_open0(b.y), u32_open0(b.z)};
+  double x[3];
+  const double l = grid_sample(node, cdf, g, u53(a.x, a.y), u53(a.z, a.w), ua, x);
+  for (int k = 0; k < 3; ++k) f[3 * i + k] = x[k];
+  lnq[i] = l;
+}
+
+__global__ void proposal_density_kernel(const float *node, const double *cdf, int g, const double *f, int64_t n,
+                                        double *lnq) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x[3] = {f[3 * i], f[3 * i + 1], f[3 * i + 2]};
+  lnq[i] = grid_log_q(node, cdf, g, x);
+}
+
+inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// Forward pass of rows [row0, row0 + c) into w (activations) and g_out.
+int32_t forward_chunk(const kups_mlp *net, const double *x, int64_t row0, int64_t c, int grid, const MlpWork &w,
+                      float *g_out, kups_status *status, cudaStream_t st) {
+  const __nv_bfloat16 *pb = (const __nv_bfloat16 *)net->param_bf16;
+  const float *p = net->param;
+  features_kernel<<<blocks(c, 256), 256, 0, st>>>(x, row0, c, grid, net->freq, w.feat);
+  int32_t rc;
+  rc = gemm_call(Op{w.feat, 1, kIn, 1}, Op{pb + kOffW1, 1, kIn, 1}, w.h1, kHid, 1, w.h1b, p + kOffB1, nullptr, 0,
+                 (int)c, kHid, kIn, 0.f, 2, 1, status, st);
+  if (rc) return rc;
+  rc = gemm_call(Op{w.h1b, 1, kHid, 1}, Op{pb + kOffW2, 1, kHid, 1}, w.h2, kHid, 1, w.h2b, p + kOffB2, nullptr, 0,
+                 (int)c, kHid, kHid, 0.f, 2, 1, status, st);
+  if (rc) return rc;
+  rc = gemm_call(Op{w.h2b, 1, kHid, 1}, Op{pb + kOffW3, 1, kHid, 1}, w.h3, kHid, 1, nullptr, p + kOffB3, nullptr, 0,
+                 (int)c, kHid, kHid, 0.f, 2, 1, status, st);
+  if (rc) return rc;
+  if (g_out != nullptr) head_kernel<<<blocks(c * 32, 256), 256, 0, st>>>(w.h3, c, p + kOffW4, p + kOffB4, g_out);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+int split_for(int64_t k) {
+  const int64_t chunks = (k + kBK - 1) / kBK;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(74, chunks / 4));
 }
 
 }  // namespace
@@ -234,16 +640,135 @@ extern "C" int32_t kups_gemm_bf16(const void *a, int32_t a_bf16, int64_t sa_row,
                                   int32_t c2_bf16, int64_t sc2_row, int64_t sc2_col, const float *bias,
                                   const float *gate, int32_t gate_kind, int64_t sg_row, int64_t sg_col,
                                   int32_t m, int32_t n, int32_t k, float alpha, float beta, int32_t act,
-                                  kups_status *status, void *stream) {
-  if (m <= 0 || n <= 0 || k <= 0 || act < 0 || act > 2 || gate_kind < 0 || gate_kind > 2) return KUPS_ERR_INVALID;
+                                  int32_t split_k, kups_status *status, void *stream) {
+  if (m <= 0 || n <= 0 || k <= 0 || act < 0 || act > 2 || gate_kind < 0 || gate_kind > 3 || split_k < 1 ||
+      split_k > 65535)
+    return KUPS_ERR_INVALID;
+  // split-K accumulates into float32 C with atomics: no epilogue terms but alpha
+  if (split_k > 1 && (c_bf16 || c2 || bias || gate_kind || act || beta != 1.f)) return KUPS_ERR_INVALID;
   GemmArgs g;
   g.a = a; g.b = b; g.c = c; g.c2 = c2; g.bias = bias; g.gate = gate;
   g.sar = sa_row; g.sac = sa_col; g.sbr = sb_row; g.sbc = sb_col; g.scr = sc_row; g.scc = sc_col;
   g.sc2r = sc2_row; g.sc2c = sc2_col; g.sgr = sg_row; g.sgc = sg_col;
   g.m = m; g.n = n; g.k = k; g.alpha = alpha; g.beta = beta; g.act = act;
   g.a_bf16 = a_bf16; g.b_bf16 = b_bf16; g.c_bf16 = c_bf16; g.c2_bf16 = c2_bf16; g.gate_kind = gate_kind;
+  g.split_k = split_k;
+  return dispatch_gemm(g, status, (cudaStream_t)stream);
+}
+
+extern "C" size_t kups_mlp_workspace_bytes(int64_t n_points) {
+  return work_bytes(std::max<int64_t>(1, std::min<int64_t>(n_points, kChunk)));
+}
+
+extern "C" int32_t kups_mlp_init(const kups_mlp *net, uint64_t seed, void *stream) {
+  if (net == nullptr) return KUPS_ERR_INVALID;
+  init_kernel<<<blocks(kParams, 256), 256, 0, (cudaStream_t)stream>>>(
+      net->param, (__nv_bfloat16 *)net->param_bf16, net->grad, net->adam_m, net->adam_v, seed);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_mlp_fwd(const kups_mlp *net, const double *x, int64_t n, float *g, void *workspace,
+                                size_t workspace_bytes, kups_status *status, void *stream) {
+  if (net == nullptr || n < 0 || (n > 0 && (x == nullptr || g == nullptr))) return KUPS_ERR_INVALID;
+  if (workspace_bytes < kups_mlp_workspace_bytes(n)) return KUPS_ERR_INVALID;
+  const int64_t cmax = std::min<int64_t>(n, kChunk);
+  const MlpWork w = carve(workspace, std::max<int64_t>(cmax, 1));
+  for (int64_t r0 = 0; r0 < n; r0 += kChunk) {
+    const int64_t c = std::min<int64_t>(kChunk, n - r0);
+    const int32_t rc = forward_chunk(net, x, r0, c, 0, w, g + r0, status, (cudaStream_t)stream);
+    if (rc) return rc;
+  }
+  return KUPS_OK;
+}
+
+extern "C" int32_t kups_mlp_nce_batch(const double *data, int64_t n_data, int32_t batch, uint64_t seed,
+                                      uint64_t step, double *x, float *label, void *stream) {
+  if (n_data <= 0 || batch <= 0 || (batch & 1)) return KUPS_ERR_INVALID;
+  nce_batch_kernel<<<blocks(batch, 256), 256, 0, (cudaStream_t)stream>>>(data, n_data, batch, seed, step, x, label);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_mlp_bwd(const kups_mlp *net, const double *x, const float *label, int32_t n, float *loss,
+                                void *workspace, size_t workspace_bytes, kups_status *status, void *stream) {
+  if (net == nullptr || n <= 0 || n > kChunk) return KUPS_ERR_INVALID;
+  if (workspace_bytes < kups_mlp_workspace_bytes(n)) return KUPS_ERR_INVALID;
   cudaStream_t st = (cudaStream_t)stream;
-  if (n <= 64) return launch_gemm<64>(g, status, st);
-  if (n <= 128) return launch_gemm<128>(g, status, st);
-  return launch_gemm<256>(g, status, st);
+  const MlpWork w = carve(workspace, n);
+  int32_t rc = forward_chunk(net, x, 0, n, 0, w, nullptr, status, st);
+  if (rc) return rc;
+  const __nv_bfloat16 *pb = (const __nv_bfloat16 *)net->param_bf16;
+  const float *p = net->param;
+  float *gr = net->grad;
+  const int sms = 148;
+  head_nce_kernel<<<std::min<int64_t>(blocks(n, 8), 4 * sms), 256, 0, st>>>(
+      w.h3, n, p + kOffW4, p + kOffB4, label, w.dza, gr + kOffW4, gr + kOffB4, loss);
+  const int split = split_for(n);
+  const unsigned cs_blocks = (unsigned)std::min<int64_t>(blocks(n, 64), 2 * sms);
+  // layer 3: dW3 += dz3^T h2, db3 += colsum dz3, dz2 = (dz3 W3) * (1 - exp(-h2))
+  rc = gemm_call(Op{w.dza, 0, 1, kHid}, Op{w.h2b, 1, 1, kHid}, gr + kOffW3, kHid, 1, nullptr, nullptr, nullptr, 0,
+                 kHid, kHid, n, 1.f, 0, split, status, st);
+  if (rc) return rc;
+  colsum_kernel<<<cs_blocks, kHid, 0, st>>>(w.dza, n, gr + kOffB3);
+  rc = gemm_call(Op{w.dza, 0, kHid, 1}, Op{pb + kOffW3, 1, 1, kHid}, w.dzb, kHid, 1, nullptr, nullptr, w.h2, 3, n,
+                 kHid, kHid, 0.f, 0, 1, status, st);
+  if (rc) return rc;
+  // layer 2
+  rc = gemm_call(Op{w.dzb, 0, 1, kHid}, Op{w.h1b, 1, 1, kHid}, gr + kOffW2, kHid, 1, nullptr, nullptr, nullptr, 0,
+                 kHid, kHid, n, 1.f, 0, split, status, st);
+  if (rc) return rc;
+  colsum_kernel<<<cs_blocks, kHid, 0, st>>>(w.dzb, n, gr + kOffB2);
+  rc = gemm_call(Op{w.dzb, 0, kHid, 1}, Op{pb + kOffW2, 1, 1, kHid}, w.dza, kHid, 1, nullptr, nullptr, w.h1, 3, n,
+                 kHid, kHid, 0.f, 0, 1, status, st);
+  if (rc) return rc;
+  // layer 1 (no gradient into the features)
+  rc = gemm_call(Op{w.dza, 0, 1, kHid}, Op{w.feat, 1, 1, kIn}, gr + kOffW1, kIn, 1, nullptr, nullptr, nullptr, 0,
+                 kHid, kIn, n, 1.f, 0, split, status, st);
+  if (rc) return rc;
+  colsum_kernel<<<cs_blocks, kHid, 0, st>>>(w.dza, n, gr + kOffB1);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_mlp_adam(const kups_mlp *net, int64_t t, float lr, float beta1, float beta2, float eps,
+                                 void *stream) {
+  if (net == nullptr || t < 1) return KUPS_ERR_INVALID;
+  const float c1 = (float)(1.0 / (1.0 - pow((double)beta1, (double)t)));
+  const float c2 = (float)(1.0 / (1.0 - pow((double)beta2, (double)t)));
+  adam_kernel<<<blocks(kParams, 256), 256, 0, (cudaStream_t)stream>>>(
+      net->param, (__nv_bfloat16 *)net->param_bf16, net->grad, net->adam_m, net->adam_v, kParams, lr, beta1, beta2,
+      eps, c1, c2);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float floor_frac, float *node,
+                                      double *cdf, void *workspace, size_t workspace_bytes, kups_status *status,
+                                      void *stream) {
+  if (net == nullptr || grid < 2 || grid > 256 || !(floor_frac > 0.f)) return KUPS_ERR_INVALID;
+  const int64_t n = (int64_t)grid * grid * grid;
+  if (workspace_bytes < kups_mlp_workspace_bytes(n)) return KUPS_ERR_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  const MlpWork w = carve(workspace, std::min<int64_t>(n, kChunk));
+  for (int64_t r0 = 0; r0 < n; r0 += kChunk) {
+    const int64_t c = std::min<int64_t>(kChunk, n - r0);
+    const int32_t rc = forward_chunk(net, nullptr, r0, c, grid, w, node + r0, status, st);
+    if (rc) return rc;
+  }
+  grid_normalise_kernel<<<1, 1024, 0, st>>>(node, n, floor_frac, status);
+  grid_cdf_kernel<<<1, 1024, 0, st>>>(node, grid, cdf);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_proposal_sample(const float *node, const double *cdf, int32_t grid, int64_t n,
+                                        uint64_t seed, double *f, double *log_q, void *stream) {
+  if (grid < 2 || n < 0) return KUPS_ERR_INVALID;
+  if (n == 0) return KUPS_OK;
+  proposal_sample_kernel<<<blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(node, cdf, grid, n, seed, f, log_q);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_proposal_log_density(const float *node, const double *cdf, int32_t grid, const double *f,
+                                             int64_t n, double *log_q, void *stream) {
+  if (grid < 2 || n < 0) return KUPS_ERR_INVALID;
+  if (n == 0) return KUPS_OK;
+  proposal_density_kernel<<<blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(node, cdf, grid, f, n, log_q);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

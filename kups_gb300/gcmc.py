@@ -187,6 +187,7 @@ class GCMC:
         self.seed = seed
         self.step = 0
         self.status = new_status()
+        self.proposal = None  # learned insertion density (LearnedInsertionProposal) or None: uniform
 
     def _min_half_width(self):
         out = []
@@ -232,6 +233,9 @@ class GCMC:
         a.attempted, a.accepted = self.attempted.data_ptr(), self.accepted.data_ptr()
         a.proposals = proposals.data_ptr() if proposals is not None else None
         a.out_delta = out_delta.data_ptr() if out_delta is not None else None
+        if self.proposal is not None:
+            a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
+            a.proposal_grid = self.proposal.grid
         for i in range(3):
             a.move_cum[i] = float(self.move_cum[i])
         a.coulomb_k = TO_STANDARD_UNITS
@@ -274,6 +278,26 @@ class GCMC:
         out = torch.zeros((s, 4), dtype=torch.float64, device="cuda")
         self.launch(1, proposals=buf, out_delta=out)
         return out.cpu().numpy()
+
+    def use_proposal(self, proposal):
+        """Draw insertions from ``proposal``'s grid density (None: uniform, as the reference does)."""
+        self.proposal = proposal
+
+    def molecule_centres_frac(self) -> torch.Tensor:
+        """Fractional coordinates in [0, 1) of every molecule's atom mean (atoms unwrapped against
+        atom 0), all systems concatenated: the positions the learned proposal is trained on."""
+        t = self.tril
+        L = torch.zeros((t.shape[0], 3, 3), dtype=torch.float64, device=t.device)
+        L[:, 0, 0], L[:, 1, 0], L[:, 1, 1], L[:, 2, 0], L[:, 2, 1], L[:, 2, 2] = t.unbind(1)
+        inv = torch.linalg.inv(L)
+        p = self.guest[..., :3].to(torch.float64)  # [S, M, apm, 3]
+        f = torch.einsum("smai,sij->smaj", p, inv)
+        d = f - f[:, :, :1]
+        d = d - torch.round(d)
+        c = f[:, :, 0] + d.mean(2)
+        c = c - torch.floor(c)
+        mask = torch.arange(p.shape[1], device=p.device)[None, :] < self.n_mol[:, None]
+        return c[mask]
 
     def guest_positions(self) -> list[np.ndarray]:
         g = self.guest.cpu().numpy()

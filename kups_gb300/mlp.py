@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -28,8 +29,10 @@ from .neighborlist import _stream, new_status, read_status
 
 def gemm(a: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None, bias=None, act: int = 0,
          alpha: float = 1.0, beta: float = 0.0, out2: torch.Tensor | None = None, gate=None, gate_kind: int = 0,
-         status=None) -> torch.Tensor:
-    """out = act(alpha * a @ b.T + beta * out + bias) (* gate'), tensors of any strides (2-D)."""
+         split_k: int = 1, status=None) -> torch.Tensor:
+    """out = act(alpha * a @ b.T + beta * out + bias) (* gate'), tensors of any strides (2-D).
+
+    split_k > 1 adds alpha * a @ b.T into a float32 ``out`` (beta must be 1)."""
     m, k = a.shape
     n, k2 = b.shape
     if k != k2:
@@ -49,8 +52,147 @@ def gemm(a: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None, bias
         out2.stride(0) if out2 is not None else 0, out2.stride(1) if out2 is not None else 0,
         bias.data_ptr() if bias is not None else None, g.data_ptr() if g is not None else None, int(gate_kind),
         g.stride(0) if g is not None else 0, g.stride(1) if g is not None else 0, m, n, k, float(alpha),
-        float(beta), int(act), st.data_ptr(), _stream())
+        float(beta), int(act), int(split_k), st.data_ptr(), _stream())
     _lib.check(rc, "kups_gemm_bf16")
     if status is None:
         _lib.raise_status(read_status(st))
     return out
+
+
+N_PARAMS = 148481
+OFFSETS = {"W1": (0, (256, 64)), "b1": (16384, (256,)), "W2": (16640, (256, 256)), "b2": (82176, (256,)),
+           "W3": (82432, (256, 256)), "b3": (147968, (256,)), "w4": (148224, (256,)), "b4": (148480, (1,))}
+
+
+def default_frequencies(seed: int = 7, max_order: int = 4) -> np.ndarray:
+    """32 integer frequency vectors: the 13 of the half space of {-1, 0, 1}^3 \\ {0},
+    then 19 distinct seeded draws from [-max_order, max_order]^3 (no sign-duplicates)."""
+    out, seen = [], set()
+
+    def add(m):
+        m = tuple(int(v) for v in m)
+        neg = tuple(-v for v in m)
+        if m == (0, 0, 0) or m in seen or neg in seen:
+            return
+        seen.add(m)
+        out.append(m)
+
+    for m in np.stack(np.meshgrid(*[np.arange(-1, 2)] * 3, indexing="ij"), -1).reshape(-1, 3):
+        add(m)
+    rng = np.random.default_rng(seed)
+    while len(out) < 32:
+        add(rng.integers(-max_order, max_order + 1, 3))
+    return np.array(out[:32], np.int32)
+
+
+class LearnedInsertionProposal:
+    """MLP log-density g(f) on fractional coordinates and its 64^3 grid sampler.
+
+    Every step runs on the library's kernels: kups_mlp_nce_batch draws the
+    batch, kups_mlp_bwd runs forward + backward on the tensor cores,
+    kups_mlp_adam updates; kups_mlp_grid_norm evaluates the network on the grid
+    nodes and builds the sampler's float64 CDF.
+    """
+
+    def __init__(self, seed: int = 0, freq: np.ndarray | None = None, grid: int = 64, floor: float = 0.05):
+        dev = "cuda"
+        self.param = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
+        self.param_bf16 = torch.zeros(N_PARAMS, dtype=torch.bfloat16, device=dev)
+        self.grad = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
+        self.m = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
+        self.v = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
+        self.freq = torch.as_tensor(default_frequencies() if freq is None else np.asarray(freq, np.int32),
+                                    device=dev).contiguous()
+        self.net = _lib.Mlp(self.param.data_ptr(), self.param_bf16.data_ptr(), self.grad.data_ptr(),
+                            self.m.data_ptr(), self.v.data_ptr(), self.freq.data_ptr())
+        self.grid, self.floor = int(grid), float(floor)
+        self.node = torch.zeros(self.grid ** 3, dtype=torch.float32, device=dev)
+        self.cdf = torch.zeros(self.grid ** 3 + 1, dtype=torch.float64, device=dev)
+        self.status = new_status()
+        self.t = 0
+        self._ws = None
+        _lib.check(_lib.load().kups_mlp_init(C.byref(self.net), int(seed) & (2**64 - 1), _stream()), "kups_mlp_init")
+
+    def _workspace(self, n):
+        nbytes = _lib.load().kups_mlp_workspace_bytes(int(n))
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        return self._ws
+
+    def params(self) -> dict:
+        flat = self.param.cpu().numpy()
+        return {k: flat[o:o + int(np.prod(s))].reshape(s) for k, (o, s) in OFFSETS.items()}
+
+    def forward(self, f: torch.Tensor) -> torch.Tensor:
+        f = f.to(torch.float64).contiguous()
+        g = torch.empty(f.shape[0], dtype=torch.float32, device="cuda")
+        ws = self._workspace(f.shape[0])
+        _lib.check(_lib.load().kups_mlp_fwd(C.byref(self.net), f.data_ptr(), f.shape[0], g.data_ptr(), ws.data_ptr(),
+                                            ws.numel(), self.status.data_ptr(), _stream()), "kups_mlp_fwd")
+        return g
+
+    def backward(self, f: torch.Tensor, label: torch.Tensor, loss: torch.Tensor | None = None):
+        """Adds dL/dparam of the batch to ``self.grad`` (and L to ``loss``)."""
+        f = f.to(torch.float64).contiguous()
+        label = label.to(torch.float32).contiguous()
+        ws = self._workspace(f.shape[0])
+        _lib.check(_lib.load().kups_mlp_bwd(C.byref(self.net), f.data_ptr(), label.data_ptr(), f.shape[0],
+                                            loss.data_ptr() if loss is not None else None, ws.data_ptr(), ws.numel(),
+                                            self.status.data_ptr(), _stream()), "kups_mlp_bwd")
+
+    def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8):
+        self.t += 1
+        _lib.check(_lib.load().kups_mlp_adam(C.byref(self.net), self.t, lr, beta1, beta2, eps, _stream()),
+                   "kups_mlp_adam")
+
+    def train(self, data: torch.Tensor, steps: int, batch: int = 16384, lr: float = 2e-3, seed: int = 1,
+              lr_final: float | None = None, log_every: int = 0):
+        """Noise-contrastive training on fractional positions ``data`` [N, 3]; returns sampled losses."""
+        lib = _lib.load()
+        data = data.to(torch.float64).contiguous()
+        x = torch.empty((batch, 3), dtype=torch.float64, device="cuda")
+        y = torch.empty(batch, dtype=torch.float32, device="cuda")
+        loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+        losses = []
+        lr_final = lr if lr_final is None else lr_final
+        for it in range(steps):
+            _lib.check(lib.kups_mlp_nce_batch(data.data_ptr(), data.shape[0], batch, int(seed), it, x.data_ptr(),
+                                              y.data_ptr(), _stream()), "kups_mlp_nce_batch")
+            log = log_every and (it % log_every == 0 or it == steps - 1)
+            if log:
+                loss.zero_()
+            self.backward(x, y, loss if log else None)
+            frac = it / max(1, steps - 1)
+            self.adam(lr * (lr_final / lr) ** frac)
+            if log:
+                losses.append((it, float(loss.item())))
+        self.check()
+        return losses
+
+    def build_grid(self):
+        """Node values and CDF of the sampler from the current network."""
+        n = self.grid ** 3
+        ws = self._workspace(n)
+        _lib.check(_lib.load().kups_mlp_grid_norm(C.byref(self.net), self.grid, self.floor, self.node.data_ptr(),
+                                                  self.cdf.data_ptr(), ws.data_ptr(), ws.numel(),
+                                                  self.status.data_ptr(), _stream()), "kups_mlp_grid_norm")
+        self.check()
+        return self.node, self.cdf
+
+    def sample(self, n: int, seed: int = 0):
+        f = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        lq = torch.empty(n, dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().kups_proposal_sample(self.node.data_ptr(), self.cdf.data_ptr(), self.grid, n, seed,
+                                                    f.data_ptr(), lq.data_ptr(), _stream()), "kups_proposal_sample")
+        return f, lq
+
+    def log_density(self, f: torch.Tensor) -> torch.Tensor:
+        f = f.to(torch.float64).contiguous()
+        lq = torch.empty(f.shape[0], dtype=torch.float64, device="cuda")
+        _lib.check(_lib.load().kups_proposal_log_density(self.node.data_ptr(), self.cdf.data_ptr(), self.grid,
+                                                         f.data_ptr(), f.shape[0], lq.data_ptr(), _stream()),
+                   "kups_proposal_log_density")
+        return lq
+
+    def check(self):
+        _lib.raise_status(read_status(self.status))

@@ -141,3 +141,98 @@ def test_ideal_gas_loading_is_poisson():
     assert abs(mean - target) < 4 * se, (mean, se)
     st = mc.statistics()
     assert st["insert"][0] > 0 and st["delete"][0] > 0
+
+
+# ----------------------------------------------------------------------------- learned insertion proposal
+def _blob_proposal(seed=0, grid=16):
+    from kups_gb300.mlp import LearnedInsertionProposal
+
+    rng = np.random.default_rng(seed)
+    c = np.array([[0.2, 0.3, 0.4], [0.7, 0.75, 0.1]])[rng.integers(0, 2, 100000)]
+    data = (c + 0.05 * rng.normal(size=c.shape)) % 1.0
+    net = LearnedInsertionProposal(seed=seed + 1, grid=grid)
+    net.train(torch.as_tensor(data, device="cuda"), steps=200, batch=8192, lr=3e-3)
+    net.build_grid()
+    return net
+
+
+def _anchor_frac(pos, tril):
+    """Atom mean (unwrapped against atom 0) of float32 positions, fractional, in float64."""
+    L = ouc.lattice_from_tril(tril)
+    inv = np.linalg.inv(L)
+    p = np.asarray(pos, np.float32).astype(np.float64)
+    d = (p - p[0]) @ inv
+    d -= np.round(d)
+    return (p[0] @ inv + d.mean(0)) % 1.0
+
+
+@pytest.mark.parametrize("kind", ["insert", "delete"])
+def test_learned_proposal_log_ratio_matches_oracle(kind):
+    """ln acc with the learned density minus ln acc with uniform insertion is -ln q_f(centre)
+    for an insertion and +ln q_f(centre) for a deletion (bar: 1e-4 absolute, the float32
+    centre of the molecule)."""
+    from kups_gb300 import gcmc
+    from oracle import mlp as om
+
+    net = _blob_proposal()
+    node, cdf = net.node.cpu().numpy(), net.cdf.cpu().numpy()
+    setup = small_setup(n_sys=3)
+    rng = np.random.default_rng(7)
+    L = ouc.lattice_from_tril(setup.tril[0])
+    guests = [np.concatenate([wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0])
+                              for _ in range(4)]) for _ in range(3)]
+    code = gcmc.MOVES.index(kind)
+    mols = [int(m) for m in rng.integers(0, 4, 3)]
+    news = [wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0]) if kind == "insert" else None
+            for _ in range(3)]
+    outs = []
+    for proposal in (None, net):
+        mc = gcmc.GCMC(setup, seed=5)
+        mc.set_guests(guests)
+        mc.use_proposal(proposal)
+        outs.append(mc.evaluate([code] * 3, mols, news))
+    got = outs[1][:, 3] - outs[0][:, 3]
+    exp = []
+    for i in range(3):
+        mol = news[i] if kind == "insert" else guests[i].reshape(4, 3, 3)[mols[i]]
+        lq = om.log_q(node, cdf, net.grid, _anchor_frac(mol, setup.tril[0])[None])[0]
+        exp.append(-lq if kind == "insert" else lq)
+    np.testing.assert_allclose(got, exp, atol=1e-4)
+    np.testing.assert_allclose(outs[1][:, 0], outs[0][:, 0], rtol=1e-12)  # same energy change
+
+
+def test_ideal_gas_with_learned_proposal_stays_uniform_and_poisson():
+    """Detailed balance of the learned insertion: without interactions the loading must stay
+    Poisson with mean a V and the molecules must fill the cell uniformly, although insertions
+    are drawn mostly inside two blobs (2 % of the volume)."""
+    from kups_gb300 import gcmc
+
+    net = _blob_proposal(3)
+    setup = small_setup(n_sys=64, tail=False, charges=False)
+    setup.epsilon = np.zeros_like(setup.epsilon)
+    vol = abs(np.prod(setup.tril[0, [0, 2, 5]]))
+    target = 3.0
+    setup.log_activity = np.full(64, np.log(target / vol))
+    mc = gcmc.GCMC(setup, seed=13)
+    mc.use_proposal(net)
+    mc.launch(2000)
+    samples, centres = [], []
+    for _ in range(120):
+        mc.launch(50)
+        samples.append(mc.n_mol.cpu().numpy().copy())
+        centres.append(mc.molecule_centres_frac().cpu().numpy())
+    mc.check()
+    n = np.array(samples, float)
+    t = n.mean(1)
+    se = t.std(ddof=1) / np.sqrt(len(t))
+    assert abs(n.mean() - target) < 4 * se, (n.mean(), se)
+    c = np.concatenate(centres)
+    blobs = np.array([[0.2, 0.3, 0.4], [0.7, 0.75, 0.1]])
+    d = c[:, None, :] - blobs[None]
+    d -= np.round(d)
+    r = np.sqrt(((d @ ouc.lattice_from_tril(setup.tril[0])) ** 2).sum(-1)).min(1)  # Cartesian distance
+    inside = float((r < 2.0).mean())
+    expected = 2 * 4 / 3 * np.pi * 2.0**3 / vol
+    assert abs(inside - expected) < 0.5 * expected + 0.005, (inside, expected)
+    st = mc.statistics()
+    assert st["insert"][1] > 100 and st["delete"][1] > 100
