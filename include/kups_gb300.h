@@ -443,12 +443,13 @@ int32_t kups_mlp_bwd(const kups_mlp *net, const double *x, const float *label, i
 /* Adam step t >= 1 (Kingma & Ba); refreshes param_bf16 and zeroes grad */
 int32_t kups_mlp_adam(const kups_mlp *net, int64_t t, float lr, float beta1, float beta2, float eps,
                       void *stream);
-/* Grid density for the sampler: node[(i G + j) G + k] = exp(g(i/G, j/G, k/G) - max g)
+/* Grid density for the sampler: node[(i G + j) G + k] = exp(temper (g(i/G, j/G, k/G) - max g))
  * + floor_frac * mean (so every cell has positive mass), cdf [G^3 + 1] = running
- * sums of cell masses (mean of the 8 corners), float64.  2 <= G <= 256. */
-int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float floor_frac, float *node,
-                           double *cdf, void *workspace, size_t workspace_bytes, kups_status *status,
-                           void *stream);
+ * sums of cell masses (mean of the 8 corners), float64.  2 <= G <= 256; temper > 0
+ * flattens (< 1) or sharpens (> 1) the learned density. */
+int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float temper, float floor_frac,
+                           float *node, double *cdf, void *workspace, size_t workspace_bytes,
+                           kups_status *status, void *stream);
 /* n exact draws f [n, 3] from the piecewise-trilinear grid density (cell by its
  * mass, corner by its value, per-axis sqrt transform) with ln q_f(f), the
  * density in fractional measure (the insertion's log ratio is -ln q_f) */

@@ -518,10 +518,10 @@ __device__ inline double block_sum_d(double v, double *red) {
   return r;
 }
 
-// node holds g on entry; on exit d = exp(g - max g) + floor_frac * mean(exp(g - max g)).
+// node holds g on entry; on exit d = exp(temper (g - max g)) + floor_frac * mean(exp(temper (g - max g))).
 // One block of 1024 threads.
-__global__ void __launch_bounds__(1024) grid_normalise_kernel(float *node, int64_t n, float floor_frac,
-                                                              kups_status *status) {
+__global__ void __launch_bounds__(1024) grid_normalise_kernel(float *node, int64_t n, float temper,
+                                                              float floor_frac, kups_status *status) {
   __shared__ float redf[32];
   __shared__ double redd[32];
   float mx = -INFINITY;
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(1024) grid_normalise_kernel(float *node, int64
   mx = block_max1024(mx, redf);
   double s = 0.0;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const float e = expf(node[i] - mx);
+    const float e = expf(temper * (node[i] - mx));
     node[i] = e;
     s += e;
   }
@@ -739,10 +739,10 @@ extern "C" int32_t kups_mlp_adam(const kups_mlp *net, int64_t t, float lr, float
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 
-extern "C" int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float floor_frac, float *node,
-                                      double *cdf, void *workspace, size_t workspace_bytes, kups_status *status,
-                                      void *stream) {
-  if (net == nullptr || grid < 2 || grid > 256 || !(floor_frac > 0.f)) return KUPS_ERR_INVALID;
+extern "C" int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float temper, float floor_frac,
+                                      float *node, double *cdf, void *workspace, size_t workspace_bytes,
+                                      kups_status *status, void *stream) {
+  if (net == nullptr || grid < 2 || grid > 256 || !(floor_frac > 0.f) || !(temper > 0.f)) return KUPS_ERR_INVALID;
   const int64_t n = (int64_t)grid * grid * grid;
   if (workspace_bytes < kups_mlp_workspace_bytes(n)) return KUPS_ERR_INVALID;
   cudaStream_t st = (cudaStream_t)stream;
@@ -752,7 +752,7 @@ extern "C" int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float f
     const int32_t rc = forward_chunk(net, nullptr, r0, c, grid, w, node + r0, status, st);
     if (rc) return rc;
   }
-  grid_normalise_kernel<<<1, 1024, 0, st>>>(node, n, floor_frac, status);
+  grid_normalise_kernel<<<1, 1024, 0, st>>>(node, n, temper, floor_frac, status);
   grid_cdf_kernel<<<1, 1024, 0, st>>>(node, grid, cdf);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

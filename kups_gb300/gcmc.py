@@ -279,6 +279,18 @@ class GCMC:
         self.launch(1, proposals=buf, out_delta=out)
         return out.cpu().numpy()
 
+    _STATE = ("guest", "n_mol", "sk", "energy", "width", "history", "history_index")
+
+    def clone(self, seed: int | None = None) -> "GCMC":
+        """A sampler on the same setup starting from this one's state (positions, counts,
+        structure factors, energies, step widths); counters and statistics start at zero."""
+        other = GCMC(self.setup, seed=self.seed if seed is None else seed)
+        for k in self._STATE:
+            getattr(other, k).copy_(getattr(self, k))
+        other.step = self.step
+        other.proposal = self.proposal
+        return other
+
     def use_proposal(self, proposal):
         """Draw insertions from ``proposal``'s grid density (None: uniform, as the reference does)."""
         self.proposal = proposal

@@ -94,7 +94,8 @@ class LearnedInsertionProposal:
     nodes and builds the sampler's float64 CDF.
     """
 
-    def __init__(self, seed: int = 0, freq: np.ndarray | None = None, grid: int = 64, floor: float = 0.05):
+    def __init__(self, seed: int = 0, freq: np.ndarray | None = None, grid: int = 64, floor: float = 0.05,
+                 temper: float = 1.0):
         dev = "cuda"
         self.param = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
         self.param_bf16 = torch.zeros(N_PARAMS, dtype=torch.bfloat16, device=dev)
@@ -105,7 +106,7 @@ class LearnedInsertionProposal:
                                     device=dev).contiguous()
         self.net = _lib.Mlp(self.param.data_ptr(), self.param_bf16.data_ptr(), self.grad.data_ptr(),
                             self.m.data_ptr(), self.v.data_ptr(), self.freq.data_ptr())
-        self.grid, self.floor = int(grid), float(floor)
+        self.grid, self.floor, self.temper = int(grid), float(floor), float(temper)
         self.node = torch.zeros(self.grid ** 3, dtype=torch.float32, device=dev)
         self.cdf = torch.zeros(self.grid ** 3 + 1, dtype=torch.float64, device=dev)
         self.status = new_status()
@@ -173,7 +174,8 @@ class LearnedInsertionProposal:
         """Node values and CDF of the sampler from the current network."""
         n = self.grid ** 3
         ws = self._workspace(n)
-        _lib.check(_lib.load().kups_mlp_grid_norm(C.byref(self.net), self.grid, self.floor, self.node.data_ptr(),
+        _lib.check(_lib.load().kups_mlp_grid_norm(C.byref(self.net), self.grid, self.temper, self.floor,
+                                                  self.node.data_ptr(),
                                                   self.cdf.data_ptr(), ws.data_ptr(), ws.numel(),
                                                   self.status.data_ptr(), _stream()), "kups_mlp_grid_norm")
         self.check()
@@ -196,3 +198,85 @@ class LearnedInsertionProposal:
 
     def check(self):
         _lib.raise_status(read_status(self.status))
+
+
+def _timed_run(mc, steps, block):
+    """Runs ``steps`` MC steps in blocks; returns device ms, accepted/attempted per move kind
+    and the per-block mean loading [blocks, S] (loading sampled every 100 steps)."""
+    att0, acc0 = mc.attempted.clone(), mc.accepted.clone()
+    loads, ms = [], 0.0
+    sample = min(100, block)
+    for _ in range(steps // block):
+        acc_load = torch.zeros_like(mc.n_mol, dtype=torch.float64)
+        for _ in range(block // sample):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            mc.launch(sample)
+            e1.record()
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+            acc_load += mc.n_mol.to(torch.float64)
+        loads.append((acc_load / (block // sample)).cpu().numpy())
+    mc.check()
+    att = (mc.attempted - att0).sum(0).cpu().numpy()
+    acc = (mc.accepted - acc0).sum(0).cpu().numpy()
+    return ms, att, acc, np.array(loads)
+
+
+def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, train_steps=3000, batch=16384,
+                     equil_steps=10000, prod_steps=5000, block=500, temper=0.5, floor=0.05, grid=64, seed=0,
+                     groups=8):
+    """Plain GCMC from empty, centres of the molecules it holds as training data, NCE training,
+    equilibration with the learned proposal, then plain and learned production runs from copies
+    of that state.  Returns rates (accepted insertions / moves per second, device time) and the
+    loading of each pressure group (replicas in order, ``groups`` equal groups) with its
+    block-averaged standard error."""
+    from . import gcmc
+
+    mc = gcmc.GCMC(setup, seed=seed + 1)
+    mc.launch(plain_steps)
+    cent = []
+    for _ in range(snapshots):
+        mc.launch(snapshot_every)
+        cent.append(mc.molecule_centres_frac())
+    mc.check()
+    data = torch.cat(cent)
+    net = LearnedInsertionProposal(seed=seed, grid=grid, floor=floor, temper=temper)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    losses = net.train(data, steps=train_steps, batch=batch, lr=2e-3, lr_final=2e-4, seed=seed + 2,
+                       log_every=max(1, train_steps // 4))
+    net.build_grid()
+    e1.record()
+    torch.cuda.synchronize()
+    train_ms = e0.elapsed_time(e1)
+    mc.use_proposal(net)
+    mc.launch(equil_steps)
+    mc.check()
+    out = {"training_positions": int(data.shape[0]), "train_ms": train_ms, "losses": losses,
+           "replicas": setup.n_systems}
+    S = setup.n_systems
+    for tag, proposal in (("plain", None), ("learned", net)):
+        run = mc.clone(seed=seed + 3)
+        run.use_proposal(proposal)
+        ms, att, acc, loads = _timed_run(run, prod_steps, block)
+        g = loads.reshape(len(loads), groups, S // groups).mean(2)  # [blocks, groups]
+        out[tag] = {
+            "ms_per_step": ms / prod_steps,
+            "accepted_insertions_per_s": float(acc[3] / ms * 1e3),
+            "accepted_moves_per_s": float(acc.sum() / ms * 1e3),
+            "attempted_moves_per_s": float(att.sum() / ms * 1e3),
+            "insert_acceptance": float(acc[3] / max(att[3], 1)),
+            "delete_acceptance": float(acc[4] / max(att[4], 1)),
+            "loading": g.mean(0).tolist(),
+            "loading_se": (g.std(0, ddof=1) / np.sqrt(len(g))).tolist(),
+            "loading_all": float(loads.mean()),
+            "loading_all_se": float(loads.mean(1).std(ddof=1) / np.sqrt(len(loads))),
+        }
+    lp, ll = np.array(out["plain"]["loading"]), np.array(out["learned"]["loading"])
+    sp, sl = np.array(out["plain"]["loading_se"]), np.array(out["learned"]["loading_se"])
+    out["loading_z"] = ((ll - lp) / np.sqrt(sp**2 + sl**2)).tolist()
+    out["loading_all_z"] = (out["learned"]["loading_all"] - out["plain"]["loading_all"]) / np.sqrt(
+        out["learned"]["loading_all_se"] ** 2 + out["plain"]["loading_all_se"] ** 2)
+    out["insertion_gain"] = out["learned"]["accepted_insertions_per_s"] / max(out["plain"]["accepted_insertions_per_s"], 1e-30)
+    return out

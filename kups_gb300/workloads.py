@@ -172,10 +172,16 @@ def ionic_melt(n_ions=4000, box=40.0, min_sep=2.2, temperature=1200.0, dt_fs=1.0
 
 def porous_framework(rng, tril, n_atoms, channel_radius=6.0, jitter=0.2):
     """Rigid host: a random subset of a fractional grid outside a cylindrical channel
-    along c through the cell centre (positions stored in [0, 1) fractional, as a CIF
-    host is).  2000 sites at >= 2.8 A separation do not fit in a 25 A, 120 degree cell
-    (packing fraction above one), so the grid spacing is the densest that leaves the
-    channel empty."""
+    along c through the origin, positions wrapped into the primary cell [-0.5, 0.5) as
+    the reference's host loader leaves them when it builds a supercell
+    (src/kups/application/mcmc/data.py:368-371).  The wrap matters: when some axes need
+    several periodic images and others one, the reference's pair search applies the
+    image offsets to the raw fractional difference (core/neighborlist.py:542-564,
+    595-624), so along a one-image axis only atoms stored in the same period as a guest
+    (guests are wrapped into [-0.5, 0.5) by every move) are seen.
+    2000 sites at >= 2.8 A separation do not fit in a 25 A, 120 degree cell (packing
+    fraction above one), so the grid spacing is the densest that leaves the channel
+    empty."""
     t = np.asarray(tril, float)
     L = np.array([[t[0], 0, 0], [t[1], t[2], 0], [t[3], t[4], t[5]]])
     n = 8
@@ -189,17 +195,44 @@ def porous_framework(rng, tril, n_atoms, channel_radius=6.0, jitter=0.2):
         if keep.sum() >= n_atoms:
             break
         n += 1
-    f = f[keep]
+    f = f[keep] - 0.5  # channel axis at the origin
     pick = rng.choice(len(f), size=n_atoms, replace=False)
     f = f[pick] + rng.uniform(-1, 1, (n_atoms, 3)) * (jitter / np.array([t[0], t[2], t[5]]))
-    return (f % 1.0) @ L
+    return ((f + 0.5) % 1.0 - 0.5) @ L
+
+
+def replicate_host(positions, tril, reps):
+    """Supercell of a host, as the reference's HostConfig.unitcell_replication builds it
+    (core/unitcell.py:196-244, 477-506): cell rows scaled by the multiplicities, copies
+    shifted by integer lattice vectors and wrapped into the new primary cell [-0.5, 0.5)."""
+    t = np.asarray(tril, float)
+    L = np.array([[t[0], 0, 0], [t[1], t[2], 0], [t[3], t[4], t[5]]])
+    shifts = np.stack(np.meshgrid(*[np.arange(m) for m in reps], indexing="ij"), -1).reshape(-1, 3)
+    m = np.asarray(reps, float)
+    t2 = t * np.array([m[0], m[1], m[1], m[2], m[2], m[2]])
+    L2 = L * m[:, None]
+    pos = (np.asarray(positions, float)[None] + (shifts @ L)[:, None]).reshape(-1, 3)
+    f = pos @ np.linalg.inv(L2)
+    return ((f + 0.5) % 1.0 - 0.5) @ L2, t2
 
 
 def gcmc_co2_framework(n_replicas=1024, n_fw=2000, p_min_bar=0.1, p_max_bar=10.0, temperature=298.0, rc=12.0,
-                       alpha=0.25, precision=1e-6, max_mol=64, seed=3):
+                       alpha=0.25, precision=1e-6, max_mol=192, seed=3, replicate=(2, 2, 1), eps_scale=1.0,
+                       charge_scale=1.0):
     """Rigid 3-site CO2 in a synthetic rigid framework (4 LJ types, Gaussian charges shifted
     to net zero), replicas at log-spaced pressures; critical constants of CO2 for the
-    Peng-Robinson fugacity: Tc 303.75 K, Pc 7.84 MPa, omega 0.22394."""
+    Peng-Robinson fugacity: Tc 303.75 K, Pc 7.84 MPa, omega 0.22394.
+
+    The host's cell (25 A, 90/90/120 degrees) has perpendicular widths 21.65, 21.65 and
+    25 A, so with a 12 A cutoff the reference's pair search needs three images along a
+    and b and one along c, and in that mixed case it applies the image offsets to raw
+    fractional differences: every pair across the c faces is missed and guests overlap
+    there without bound.  ``replicate`` (the reference's unitcell_replication) builds
+    the simulation box from copies of the host cell; (2, 2, 1) makes every width at
+    least twice the cutoff, so every pair is found by minimum image.  ``replicate=None``
+    keeps the single cell (the reference's mixed-image behaviour, used by the parity
+    tests).  ``eps_scale`` / ``charge_scale`` weaken the host (test systems that
+    equilibrate quickly)."""
     from . import gcmc
     from .ewald import kvecs_from_kmax
     from .units import PASCAL
@@ -211,9 +244,14 @@ def gcmc_co2_framework(n_replicas=1024, n_fw=2000, p_min_bar=0.1, p_max_bar=10.0
     fw = porous_framework(rng, tril, n_fw)
     fw_sp = rng.integers(0, 4, n_fw)
     q = rng.normal(0, 0.3, n_fw)
-    q -= q.mean()
+    q = (q - q.mean()) * charge_scale
+    if replicate is not None and tuple(replicate) != (1, 1, 1):
+        k = int(np.prod(replicate))
+        fw, tril = replicate_host(fw, tril, replicate)
+        fw_sp, q = np.tile(fw_sp, k), np.tile(q, k)
+        n_fw = len(fw)
     sig = np.concatenate([rng.uniform(2.5, 3.5, 4), [2.80, 3.05]])
-    eps = np.concatenate([rng.uniform(20, 80, 4), [27.0, 79.0]]) * BOLTZMANN_CONSTANT
+    eps = np.concatenate([rng.uniform(20, 80, 4) * eps_scale, [27.0, 79.0]]) * BOLTZMANN_CONSTANT
     sigma, epsilon = gcmc.lorentz_berthelot(sig, eps)
     kmax = 2 * alpha * np.sqrt(-np.log(precision / 2))
     kn = kvecs_from_kmax(tril, kmax)

@@ -109,9 +109,9 @@ def grid_nodes(grid):
     return np.stack([i // grid**2, (i // grid) % grid, i % grid], 1) / grid
 
 
-def grid_density(g_nodes, floor_frac):
+def grid_density(g_nodes, floor_frac, temper=1.0):
     """Node values d from g at the nodes (flat, (i G + j) G + k order)."""
-    e = np.exp(np.asarray(g_nodes, np.float64) - np.max(g_nodes))
+    e = np.exp(temper * (np.asarray(g_nodes, np.float64) - np.max(g_nodes)))
     return e + floor_frac * e.mean()
 
 
