@@ -242,12 +242,19 @@ __device__ inline double tail_energy(const double *counts, int nsp, const double
   return e;
 }
 
-__global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_status *status) {
+// 7 resident CTAs per SM (at most 73 registers a thread): 1024 replicas run in one wave
+// on 152 SMs, each CTA keeping its system for all n_steps.
+constexpr int kMinCtasPerSm = 7;
+
+__global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc_args a, kups_status *status) {
   __shared__ StepShared sh;
   __shared__ float2 lj[kMaxSpeciesMC * kMaxSpeciesMC];
-  __shared__ float2 dS[kMaxKVec];
+  extern __shared__ float2 dS[];  // [n_kvecs] structure-factor change of the step
   __shared__ double red[40];
   __shared__ float Lf[6], If[6];
+  __shared__ float4 mfa[2 * kMaxApm];  // moved atoms (old, then new): fractional xyz, species bits
+  __shared__ float mq[2 * kMaxApm];
+  __shared__ int mon[2 * kMaxApm];
   const int s = blockIdx.x;
   const int tid = threadIdx.x;
   const int apm = a.atoms_per_mol;
@@ -289,6 +296,8 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
       c.rc2 = (float)(rcs[t] * rcs[t]);
     }
   }
+  const bool min_image = !li.image_mode && !ei.image_mode;
+  const float rc2_any = fmaxf(li.rc2, ei.rc2);
   const float alpha = (float)a.alpha[s];
   const float ke = (float)a.coulomb_k;
   const double kT = a.kT[s];
@@ -442,6 +451,51 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
     float e_acc = 0.f;
     const int nmol = a.n_mol[s];
     const int n_other = fwn + nmol * apm;
+    // moved atoms (old state, then new) in fractional coordinates, staged once per step
+    if (tid < 2 * apm) {
+      const int st = tid / apm, i = tid % apm;
+      const float4 p = st == 0 ? sh.old_pos[i] : sh.new_pos[i];
+      float f[3];
+      frac32(If, p.x, p.y, p.z, f);
+      mfa[tid] = make_float4(f[0], f[1], f[2], p.w);
+      mq[tid] = sh.q[i];
+      mon[tid] = st == 0 ? has_old : has_new;
+    }
+    __syncthreads();
+    const int nm = 2 * apm;
+    if (min_image) {
+      // every axis has one image: the pair is taken at its minimum image, one rounding
+      // per moved atom and partner
+      for (int j = tid; j < n_other; j += kThreads) {
+        float4 pj;
+        float qj;
+        if (j < fwn) {
+          pj = fwp[fw0 + j];
+          qj = a.fw_charge[fw0 + j];
+        } else {
+          const int g = j - fwn;
+          if (has_old && g / apm == mol) continue;  // the moved molecule itself
+          pj = gpos[g];
+          qj = a.motif_charge[g % apm];
+        }
+        float fj[3];
+        frac32(If, pj.x, pj.y, pj.z, fj);
+        const int tj = __float_as_int(pj.w);
+        for (int m = 0; m < nm; ++m) {
+          if (!mon[m]) continue;
+          const float4 fa = mfa[m];
+          float d[3] = {fa.x - fj[0], fa.y - fj[1], fa.z - fj[2]}, c[3];
+          d[0] -= rintf(d[0]);
+          d[1] -= rintf(d[1]);
+          d[2] -= rintf(d[2]);
+          cart32(Lf, d, c);
+          const float r2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+          if (r2 >= rc2_any) continue;
+          const float sg = m < apm ? -1.f : 1.f;
+          e_acc += sg * pair_u(r2, __float_as_int(fa.w), tj, mq[m] * qj, lj, nsp, li, ei, alpha, ke, true, true);
+        }
+      }
+    } else
     for (int j = tid; j < n_other; j += kThreads) {
       float4 pj;
       float qj;
@@ -488,20 +542,16 @@ __global__ void __launch_bounds__(kThreads) gcmc_kernel(kups_gcmc_args a, kups_s
     for (int k = tid; k < nk; k += kThreads) {
       const int n0 = kn[3 * k], n1 = kn[3 * k + 1], n2 = kn[3 * k + 2];
       float dc = 0.f, ds = 0.f;
-      for (int st = 0; st < 2; ++st) {
-        if ((st == 0 && !has_old) || (st == 1 && !has_new)) continue;
-        const float sign = st == 0 ? -1.f : 1.f;
-        for (int i = 0; i < apm; ++i) {
-          const float4 p = st == 0 ? sh.old_pos[i] : sh.new_pos[i];
-          float f[3];
-          frac32(If, p.x, p.y, p.z, f);
-          float t = n0 * f[0] + n1 * f[1] + n2 * f[2];
-          t -= rintf(t);
-          float sn, cs;
-          sincospif(2.0f * t, &sn, &cs);
-          dc += sign * sh.q[i] * cs;
-          ds += sign * sh.q[i] * sn;
-        }
+      for (int m = 0; m < nm; ++m) {
+        if (!mon[m]) continue;
+        const float4 f = mfa[m];
+        float t = n0 * f.x + n1 * f.y + n2 * f.z;
+        t -= rintf(t);
+        float sn, cs;
+        sincospif(2.0f * t, &sn, &cs);
+        const float w = m < apm ? -mq[m] : mq[m];
+        dc += w * cs;
+        ds += w * sn;
       }
       dS[k] = make_float2(dc, ds);
       const double sc = sk[2 * k], ss = sk[2 * k + 1];
@@ -621,6 +671,6 @@ extern "C" int32_t kups_gcmc_run(const kups_gcmc_args *a, kups_status *status, v
   if (a->proposal_node != nullptr && (a->proposal_cdf == nullptr || a->proposal_grid < 2 || a->proposal_grid > 256))
     return KUPS_ERR_INVALID;
   if (a->n_systems == 0 || a->n_steps == 0) return KUPS_OK;
-  gcmc_kernel<<<a->n_systems, kThreads, 0, (cudaStream_t)stream>>>(*a, status);
+  gcmc_kernel<<<a->n_systems, kThreads, sizeof(float2) * (size_t)a->n_kvecs, (cudaStream_t)stream>>>(*a, status);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

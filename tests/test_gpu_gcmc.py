@@ -20,7 +20,7 @@ def co2_template():
     return np.array([[0.0, 0, 0], [1.16, 0, 0], [-1.16, 0, 0]]), np.array([4, 5, 5]), np.array([0.70, -0.35, -0.35])
 
 
-def small_setup(n_sys=2, seed=0, tail=True, charges=True):
+def small_setup(n_sys=2, seed=0, tail=True, charges=True, rc=7.0):
     from kups_gb300 import gcmc
     from kups_gb300.ewald import kvecs_from_kmax
     from kups_gb300.units import BOLTZMANN_CONSTANT
@@ -40,7 +40,7 @@ def small_setup(n_sys=2, seed=0, tail=True, charges=True):
     sig_i = np.array([2.5, 2.9, 3.2, 3.5, 2.80, 3.05])
     eps_i = np.array([20, 40, 60, 80, 27, 79]) * BOLTZMANN_CONSTANT
     sigma, epsilon = gcmc.lorentz_berthelot(sig_i, eps_i)
-    rc, alpha = 7.0, 0.35
+    alpha = 0.35
     kn = kvecs_from_kmax(tril, 1.6)
     setup = gcmc.GCMCSetup(
         fw_positions=fw_pos, fw_species=fw_sp, fw_charges=q, fw_start=np.zeros(n_sys, int),
@@ -69,11 +69,12 @@ def wrapped(p, tril):
     return ouc.wrap(p, tril)
 
 
+@pytest.mark.parametrize("rc", [7.0, 5.0])  # 3 x 3 x 3 image offsets / minimum image (widths 10.4, 10.4, 13 A)
 @pytest.mark.parametrize("kind", ["translate", "rotate", "insert", "delete"])
-def test_move_energy_change_matches_oracle(kind):
+def test_move_energy_change_matches_oracle(kind, rc):
     from kups_gb300 import gcmc
 
-    setup = small_setup(n_sys=3)
+    setup = small_setup(n_sys=3, rc=rc)
     rng = np.random.default_rng({"translate": 1, "rotate": 2, "insert": 3, "delete": 4}[kind])
     L = ouc.lattice_from_tril(setup.tril[0])
     mpos = setup.motif_positions
