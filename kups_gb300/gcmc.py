@@ -123,6 +123,24 @@ def tail_coefficients(sigma, epsilon, rc, volume, enabled=True):
     return np.where(epsilon > 0, c, 0.0) if enabled else np.zeros_like(c)
 
 
+def _morton_order(pos, tril, cell=3.2):
+    """Permutation putting host atoms in Z-order of ~``cell`` A cells, so the 32 atoms a warp
+    reads lie close together and agree on being inside or outside the cutoff."""
+    t = np.asarray(tril, float)
+    L = np.array([[t[0], 0, 0], [t[1], t[2], 0], [t[3], t[4], t[5]]])
+    f = np.asarray(pos, float) @ np.linalg.inv(L)
+    f -= np.floor(f)
+    vol = abs(np.linalg.det(L))
+    w = np.array([vol / np.linalg.norm(np.cross(L[(a + 1) % 3], L[(a + 2) % 3])) for a in range(3)])
+    n = np.maximum(1, np.floor(w / cell)).astype(np.int64)
+    c = np.minimum((f * n).astype(np.int64), n - 1)
+    key = np.zeros(len(c), np.int64)
+    for bit in range(10):
+        for a in range(3):
+            key |= ((c[:, a] >> bit) & 1) << (3 * bit + a)
+    return np.argsort(key, kind="stable")
+
+
 class GCMC:
     """Device state + the propagator ``__call__(key, n_steps)``."""
 
@@ -143,8 +161,14 @@ class GCMC:
         f64 = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)
         i32 = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.int32, device=dev)
         sp_bits = lambda sp: np.asarray(sp, np.int32).view(np.float32)
-        self.fw_pos = f32(np.concatenate([setup.fw_positions, sp_bits(setup.fw_species)[:, None]], 1))
-        self.fw_q = f32(setup.fw_charges)
+        # host atoms of each block in spatial (Z) order on the device; energies do not depend
+        # on the order, only the float32 summation order does
+        perm = np.arange(len(setup.fw_positions))
+        for blk, (a0, n) in enumerate(sorted(set(zip(setup.fw_start.tolist(), setup.fw_count.tolist())))):
+            first = int(np.nonzero((setup.fw_start == a0) & (setup.fw_count == n))[0][0])
+            perm[a0:a0 + n] = a0 + _morton_order(setup.fw_positions[a0:a0 + n], setup.tril[first])
+        self.fw_pos = f32(np.concatenate([setup.fw_positions[perm], sp_bits(setup.fw_species[perm])[:, None]], 1))
+        self.fw_q = f32(setup.fw_charges[perm])
         self.fw_start, self.fw_count = i32(setup.fw_start), i32(setup.fw_count)
         self.guest = torch.zeros((s, setup.max_mol, apm, 4), dtype=torch.float32, device=dev)
         self.n_mol = torch.zeros(s, dtype=torch.int32, device=dev)
