@@ -53,6 +53,14 @@ class MDWorkload:
     def n_systems(self) -> int:
         return int(self.tril.shape[0])
 
+    def subset(self, lo: int, hi: int) -> "MDWorkload":
+        """Systems [lo, hi) (atoms grouped by system), renumbered from 0."""
+        sel = (self.system >= lo) & (self.system < hi)
+        return MDWorkload(self.positions[sel], self.momenta[sel], self.masses[sel], self.species[sel],
+                          (self.system[sel] - lo).astype(np.int32), self.tril[lo:hi], self.temperature[lo:hi],
+                          self.time_step[lo:hi], self.friction[lo:hi], self.sigma, self.epsilon, self.cutoff, self.skin,
+                          None if self.charges is None else self.charges[sel])
+
 
 def _mb_momenta(rng, masses, kT, system, n_sys):
     std = np.sqrt(masses * kT[system])
