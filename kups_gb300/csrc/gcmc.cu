@@ -538,7 +538,9 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
     }
     const double de_real = block_sum((double)e_acc, red);
     // ---------------------------------------------------------------- reciprocal space
-    double de_rec = 0.0;
+    // per-k terms in float32 (|term| <~ 15 eV: ~1e-6 eV rounding each), the k sum of a
+    // thread in float32, the block sum and S(k) itself in float64
+    float de_rec_f = 0.f;
     for (int k = tid; k < nk; k += kThreads) {
       const int n0 = kn[3 * k], n1 = kn[3 * k + 1], n2 = kn[3 * k + 2];
       float dc = 0.f, ds = 0.f;
@@ -554,11 +556,11 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
         ds += w * sn;
       }
       dS[k] = make_float2(dc, ds);
-      const double sc = sk[2 * k], ss = sk[2 * k + 1];
-      de_rec += pk[k] * (2.0 * (sc * dc + ss * ds) + (double)dc * dc + (double)ds * ds);
+      const float sc = (float)sk[2 * k], ss = (float)sk[2 * k + 1];
+      de_rec_f = fmaf((float)pk[k], fmaf(2.f, fmaf(sc, dc, ss * ds), fmaf(dc, dc, ds * ds)), de_rec_f);
     }
     __syncthreads();
-    de_rec = block_sum(de_rec, red) * a.coulomb_k;
+    const double de_rec = block_sum((double)de_rec_f, red) * a.coulomb_k;
     // ---------------------------------------------------------------- acceptance (thread 0)
     if (tid == 0) {
       double de = de_real + de_rec;

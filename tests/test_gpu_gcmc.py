@@ -263,3 +263,54 @@ def test_learned_proposal_gain_and_loading_in_a_porous_host():
     # replicas share the move-kind sequence, so their loadings are correlated)
     assert abs(out["loading_all_z"]) < 3.0, (out["plain"], out["learned"])
     assert np.all(np.abs(out["loading_z"]) < 4.0), out["loading_z"]
+
+
+@pytest.mark.parametrize("kind", ["translate", "insert", "delete"])
+def test_reciprocal_delta_on_the_full_host_matches_full_recomputation(kind):
+    """On the 8000-atom replicated host (|S(k)| up to ~50, 3336 k vectors) the incremental
+    reciprocal-space change of a move (float32 per-k terms, float64 sums) equals the difference
+    of two full float64 structure-factor evaluations (kups_ewald_recip) within 2e-5 eV."""
+    from kups_gb300 import gcmc, workloads
+    from kups_gb300.ewald import ewald_recip
+
+    setup = workloads.gcmc_co2_framework(n_replicas=2, max_mol=32)
+    rng = np.random.default_rng({"translate": 1, "insert": 2, "delete": 3}[kind])
+    L = ouc.lattice_from_tril(setup.tril[0])
+    guests = [np.concatenate([wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0])
+                              for _ in range(12)]) for _ in range(2)]
+    mc = gcmc.GCMC(setup, seed=3)
+    mc.set_guests(guests)
+    mols = [int(m) for m in rng.integers(0, 12, 2)]
+    news = []
+    afters = []
+    for i in range(2):
+        g = guests[i].reshape(12, 3, 3)
+        if kind == "translate":
+            new = wrapped(g[mols[i]] + rng.normal(0, 0.7, 3), setup.tril[0])
+            gg = g.copy()
+            gg[mols[i]] = new
+            after = gg.reshape(-1, 3)
+        elif kind == "insert":
+            new = wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0])
+            after = np.concatenate([guests[i], new])
+        else:
+            new = None
+            after = np.concatenate([g[j] for j in range(12) if j != mols[i]])
+        news.append(new)
+        afters.append(after)
+    out = mc.evaluate([gcmc.MOVES.index(kind)] * 2, mols, news)
+
+    def e_rec(guest_sets):
+        pos, q, off = [], [], [0]
+        for gp in guest_sets:
+            gp = np.asarray(gp, np.float32).astype(np.float64)  # the positions the kernel holds
+            pos.append(np.concatenate([setup.fw_positions, gp]))
+            q.append(np.concatenate([setup.fw_charges, np.tile(setup.motif_charges, len(gp) // 3)]))
+            off.append(off[-1] + len(pos[-1]))
+        P = torch.as_tensor(np.concatenate(pos), device="cuda")
+        Q = torch.as_tensor(np.concatenate(q), device="cuda")
+        O = torch.as_tensor(np.array(off, np.int32), device="cuda")
+        e, _, _, _, _ = ewald_recip(P, Q, O, int(np.diff(off).max()), mc.tril, mc.kn, mc.alpha, grad_tril=False)
+        return e.cpu().numpy()
+
+    np.testing.assert_allclose(out[:, 2], e_rec(afters) - e_rec(guests), atol=2e-5)
