@@ -422,6 +422,7 @@ typedef struct kups_mlp {
   float *adam_m;       /* [KUPS_MLP_PARAMS] */
   float *adam_v;       /* [KUPS_MLP_PARAMS] */
   const int32_t *freq; /* [32, 3] integer frequency vectors */
+  void *param_bf16_t;  /* [2, 256, 256] bfloat16 W2^T, W3^T (kept by init / Adam) */
 } kups_mlp;
 
 /* workspace for kups_mlp_fwd / kups_mlp_bwd / kups_mlp_grid_norm over n points

@@ -73,7 +73,7 @@ class GcmcArgs(C.Structure):
 
 class Mlp(C.Structure):
     _fields_ = [("param", C.c_void_p), ("param_bf16", C.c_void_p), ("grad", C.c_void_p), ("adam_m", C.c_void_p),
-                ("adam_v", C.c_void_p), ("freq", C.c_void_p)]
+                ("adam_v", C.c_void_p), ("freq", C.c_void_p), ("param_bf16_t", C.c_void_p)]
 
 
 # Every symbol declared in include/kups_gb300.h: name -> (restype, argtypes)

@@ -101,15 +101,69 @@ struct GemmArgs {
   int gate_kind;      // 0 none, 1: multiply by relu'(gate) (gate > 0), 2: by softplus'(gate) = sigmoid,
                       // 3: by softplus' expressed through its output h = softplus(z): 1 - exp(-h)
   int split_k;        // > 1: blockIdx.z takes a slice of K and atomically adds alpha * partial to C
+  void *c3;           // optional third output, bfloat16, its own strides (a transposed copy)
+  int64_t sc3r, sc3c;
 };
 
+__device__ inline void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ inline void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Stages rows [r0, r0 + ROWS) x columns [k0, k0 + 64) of an operand into the
+// no-swizzle K-major core-matrix layout: element (r, kk) at
+//   ((r / 8) * 8 + kk / 8) * 64 + (r % 8) * 8 + kk % 8.
+// Fast path (bfloat16, unit K stride, 16-byte rows): one 16-byte cp.async per
+// core-matrix row; thread e copies row (e / 64) * 8 + e % 8, K group (e / 8) % 8,
+// whose shared-memory destination is element 8 e (a warp fills 512 contiguous
+// bytes and reads 64 contiguous bytes of each of 8 rows).  Rows past the end
+// are zero-filled (source size 0).  Otherwise every element is loaded,
+// converted and stored.
+template <int ROWS>
+__device__ inline void stage_operand(__nv_bfloat16 *s, const void *p, int is_bf16, int64_t sr, int64_t sc, bool fast,
+                                     int r0, int nrows, int k0, int k, int tid) {
+  if (fast) {
+    const __nv_bfloat16 *base = (const __nv_bfloat16 *)p;
+    const uint32_t s0 = smem_u32(s);
+    for (int e = tid; e < ROWS * (kBK / 8); e += kGemmThreads) {
+      const int r = (e >> 6) * 8 + (e & 7), kg = (e >> 3) & 7;
+      const int gr = r0 + r, gk = k0 + kg * 8;
+      const bool in = gr < nrows && gk < k;
+      const __nv_bfloat16 *src = in ? base + (int64_t)gr * sr + gk : base;
+      cp_async16(s0 + (uint32_t)e * 16u, src, in ? 16u : 0u);
+    }
+  } else {
+    const bool rows_fast = sr == 1 && sc != 1;  // walk along the unit-stride index
+    for (int e = tid; e < ROWS * kBK; e += kGemmThreads) {
+      const int r = rows_fast ? e % ROWS : e / kBK, kk = rows_fast ? e / ROWS : e % kBK;
+      const int gr = r0 + r, gk = k0 + kk;
+      float v = 0.f;
+      if (gr < nrows && gk < k)
+        v = is_bf16 ? ld_el((const __nv_bfloat16 *)p, gr, gk, sr, sc) : ld_el((const float *)p, gr, gk, sr, sc);
+      s[((r >> 3) * (kBK / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7)] = __float2bfloat16(v);
+    }
+  }
+}
+
+__device__ inline bool fast_operand(const void *p, int is_bf16, int64_t sr, int64_t sc, int k) {
+  return is_bf16 && sc == 1 && (sr % 8) == 0 && (k % 8) == 0 && (((uintptr_t)p) & 15) == 0;
+}
+
+// Two-stage pipeline: the 16-byte copies of K chunk c + 1 are in flight while
+// the tensor cores work on chunk c; a stage is refilled only after the
+// mbarrier of the MMAs that read it has completed.
 template <int BN>
 __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, kups_status *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __nv_bfloat16 *sa = reinterpret_cast<__nv_bfloat16 *>(smem);                      // 128 x 64
-  __nv_bfloat16 *sb = reinterpret_cast<__nv_bfloat16 *>(smem + kBM * kBK * 2);      // BN x 64
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + (kBM + BN) * kBK * 2);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+  constexpr int kStageBytes = (kBM + BN) * kBK * 2;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * kStageBytes);  // [2]
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
+  auto sa = [&](int st) { return reinterpret_cast<__nv_bfloat16 *>(smem + st * kStageBytes); };
+  auto sb = [&](int st) { return reinterpret_cast<__nv_bfloat16 *>(smem + st * kStageBytes + kBM * kBK * 2); };
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
   if (warp == 0) {
@@ -118,39 +172,47 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
                  "r"(cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) mbar_init(smem_u32(mbar), 1);
+  if (tid == 0) {
+    mbar_init(smem_u32(&mbar[0]), 1);
+    mbar_init(smem_u32(&mbar[1]), 1);
+  }
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const uint32_t idesc = make_idesc(kBM, BN);
-  uint32_t phase = 0;
-  bool ok = true;
   const int nk_all = (g.k + kBK - 1) / kBK;
   const int per_split = (nk_all + g.split_k - 1) / g.split_k;
   const int kc_begin = blockIdx.z * per_split;
   const int kc_end = min(nk_all, kc_begin + per_split);
-  // walk the staging loops along whichever operand index has unit stride
-  const bool a_rows = g.sar == 1 && g.sac != 1, b_rows = g.sbr == 1 && g.sbc != 1;
-  for (int kc = kc_begin; kc < kc_end && ok; ++kc) {
-    const int k0 = kc * kBK;
-    // stage A (128 x 64) and B (BN x 64) as bf16 core matrices: element (r, kk) at
-    // ((r / 8) * 8 + kk / 8) * 64 + (r % 8) * 8 + kk % 8   (elements)
-    for (int e = tid; e < kBM * kBK; e += kGemmThreads) {
-      const int r = a_rows ? e % kBM : e / kBK, kk = a_rows ? e / kBM : e % kBK;
-      const int gr = m0 + r, gk = k0 + kk;
-      float v = 0.f;
-      if (gr < g.m && gk < g.k)
-        v = g.a_bf16 ? ld_el((const __nv_bfloat16 *)g.a, gr, gk, g.sar, g.sac) : ld_el((const float *)g.a, gr, gk, g.sar, g.sac);
-      sa[((r >> 3) * (kBK / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7)] = __float2bfloat16(v);
-    }
-    for (int e = tid; e < BN * kBK; e += kGemmThreads) {
-      const int r = b_rows ? e % BN : e / kBK, kk = b_rows ? e / BN : e % kBK;
-      const int gr = n0 + r, gk = k0 + kk;
-      float v = 0.f;
-      if (gr < g.n && gk < g.k)
-        v = g.b_bf16 ? ld_el((const __nv_bfloat16 *)g.b, gr, gk, g.sbr, g.sbc) : ld_el((const float *)g.b, gr, gk, g.sbr, g.sbc);
-      sb[((r >> 3) * (kBK / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7)] = __float2bfloat16(v);
+  const bool fa = fast_operand(g.a, g.a_bf16, g.sar, g.sac, g.k);
+  const bool fb = fast_operand(g.b, g.b_bf16, g.sbr, g.sbc, g.k);
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  bool ok = true;
+  if (kc_begin < kc_end) {
+    stage_operand<kBM>(sa(0), g.a, g.a_bf16, g.sar, g.sac, fa, m0, g.m, kc_begin * kBK, g.k, tid);
+    stage_operand<BN>(sb(0), g.b, g.b_bf16, g.sbr, g.sbc, fb, n0, g.n, kc_begin * kBK, g.k, tid);
+    cp_async_commit();
+  }
+  for (int kc = kc_begin; kc < kc_end; ++kc) {
+    const int st = (kc - kc_begin) & 1, nx = st ^ 1;
+    if (kc + 1 < kc_end) {
+      if (pending[nx]) {  // the MMAs of chunk kc - 1 read stage nx
+        ok = mbar_wait(smem_u32(&mbar[nx]), phase[nx]);
+        phase[nx] ^= 1u;
+        pending[nx] = false;
+      }
+      if (!__syncthreads_and(ok)) {
+        ok = false;
+        break;
+      }
+      stage_operand<kBM>(sa(nx), g.a, g.a_bf16, g.sar, g.sac, fa, m0, g.m, (kc + 1) * kBK, g.k, tid);
+      stage_operand<BN>(sb(nx), g.b, g.b_bf16, g.sbr, g.sbc, fb, n0, g.n, (kc + 1) * kBK, g.k, tid);
+      cp_async_commit();
+      cp_async_wait<1>();  // chunk kc has landed (this thread's copies)
+    } else {
+      cp_async_wait<0>();
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -158,8 +220,8 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (int ks = 0; ks < kBK / 16; ++ks) {
         // K step of 16 = two core matrices along K = 256 bytes
-        const uint64_t ad = make_sdesc(smem_u32(sa) + ks * 256, 128, (kBK / 8) * 128);
-        const uint64_t bd = make_sdesc(smem_u32(sb) + ks * 256, 128, (kBK / 8) * 128);
+        const uint64_t ad = make_sdesc(smem_u32(sa(st)) + ks * 256, 128, (kBK / 8) * 128);
+        const uint64_t bd = make_sdesc(smem_u32(sb(st)) + ks * 256, 128, (kBK / 8) * 128);
         const uint32_t accumulate = (kc > kc_begin || ks > 0) ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -167,33 +229,46 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
             "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(mbar))
+                       smem_u32(&mbar[st]))
                    : "memory");
     }
-    ok = mbar_wait(smem_u32(mbar), phase);
-    phase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    __syncthreads();
+    pending[st] = true;
   }
+  cp_async_wait<0>();
+  for (int st = 0; st < 2; ++st)
+    if (pending[st] && ok) {
+      ok = mbar_wait(smem_u32(&mbar[st]), phase[st]);
+      phase[st] ^= 1u;
+    }
+  ok = __syncthreads_and(ok);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (!ok) {
     if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
   } else if (kc_begin < kc_end) {  // an empty K slice holds no accumulator
-    // epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (rows), 16 columns at a time
+    // epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (one row each), 32 columns at a
+    // time.  Row-major float32 / bfloat16 outputs go through a padded 32 x 33 shared-memory
+    // block so that a warp stores 128 contiguous bytes of one row per instruction; the
+    // transposed bfloat16 copy (c3) is written straight from the lane = row layout.
     const int row = m0 + warp * 32 + lane;
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t r[16];
+    const bool staged = g.split_k == 1 && g.scc == 1 && !g.c_bf16 && (g.c2 == nullptr || (g.c2_bf16 && g.sc2c == 1));
+    float *blk = reinterpret_cast<float *>(smem) + warp * 32 * 33;  // pipeline stages are free now
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t r[32];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
       asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-          "%14, %15}, [%16];"
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+          "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
           : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (row < g.m) {
-        for (int i = 0; i < 16; ++i) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
           const int col = n0 + c0 + i;
-          if (col >= g.n) break;
+          if (col >= g.n) continue;
           float v = g.alpha * __uint_as_float(r[i]);
           if (g.split_k > 1) {
             atomicAdd((float *)g.c + (int64_t)row * g.scr + (int64_t)col * g.scc, v);
@@ -211,6 +286,11 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
                                     : -expm1f(-pre);
           }
           v = act_fn(v, g.act);
+          if (g.c3) ((__nv_bfloat16 *)g.c3)[(int64_t)row * g.sc3r + (int64_t)col * g.sc3c] = __float2bfloat16(v);
+          if (staged) {
+            blk[lane * 33 + i] = v;
+            continue;
+          }
           const int64_t o = (int64_t)row * g.scr + (int64_t)col * g.scc;
           if (g.c_bf16) ((__nv_bfloat16 *)g.c)[o] = __float2bfloat16(v);
           else ((float *)g.c)[o] = v;
@@ -220,6 +300,18 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
             else ((float *)g.c2)[o2] = v;
           }
         }
+      }
+      if (staged) {
+        __syncwarp();
+        const int col = n0 + c0 + lane;
+        for (int rr = 0; rr < 32; ++rr) {
+          const int row2 = m0 + warp * 32 + rr;
+          if (row2 >= g.m || col >= g.n) continue;
+          const float v = blk[rr * 33 + lane];
+          ((float *)g.c)[(int64_t)row2 * g.scr + col] = v;
+          if (g.c2) ((__nv_bfloat16 *)g.c2)[(int64_t)row2 * g.sc2r + col] = __float2bfloat16(v);
+        }
+        __syncwarp();
       }
     }
   }
@@ -233,7 +325,7 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
 
 template <int BN>
 int32_t launch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t stream) {
-  const size_t smem = (size_t)(kBM + BN) * kBK * 2 + 64;
+  const size_t smem = (size_t)2 * (kBM + BN) * kBK * 2 + 64;
   KUPS_CUDA_TRY(cudaFuncSetAttribute(gemm_tcgen05_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((g.m + kBM - 1) / kBM, (g.n + BN - 1) / BN, g.split_k);
   gemm_tcgen05_kernel<BN><<<grid, kGemmThreads, smem, stream>>>(g, status);
@@ -253,11 +345,14 @@ struct Op {
   int64_t sr, sc;
 };
 
+// c: float32 with strides (scr, scc); c2: bfloat16 copy, same strides; c3: bfloat16
+// transposed copy (element (r, col) at col * m + r).
 int32_t gemm_call(Op a, Op b, void *c, int64_t scr, int64_t scc, void *c2, const float *bias, const float *gate,
                   int gate_kind, int m, int n, int k, float beta, int act, int split, kups_status *status,
-                  cudaStream_t st) {
+                  cudaStream_t st, void *c3 = nullptr) {
   GemmArgs g;
   g.a = a.p; g.b = b.p; g.c = c; g.c2 = c2; g.bias = bias; g.gate = gate;
+  g.c3 = c3; g.sc3r = 1; g.sc3c = m;
   g.sar = a.sr; g.sac = a.sc; g.sbr = b.sr; g.sbc = b.sc; g.scr = scr; g.scc = scc;
   g.sc2r = scr; g.sc2c = scc; g.sgr = scr; g.sgc = scc;
   g.m = m; g.n = n; g.k = k; g.alpha = 1.f; g.beta = beta; g.act = act;
@@ -288,8 +383,11 @@ constexpr int64_t kChunk = 65536;  // points per forward pass over the workspace
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Activations of c points: float32 (the head and the gates read them), bfloat16
+// row-major (the next layer's A operand) and bfloat16 transposed [width, c]
+// (the weight-gradient GEMMs' operands, K = points contiguous).
 struct MlpWork {
-  __nv_bfloat16 *feat, *h1b, *h2b;
+  __nv_bfloat16 *feat, *featT, *h1b, *h1T, *h2b, *h2T, *dzab, *dzaT, *dzbb, *dzbT;
   float *h1, *h2, *h3, *dza, *dzb, *g;
 };
 
@@ -302,8 +400,15 @@ MlpWork carve(void *ws, int64_t c) {
     return (void *)q;
   };
   w.feat = (__nv_bfloat16 *)take(2 * (size_t)c * kIn);
+  w.featT = (__nv_bfloat16 *)take(2 * (size_t)c * kIn);
   w.h1b = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.h1T = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
   w.h2b = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.h2T = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.dzab = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.dzaT = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.dzbb = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
+  w.dzbT = (__nv_bfloat16 *)take(2 * (size_t)c * kHid);
   w.h1 = (float *)take(4 * (size_t)c * kHid);
   w.h2 = (float *)take(4 * (size_t)c * kHid);
   w.h3 = (float *)take(4 * (size_t)c * kHid);
@@ -314,7 +419,7 @@ MlpWork carve(void *ws, int64_t c) {
 }
 
 size_t work_bytes(int64_t c) {
-  return align256(2 * (size_t)c * kIn) + 2 * align256(2 * (size_t)c * kHid) + 5 * align256(4 * (size_t)c * kHid) +
+  return 2 * align256(2 * (size_t)c * kIn) + 8 * align256(2 * (size_t)c * kHid) + 5 * align256(4 * (size_t)c * kHid) +
          align256(4 * (size_t)c) + 256;
 }
 
@@ -328,7 +433,7 @@ __device__ inline float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)
 // Features of point row0 + r: from x (fractional, f64 [., 3]) or, with x null,
 // of grid node row0 + r of a grid^3 lattice.
 __global__ void features_kernel(const double *x, int64_t row0, int64_t n, int grid, const int32_t *freq,
-                                __nv_bfloat16 *feat) {
+                                __nv_bfloat16 *feat, __nv_bfloat16 *featT) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= n) return;
   double f[3];
@@ -347,6 +452,10 @@ __global__ void features_kernel(const double *x, int64_t row0, int64_t n, int gr
     float sn, cs;
     sincospif(2.0f * (float)t, &sn, &cs);
     o[j] = __floats2bfloat162_rn(sn, cs);
+    if (featT != nullptr) {
+      featT[(int64_t)(2 * j) * n + r] = __float2bfloat16(sn);
+      featT[(int64_t)(2 * j + 1) * n + r] = __float2bfloat16(cs);
+    }
   }
 }
 
@@ -385,8 +494,9 @@ __global__ void head_kernel(const float *h, int64_t n, const float *w4, const fl
 //   dL/dg = (sigmoid(g) - y) / n,  dz3 = dL/dg * w4 * (1 - exp(-h3)),
 //   grad_w4 += sum_rows dL/dg h3,  grad_b4 += sum_rows dL/dg,  loss += L.
 __global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n, const float *w4, const float *b4,
-                                                       const float *label, float *dz, float *grad_w4,
-                                                       float *grad_b4, float *loss) {
+                                                       const float *label, float *dz, __nv_bfloat16 *dzb,
+                                                       __nv_bfloat16 *dzT, float *grad_w4, float *grad_b4,
+                                                       float *loss) {
   __shared__ float red_w[8][kHid];
   __shared__ float red_b[8], red_l[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -413,7 +523,11 @@ __global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n
     }
     for (int j = 0; j < 8; ++j) {
       dw[j] = fmaf(dg, hv[j], dw[j]);
-      dz[row * kHid + lane + 32 * j] = dg * wl[j] * -expm1f(-hv[j]);
+      const float d = dg * wl[j] * -expm1f(-hv[j]);
+      const int col = lane + 32 * j;
+      dz[row * kHid + col] = d;
+      dzb[row * kHid + col] = __float2bfloat16(d);
+      dzT[(int64_t)col * n + row] = __float2bfloat16(d);
     }
   }
   for (int j = 0; j < 8; ++j) red_w[warp][lane + 32 * j] = dw[j];
@@ -451,8 +565,22 @@ __global__ void __launch_bounds__(kHid) colsum_kernel(const float *z, int64_t n,
 
 // Adam (Kingma & Ba 2015) with bias corrections c1 = 1 / (1 - beta1^t),
 // c2 = 1 / (1 - beta2^t); refreshes the bfloat16 copy and zeroes the gradient.
-__global__ void adam_kernel(float *p, __nv_bfloat16 *pb, float *g, float *m, float *v, int64_t n, float lr,
-                            float b1, float b2, float eps, float c1, float c2) {
+// bfloat16 copies of a parameter: the flat copy, and for W2 / W3 the transposed copy
+// (W^T[in][out]) that the backward GEMMs read as a K-contiguous operand.
+__device__ inline void store_bf16(__nv_bfloat16 *pb, __nv_bfloat16 *pbt, int64_t i, float v) {
+  const __nv_bfloat16 b = __float2bfloat16(v);
+  pb[i] = b;
+  if (i >= kOffW2 && i < kOffB2) {
+    const int64_t l = i - kOffW2;
+    pbt[(l % kHid) * kHid + l / kHid] = b;
+  } else if (i >= kOffW3 && i < kOffB3) {
+    const int64_t l = i - kOffW3;
+    pbt[kHid * kHid + (l % kHid) * kHid + l / kHid] = b;
+  }
+}
+
+__global__ void adam_kernel(float *p, __nv_bfloat16 *pb, __nv_bfloat16 *pbt, float *g, float *m, float *v, int64_t n,
+                            float lr, float b1, float b2, float eps, float c1, float c2) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i];
@@ -462,13 +590,14 @@ __global__ void adam_kernel(float *p, __nv_bfloat16 *pb, float *g, float *m, flo
   v[i] = vi;
   const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
   p[i] = pi;
-  pb[i] = __float2bfloat16(pi);
+  store_bf16(pb, pbt, i, pi);
   g[i] = 0.f;
 }
 
 // Weights uniform with variance 1 / fan_in (Philox keyed by (seed, index)),
 // biases zero; optimiser state and gradients zero.
-__global__ void init_kernel(float *p, __nv_bfloat16 *pb, float *g, float *m, float *v, uint64_t seed) {
+__global__ void init_kernel(float *p, __nv_bfloat16 *pb, __nv_bfloat16 *pbt, float *g, float *m, float *v,
+                            uint64_t seed) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= kParams) return;
   float fan = 0.f;
@@ -482,7 +611,7 @@ __global__ void init_kernel(float *p, __nv_bfloat16 *pb, float *g, float *m, flo
     val = (2.f * u - 1.f) * sqrtf(3.f / fan);
   }
   p[i] = val;
-  pb[i] = __float2bfloat16(val);
+  store_bf16(pb, pbt, i, val);
   g[i] = 0.f;
   m[i] = 0.f;
   v[i] = 0.f;
@@ -547,38 +676,75 @@ __global__ void __launch_bounds__(1024) grid_normalise_kernel(float *node, int64
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) node[i] += fl;
 }
 
-// cdf[c] = sum_{c' < c} mass(c'), mass = mean of the cell's 8 corners (float64);
-// one block of 1024 threads, each owning a contiguous run of cells.
-__global__ void __launch_bounds__(1024) grid_cdf_kernel(const float *node, int g, double *cdf) {
-  __shared__ double part[1024];
-  const int64_t n = (int64_t)g * g * g;
-  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
-  const int64_t c0 = (int64_t)threadIdx.x * per, c1 = min(n, c0 + per);
-  auto mass = [&](int64_t c) {
-    const int i = (int)(c / ((int64_t)g * g)), j = (int)((c / g) % g), k = (int)(c % g);
-    double d[8];
-    grid_corners(node, g, i, j, k, d);
-    double s = 0.0;
-    for (int b = 0; b < 8; ++b) s += d[b];
-    return s * 0.125;
-  };
-  double local = 0.0;
-  for (int64_t c = c0; c < c1; ++c) local += mass(c);
-  part[threadIdx.x] = local;
+// cdf[c] = sum_{c' < c} mass(c'), mass = mean of the cell's 8 corners (float64),
+// in three passes: each block of 256 threads scans kCdfPerBlock cells (8 per thread)
+// and records its total, one block scans the totals, and the block offsets are added.
+constexpr int kCdfThreads = 256, kCdfPerThread = 8, kCdfPerBlock = kCdfThreads * kCdfPerThread;
+
+__device__ inline double cell_mass(const float *node, int g, int64_t c) {
+  const int i = (int)(c / ((int64_t)g * g)), j = (int)((c / g) % g), k = (int)(c % g);
+  double d[8];
+  grid_corners(node, g, i, j, k, d);
+  double s = 0.0;
+  for (int b = 0; b < 8; ++b) s += d[b];
+  return s * 0.125;
+}
+
+// inclusive scan of one double per thread over a block of kCdfThreads threads
+__device__ inline double block_inclusive_scan(double v, double *sh) {
+  sh[threadIdx.x] = v;
   __syncthreads();
-  // inclusive Hillis-Steele scan over the 1024 partial sums
-  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-    const double add = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0.0;
+  for (int o = 1; o < kCdfThreads; o <<= 1) {
+    const double add = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0.0;
     __syncthreads();
-    part[threadIdx.x] += add;
+    sh[threadIdx.x] += add;
     __syncthreads();
   }
-  double run = part[threadIdx.x] - local;
-  for (int64_t c = c0; c < c1; ++c) {
-    cdf[c] = run;
-    run += mass(c);
+  const double r = sh[threadIdx.x];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kCdfThreads) grid_cdf_local_kernel(const float *node, int g, double *cdf,
+                                                                      double *block_total) {
+  __shared__ double sh[kCdfThreads];
+  const int64_t n = (int64_t)g * g * g;
+  const int64_t c0 = (int64_t)blockIdx.x * kCdfPerBlock + (int64_t)threadIdx.x * kCdfPerThread;
+  double m[kCdfPerThread], local = 0.0;
+  for (int t = 0; t < kCdfPerThread; ++t) {
+    m[t] = c0 + t < n ? cell_mass(node, g, c0 + t) : 0.0;
+    local += m[t];
   }
-  if (c0 < c1 && c1 == n) cdf[n] = run;
+  double run = block_inclusive_scan(local, sh) - local;
+  for (int t = 0; t < kCdfPerThread; ++t) {
+    if (c0 + t < n) cdf[c0 + t] = run;
+    run += m[t];
+  }
+  if (threadIdx.x == kCdfThreads - 1) block_total[blockIdx.x] = run;
+}
+
+// exclusive scan of the block totals (one block; offsets written in place), cdf[n] = total
+__global__ void __launch_bounds__(kCdfThreads) grid_cdf_totals_kernel(double *block_total, int n_blocks, double *cdf,
+                                                                       int64_t n) {
+  __shared__ double sh[kCdfThreads];
+  __shared__ double round_total;
+  double carry = 0.0;
+  for (int b0 = 0; b0 < n_blocks; b0 += kCdfThreads) {
+    const int b = b0 + threadIdx.x;
+    const double v = b < n_blocks ? block_total[b] : 0.0;
+    const double inc = block_inclusive_scan(v, sh);
+    if (b < n_blocks) block_total[b] = carry + inc - v;
+    if (threadIdx.x == kCdfThreads - 1) round_total = inc;
+    __syncthreads();
+    carry += round_total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cdf[n] = carry;
+}
+
+__global__ void grid_cdf_offset_kernel(double *cdf, int64_t n, const double *block_offset) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c < n) cdf[c] += block_offset[c / kCdfPerBlock];
 }
 
 __global__ void proposal_sample_kernel(const float *node, const double *cdf, int g, int64_t n, uint64_t seed,
@@ -604,18 +770,19 @@ __global__ void proposal_density_kernel(const float *node, const double *cdf, in
 
 inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-// Forward pass of rows [row0, row0 + c) into w (activations) and g_out.
+// Forward pass of rows [row0, row0 + c) into w (activations) and g_out; ``train``
+// also writes the transposed copies the weight gradients need.
 int32_t forward_chunk(const kups_mlp *net, const double *x, int64_t row0, int64_t c, int grid, const MlpWork &w,
-                      float *g_out, kups_status *status, cudaStream_t st) {
+                      float *g_out, kups_status *status, cudaStream_t st, bool train = false) {
   const __nv_bfloat16 *pb = (const __nv_bfloat16 *)net->param_bf16;
   const float *p = net->param;
-  features_kernel<<<blocks(c, 256), 256, 0, st>>>(x, row0, c, grid, net->freq, w.feat);
+  features_kernel<<<blocks(c, 256), 256, 0, st>>>(x, row0, c, grid, net->freq, w.feat, train ? w.featT : nullptr);
   int32_t rc;
   rc = gemm_call(Op{w.feat, 1, kIn, 1}, Op{pb + kOffW1, 1, kIn, 1}, w.h1, kHid, 1, w.h1b, p + kOffB1, nullptr, 0,
-                 (int)c, kHid, kIn, 0.f, 2, 1, status, st);
+                 (int)c, kHid, kIn, 0.f, 2, 1, status, st, train ? w.h1T : nullptr);
   if (rc) return rc;
   rc = gemm_call(Op{w.h1b, 1, kHid, 1}, Op{pb + kOffW2, 1, kHid, 1}, w.h2, kHid, 1, w.h2b, p + kOffB2, nullptr, 0,
-                 (int)c, kHid, kHid, 0.f, 2, 1, status, st);
+                 (int)c, kHid, kHid, 0.f, 2, 1, status, st, train ? w.h2T : nullptr);
   if (rc) return rc;
   rc = gemm_call(Op{w.h2b, 1, kHid, 1}, Op{pb + kOffW3, 1, kHid, 1}, w.h3, kHid, 1, nullptr, p + kOffB3, nullptr, 0,
                  (int)c, kHid, kHid, 0.f, 2, 1, status, st);
@@ -653,6 +820,8 @@ extern "C" int32_t kups_gemm_bf16(const void *a, int32_t a_bf16, int64_t sa_row,
   g.m = m; g.n = n; g.k = k; g.alpha = alpha; g.beta = beta; g.act = act;
   g.a_bf16 = a_bf16; g.b_bf16 = b_bf16; g.c_bf16 = c_bf16; g.c2_bf16 = c2_bf16; g.gate_kind = gate_kind;
   g.split_k = split_k;
+  g.c3 = nullptr;
+  g.sc3r = g.sc3c = 0;
   return dispatch_gemm(g, status, (cudaStream_t)stream);
 }
 
@@ -663,7 +832,8 @@ extern "C" size_t kups_mlp_workspace_bytes(int64_t n_points) {
 extern "C" int32_t kups_mlp_init(const kups_mlp *net, uint64_t seed, void *stream) {
   if (net == nullptr) return KUPS_ERR_INVALID;
   init_kernel<<<blocks(kParams, 256), 256, 0, (cudaStream_t)stream>>>(
-      net->param, (__nv_bfloat16 *)net->param_bf16, net->grad, net->adam_m, net->adam_v, seed);
+      net->param, (__nv_bfloat16 *)net->param_bf16, (__nv_bfloat16 *)net->param_bf16_t, net->grad, net->adam_m,
+      net->adam_v, seed);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 
@@ -694,35 +864,37 @@ extern "C" int32_t kups_mlp_bwd(const kups_mlp *net, const double *x, const floa
   if (workspace_bytes < kups_mlp_workspace_bytes(n)) return KUPS_ERR_INVALID;
   cudaStream_t st = (cudaStream_t)stream;
   const MlpWork w = carve(workspace, n);
-  int32_t rc = forward_chunk(net, x, 0, n, 0, w, nullptr, status, st);
+  int32_t rc = forward_chunk(net, x, 0, n, 0, w, nullptr, status, st, true);
   if (rc) return rc;
-  const __nv_bfloat16 *pb = (const __nv_bfloat16 *)net->param_bf16;
+  const __nv_bfloat16 *pbt = (const __nv_bfloat16 *)net->param_bf16_t;  // W2^T, W3^T
   const float *p = net->param;
   float *gr = net->grad;
   const int sms = 148;
   head_nce_kernel<<<std::min<int64_t>(blocks(n, 8), 4 * sms), 256, 0, st>>>(
-      w.h3, n, p + kOffW4, p + kOffB4, label, w.dza, gr + kOffW4, gr + kOffB4, loss);
+      w.h3, n, p + kOffW4, p + kOffB4, label, w.dza, w.dzab, w.dzaT, gr + kOffW4, gr + kOffB4, loss);
   const int split = split_for(n);
   const unsigned cs_blocks = (unsigned)std::min<int64_t>(blocks(n, 64), 2 * sms);
+  // Every GEMM operand is bfloat16 with K contiguous: the weight gradients read the
+  // transposed copies ([width, n], K = points), the input gradients W^T.
   // layer 3: dW3 += dz3^T h2, db3 += colsum dz3, dz2 = (dz3 W3) * (1 - exp(-h2))
-  rc = gemm_call(Op{w.dza, 0, 1, kHid}, Op{w.h2b, 1, 1, kHid}, gr + kOffW3, kHid, 1, nullptr, nullptr, nullptr, 0,
-                 kHid, kHid, n, 1.f, 0, split, status, st);
+  rc = gemm_call(Op{w.dzaT, 1, n, 1}, Op{w.h2T, 1, n, 1}, gr + kOffW3, kHid, 1, nullptr, nullptr, nullptr, 0, kHid,
+                 kHid, n, 1.f, 0, split, status, st);
   if (rc) return rc;
   colsum_kernel<<<cs_blocks, kHid, 0, st>>>(w.dza, n, gr + kOffB3);
-  rc = gemm_call(Op{w.dza, 0, kHid, 1}, Op{pb + kOffW3, 1, 1, kHid}, w.dzb, kHid, 1, nullptr, nullptr, w.h2, 3, n,
-                 kHid, kHid, 0.f, 0, 1, status, st);
+  rc = gemm_call(Op{w.dzab, 1, kHid, 1}, Op{pbt + kHid * kHid, 1, kHid, 1}, w.dzb, kHid, 1, w.dzbb, nullptr, w.h2, 3,
+                 n, kHid, kHid, 0.f, 0, 1, status, st, w.dzbT);
   if (rc) return rc;
   // layer 2
-  rc = gemm_call(Op{w.dzb, 0, 1, kHid}, Op{w.h1b, 1, 1, kHid}, gr + kOffW2, kHid, 1, nullptr, nullptr, nullptr, 0,
-                 kHid, kHid, n, 1.f, 0, split, status, st);
+  rc = gemm_call(Op{w.dzbT, 1, n, 1}, Op{w.h1T, 1, n, 1}, gr + kOffW2, kHid, 1, nullptr, nullptr, nullptr, 0, kHid,
+                 kHid, n, 1.f, 0, split, status, st);
   if (rc) return rc;
   colsum_kernel<<<cs_blocks, kHid, 0, st>>>(w.dzb, n, gr + kOffB2);
-  rc = gemm_call(Op{w.dzb, 0, kHid, 1}, Op{pb + kOffW2, 1, 1, kHid}, w.dza, kHid, 1, nullptr, nullptr, w.h1, 3, n,
-                 kHid, kHid, 0.f, 0, 1, status, st);
+  rc = gemm_call(Op{w.dzbb, 1, kHid, 1}, Op{pbt, 1, kHid, 1}, w.dza, kHid, 1, nullptr, nullptr, w.h1, 3, n, kHid,
+                 kHid, 0.f, 0, 1, status, st, w.dzaT);
   if (rc) return rc;
   // layer 1 (no gradient into the features)
-  rc = gemm_call(Op{w.dza, 0, 1, kHid}, Op{w.feat, 1, 1, kIn}, gr + kOffW1, kIn, 1, nullptr, nullptr, nullptr, 0,
-                 kHid, kIn, n, 1.f, 0, split, status, st);
+  rc = gemm_call(Op{w.dzaT, 1, n, 1}, Op{w.featT, 1, n, 1}, gr + kOffW1, kIn, 1, nullptr, nullptr, nullptr, 0, kHid,
+                 kIn, n, 1.f, 0, split, status, st);
   if (rc) return rc;
   colsum_kernel<<<cs_blocks, kHid, 0, st>>>(w.dza, n, gr + kOffB1);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
@@ -734,8 +906,8 @@ extern "C" int32_t kups_mlp_adam(const kups_mlp *net, int64_t t, float lr, float
   const float c1 = (float)(1.0 / (1.0 - pow((double)beta1, (double)t)));
   const float c2 = (float)(1.0 / (1.0 - pow((double)beta2, (double)t)));
   adam_kernel<<<blocks(kParams, 256), 256, 0, (cudaStream_t)stream>>>(
-      net->param, (__nv_bfloat16 *)net->param_bf16, net->grad, net->adam_m, net->adam_v, kParams, lr, beta1, beta2,
-      eps, c1, c2);
+      net->param, (__nv_bfloat16 *)net->param_bf16, (__nv_bfloat16 *)net->param_bf16_t, net->grad, net->adam_m,
+      net->adam_v, kParams, lr, beta1, beta2, eps, c1, c2);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 
@@ -753,7 +925,12 @@ extern "C" int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float t
     if (rc) return rc;
   }
   grid_normalise_kernel<<<1, 1024, 0, st>>>(node, n, temper, floor_frac, status);
-  grid_cdf_kernel<<<1, 1024, 0, st>>>(node, grid, cdf);
+  // three-pass scan; the block totals live in the (no longer needed) activation buffer
+  const int n_blocks = (int)((n + kCdfPerBlock - 1) / kCdfPerBlock);
+  double *totals = reinterpret_cast<double *>(w.h1);
+  grid_cdf_local_kernel<<<n_blocks, kCdfThreads, 0, st>>>(node, grid, cdf, totals);
+  grid_cdf_totals_kernel<<<1, kCdfThreads, 0, st>>>(totals, n_blocks, cdf, n);
+  grid_cdf_offset_kernel<<<blocks(n, 256), 256, 0, st>>>(cdf, n, totals);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 

@@ -99,13 +99,14 @@ class LearnedInsertionProposal:
         dev = "cuda"
         self.param = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
         self.param_bf16 = torch.zeros(N_PARAMS, dtype=torch.bfloat16, device=dev)
+        self.param_bf16_t = torch.zeros(2 * 256 * 256, dtype=torch.bfloat16, device=dev)
         self.grad = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
         self.m = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
         self.v = torch.zeros(N_PARAMS, dtype=torch.float32, device=dev)
         self.freq = torch.as_tensor(default_frequencies() if freq is None else np.asarray(freq, np.int32),
                                     device=dev).contiguous()
         self.net = _lib.Mlp(self.param.data_ptr(), self.param_bf16.data_ptr(), self.grad.data_ptr(),
-                            self.m.data_ptr(), self.v.data_ptr(), self.freq.data_ptr())
+                            self.m.data_ptr(), self.v.data_ptr(), self.freq.data_ptr(), self.param_bf16_t.data_ptr())
         self.grid, self.floor, self.temper = int(grid), float(floor), float(temper)
         self.node = torch.zeros(self.grid ** 3, dtype=torch.float32, device=dev)
         self.cdf = torch.zeros(self.grid ** 3 + 1, dtype=torch.float64, device=dev)

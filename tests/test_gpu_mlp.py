@@ -210,3 +210,16 @@ def test_training_concentrates_the_density_on_the_data():
     # ln q of the two blobs (width 0.06 of the cell) averages ~ 3 nats for the true
     # density; a 16^3 grid and the 5 % floor keep part of it
     assert mean_lq > 1.5, mean_lq
+
+
+@pytest.mark.parametrize("m,n,k", [(200, 100, 136), (384, 256, 512), (64, 64, 64), (1000, 256, 256)])
+def test_gemm_bf16_row_major_operands(m, n, k):
+    """bfloat16, K-contiguous operands (16-byte copies into shared memory): ragged M / N
+    (zero-filled rows) and K not a multiple of the 64-wide K chunk."""
+    from kups_gb300.mlp import gemm
+
+    g = torch.Generator(device="cuda").manual_seed(m * 7 + n + k)
+    a = torch.randn(m, k, device="cuda", generator=g).bfloat16()
+    b = torch.randn(n, k, device="cuda", generator=g).bfloat16()
+    c = gemm(a, b)
+    assert rel(c, a.float() @ b.float().T) < 1e-5
