@@ -27,7 +27,7 @@ namespace {
 
 constexpr int kBM = 128;
 constexpr int kBK = 64;
-constexpr int kGemmThreads = 128;
+constexpr int kGemmThreads = 256;  // 8 warps: warps w and w + 4 share TMEM lanes 32 (w % 4) ..
 constexpr long long kWaitLimit = 1LL << 26;
 
 __device__ inline uint32_t smem_u32(const void *p) {
@@ -72,7 +72,7 @@ __device__ inline bool mbar_wait(uint32_t addr, uint32_t phase) {
 
 __device__ inline float act_fn(float x, int act) {
   if (act == 1) return fmaxf(x, 0.f);                      // ReLU
-  if (act == 2) return x > 20.f ? x : log1pf(expf(x));     // softplus
+  if (act == 2) return x > 20.f ? x : log1pf(__expf(x));  // softplus (SFU exp)
   return x;
 }
 
@@ -245,16 +245,18 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
   if (!ok) {
     if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
   } else if (kc_begin < kc_end) {  // an empty K slice holds no accumulator
-    // epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (one row each), 32 columns at a
-    // time.  Row-major float32 / bfloat16 outputs go through a padded 32 x 33 shared-memory
-    // block so that a warp stores 128 contiguous bytes of one row per instruction; the
-    // transposed bfloat16 copy (c3) is written straight from the lane = row layout.
-    const int row = m0 + warp * 32 + lane;
-    const bool staged = g.split_k == 1 && g.scc == 1 && !g.c_bf16 && (g.c2 == nullptr || (g.c2_bf16 && g.sc2c == 1));
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (one row each) and the column
+    // half w / 4, 32 columns at a time.  Row-major float32 / bfloat16 outputs go through a
+    // padded 32 x 33 shared-memory block so that a warp stores 128 contiguous bytes of one
+    // row per instruction; the transposed bfloat16 copy (c3) is written straight from the
+    // lane = row layout.
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = m0 + quarter * 32 + lane;
+    const bool staged = g.scc == 1 && !g.c_bf16 && (g.c2 == nullptr || (g.c2_bf16 && g.sc2c == 1));
     float *blk = reinterpret_cast<float *>(smem) + warp * 32 * 33;  // pipeline stages are free now
-    for (int c0 = 0; c0 < BN; c0 += 32) {
+    for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
       uint32_t r[32];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
           "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
@@ -271,7 +273,8 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
           if (col >= g.n) continue;
           float v = g.alpha * __uint_as_float(r[i]);
           if (g.split_k > 1) {
-            atomicAdd((float *)g.c + (int64_t)row * g.scr + (int64_t)col * g.scc, v);
+            if (staged) blk[lane * 33 + i] = v;
+            else atomicAdd((float *)g.c + (int64_t)row * g.scr + (int64_t)col * g.scc, v);
             continue;
           }
           if (g.beta != 0.f) {
@@ -305,9 +308,13 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
         __syncwarp();
         const int col = n0 + c0 + lane;
         for (int rr = 0; rr < 32; ++rr) {
-          const int row2 = m0 + warp * 32 + rr;
+          const int row2 = m0 + quarter * 32 + rr;
           if (row2 >= g.m || col >= g.n) continue;
           const float v = blk[rr * 33 + lane];
+          if (g.split_k > 1) {  // a warp adds 32 consecutive floats of one row
+            atomicAdd((float *)g.c + (int64_t)row2 * g.scr + col, v);
+            continue;
+          }
           ((float *)g.c)[(int64_t)row2 * g.scr + col] = v;
           if (g.c2) ((__nv_bfloat16 *)g.c2)[(int64_t)row2 * g.sc2r + col] = __float2bfloat16(v);
         }
@@ -332,9 +339,14 @@ int32_t launch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t stream)
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 
+// Tile width: the widest of 256 / 128 / 64 that still covers N, narrowed while the grid
+// would leave SMs idle (fewer than two CTAs per SM of 148).
 int32_t dispatch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t st) {
-  if (g.n <= 64) return launch_gemm<64>(g, status, st);
-  if (g.n <= 128) return launch_gemm<128>(g, status, st);
+  const int64_t rows = ((int64_t)g.m + kBM - 1) / kBM * g.split_k;
+  int bn = g.n <= 64 ? 64 : g.n <= 128 ? 128 : 256;
+  while (bn > 64 && rows * ((g.n + bn - 1) / bn) < 2 * 148) bn >>= 1;
+  if (bn == 64) return launch_gemm<64>(g, status, st);
+  if (bn == 128) return launch_gemm<128>(g, status, st);
   return launch_gemm<256>(g, status, st);
 }
 
