@@ -245,14 +245,13 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
   if (!ok) {
     if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
   } else if (kc_begin < kc_end) {  // an empty K slice holds no accumulator
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (one row each) and the column
-    // half w / 4, 32 columns at a time.  Row-major float32 / bfloat16 outputs go through a
-    // padded 32 x 33 shared-memory block so that a warp stores 128 contiguous bytes of one
-    // row per instruction; the transposed bfloat16 copy (c3) is written straight from the
-    // lane = row layout.
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) and the column half
+    // w / 4, 32 columns at a time, into a padded 32 x 33 shared-memory block.  The
+    // elementwise terms run with lane = column (coalesced bias / gate / C loads and
+    // row-major stores, 128 contiguous bytes of one row per instruction); the transposed
+    // bfloat16 copy (c3) is written back with lane = row (coalesced as well).
     const int quarter = warp & 3, half = warp >> 2;
-    const int row = m0 + quarter * 32 + lane;
-    const bool staged = g.scc == 1 && !g.c_bf16 && (g.c2 == nullptr || (g.c2_bf16 && g.sc2c == 1));
+    const int rbase = m0 + quarter * 32;
     float *blk = reinterpret_cast<float *>(smem) + warp * 32 * 33;  // pipeline stages are free now
     for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
       uint32_t r[32];
@@ -266,22 +265,24 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
             "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < g.m) {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const int col = n0 + c0 + i;
-          if (col >= g.n) continue;
-          float v = g.alpha * __uint_as_float(r[i]);
+      for (int i = 0; i < 32; ++i) blk[lane * 33 + i] = __uint_as_float(r[i]);
+      __syncwarp();
+      const int col = n0 + c0 + lane;
+      if (col < g.n) {
+        const float bias = g.bias ? g.bias[col] : 0.f;
+#pragma unroll 1
+        for (int rr = 0; rr < 32; ++rr) {
+          const int row = rbase + rr;
+          if (row >= g.m) break;
+          float v = g.alpha * blk[rr * 33 + lane];
+          const int64_t o = (int64_t)row * g.scr + (int64_t)col * g.scc;
           if (g.split_k > 1) {
-            if (staged) blk[lane * 33 + i] = v;
-            else atomicAdd((float *)g.c + (int64_t)row * g.scr + (int64_t)col * g.scc, v);
+            atomicAdd((float *)g.c + o, v);
             continue;
           }
-          if (g.beta != 0.f) {
-            const int64_t o = (int64_t)row * g.scr + (int64_t)col * g.scc;
-            v += g.beta * (g.c_bf16 ? __bfloat162float(((__nv_bfloat16 *)g.c)[o]) : ((float *)g.c)[o]);
-          }
-          if (g.bias) v += g.bias[col];
+          if (g.beta != 0.f) v += g.beta * (g.c_bf16 ? __bfloat162float(((__nv_bfloat16 *)g.c)[o]) : ((float *)g.c)[o]);
+          v += bias;
           if (g.gate_kind) {
             const float pre = g.gate[(int64_t)row * g.sgr + (int64_t)col * g.sgc];
             v *= g.gate_kind == 1 ? (pre > 0.f ? 1.f : 0.f)
@@ -289,12 +290,6 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
                                     : -expm1f(-pre);
           }
           v = act_fn(v, g.act);
-          if (g.c3) ((__nv_bfloat16 *)g.c3)[(int64_t)row * g.sc3r + (int64_t)col * g.sc3c] = __float2bfloat16(v);
-          if (staged) {
-            blk[lane * 33 + i] = v;
-            continue;
-          }
-          const int64_t o = (int64_t)row * g.scr + (int64_t)col * g.scc;
           if (g.c_bf16) ((__nv_bfloat16 *)g.c)[o] = __float2bfloat16(v);
           else ((float *)g.c)[o] = v;
           if (g.c2) {
@@ -302,24 +297,23 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
             if (g.c2_bf16) ((__nv_bfloat16 *)g.c2)[o2] = __float2bfloat16(v);
             else ((float *)g.c2)[o2] = v;
           }
+          blk[rr * 33 + lane] = v;
         }
       }
-      if (staged) {
-        __syncwarp();
-        const int col = n0 + c0 + lane;
-        for (int rr = 0; rr < 32; ++rr) {
-          const int row2 = m0 + quarter * 32 + rr;
-          if (row2 >= g.m || col >= g.n) continue;
-          const float v = blk[rr * 33 + lane];
-          if (g.split_k > 1) {  // a warp adds 32 consecutive floats of one row
-            atomicAdd((float *)g.c + (int64_t)row2 * g.scr + col, v);
-            continue;
+      __syncwarp();
+      if (g.c3 != nullptr && g.split_k == 1) {
+        const int row = rbase + lane;
+        if (row < g.m) {
+#pragma unroll 1
+          for (int i = 0; i < 32; ++i) {
+            const int cc = n0 + c0 + i;
+            if (cc >= g.n) break;
+            ((__nv_bfloat16 *)g.c3)[(int64_t)row * g.sc3r + (int64_t)cc * g.sc3c] =
+                __float2bfloat16(blk[lane * 33 + i]);
           }
-          ((float *)g.c)[(int64_t)row2 * g.scr + col] = v;
-          if (g.c2) ((__nv_bfloat16 *)g.c2)[(int64_t)row2 * g.sc2r + col] = __float2bfloat16(v);
         }
-        __syncwarp();
       }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
