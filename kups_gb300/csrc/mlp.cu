@@ -333,11 +333,12 @@ int32_t launch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t stream)
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 
-// Tile width: the widest of 256 / 128 / 64 that still covers N, narrowed while the grid
-// would leave SMs idle (fewer than two CTAs per SM of 148).
+// Tile width: 128 (64 for N <= 64), narrowed to 64 while the grid would leave SMs idle
+// (fewer than two CTAs per SM of 148).  128-wide tiles (64 KB of pipeline buffers, three
+// CTAs per SM) beat 256-wide ones (two CTAs per SM) on the network's K <= 256 GEMMs.
 int32_t dispatch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t st) {
   const int64_t rows = ((int64_t)g.m + kBM - 1) / kBM * g.split_k;
-  int bn = g.n <= 64 ? 64 : g.n <= 128 ? 128 : 256;
+  int bn = g.n <= 64 ? 64 : 128;
   while (bn > 64 && rows * ((g.n + bn - 1) / bn) < 2 * 148) bn >>= 1;
   if (bn == 64) return launch_gemm<64>(g, status, st);
   if (bn == 128) return launch_gemm<128>(g, status, st);
