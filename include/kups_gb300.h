@@ -263,6 +263,20 @@ int32_t kups_ewald_recip_static(const double *positions, const double *charges,
                                 double *structure_factor, kups_status *status, void *stream);
 int32_t kups_ewald_self(const double *charges, const int32_t *sys_offset, int32_t n_systems,
                         const double *alpha, double coulomb_k, double *energy, void *stream);
+/* kups_lj_ewald_real_forces: the same real-space sum as kups_pair_edges with
+ * terms 1 | 2 over the neighbour list at the cutoff, for systems grouped by
+ * sys_offset whose cell widths are all at least twice the larger cutoff (every
+ * pair within a cutoff is then its minimum image; otherwise the system is skipped
+ * and KUPS_ERR_UNSUPPORTED is recorded): all pairs of a system in shared-memory
+ * tiles, no stored list, float32 pair arithmetic (differences formed in
+ * float64), energy [S] float64 (written), grad = dE/dx [N, 3] (written).
+ * Used by the LJ + Ewald MD propagator; 1 <= n_species <= 8. */
+int32_t kups_lj_ewald_real_forces(const double *positions, const double *charges, const int32_t *species,
+                                  const int32_t *sys_offset, int32_t n_systems, int32_t max_atoms_per_system,
+                                  const double *tril, const double *lj_sigma, const double *lj_epsilon,
+                                  int32_t n_species, const double *lj_cutoff, const double *alpha,
+                                  const double *ewald_cutoff, double coulomb_k, int32_t terms, double *energy,
+                                  double *grad, kups_status *status, void *stream);
 int32_t kups_pair_edges(const double *positions, const int32_t *system, const int32_t *species,
                         const double *charges, int64_t n_particles, const double *tril,
                         int32_t n_systems, const double *lj_sigma, const double *lj_epsilon,

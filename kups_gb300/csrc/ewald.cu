@@ -21,6 +21,7 @@
 // e^{i theta} is built per atom from per-axis tables e^{2 pi i m f_a},
 // m in [-M, M] (the standard Ewald recurrence), so each (atom, k) costs two
 // complex products.
+#include <algorithm>
 #include <mutex>
 
 #include "common.cuh"
@@ -58,10 +59,20 @@ __device__ inline void kvec(const double *inv, const int n[3], double k[3]) {
   k[2] = tp * (inv[3] * n[0] + inv[4] * n[1] + inv[5] * n[2]);
 }
 
+// One block per system: cell, inverse, volume, and the largest |n_a| over the
+// system's k vectors (block reduction).
 __global__ void recip_setup_kernel(const double *tril, const int32_t *kn, int32_t s, int32_t nk,
                                    RecipSys *sys, kups_status *status) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s) return;
+  __shared__ int mx[3];
+  const int i = blockIdx.x;
+  if (threadIdx.x < 3) mx[threadIdx.x] = 0;
+  __syncthreads();
+  int m[3] = {0, 0, 0};
+  for (int k = threadIdx.x; k < nk; k += blockDim.x)
+    for (int a = 0; a < 3; ++a) m[a] = max(m[a], abs(kn[((int64_t)i * nk + k) * 3 + a]));
+  for (int a = 0; a < 3; ++a) atomicMax(&mx[a], m[a]);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   RecipSys r;
   const Tril64 L = load_tril64(tril + 6 * (int64_t)i);
   const Tril64 inv = inverse_tril64(L);
@@ -70,15 +81,13 @@ __global__ void recip_setup_kernel(const double *tril, const int32_t *kn, int32_
     r.inv[k] = inv.t[k];
   }
   r.volume = fabs(L.t[0] * L.t[2] * L.t[5]);
-  int m[3] = {0, 0, 0};
-  for (int k = 0; k < nk; ++k)
-    for (int a = 0; a < 3; ++a) m[a] = max(m[a], abs(kn[((int64_t)i * nk + k) * 3 + a]));
   for (int a = 0; a < 3; ++a) {
-    if (m[a] > kMaxM) {
+    int v = mx[a];
+    if (v > kMaxM) {
       status_error(status, KUPS_ERR_UNSUPPORTED, i);
-      m[a] = kMaxM;
+      v = kMaxM;
     }
-    r.m[a] = m[a];
+    r.m[a] = v;
   }
   sys[i] = r;
 }
@@ -151,14 +160,14 @@ __global__ void recip_energy_kernel(const int32_t *kn, int32_t nk, const double 
                                     const RecipSys *sysp, const double *sk, double ke,
                                     Coef *coef, double *energy, double *dtril) {
   __shared__ double red[40];
-  const int s = blockIdx.x;
+  const int s = blockIdx.y;
   const RecipSys &P = sysp[s];
   const double a = alpha[s];
   const double tp = 6.283185307179586476925286766559;
   double e = 0.0, w[6] = {0, 0, 0, 0, 0, 0};
   // L^-T k: (L^-T)_{ab} = inv_{ba}
   const double *iv = P.inv;
-  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nk; k += gridDim.x * blockDim.x) {
     const int *nv = kn + ((int64_t)s * nk + k) * 3;
     const int n3[3] = {nv[0], nv[1], nv[2]};
     double kv[3];
@@ -191,15 +200,16 @@ __global__ void recip_energy_kernel(const int32_t *kn, int32_t nk, const double 
     wt[c] = block_sum(w[c], red);
     __syncthreads();
   }
+  // blocks of k vectors add their shares (energy and dtril zeroed by the launcher)
   if (threadIdx.x == 0) {
-    energy[s] = et;
+    atomicAdd(&energy[s], et);
     if (dtril) {
       const int diag[6] = {1, 0, 1, 0, 0, 1};
       const int dk[6] = {0, -1, 2, -1, -1, 5};
       for (int c = 0; c < 6; ++c) {
         double v = -wt[c];
         if (diag[c]) v -= et / P.L[dk[c]];
-        dtril[6 * (int64_t)s + c] = v;  // the sum_i f F part is added by the force kernel
+        atomicAdd(&dtril[6 * (int64_t)s + c], v);  // the sum_i f F part is added by the force kernel
       }
     }
   }
@@ -380,6 +390,112 @@ __global__ void pair_edges_kernel(const double *pos, const int32_t *system, cons
   }
 }
 
+// Real-space Lennard-Jones + Ewald forces of systems whose cell widths are all at
+// least twice the larger cutoff, so that every pair within a cutoff is its minimum
+// image and each ordered pair (i, j != i) is counted once: the edge set of
+// neighbour_list at rc with the energies of lennard_jones_energy /
+// ewald_short_range_energy (each pair term halved over the two directions), with no
+// stored list.  A block owns 16 atoms; each half-warp holds all 16 (lane % 16 = atom)
+// and the 32 half-warps split the partners j, so a half-warp reads one partner at a
+// time (a broadcast from L1).  The difference is formed in float64, the minimum image
+// and pair terms in float32, the 32 partial forces are summed in a fixed order through
+// shared memory and the energy is float64.
+constexpr int kRealAtoms = 16, kRealWarps = 16, kRealStreams = 2 * kRealWarps;
+
+__global__ void __launch_bounds__(32 * kRealWarps) real_allpairs_kernel(
+    const double *pos, const double *q, const int32_t *species, const int32_t *sys_offset, const double *tril,
+    const double *lj_sigma, const double *lj_eps, int nsp, const double *rc_lj, const double *alpha,
+    const double *rc_ew, double ke, int terms, double *energy, double *grad, kups_status *status) {
+  __shared__ float2 ljt[64];
+  __shared__ float part[kRealStreams][kRealAtoms][3];
+  __shared__ double red[40];
+  const int s = blockIdx.y;
+  const int a0 = sys_offset[s], n = sys_offset[s + 1] - a0;
+  if ((int)blockIdx.x * kRealAtoms >= n) return;  // uniform over the block
+  const Tril64 L64 = load_tril64(tril + 6 * (int64_t)s);
+  const Tril64 I64 = inverse_tril64(L64);
+  double w[3];
+  perpendicular_widths64(L64, w);
+  const double rlj = (terms & 1) ? rc_lj[s] : 0.0, rew = (terms & 2) ? rc_ew[s] : 0.0;
+  const double rmax = fmax(rlj, rew);
+  if (fmin(w[0], fmin(w[1], w[2])) < 2.0 * rmax) {
+    if (threadIdx.x == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
+    return;
+  }
+  float L[6], I[6];
+  for (int k = 0; k < 6; ++k) {
+    L[k] = (float)L64.t[k];
+    I[k] = (float)I64.t[k];
+  }
+  if ((terms & 1) && nsp * nsp <= 64)
+    for (int k = threadIdx.x; k < nsp * nsp; k += blockDim.x) {
+      const double sg = lj_sigma[k];
+      ljt[k] = make_float2((float)(sg * sg), (float)(4.0 * lj_eps[k]));
+    }
+  __syncthreads();
+  const float rc2_lj = (float)(rlj * rlj), rc2_ew = (float)(rew * rew), rc2 = (float)(rmax * rmax);
+  const float al = (terms & 2) ? (float)alpha[s] : 0.f;
+  const float two_al_rsqrtpi = 2.0f * al * 0.56418958354775628695f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = lane & (kRealAtoms - 1), stream_id = warp * 2 + (lane >> 4);
+  const int il = blockIdx.x * kRealAtoms + slot;
+  const bool act = il < n;
+  const int gi = a0 + (act ? il : 0);
+  const double xi = pos[3 * (int64_t)gi], yi = pos[3 * (int64_t)gi + 1], zi = pos[3 * (int64_t)gi + 2];
+  const float qi = (float)(q[gi] * ke);
+  const int ti = (terms & 1) ? species[gi] : 0;
+  float fx = 0.f, fy = 0.f, fz = 0.f;  // dE/dx_i, this warp's partners
+  float ef = 0.f;
+  const int per = (n + kRealStreams - 1) / kRealStreams;
+  const int j0 = stream_id * per, j1 = min(n, j0 + per);
+  for (int j = j0; j < j1; ++j) {
+    const int gj = a0 + j;
+    const float d0 = (float)(pos[3 * (int64_t)gj] - xi), d1 = (float)(pos[3 * (int64_t)gj + 1] - yi),
+                d2 = (float)(pos[3 * (int64_t)gj + 2] - zi);
+    float f0 = (d0 * I[0] + d1 * I[1]) + d2 * I[3], f1 = d1 * I[2] + d2 * I[4], f2 = d2 * I[5];
+    f0 -= rintf(f0);
+    f1 -= rintf(f1);
+    f2 -= rintf(f2);
+    const float dx = (f0 * L[0] + f1 * L[1]) + f2 * L[3], dy = f1 * L[2] + f2 * L[4], dz = f2 * L[5];
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    if (r2 >= rc2 || j == il || !act) continue;
+    float dedr2 = 0.f;  // dE/d(r^2) of the pair
+    if ((terms & 1) && r2 < rc2_lj) {
+      const float2 c = ljt[ti * nsp + species[gj]];
+      const float inv = 1.f / r2, s2 = c.x * inv, c6 = s2 * s2 * s2;
+      ef += c.y * (c6 * c6 - c6);
+      dedr2 += -0.5f * c.y * c6 * (12.f * c6 - 6.f) * inv;
+    }
+    if ((terms & 2) && r2 < rc2_ew) {
+      const float r = sqrtf(r2), ir = 1.f / r, qq = qi * (float)q[gj];
+      const float er = erfcf(al * r);
+      ef += qq * er * ir;
+      dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * expf(-al * al * r2) * ir);
+    }
+    // d = x_j - x_i: dE/dx_i = -2 dE/d(r^2) d for this ordered pair (both halves)
+    fx = fmaf(-2.f * dedr2, dx, fx);
+    fy = fmaf(-2.f * dedr2, dy, fy);
+    fz = fmaf(-2.f * dedr2, dz, fz);
+  }
+  part[stream_id][slot][0] = fx;
+  part[stream_id][slot][1] = fy;
+  part[stream_id][slot][2] = fz;
+  __syncthreads();
+  if (threadIdx.x < kRealAtoms && act) {
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int k = 0; k < kRealStreams; ++k) {
+      gx += part[k][slot][0];
+      gy += part[k][slot][1];
+      gz += part[k][slot][2];
+    }
+    grad[3 * (int64_t)gi] = gx;
+    grad[3 * (int64_t)gi + 1] = gy;
+    grad[3 * (int64_t)gi + 2] = gz;
+  }
+  const double esum = block_sum(0.5 * (double)ef, red);
+  if (threadIdx.x == 0) atomicAdd(&energy[s], esum);
+}
+
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace
@@ -407,7 +523,7 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
   char *base = (char *)(((uintptr_t)workspace + 255) & ~uintptr_t(255));
   RecipSys *sysp = (RecipSys *)base;
   Coef *coef = (Coef *)(base + align256(sizeof(RecipSys) * (size_t)n_systems));
-  recip_setup_kernel<<<(n_systems + 127) / 128, 128, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
+  recip_setup_kernel<<<n_systems, 256, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
                                                                    sysp, status);
   KUPS_CUDA_TRY(cudaMemsetAsync(structure_factor, 0, sizeof(double) * 2 * (size_t)n_systems * n_kvecs, stream));
   const int chunks = (max_atoms_per_system + kAtomsPerChunk - 1) / kAtomsPerChunk;
@@ -416,8 +532,10 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
     structure_factor_kernel<<<g, kKPerBlock, 0, stream>>>(positions, charges, sys_offset, kvec_n,
                                                           n_kvecs, sysp, structure_factor);
   }
-  recip_energy_kernel<<<n_systems, 256, 0, stream>>>(kvec_n, n_kvecs, alpha, sysp, structure_factor,
-                                                     coulomb_k, coef, energy, grad_tril);
+  KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
+  if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * (size_t)n_systems, stream));
+  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 255) / 256), n_systems), 256, 0, stream>>>(
+      kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, grad_tril);
   if (chunks > 0) {
     dim3 g(chunks, n_systems);
     recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
@@ -483,7 +601,7 @@ extern "C" int32_t kups_ewald_recip_static(const double *positions, const double
   }
   RecipSys *sysp = (RecipSys *)base;
   Coef *coef = (Coef *)(base + sys_bytes);
-  recip_setup_kernel<<<(n_systems + 127) / 128, 128, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
+  recip_setup_kernel<<<n_systems, 256, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
                                                                    sysp, status);
   KUPS_CUDA_TRY(cudaMemsetAsync(structure_factor, 0, sizeof(double) * 2 * (size_t)n_systems * n_kvecs, stream));
   const int chunks = (max_atoms_per_system + kAtomsPerChunk - 1) / kAtomsPerChunk;
@@ -492,8 +610,10 @@ extern "C" int32_t kups_ewald_recip_static(const double *positions, const double
     structure_factor_kernel<<<g, kKPerBlock, 0, stream>>>(positions, charges, sys_offset, kvec_n,
                                                           n_kvecs, sysp, structure_factor);
   }
-  recip_energy_kernel<<<n_systems, 256, 0, stream>>>(kvec_n, n_kvecs, alpha, sysp, structure_factor,
-                                                     coulomb_k, coef, energy, grad_tril);
+  KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
+  if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * (size_t)n_systems, stream));
+  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 255) / 256), n_systems), 256, 0, stream>>>(
+      kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, grad_tril);
   if (chunks > 0) {
     dim3 g(chunks, n_systems);
     recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
@@ -536,5 +656,28 @@ extern "C" int32_t kups_pair_edges(const double *positions, const int32_t *syste
       lj_cutoff, alpha, ewald_cutoff, coulomb_k, terms, edges, shifts, n_edges, energy, grad,
       grad_tril);
   (void)status;
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" int32_t kups_lj_ewald_real_forces(const double *positions, const double *charges,
+                                             const int32_t *species, const int32_t *sys_offset,
+                                             int32_t n_systems, int32_t max_atoms_per_system,
+                                             const double *tril, const double *lj_sigma,
+                                             const double *lj_epsilon, int32_t n_species,
+                                             const double *lj_cutoff, const double *alpha,
+                                             const double *ewald_cutoff, double coulomb_k, int32_t terms,
+                                             double *energy, double *grad, kups_status *status,
+                                             void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_systems < 0 || max_atoms_per_system < 0 || terms < 1 || terms > 3) return KUPS_ERR_INVALID;
+  if ((terms & 1) && (n_species < 1 || n_species > 8 || lj_sigma == nullptr || lj_epsilon == nullptr))
+    return KUPS_ERR_INVALID;
+  if (n_systems == 0) return KUPS_OK;
+  KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
+  if (max_atoms_per_system == 0) return KUPS_OK;
+  dim3 g((max_atoms_per_system + kRealAtoms - 1) / kRealAtoms, n_systems);
+  real_allpairs_kernel<<<g, 32 * kRealWarps, 0, stream>>>(positions, charges, species, sys_offset, tril, lj_sigma,
+                                                    lj_epsilon, n_species, lj_cutoff, alpha, ewald_cutoff,
+                                                    coulomb_k, terms, energy, grad, status);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

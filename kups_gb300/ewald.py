@@ -265,6 +265,16 @@ class LJEwaldPotential:
 
 
 # ----------------------------------------------------------------------------- MD
+def _perpendicular_widths(tril) -> np.ndarray:
+    """[S, 3] distances between opposite faces of each lower-triangular cell (host, float64)."""
+    t = np.asarray(torch.as_tensor(tril).detach().cpu().numpy(), np.float64).reshape(-1, 6)
+    L = np.zeros((len(t), 3, 3))
+    L[:, 0, 0], L[:, 1, 0], L[:, 1, 1], L[:, 2, 0], L[:, 2, 1], L[:, 2, 2] = t.T
+    vol = np.abs(L[:, 0, 0] * L[:, 1, 1] * L[:, 2, 2])
+    cross = lambda a, b: np.linalg.norm(np.cross(L[:, a], L[:, b]), axis=1)
+    return np.stack([vol / cross(1, 2), vol / cross(2, 0), vol / cross(0, 1)], 1)
+
+
 class LJEwaldMD:
     """VV (NVE) or BAOAB steps of LJ + Ewald dynamics on the float64 particle table.
 
@@ -272,8 +282,12 @@ class LJEwaldMD:
     pairs / reciprocal space / self / kick, all stream-ordered with no host
     synchronisation (the edge list is passed at capacity; padded rows are
     skipped in the kernel), so a step is captured once in a CUDA graph and
-    replayed.  The neighbour list is rebuilt every step, as the reference MD
-    application does.
+    replayed.  Real space: when every cell width is at least twice the cutoff
+    (every pair within it is its minimum image) all pairs of a system are
+    evaluated from shared-memory tiles with no stored list
+    (kups_lj_ewald_real_forces); otherwise the neighbour list is rebuilt every
+    step, as the reference MD application does, and the edges are evaluated by
+    kups_pair_edges.
     """
 
     def __init__(self, particles: EwaldParticles, masses, tril, ewald: EwaldParameters, time_step, lj_sigma=None,
@@ -303,6 +317,10 @@ class LJEwaldMD:
             self.rc_nl = self.rc_ew.clone()
         self.off, self.max_atoms = _offsets(self.system, self.s)
         vol = float((self.tril[:, 0] * self.tril[:, 2] * self.tril[:, 5]).abs().min())
+        nsp = int(self.sig.shape[0]) if self.lj else 1
+        grouped = bool((self.system[1:] >= self.system[:-1]).all()) if self.n > 1 else True
+        self.allpairs = grouped and nsp <= 8 and bool(
+            (_perpendicular_widths(self.tril).min(1) >= 2.0 * self.rc_nl.cpu().numpy()).all())
         if avg_edges is None:
             avg_edges = int(4 / 3 * math.pi * float(self.rc_nl.max()) ** 3 * self.n / vol * 1.5) + 64
         self.cap = avg_edges * self.n
@@ -330,6 +348,22 @@ class LJEwaldMD:
     def _forces(self):
         lib = _lib.load()
         pos = self.p.positions
+        if self.allpairs:
+            terms = TERM_EWALD_REAL | (TERM_LJ if self.lj else 0)
+            nsp = int(self.sig.shape[0]) if self.lj else 1
+            rc = lib.kups_lj_ewald_real_forces(
+                pos.data_ptr(), self.q.data_ptr(), self.species.data_ptr(), self.off.data_ptr(), self.s,
+                self.max_atoms, self.tril.data_ptr(), self.sig.data_ptr() if self.lj else None,
+                self.eps.data_ptr() if self.lj else None, nsp, self.rc_lj.data_ptr() if self.lj else None,
+                self.alpha.data_ptr(), self.rc_ew.data_ptr(), TO_STANDARD_UNITS, terms, self.e_pair.data_ptr(),
+                self.g_pair.data_ptr(), self.status.data_ptr(), _stream())
+            _lib.check(rc, "kups_lj_ewald_real_forces")
+            ewald_recip(pos, self.q, self.off, self.max_atoms, self.tril, self.kn, self.alpha, grad_tril=False,
+                        ws=self.rws, out=(self.e_rec, self.g_rec, self.t_rec, self.sk), status=self.status)
+            torch.add(self.g_pair, self.g_rec, out=self.grad)
+            torch.add(self.e_pair, self.e_rec, out=self.energy)
+            self.energy.add_(self.e_self)
+            return
         rc = lib.kups_neighborlist_build(pos.data_ptr(), self.system.data_ptr(), self.incl.data_ptr(),
                                          self.excl.data_ptr(), self.n, self.s, self.tril.data_ptr(),
                                          self.rc_nl.data_ptr(), self.s, self.edges.data_ptr(), self.shifts.data_ptr(),

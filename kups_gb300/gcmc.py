@@ -322,10 +322,10 @@ class GCMC:
     def molecule_centres_frac(self) -> torch.Tensor:
         """Fractional coordinates in [0, 1) of every molecule's atom mean (atoms unwrapped against
         atom 0), all systems concatenated: the positions the learned proposal is trained on."""
-        t = self.tril
-        L = torch.zeros((t.shape[0], 3, 3), dtype=torch.float64, device=t.device)
-        L[:, 0, 0], L[:, 1, 0], L[:, 1, 1], L[:, 2, 0], L[:, 2, 1], L[:, 2, 2] = t.unbind(1)
-        inv = torch.linalg.inv(L)
+        t = self.setup.tril  # host copy: the 3 x 3 inverses are formed with NumPy
+        L = np.zeros((len(t), 3, 3))
+        L[:, 0, 0], L[:, 1, 0], L[:, 1, 1], L[:, 2, 0], L[:, 2, 1], L[:, 2, 2] = np.asarray(t, np.float64).T
+        inv = torch.as_tensor(np.linalg.inv(L), device="cuda")
         p = self.guest[..., :3].to(torch.float64)  # [S, M, apm, 3]
         f = torch.einsum("smai,sij->smaj", p, inv)
         d = f - f[:, :, :1]

@@ -148,3 +148,62 @@ def test_lj_ewald_md_conserves_energy_with_graph_replay():
     md.check()
     e1 = float((md.energy + md.kinetic_energy()).item())
     assert abs(e1 - e0) / abs(e0) < 2e-3, (e0, e1)
+
+
+def test_allpairs_real_space_matches_edge_sum():
+    """kups_lj_ewald_real_forces (all pairs, float32 pair arithmetic) against the float64
+    oracle sum over the neighbour list at the cutoff: energy relative 1e-5, force RMS
+    relative 1e-5; a cell narrower than twice the cutoff is refused (KUPS_ERR_UNSUPPORTED)."""
+    import ctypes as C
+
+    from kups_gb300 import _lib
+    from kups_gb300.ewald import TERM_EWALD_REAL, TERM_LJ
+    from kups_gb300.neighborlist import new_status, read_status
+
+    rng = np.random.default_rng(9)
+    pos, q, sysi, trils = [], [], [], []
+    for s, n in enumerate((150, 230)):
+        L = ouc.lattice_from_lengths_angles(rng.uniform(17, 20, 3), rng.uniform(85, 95, 3))
+        from kups_gb300.workloads import lattice_positions
+
+        f = lattice_positions(rng, n, 1.0, 0.1)  # fractional, min separation 0.1 of the cell
+        pos.append((f - 0.5) @ L)
+        qq = rng.normal(0, 1, n)
+        q.append(qq - qq.mean())
+        sysi += [s] * n
+        trils.append(ouc.tril_from_lattice(L))
+    pos, q, sysi, tril = np.concatenate(pos), np.concatenate(q), np.array(sysi), np.stack(trils)
+    sp = rng.integers(0, 2, len(q)).astype(np.int32)
+    sig, eps = olj.lorentz_berthelot([1.6, 2.0], [0.004, 0.006])
+    rc = np.array([7.5, 8.0])
+    alpha = np.array([0.35, 0.33])
+    e, s = onl.neighbor_list(pos, sysi, tril, rc)
+    el, gl, _ = olj.lj_from_edges(pos, sysi, sp, tril, sig, eps, rc, e, s)
+    ee, ge, _ = oew.short_range_from_edges(pos, q, sysi, tril, alpha, rc, e, s)
+    off, mx = offsets(sysi, 2)
+    en = torch.empty(2, dtype=torch.float64, device="cuda")
+    gr = torch.empty((len(q), 3), dtype=torch.float64, device="cuda")
+    st = new_status()
+    args = [cuda(pos), cuda(q), cuda(sp, torch.int32), off, cuda(tril), cuda(sig), cuda(eps), cuda(rc), cuda(alpha)]
+    lib = _lib.load()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc_ = lib.kups_lj_ewald_real_forces(args[0].data_ptr(), args[1].data_ptr(), args[2].data_ptr(), off.data_ptr(), 2, mx,
+                                        args[4].data_ptr(), args[5].data_ptr(), args[6].data_ptr(), 2,
+                                        args[7].data_ptr(), args[8].data_ptr(), args[7].data_ptr(), KE,
+                                        TERM_LJ | TERM_EWALD_REAL, en.data_ptr(), gr.data_ptr(), st.data_ptr(), stream)
+    assert rc_ == 0
+    torch.cuda.synchronize()
+    assert read_status(st).code == 0
+    np.testing.assert_allclose(en.cpu().numpy(), el + ee, rtol=1e-5)
+    g = gl + ge
+    rms = np.sqrt(np.mean((gr.cpu().numpy() - g) ** 2) / np.mean(g**2))
+    assert rms < 1e-5, rms
+    # cutoff above half the narrowest width: refused, status records it
+    st2 = new_status()
+    big = cuda(np.array([9.9, 10.0]))
+    lib.kups_lj_ewald_real_forces(args[0].data_ptr(), args[1].data_ptr(), args[2].data_ptr(), off.data_ptr(), 2, mx,
+                                  args[4].data_ptr(), args[5].data_ptr(), args[6].data_ptr(), 2, big.data_ptr(),
+                                  args[8].data_ptr(), big.data_ptr(), KE, TERM_LJ | TERM_EWALD_REAL, en.data_ptr(),
+                                  gr.data_ptr(), st2.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert read_status(st2).code == _lib.KUPS_ERR_UNSUPPORTED
