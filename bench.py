@@ -321,6 +321,7 @@ def run_ours(a):
         line["cpu_baseline"] = {"value": rate, "unit": "atom-steps/s", "cores": cores, "kind": "port",
                                 "sample": sample}
     if rank == 0 and not a.no_ewald:
+        line["argon_nvt"] = run_argon(a, torch)
         line["lj_ewald_md"] = run_ewald_md(a)
     if rank == 0 and not a.no_gcmc:
         line["gcmc"] = run_gcmc(a)
@@ -328,6 +329,27 @@ def run_ours(a):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_argon(a, torch):
+    """Latency of the single-system argon NVT workload (864 atoms, fcc a = 5.74 A, rc 8.5 A +
+    1 A skin, BAOAB dt 2 fs, 94.4 K): one persistent launch of 1000 steps on one CTA."""
+    from kups_gb300 import md, workloads
+
+    W = workloads.argon_fcc()
+    prop = md.make_baoab_langevin_step()
+    packed = md.pack(state_from_workload(W, torch))
+    prop.run_packed(packed, 20, seed=3, step0=0)
+    torch.cuda.synchronize()
+    steps = 1000
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    prop.launch(packed, steps, seed=3, step0=20, virial=False)
+    t1.record()
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    return {"workload": "argon NVT: 864 atoms (6x6x6 fcc, a 5.74 A), rc 8.5 A + 1 A skin, BAOAB dt 2 fs, 94.4 K",
+            "us_per_step": ms / steps * 1e3, "value": W.n_atoms * steps / (ms / 1e3), "unit": "atom-steps/s"}
 
 
 def run_ewald_md(a):
