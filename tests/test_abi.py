@@ -67,3 +67,37 @@ def test_key_to_seed_is_deterministic():
     from kups_gb300.md import key_to_seed
 
     assert key_to_seed([1, 2]) == key_to_seed([1, 2]) != key_to_seed([2, 1])
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Compile a C program against include/kups_gb300.h and compare sizeof / offsetof of every
+    ABI struct with the ctypes mirrors (no GPU needed)."""
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+
+    from kups_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    structs = {"kups_status": _lib.Status, "kups_md_args": _lib.MdArgs, "kups_gcmc_proposal": _lib.GcmcProposal,
+               "kups_gcmc_args": _lib.GcmcArgs, "kups_mlp": _lib.Mlp}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "kups_gb300.h"', 'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(root, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
