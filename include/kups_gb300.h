@@ -370,6 +370,7 @@ typedef struct kups_gcmc_args {
   double *out_delta;            /* [S, 4] or NULL */
   const float *proposal_node;   /* [G^3] learned insertion density (kups_mlp_grid_norm) or NULL */
   const double *proposal_cdf;   /* [G^3 + 1] */
+  void *workspace;              /* [S, n_kvecs] float2 scratch: the step's S(k) change */
   float move_cum[3];
   float pad0;
   double coulomb_k;

@@ -35,6 +35,8 @@ constexpr int kMaxApm = 8;       // atoms per molecule
 constexpr int kMaxSpeciesMC = 8;
 constexpr int kMaxKVec = 4096;
 constexpr int kMaxImg = 5;       // odd image count per axis
+constexpr int kMaxM = 16;        // |n_a| of a k vector
+constexpr int kTab = 2 * kMaxM + 1;
 
 struct ImgCfg {
   int n[3];
@@ -249,7 +251,8 @@ constexpr int kMinCtasPerSm = 7;
 __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc_args a, kups_status *status) {
   __shared__ StepShared sh;
   __shared__ float2 lj[kMaxSpeciesMC * kMaxSpeciesMC];
-  extern __shared__ float2 dS[];  // [n_kvecs] structure-factor change of the step
+  // per-axis phase tables of the step's moved atoms: e^{2 pi i n f_a}, |n| <= kMaxM
+  extern __shared__ float2 ph[];  // [2 apm][3][kTab]
   __shared__ double red[40];
   __shared__ float Lf[6], If[6];
   __shared__ float4 mfa[2 * kMaxApm];  // moved atoms (old, then new): fractional xyz, species bits
@@ -309,7 +312,17 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
   double *sk = a.structure_factor + (int64_t)s * nk * 2;
   const double *pk = a.prefactor + (int64_t)s * nk;
   const int32_t *kn = a.kvec_n + (int64_t)s * nk * 3;
+  float2 *dS = reinterpret_cast<float2 *>(a.workspace) + (int64_t)s * nk;  // the step's structure-factor change
 
+  // the phase tables hold |n_a| <= kMaxM: a system with a larger k vector is refused
+  {
+    int bad = 0;
+    for (int e = tid; e < 3 * nk; e += kThreads) bad |= abs(kn[e]) > kMaxM;
+    if (__syncthreads_or(bad)) {
+      if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
+      return;
+    }
+  }
   const bool learned = a.proposal_node != nullptr;
   for (int step = 0; step < a.n_steps; ++step) {
     const uint64_t ctr = a.step0 + (uint64_t)step;
@@ -541,16 +554,27 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
     // per-k terms in float32 (|term| <~ 15 eV: ~1e-6 eV rounding each), the k sum of a
     // thread in float32, the block sum and S(k) itself in float64
     float de_rec_f = 0.f;
+    // e^{2 pi i n . f} = prod_a e^{2 pi i n_a f_a}: each table entry from sincospif of the
+    // reduced phase, each k from two complex products of three entries
+    for (int e = tid; e < nm * 3 * kTab; e += kThreads) {
+      const int m = e / (3 * kTab), ax = (e / kTab) % 3, nn = e % kTab - kMaxM;
+      const float4 f = mfa[m];
+      float t = nn * (ax == 0 ? f.x : ax == 1 ? f.y : f.z);
+      t -= rintf(t);
+      float sn, cs;
+      sincospif(2.0f * t, &sn, &cs);
+      ph[e] = make_float2(cs, sn);
+    }
+    __syncthreads();
     for (int k = tid; k < nk; k += kThreads) {
-      const int n0 = kn[3 * k], n1 = kn[3 * k + 1], n2 = kn[3 * k + 2];
+      const int n0 = kn[3 * k] + kMaxM, n1 = kn[3 * k + 1] + kMaxM, n2 = kn[3 * k + 2] + kMaxM;
       float dc = 0.f, ds = 0.f;
       for (int m = 0; m < nm; ++m) {
         if (!mon[m]) continue;
-        const float4 f = mfa[m];
-        float t = n0 * f.x + n1 * f.y + n2 * f.z;
-        t -= rintf(t);
-        float sn, cs;
-        sincospif(2.0f * t, &sn, &cs);
+        const float2 *t = ph + m * 3 * kTab;
+        const float2 a = t[n0], b = t[kTab + n1], c = t[2 * kTab + n2];
+        const float abr = a.x * b.x - a.y * b.y, abi = a.x * b.y + a.y * b.x;
+        const float cs = abr * c.x - abi * c.y, sn = abr * c.y + abi * c.x;
         const float w = m < apm ? -mq[m] : mq[m];
         dc += w * cs;
         ds += w * sn;
@@ -673,6 +697,8 @@ extern "C" int32_t kups_gcmc_run(const kups_gcmc_args *a, kups_status *status, v
   if (a->proposal_node != nullptr && (a->proposal_cdf == nullptr || a->proposal_grid < 2 || a->proposal_grid > 256))
     return KUPS_ERR_INVALID;
   if (a->n_systems == 0 || a->n_steps == 0) return KUPS_OK;
-  gcmc_kernel<<<a->n_systems, kThreads, sizeof(float2) * (size_t)a->n_kvecs, (cudaStream_t)stream>>>(*a, status);
+  if (a->n_kvecs > 0 && a->workspace == nullptr) return KUPS_ERR_INVALID;
+  const size_t smem = sizeof(float2) * 2 * (size_t)a->atoms_per_mol * 3 * kTab;
+  gcmc_kernel<<<a->n_systems, kThreads, smem, (cudaStream_t)stream>>>(*a, status);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

@@ -185,6 +185,7 @@ class GCMC:
         nk = setup.kvec_n.shape[1]
         self.pk = f64(np.stack([prefactor(setup.tril[i], setup.kvec_n[i], setup.alpha[i]) for i in range(s)]))
         self.sk = torch.zeros((s, nk, 2), dtype=torch.float64, device=dev)
+        self.ws = torch.empty((s, max(nk, 1), 2), dtype=torch.float32, device=dev)  # per-step S(k) change
         self.lj_table = f32(np.stack([setup.sigma**2, 4 * setup.epsilon], -1).reshape(-1))
         vol = np.abs(setup.tril[:, 0] * setup.tril[:, 2] * setup.tril[:, 5])
         self.volume = vol
@@ -257,6 +258,7 @@ class GCMC:
         a.attempted, a.accepted = self.attempted.data_ptr(), self.accepted.data_ptr()
         a.proposals = proposals.data_ptr() if proposals is not None else None
         a.out_delta = out_delta.data_ptr() if out_delta is not None else None
+        a.workspace = self.ws.data_ptr()
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid
