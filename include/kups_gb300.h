@@ -371,6 +371,10 @@ typedef struct kups_gcmc_args {
   const float *proposal_node;   /* [G^3] learned insertion density (kups_mlp_grid_norm) or NULL */
   const double *proposal_cdf;   /* [G^3 + 1] */
   void *workspace;              /* [S, n_kvecs] float2 scratch: the step's S(k) change */
+  const void *fw_group;         /* float4 [host atoms / 32][2] or NULL: per 32 host atoms
+                                   (blocks start on multiples of 32) the fractional centre and
+                                   per-axis half extents; used when every cell width is at
+                                   least twice the cutoffs, to skip groups beyond the cutoff */
   float move_cum[3];
   float pad0;
   double coulomb_k;

@@ -276,10 +276,12 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
   __syncthreads();
   // image configurations of the two terms (neighborlist.py:461-466)
   ImgCfg li, ei;
+  float wdt[3];  // perpendicular widths
   {
     const Tril64 L = load_tril64(a.tril + 6 * (int64_t)s);
     double w[3];
     perpendicular_widths64(L, w);
+    for (int d = 0; d < 3; ++d) wdt[d] = (float)w[d];
     const double rcs[2] = {a.rc_lj[s], a.rc_ew[s]};
     for (int t = 0; t < 2; ++t) {
       ImgCfg &c = t == 0 ? li : ei;
@@ -300,7 +302,9 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
     }
   }
   const bool min_image = !li.image_mode && !ei.image_mode;
-  const float rc2_any = fmaxf(li.rc2, ei.rc2);
+  const float rc2_any = fmaxf(li.rc2, ei.rc2), rc_any = sqrtf(rc2_any);
+  const float4 *grp = reinterpret_cast<const float4 *>(a.fw_group);
+  const int lane = tid & 31;
   const float alpha = (float)a.alpha[s];
   const float ke = (float)a.coulomb_k;
   const double kT = a.kT[s];
@@ -478,14 +482,56 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
     const int nm = 2 * apm;
     if (min_image) {
       // every axis has one image: the pair is taken at its minimum image, one rounding
-      // per moved atom and partner
-      for (int j = tid; j < n_other; j += kThreads) {
+      // per moved atom and partner.  Host atoms go by warp in aligned groups of 32; a
+      // group is skipped for a moved atom when, along some axis a, the circular distance
+      // of the atom's fractional coordinate to the group's centre minus the group's half
+      // extent, times the width w_a, reaches the cutoff (|cart(d)| >= |d_a| w_a, and the
+      // rounded image's d_a is the circular distance, so no pair within it is dropped).
+      unsigned on_mask = 0u;
+      for (int m = 0; m < nm; ++m) on_mask |= mon[m] ? (1u << m) : 0u;
+      for (int base = (tid & ~31); base < fwn; base += kThreads) {
+        unsigned near = on_mask;
+        if (grp != nullptr) {
+          bool close = false;
+          if (lane < nm && ((on_mask >> lane) & 1u)) {
+            const int gi = (fw0 + base) >> 5;
+            const float4 c = grp[2 * gi], h = grp[2 * gi + 1], fa = mfa[lane];
+            float dx = fa.x - c.x, dy = fa.y - c.y, dz = fa.z - c.z;
+            dx = fabsf(dx - rintf(dx));
+            dy = fabsf(dy - rintf(dy));
+            dz = fabsf(dz - rintf(dz));
+            const float sep = fmaxf(fmaxf(fmaxf(dx - h.x, 0.f) * wdt[0], fmaxf(dy - h.y, 0.f) * wdt[1]),
+                                    fmaxf(dz - h.z, 0.f) * wdt[2]);
+            close = sep < rc_any;
+          }
+          near = __ballot_sync(0xffffffffu, close);
+        }
+        const int j = base + lane;
+        if (j >= fwn || near == 0u) continue;
+        const float4 pj = fwp[fw0 + j];
+        const float qj = a.fw_charge[fw0 + j];
+        float fj[3];
+        frac32(If, pj.x, pj.y, pj.z, fj);
+        const int tj = __float_as_int(pj.w);
+        for (unsigned mm = near; mm != 0u; mm &= mm - 1u) {
+          const int m = __ffs(mm) - 1;
+          const float4 fa = mfa[m];
+          float d[3] = {fa.x - fj[0], fa.y - fj[1], fa.z - fj[2]}, c[3];
+          d[0] -= rintf(d[0]);
+          d[1] -= rintf(d[1]);
+          d[2] -= rintf(d[2]);
+          cart32(Lf, d, c);
+          const float r2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+          if (r2 >= rc2_any) continue;
+          const float sg = m < apm ? -1.f : 1.f;
+          e_acc += sg * pair_u(r2, __float_as_int(fa.w), tj, mq[m] * qj, lj, nsp, li, ei, alpha, ke, true, true);
+        }
+      }
+      // guest atoms (not grouped)
+      for (int j = fwn + tid; j < n_other; j += kThreads) {
         float4 pj;
         float qj;
-        if (j < fwn) {
-          pj = fwp[fw0 + j];
-          qj = a.fw_charge[fw0 + j];
-        } else {
+        {
           const int g = j - fwn;
           if (has_old && g / apm == mol) continue;  // the moved molecule itself
           pj = gpos[g];

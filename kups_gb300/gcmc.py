@@ -141,6 +141,32 @@ def _morton_order(pos, tril, cell=3.2):
     return np.argsort(key, kind="stable")
 
 
+def _group_bounds(pos, tril, one_cell, n_groups):
+    """[n_groups, 2, 4] per 32 consecutive atoms: fractional centre (circular mean, in
+    [-0.5, 0.5)) and per-axis half extents (circular distance to the centre, + 1e-5).  A block
+    used with several different cells gets half extents of 1 (its groups are never skipped)."""
+    out = np.zeros((n_groups, 2, 4))
+    out[:, 1, :3] = 1.0
+    if not one_cell or len(pos) == 0:
+        return out
+    t = np.asarray(tril, float)
+    L = np.array([[t[0], 0, 0], [t[1], t[2], 0], [t[3], t[4], t[5]]])
+    f = np.asarray(pos, float) @ np.linalg.inv(L)
+    for g in range(n_groups):
+        fg = f[32 * g:32 * g + 32]
+        if len(fg) == 0:
+            continue
+        d = fg - fg[0]
+        d -= np.round(d)
+        c = fg[0] + d.mean(0)
+        c -= np.round(c)
+        e = fg - c
+        e -= np.round(e)
+        out[g, 0, :3] = c
+        out[g, 1, :3] = np.abs(e).max(0) + 1e-5
+    return out
+
+
 class GCMC:
     """Device state + the propagator ``__call__(key, n_steps)``."""
 
@@ -161,15 +187,29 @@ class GCMC:
         f64 = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)
         i32 = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.int32, device=dev)
         sp_bits = lambda sp: np.asarray(sp, np.int32).view(np.float32)
-        # host atoms of each block in spatial (Z) order on the device; energies do not depend
-        # on the order, only the float32 summation order does
-        perm = np.arange(len(setup.fw_positions))
-        for blk, (a0, n) in enumerate(sorted(set(zip(setup.fw_start.tolist(), setup.fw_count.tolist())))):
-            first = int(np.nonzero((setup.fw_start == a0) & (setup.fw_count == n))[0][0])
-            perm[a0:a0 + n] = a0 + _morton_order(setup.fw_positions[a0:a0 + n], setup.tril[first])
-        self.fw_pos = f32(np.concatenate([setup.fw_positions[perm], sp_bits(setup.fw_species[perm])[:, None]], 1))
-        self.fw_q = f32(setup.fw_charges[perm])
-        self.fw_start, self.fw_count = i32(setup.fw_start), i32(setup.fw_count)
+        # host atoms of each block in spatial (Z) order on the device, each block starting on a
+        # multiple of 32 atoms, with a bounding table per 32 atoms (fw_group); energies do not
+        # depend on the order, only the float32 summation order does
+        pos_d, q_d, sp_d, grp, starts = [], [], [], [], {}
+        off = 0
+        for a0, n in sorted(set(zip(setup.fw_start.tolist(), setup.fw_count.tolist()))):
+            users = np.nonzero((setup.fw_start == a0) & (setup.fw_count == n))[0]
+            t0 = setup.tril[int(users[0])]
+            one_cell = bool(np.all(setup.tril[users] == t0))
+            order = _morton_order(setup.fw_positions[a0:a0 + n], t0) if n > 0 else np.zeros(0, int)
+            P = setup.fw_positions[a0:a0 + n][order]
+            pad = (-n) % 32
+            starts[(a0, n)] = off
+            pos_d.append(np.concatenate([P, np.repeat(P[-1:] if n else np.zeros((1, 3)), pad, 0)]))
+            q_d.append(np.concatenate([setup.fw_charges[a0:a0 + n][order], np.zeros(pad)]))
+            sp_d.append(np.concatenate([setup.fw_species[a0:a0 + n][order], np.zeros(pad, int)]))
+            grp.append(_group_bounds(P, t0, one_cell, (n + pad) // 32))
+            off += n + pad
+        self.fw_pos = f32(np.concatenate([np.concatenate(pos_d), sp_bits(np.concatenate(sp_d))[:, None]], 1))
+        self.fw_q = f32(np.concatenate(q_d))
+        self.fw_group = f32(np.concatenate(grp).reshape(-1, 4)) if off > 0 else None
+        self.fw_start = i32(np.array([starts[(a, n)] for a, n in zip(setup.fw_start.tolist(), setup.fw_count.tolist())]))
+        self.fw_count = i32(setup.fw_count)
         self.guest = torch.zeros((s, setup.max_mol, apm, 4), dtype=torch.float32, device=dev)
         self.n_mol = torch.zeros(s, dtype=torch.int32, device=dev)
         self.motif = f32(np.concatenate([setup.motif_positions, sp_bits(setup.motif_species)[:, None]], 1))
@@ -259,6 +299,7 @@ class GCMC:
         a.proposals = proposals.data_ptr() if proposals is not None else None
         a.out_delta = out_delta.data_ptr() if out_delta is not None else None
         a.workspace = self.ws.data_ptr()
+        a.fw_group = self.fw_group.data_ptr() if self.fw_group is not None else None
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid

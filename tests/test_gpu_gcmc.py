@@ -314,3 +314,42 @@ def test_reciprocal_delta_on_the_full_host_matches_full_recomputation(kind):
         return e.cpu().numpy()
 
     np.testing.assert_allclose(out[:, 2], e_rec(afters) - e_rec(guests), atol=2e-5)
+
+
+@pytest.mark.parametrize("kind", ["translate", "rotate", "insert", "delete"])
+def test_host_group_skipping_changes_nothing(kind):
+    """Skipping 32-atom host groups beyond the cutoff leaves every move's energy change
+    bit-identical (a skipped group's pairs all lie outside the cutoff and add exactly 0.0)
+    on the 8000-atom replicated host."""
+    from kups_gb300 import gcmc, workloads
+
+    setup = workloads.gcmc_co2_framework(n_replicas=4, max_mol=32)
+    rng = np.random.default_rng({"translate": 5, "rotate": 6, "insert": 7, "delete": 8}[kind])
+    L = ouc.lattice_from_tril(setup.tril[0])
+    guests = [np.concatenate([wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0])
+                              for _ in range(10)]) for _ in range(4)]
+    mols = [int(m) for m in rng.integers(0, 10, 4)]
+    news = []
+    for i in range(4):
+        g = guests[i].reshape(10, 3, 3)
+        if kind == "translate":
+            news.append(wrapped(g[mols[i]] + rng.normal(0, 1.0, 3), setup.tril[0]))
+        elif kind == "rotate":
+            from scipy.spatial.transform import Rotation
+
+            c = g[mols[i]].mean(0)
+            R = Rotation.random(random_state=int(rng.integers(1 << 30))).as_matrix()
+            news.append(wrapped((g[mols[i]] - c) @ R.T + c, setup.tril[0]))
+        elif kind == "insert":
+            news.append(wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0]))
+        else:
+            news.append(None)
+    outs = []
+    for use_groups in (True, False):
+        mc = gcmc.GCMC(setup, seed=3)
+        mc.set_guests(guests)
+        if not use_groups:
+            mc.fw_group = None
+        outs.append(mc.evaluate([gcmc.MOVES.index(kind)] * 4, mols, news))
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert np.all(np.isfinite(outs[0]))
