@@ -370,7 +370,8 @@ typedef struct kups_gcmc_args {
   double *out_delta;            /* [S, 4] or NULL */
   const float *proposal_node;   /* [G^3] learned insertion density (kups_mlp_grid_norm) or NULL */
   const double *proposal_cdf;   /* [G^3 + 1] */
-  void *workspace;              /* [S, n_kvecs] float2 scratch: the step's S(k) change */
+  void *workspace;              /* float2 [3, S, n_kvecs] scratch (the step's S(k) change, float32
+                                   mirrors of S(k) and of P(k) with the packed k vector) */
   const void *fw_group;         /* float4 [host atoms / 32][2] or NULL: per 32 host atoms
                                    (blocks start on multiples of 32) the fractional centre and
                                    per-axis half extents; used when every cell width is at

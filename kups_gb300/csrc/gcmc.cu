@@ -316,12 +316,24 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
   double *sk = a.structure_factor + (int64_t)s * nk * 2;
   const double *pk = a.prefactor + (int64_t)s * nk;
   const int32_t *kn = a.kvec_n + (int64_t)s * nk * 3;
-  float2 *dS = reinterpret_cast<float2 *>(a.workspace) + (int64_t)s * nk;  // the step's structure-factor change
-
+  // scratch per system (three arrays of S x n_k): the step's S(k) change, float32 mirrors of
+  // S(k) (re-derived from the float64 value at every commit) and of P(k), and the packed
+  // table offsets of the k vectors.  Reading the mirrors keeps float64<->float32
+  // conversions (float64-pipe work) off the per-step path.
+  const int64_t snk = (int64_t)a.n_systems * nk;
+  float2 *dS = reinterpret_cast<float2 *>(a.workspace) + (int64_t)s * nk;
+  float2 *sk32 = reinterpret_cast<float2 *>(a.workspace) + snk + (int64_t)s * nk;
+  float2 *pk32 = reinterpret_cast<float2 *>(a.workspace) + 2 * snk + (int64_t)s * nk;  // (P, packed k)
   // the phase tables hold |n_a| <= kMaxM: a system with a larger k vector is refused
   {
     int bad = 0;
-    for (int e = tid; e < 3 * nk; e += kThreads) bad |= abs(kn[e]) > kMaxM;
+    for (int k = tid; k < nk; k += kThreads) {
+      const int n0 = kn[3 * k], n1 = kn[3 * k + 1], n2 = kn[3 * k + 2];
+      bad |= (abs(n0) > kMaxM) | (abs(n1) > kMaxM) | (abs(n2) > kMaxM);
+      const uint32_t packed = (uint32_t)(n0 + kMaxM) | ((uint32_t)(n1 + kMaxM) << 8) | ((uint32_t)(n2 + kMaxM) << 16);
+      pk32[k] = make_float2((float)pk[k], __uint_as_float(packed));
+      sk32[k] = make_float2((float)sk[2 * k], (float)sk[2 * k + 1]);
+    }
     if (__syncthreads_or(bad)) {
       if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
       return;
@@ -613,7 +625,9 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
     }
     __syncthreads();
     for (int k = tid; k < nk; k += kThreads) {
-      const int n0 = kn[3 * k] + kMaxM, n1 = kn[3 * k + 1] + kMaxM, n2 = kn[3 * k + 2] + kMaxM;
+      const float2 pkk = pk32[k];
+      const uint32_t packed = __float_as_uint(pkk.y);
+      const int n0 = packed & 0xffu, n1 = (packed >> 8) & 0xffu, n2 = (packed >> 16) & 0xffu;
       float dc = 0.f, ds = 0.f;
       for (int m = 0; m < nm; ++m) {
         if (!mon[m]) continue;
@@ -626,8 +640,8 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
         ds += w * sn;
       }
       dS[k] = make_float2(dc, ds);
-      const float sc = (float)sk[2 * k], ss = (float)sk[2 * k + 1];
-      de_rec_f = fmaf((float)pk[k], fmaf(2.f, fmaf(sc, dc, ss * ds), fmaf(dc, dc, ds * ds)), de_rec_f);
+      const float2 sck = sk32[k];
+      de_rec_f = fmaf(pkk.x, fmaf(2.f, fmaf(sck.x, dc, sck.y * ds), fmaf(dc, dc, ds * ds)), de_rec_f);
     }
     __syncthreads();
     const double de_rec = block_sum((double)de_rec_f, red) * a.coulomb_k;
@@ -680,8 +694,10 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
     if (accept) {
       for (int k = tid; k < nk; k += kThreads) {
         const float2 d = dS[k];
-        sk[2 * k] += (double)d.x;
-        sk[2 * k + 1] += (double)d.y;
+        const double c = sk[2 * k] + (double)d.x, sn = sk[2 * k + 1] + (double)d.y;
+        sk[2 * k] = c;
+        sk[2 * k + 1] = sn;
+        sk32[k] = make_float2((float)c, (float)sn);
       }
       if (tid == 0) {
         a.energy[s] += sh.de_total;
