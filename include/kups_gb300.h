@@ -395,6 +395,16 @@ typedef struct kups_gcmc_args {
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);
 
+/* kups_lj_tail_correction replaces global_lennard_jones_tail_correction_energy
+ * and _pressure (potential/classical/lennard_jones.py:276-340): per system
+ * (atoms grouped by sys_offset) the analytic long-range energy and pressure of
+ * the species pairs with tail_mask[a * T + b] != 0 (NULL: pairs with eps > 0),
+ * float64; energy / pressure [S] (either may be NULL).  1 <= n_species <= 64. */
+int32_t kups_lj_tail_correction(const int32_t *species, const int32_t *sys_offset, int32_t n_systems,
+                                const double *tril, const double *sigma, const double *epsilon,
+                                const int32_t *tail_mask, int32_t n_species, const double *cutoff,
+                                double *energy, double *pressure, kups_status *status, void *stream);
+
 /* ------------------------------------------------------------------------
  * Tensor-core GEMM (tcgen05, BF16 inputs, FP32 accumulation in tensor memory)
  * used by the learned insertion proposal (no counterpart in the reference;

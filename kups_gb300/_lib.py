@@ -108,6 +108,7 @@ SIGNATURES = {
     "kups_mlp_grid_norm": (_I32, [_P, _I32, C.c_float, C.c_float, _P, _P, _P, _SZ, _P, _P]),
     "kups_proposal_sample": (_I32, [_P, _P, _I32, _I64, C.c_uint64, _P, _P, _P]),
     "kups_proposal_log_density": (_I32, [_P, _P, _I32, _P, _I64, _P, _P]),
+    "kups_lj_tail_correction": (_I32, [_P, _P, _I32, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P]),
     "kups_gemm_bf16": (_I32, [_P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64,
                                _I64, _P, _P, _I32, _I64, _I64, _I32, _I32, _I32, C.c_float, C.c_float, _I32, _I32, _P, _P]),
     "kups_pair_edges": (_I32, [_P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),

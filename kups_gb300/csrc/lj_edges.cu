@@ -121,3 +121,64 @@ extern "C" int32_t kups_lj_edges(const double *positions, const int32_t *system,
                                             grad_tril, pair_fp32, status);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
+
+// Global analytic LJ tail correction (lennard_jones.py:276-340): per system, species counts
+// N_a, density N_a N_b / V, t1 = (sigma_ab / rc)^3, t2 = t1^3,
+//   E = sum_ab (8/3) pi N_a N_b / V eps_ab sigma_ab^3 (t2 / 3 - t1) mask_ab,
+//   P = sum_ab (16/3) pi N_a N_b / V^2 eps_ab sigma_ab^3 (2 t2 / 3 - t1) mask_ab.
+// One block per system counts its species in shared memory (atoms grouped by sys_offset).
+namespace kups {
+namespace {
+constexpr int kTailMaxSpecies = 64;
+__global__ void lj_tail_kernel(const int32_t *species, const int32_t *sys_offset, const double *tril,
+                               const double *sigma, const double *eps, const int32_t *mask, int nsp,
+                               const double *cutoff, double *energy, double *pressure, kups_status *status) {
+  __shared__ int cnt[kTailMaxSpecies];
+  __shared__ int bad;
+  const int s = blockIdx.x;
+  for (int t = threadIdx.x; t < nsp; t += blockDim.x) cnt[t] = 0;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  const int a0 = sys_offset[s], a1 = sys_offset[s + 1];
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+    const int t = species[i];
+    if (t < 0 || t >= nsp) bad = 1;
+    else atomicAdd(&cnt[t], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  if (bad) {
+    status_error(status, KUPS_ERR_INVALID, s);
+    return;
+  }
+  const double *t6 = tril + 6 * (int64_t)s;
+  const double v = fabs(t6[0] * t6[2] * t6[5]);
+  const double rc = cutoff[s];
+  const double pi = 3.14159265358979323846;
+  double e = 0.0, p = 0.0;
+  for (int a = 0; a < nsp; ++a)
+    for (int b = 0; b < nsp; ++b) {
+      const int k = a * nsp + b;
+      if (mask != nullptr ? mask[k] == 0 : eps[k] <= 0.0) continue;
+      const double sg = sigma[k], s3 = sg * sg * sg, t1 = s3 / (rc * rc * rc), t2 = t1 * t1 * t1;
+      const double rho = (double)cnt[a] * (double)cnt[b] / v;
+      e += (8.0 / 3.0) * pi * rho * eps[k] * s3 * (t2 / 3.0 - t1);
+      p += (16.0 / 3.0) * pi * rho / v * eps[k] * s3 * (t2 / 3.0 * 2.0 - t1);
+    }
+  if (energy) energy[s] = e;
+  if (pressure) pressure[s] = p;
+}
+}  // namespace
+}  // namespace kups
+
+extern "C" int32_t kups_lj_tail_correction(const int32_t *species, const int32_t *sys_offset, int32_t n_systems,
+                                           const double *tril, const double *sigma, const double *epsilon,
+                                           const int32_t *tail_mask, int32_t n_species, const double *cutoff,
+                                           double *energy, double *pressure, kups_status *status, void *stream) {
+  if (n_systems < 0 || n_species < 1 || n_species > kups::kTailMaxSpecies) return KUPS_ERR_INVALID;
+  if (n_systems == 0) return KUPS_OK;
+  kups::lj_tail_kernel<<<n_systems, 256, 0, (cudaStream_t)stream>>>(species, sys_offset, tril, sigma, epsilon,
+                                                                    tail_mask, n_species, cutoff, energy, pressure,
+                                                                    status);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}

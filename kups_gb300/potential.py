@@ -124,3 +124,34 @@ def lj_from_edges(positions, system, species, tril, sigma, epsilon, cutoffs, edg
 
 def make_lennard_jones_potential(neighborlist=None, pair_fp32: bool = True) -> LennardJonesPotential:
     return LennardJonesPotential(neighborlist, pair_fp32)
+
+
+def lennard_jones_tail_correction(species, system, tril, sigma, epsilon, cutoffs, tail_mask=None, status=None):
+    """Global analytic tail energy and pressure per system (lennard_jones.py:276-340).
+
+    Atoms must be grouped by system.  ``tail_mask`` [T, T] selects the corrected species pairs
+    (default: pairs with epsilon > 0).  Returns (energy [S], pressure [S]), float64.
+    """
+    from .neighborlist import _f64, _i32, _stream, new_status, read_status
+
+    t = lambda x: torch.as_tensor(x)
+    sp = _i32(t(species))
+    sysi = _i32(t(system))
+    tr = _f64(t(tril)).reshape(-1, 6).contiguous()
+    s = tr.shape[0]
+    sig, eps = _f64(t(sigma)), _f64(t(epsilon))
+    nsp = int(sig.shape[0])
+    rc = _f64(torch.as_tensor(cutoffs, dtype=torch.float64).reshape(-1).expand(s).contiguous())
+    off = torch.zeros(s + 1, dtype=torch.int32, device="cuda")
+    off[1:] = torch.cumsum(torch.bincount(sysi.to(torch.int64), minlength=s), 0).to(torch.int32)
+    mask = _i32(t(tail_mask).to(torch.int32)) if tail_mask is not None else None
+    e = torch.empty(s, dtype=torch.float64, device="cuda")
+    p = torch.empty(s, dtype=torch.float64, device="cuda")
+    st = status if status is not None else new_status()
+    rcode = _lib.load().kups_lj_tail_correction(sp.data_ptr(), off.data_ptr(), s, tr.data_ptr(), sig.data_ptr(),
+                                                eps.data_ptr(), mask.data_ptr() if mask is not None else None, nsp,
+                                                rc.data_ptr(), e.data_ptr(), p.data_ptr(), st.data_ptr(), _stream())
+    _lib.check(rcode, "kups_lj_tail_correction")
+    if status is None:
+        _lib.raise_status(read_status(st))
+    return e, p

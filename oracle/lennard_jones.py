@@ -81,3 +81,20 @@ def tail_correction_energy(species_counts, tril, sigma, epsilon, cutoffs, tail_m
         tail_mask = eps > 0
     res = res * tail_mask
     return res.sum(axis=(1, 2))
+
+
+def tail_correction_pressure(species_counts, tril, sigma, epsilon, cutoffs, tail_mask=None):
+    """Global analytic tail pressure per system (lennard_jones.py:318-340)."""
+    counts = np.asarray(species_counts, dtype=np.float64)
+    v = volume(np.asarray(tril, dtype=np.float64).reshape(-1, 6))[:, None, None]
+    density = counts[:, :, None] * counts[:, None, :] / v
+    sigma = np.asarray(sigma, dtype=np.float64)
+    eps = np.asarray(epsilon, dtype=np.float64)
+    rc = np.asarray(cutoffs, dtype=np.float64).reshape(-1)[:, None, None]
+    t1 = (sigma / rc) ** 3
+    t2 = t1**3
+    res = (16 / 3) * np.pi * density / v * eps * sigma**3 * (t2 / 3 * 2 - t1)
+    if tail_mask is None:
+        tail_mask = eps > 0
+    res = res * tail_mask
+    return res.sum(axis=(1, 2))

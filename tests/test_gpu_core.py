@@ -276,3 +276,28 @@ def test_fused_md_baoab_thermostat_temperature():
     n = np.bincount(W.system)
     T = 2 * ke / (3 * n * BOLTZMANN_CONSTANT)
     np.testing.assert_allclose(T, W.temperature, rtol=0.06)
+
+
+def test_lj_tail_correction_matches_oracle():
+    """Global tail energy and pressure (lennard_jones.py:276-340) against the float64 oracle
+    (relative 1e-12), with the default mask (eps > 0) and an explicit one."""
+    import torch
+
+    from kups_gb300.potential import lennard_jones_tail_correction
+    from oracle import lennard_jones as olj
+    from oracle import unitcell as ouc
+
+    rng = np.random.default_rng(4)
+    counts = [30, 55, 12]
+    system = np.repeat(np.arange(3), counts).astype(np.int32)
+    species = rng.integers(0, 3, len(system)).astype(np.int32)
+    tril = np.stack([ouc.tril_from_lattice(ouc.lattice_from_lengths_angles(rng.uniform(15, 25, 3),
+                                                                          rng.uniform(80, 100, 3))) for _ in range(3)])
+    sig, eps = olj.lorentz_berthelot([3.0, 3.4, 2.6], [0.01, 0.0, 0.02])
+    rc = np.array([10.0, 11.0, 12.0])
+    sc = np.stack([np.bincount(species[system == s], minlength=3) for s in range(3)])
+    for mask in (None, np.array([[1, 0, 1], [0, 1, 1], [1, 1, 0]])):
+        e, p = lennard_jones_tail_correction(species, system, tril, sig, eps, rc, tail_mask=mask)
+        m = None if mask is None else mask.astype(bool)
+        np.testing.assert_allclose(e.cpu().numpy(), olj.tail_correction_energy(sc, tril, sig, eps, rc, m), rtol=1e-12)
+        np.testing.assert_allclose(p.cpu().numpy(), olj.tail_correction_pressure(sc, tril, sig, eps, rc, m), rtol=1e-12)
