@@ -775,6 +775,193 @@ __global__ void proposal_density_kernel(const float *node, const double *cdf, in
   lnq[i] = grid_log_q(node, cdf, g, x);
 }
 
+// ============================================================================
+// Fused forward pass (inference: kups_mlp_fwd and the grid refresh).  A persistent
+// CTA (8 warps) takes tiles of 128 points: the features go straight into shared
+// memory as the first layer's A operand (bfloat16, no-swizzle K-major core
+// matrices); for each layer the weights (bfloat16 [256, K]) are staged with 16-byte
+// cp.async, tcgen05.mma accumulates the 128 x 256 tile in tensor memory, and the
+// epilogue (bias, softplus, bfloat16) writes the next layer's A operand back into
+// shared memory while the next weights stream in; the last epilogue folds in the
+// head (w4 . h3 + b4).  Operands are rounded where the layered path rounds them.
+constexpr int kFwdThreads = 512, kFwdRows = 128;  // 16 warps: 4 TMEM lane groups x 4 column quarters
+
+// softplus(x) = max(x, 0) + log1p(exp(-|x|)) (no overflow, SFU exp, accurate log1p)
+__device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + log1pf(__expf(-fabsf(x))); }
+constexpr size_t kFwdA = (size_t)kFwdRows * kHid * 2, kFwdB = (size_t)kHid * kHid * 2;
+constexpr size_t kFwdSmem = kFwdA + kFwdB + 4 * kFwdRows * 4 + 3 * kFwdRows * 8 + 64;
+
+// weights W [256, K] row-major -> core-matrix layout; chunk e covers row (e / 8K') * 8 + e % 8
+// (K' = K / 8 groups) at group (e / 8) % K' and lands at element 8 e
+__device__ inline void fwd_stage_weights(__nv_bfloat16 *sB, const __nv_bfloat16 *W, int K, int tid) {
+  const int groups = K / 8;
+  const uint32_t s0 = smem_u32(sB);
+  for (int e = tid; e < kHid * groups; e += kFwdThreads) {
+    const int lo = e & 7, kg = (e >> 3) % groups, rb = (e >> 3) / groups;
+    cp_async16(s0 + (uint32_t)e * 16u, W + (size_t)(rb * 8 + lo) * K + kg * 8, 16u);
+  }
+}
+
+__device__ inline int fwd_core(int r, int kk, int K) {
+  return ((r >> 3) * (K / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7);
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 1)
+mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq, const double *x, int64_t n,
+                   int grid, float *g_out, kups_status *status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);
+  __nv_bfloat16 *sB = reinterpret_cast<__nv_bfloat16 *>(smem + kFwdA);
+  float *part = reinterpret_cast<float *>(smem + kFwdA + kFwdB);  // [4][128] head partial sums
+  double *fr = reinterpret_cast<double *>(smem + kFwdA + kFwdB + 4 * kFwdRows * 4);  // [3][128] coordinates
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kFwdA + kFwdB + 4 * kFwdRows * 4 + 3 * kFwdRows * 8);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, cq = warp >> 2;  // TMEM lanes 32 quarter .., columns 64 cq ..
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kHid));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) mbar_init(smem_u32(mbar), 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = make_idesc(kFwdRows, kHid);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int64_t n_tiles = (n + kFwdRows - 1) / kFwdRows;
+  fwd_stage_weights(sB, pb + kOffW1, kIn, tid);
+  cp_async_commit();
+  for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+    // features of the tile's points (rows past n are zero); coordinates once per row
+    if (tid < kFwdRows) {
+      const int64_t pt = tile * kFwdRows + tid;
+      double f[3] = {0.0, 0.0, 0.0};
+      if (pt < n) {
+        if (x != nullptr) {
+          for (int a = 0; a < 3; ++a) f[a] = x[3 * pt + a];
+        } else {
+          const int64_t g2 = (int64_t)grid * grid;
+          f[0] = (double)(pt / g2) / grid;
+          f[1] = (double)((pt / grid) % grid) / grid;
+          f[2] = (double)(pt % grid) / grid;
+        }
+      }
+      for (int a = 0; a < 3; ++a) fr[a * kFwdRows + tid] = f[a];
+    }
+    __syncthreads();
+    for (int e = tid; e < kFwdRows * kFreq; e += kFwdThreads) {
+      const int r = e % kFwdRows, j = e / kFwdRows;
+      const int64_t pt = tile * kFwdRows + r;
+      float sn = 0.f, cs = 0.f;
+      if (pt < n) {
+        const double f[3] = {fr[r], fr[kFwdRows + r], fr[2 * kFwdRows + r]};
+        double t = freq[3 * j] * f[0] + freq[3 * j + 1] * f[1] + freq[3 * j + 2] * f[2];
+        t -= rint(t);
+        sincospif(2.0f * (float)t, &sn, &cs);
+      }
+      *reinterpret_cast<__nv_bfloat162 *>(sA + fwd_core(r, 2 * j, kIn)) = __floats2bfloat162_rn(sn, cs);
+    }
+    for (int layer = 0; layer < 3 && ok; ++layer) {
+      const int K = layer == 0 ? kIn : kHid;
+      const float *bias = p + (layer == 0 ? kOffB1 : layer == 1 ? kOffB2 : kOffB3);
+      cp_async_wait<0>();
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int ks = 0; ks < K / 16; ++ks) {
+          const uint64_t ad = make_sdesc(smem_u32(sA) + ks * 256, 128, (K / 8) * 128);
+          const uint64_t bd = make_sdesc(smem_u32(sB) + ks * 256, 128, (K / 8) * 128);
+          const uint32_t accumulate = ks > 0 ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(mbar))
+                     : "memory");
+      }
+      ok = mbar_wait(smem_u32(mbar), phase);
+      phase ^= 1u;
+      if (!__syncthreads_and(ok)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // the MMAs are done with A and B: stream the next weights while the epilogue runs
+      const bool more = layer < 2 || tile + gridDim.x < n_tiles;
+      if (more) {
+        fwd_stage_weights(sB, pb + (layer == 0 ? kOffW2 : layer == 1 ? kOffW3 : kOffW1), layer == 2 ? kIn : kHid, tid);
+        cp_async_commit();
+      }
+      const int row = quarter * 32 + lane;
+      float head = 0.f;
+      for (int c0 = cq * (kHid / 4); c0 < (cq + 1) * (kHid / 4); c0 += 16) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (layer < 2) {
+          // next layer's A operand: 2 core-matrix rows of 8 bfloat16 (16 bytes each)
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            __nv_bfloat162 h[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int i = q * 8 + 2 * u;
+              h[u] = __floats2bfloat162_rn(softplus_fast(__uint_as_float(r[i]) + bias[c0 + i]),
+                                           softplus_fast(__uint_as_float(r[i + 1]) + bias[c0 + i + 1]));
+            }
+            *reinterpret_cast<uint4 *>(sA + fwd_core(row, c0 + q * 8, kHid)) = *reinterpret_cast<uint4 *>(h);
+          }
+        } else {
+          const float *w4 = p + kOffW4;
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            head = fmaf(softplus_fast(__uint_as_float(r[i]) + bias[c0 + i]), w4[c0 + i], head);
+        }
+      }
+      if (layer == 2) part[cq * kFwdRows + row] = head;
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      if (layer == 2 && tid < kFwdRows) {
+        const int64_t pt = tile * kFwdRows + tid;
+        if (pt < n)
+          g_out[pt] = ((part[tid] + part[kFwdRows + tid]) + (part[2 * kFwdRows + tid] + part[3 * kFwdRows + tid])) +
+                      p[kOffB4];
+      }
+    }
+  }
+  cp_async_wait<0>();
+  if (!ok && tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kHid));
+}
+
+int32_t fused_forward(const kups_mlp *net, const double *x, int64_t n, int grid, float *g, kups_status *status,
+                      cudaStream_t st) {
+  if (n <= 0) return KUPS_OK;
+  KUPS_CUDA_TRY(cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
+  int dev = 0, sms = 148;
+  KUPS_CUDA_TRY(cudaGetDevice(&dev));
+  KUPS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t tiles = (n + kFwdRows - 1) / kFwdRows;
+  const unsigned ctas = (unsigned)std::min<int64_t>(tiles, sms);
+  mlp_forward_kernel<<<ctas, kFwdThreads, kFwdSmem, st>>>((const __nv_bfloat16 *)net->param_bf16, net->param,
+                                                          net->freq, x, n, grid, g, status);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
 inline unsigned blocks(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 // Forward pass of rows [row0, row0 + c) into w (activations) and g_out; ``train``
@@ -848,14 +1035,8 @@ extern "C" int32_t kups_mlp_fwd(const kups_mlp *net, const double *x, int64_t n,
                                 size_t workspace_bytes, kups_status *status, void *stream) {
   if (net == nullptr || n < 0 || (n > 0 && (x == nullptr || g == nullptr))) return KUPS_ERR_INVALID;
   if (workspace_bytes < kups_mlp_workspace_bytes(n)) return KUPS_ERR_INVALID;
-  const int64_t cmax = std::min<int64_t>(n, kChunk);
-  const MlpWork w = carve(workspace, std::max<int64_t>(cmax, 1));
-  for (int64_t r0 = 0; r0 < n; r0 += kChunk) {
-    const int64_t c = std::min<int64_t>(kChunk, n - r0);
-    const int32_t rc = forward_chunk(net, x, r0, c, 0, w, g + r0, status, (cudaStream_t)stream);
-    if (rc) return rc;
-  }
-  return KUPS_OK;
+  (void)workspace;
+  return fused_forward(net, x, n, 0, g, status, (cudaStream_t)stream);
 }
 
 extern "C" int32_t kups_mlp_nce_batch(const double *data, int64_t n_data, int32_t batch, uint64_t seed,
@@ -926,11 +1107,8 @@ extern "C" int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float t
   if (workspace_bytes < kups_mlp_workspace_bytes(n)) return KUPS_ERR_INVALID;
   cudaStream_t st = (cudaStream_t)stream;
   const MlpWork w = carve(workspace, std::min<int64_t>(n, kChunk));
-  for (int64_t r0 = 0; r0 < n; r0 += kChunk) {
-    const int64_t c = std::min<int64_t>(kChunk, n - r0);
-    const int32_t rc = forward_chunk(net, nullptr, r0, c, grid, w, node + r0, status, st);
-    if (rc) return rc;
-  }
+  const int32_t rc = fused_forward(net, nullptr, n, grid, node, status, st);
+  if (rc) return rc;
   grid_normalise_kernel<<<1, 1024, 0, st>>>(node, n, temper, floor_frac, status);
   // three-pass scan; the block totals live in the (no longer needed) activation buffer
   const int n_blocks = (int)((n + kCdfPerBlock - 1) / kCdfPerBlock);
