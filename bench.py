@@ -314,6 +314,19 @@ def run_ours(a):
         },
         "clocks": clk,
     }
+    # FP32 pipe: 30 flop per pair within the cutoff counted once (half list), n_half from each
+    # system's density; peak derived as SMs x 128 FP32 lanes x 2 flop x SM clock under load
+    counts = np.bincount(W.system, minlength=W.n_systems).astype(float)
+    vol = np.abs(W.tril[:, 0] * W.tril[:, 2] * W.tril[:, 5])
+    n_half = (4.0 / 3.0) * math.pi * W.cutoff**3 * (counts / vol) / 2.0
+    flop_atom_step = 30.0 * float((n_half * counts).sum() / counts.sum())
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
+    fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    fp32_achieved = value * flop_atom_step / 1e12 / max(world, 1)
+    line["fp32_roofline"] = {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                             "frac": fp32_achieved / fp32_peak, "flop_per_atom_step": flop_atom_step,
+                             "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x {mhz:.0f} MHz"}
     if not a.no_e2e:
         line["e2e"] = run_e2e(a, W, torch)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
