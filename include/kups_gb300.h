@@ -166,6 +166,10 @@ typedef struct kups_md_args {
   double *energy;
   double *kinetic;
   double *virial;
+  double *pressure;          /* [n_systems] out (may be NULL; needs virial): instantaneous
+                                pressure 2K / 3V + Tr(stress) / 3 at the last step, stress =
+                                -(sum_i dU/dr_i (x) r_i + h^T dU/dh) / V (md/observables.py:38-61,
+                                observables/stress.py:70-82), energy / length^3 */
   double *trace_pe;
   double *trace_ke;
   int32_t *rebuilds;         /* [n_systems] out (may be NULL): Verlet-list builds per system */

@@ -38,7 +38,7 @@ class MdArgs(C.Structure):
         ("sys_offset", C.c_void_p), ("order", C.c_void_p), ("tril", C.c_void_p),
         ("cutoff", C.c_void_p), ("skin", C.c_void_p), ("dt", C.c_void_p), ("kT", C.c_void_p),
         ("friction", C.c_void_p), ("lj_table", C.c_void_p),
-        ("energy", C.c_void_p), ("kinetic", C.c_void_p), ("virial", C.c_void_p),
+        ("energy", C.c_void_p), ("kinetic", C.c_void_p), ("virial", C.c_void_p), ("pressure", C.c_void_p),
         ("trace_pe", C.c_void_p), ("trace_ke", C.c_void_p), ("rebuilds", C.c_void_p), ("profile", C.c_void_p),
         ("n_atoms", C.c_int64), ("n_systems", C.c_int32), ("n_species", C.c_int32),
         ("n_steps", C.c_int32), ("integrator", C.c_int32), ("forces_valid", C.c_int32),

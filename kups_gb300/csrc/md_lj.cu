@@ -800,6 +800,12 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
           for (int c = 0; c < 3; ++c) x += Li[c][ia[k]] * W[c][ib[k]];
           a.virial[6 * (int64_t)s + k] = x + fwt[k];
         }
+        if (a.pressure != nullptr) {
+          // sum_i dU/dr_i (x) r_i + h^T dU/dh = sum over pairs of d (x) dU/dd = W for a pair
+          // potential: P = (2 K - Tr W) / 3V
+          const double vol = fabs(A * C * F);
+          a.pressure[s] = (2.0 * a.kinetic[s] - (W[0][0] + W[1][1] + W[2][2])) / (3.0 * vol);
+        }
       }
     }
     prof_add(prof, 5, t0);

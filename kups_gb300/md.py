@@ -57,6 +57,7 @@ class MDSystems:
     potential_energy: torch.Tensor | None = None
     kinetic_energy: torch.Tensor | None = None
     unitcell_gradients: torch.Tensor | None = None  # dE/dtril [S, 6]
+    pressure: torch.Tensor | None = None  # instantaneous pressure [S] (energy / length^3)
 
 
 @dataclass
@@ -92,6 +93,7 @@ class PackedMD:
     energy: torch.Tensor | None = None
     kinetic: torch.Tensor | None = None
     virial: torch.Tensor | None = None
+    pressure: torch.Tensor | None = None
     rebuilds: torch.Tensor | None = None  # int32 [S], accumulated list builds (optional)
     profile: torch.Tensor | None = None  # int64 [10], cycles per kernel phase (optional)
 
@@ -166,7 +168,7 @@ def unpack(packed: PackedMD, state: MDState) -> MDState:
     _lib.check(rc, "kups_md_unpack")
     parts = replace(state.particles, positions=pos, momenta=mom, forces=frc)
     systems = replace(state.systems, potential_energy=packed.energy, kinetic_energy=packed.kinetic,
-                      unitcell_gradients=packed.virial)
+                      unitcell_gradients=packed.virial, pressure=packed.pressure)
     return replace(state, particles=parts, systems=systems)
 
 
@@ -213,6 +215,7 @@ class FusedLennardJonesMD:
             packed.energy = torch.zeros(s, device="cuda", dtype=torch.float64)
             packed.kinetic = torch.zeros(s, device="cuda", dtype=torch.float64)
             packed.virial = torch.zeros((s, 6), device="cuda", dtype=torch.float64)
+            packed.pressure = torch.zeros(s, device="cuda", dtype=torch.float64)
         a = _lib.MdArgs()
         a.pos, a.mom, a.force = packed.pos4.data_ptr(), packed.mom4.data_ptr(), packed.frc4.data_ptr()
         a.sys_offset, a.order, a.tril = packed.sys_offset.data_ptr(), packed.order.data_ptr(), packed.tril32.data_ptr()
@@ -220,6 +223,7 @@ class FusedLennardJonesMD:
         a.kT, a.friction, a.lj_table = packed.kT.data_ptr(), packed.friction.data_ptr(), packed.lj_table.data_ptr()
         a.energy, a.kinetic = packed.energy.data_ptr(), packed.kinetic.data_ptr()
         a.virial = packed.virial.data_ptr() if virial else None
+        a.pressure = packed.pressure.data_ptr() if virial and packed.pressure is not None else None
         a.trace_pe = trace_pe.data_ptr() if trace_pe is not None else None
         a.trace_ke = trace_ke.data_ptr() if trace_ke is not None else None
         a.rebuilds = packed.rebuilds.data_ptr() if packed.rebuilds is not None else None

@@ -301,3 +301,31 @@ def test_lj_tail_correction_matches_oracle():
         m = None if mask is None else mask.astype(bool)
         np.testing.assert_allclose(e.cpu().numpy(), olj.tail_correction_energy(sc, tril, sig, eps, rc, m), rtol=1e-12)
         np.testing.assert_allclose(p.cpu().numpy(), olj.tail_correction_pressure(sc, tril, sig, eps, rc, m), rtol=1e-12)
+
+
+def test_fused_md_pressure_matches_reference_formula():
+    """Instantaneous pressure (md/observables.py:38-61) with the virial-theorem stress
+    (observables/stress.py:70-82): P = 2K / 3V + Tr(sigma) / 3,
+    sigma = -(sum_i dU/dr_i (x) r_i + h^T dU/dh) / V, from the float64 oracle's gradients at the
+    returned positions (bar: relative 1e-4, float32 pair arithmetic)."""
+    from kups_gb300 import md
+
+    W = small_batch()
+    out = md.make_baoab_langevin_step(steps_per_call=8)([3, 4], md_state(W))
+    pos = out.particles.positions.cpu().numpy()
+    mom = out.particles.momenta.cpu().numpy()
+    e, f, dt = oracle_forces(W, pos)
+    got = out.systems.pressure.cpu().numpy()
+    exp = []
+    for s in range(W.n_systems):
+        sel = W.system == s
+        L = ouc.lattice_from_tril(W.tril[s])
+        G = np.zeros((3, 3))
+        G[0, 0], G[1, 0], G[1, 1], G[2, 0], G[2, 1], G[2, 2] = dt[s]
+        vol = abs(np.linalg.det(L))
+        sigma = -((-f[sel])[:, :, None] * pos[sel][:, None, :]).sum(0)
+        sigma -= L.T @ G
+        sigma /= vol
+        ke = 0.5 * np.sum(mom[sel] ** 2 / W.masses[sel][:, None])
+        exp.append(2 * ke / (3 * vol) + np.trace(sigma) / 3)
+    np.testing.assert_allclose(got, exp, rtol=1e-4, atol=1e-4 * np.abs(exp).max())
