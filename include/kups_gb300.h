@@ -185,6 +185,17 @@ typedef struct kups_md_args {
   uint64_t step0;
   int32_t n_ctas;            /* 0 = one per SM */
   int32_t block_threads;     /* 0 = library default */
+  /* integrator 2 = CSVR (CSVRStep + velocity Verlet, md/integrators.py:469-640),
+   * integrator 3 = CSVR + stochastic cell rescaling (make_csvr_npt_step, :641-890).
+   * Per-system R1, R2 and the barostat's R are independent draws (the reference
+   * draws one scalar per call for the whole batch). */
+  const double *thermostat_tau;   /* [n_systems] tau_T (integrators 2, 3) */
+  const double *target_pressure;  /* [n_systems] P0, energy / length^3 (integrator 3) */
+  const double *barostat_tau;     /* [n_systems] tau_P (integrator 3) */
+  const double *compressibility;  /* [n_systems] beta, length^3 / energy (integrator 3) */
+  const double *min_scale;        /* [n_systems] mu clipped to [min_scale, 1 / min_scale] */
+  double *cell;                   /* [n_systems, 6] in/out (integrator 3): float64 tril of the
+                                     cell, scaled by the barostat; `tril` is not read */
 } kups_md_args;
 
 size_t kups_lj_md_workspace_bytes(const kups_md_args *args);

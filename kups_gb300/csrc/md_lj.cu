@@ -55,6 +55,11 @@ struct SysParams {
   float coff[3];  // 0.5 + m
   float cscale[3];  // cells per fractional unit
   float dt, c1, c2;
+  float rc, rl;
+  double Ld[6];   // the cell in float64 (the barostat scales it)
+  // CSVR (integrators 2, 3) and stochastic cell rescaling (integrator 3)
+  double csvr_c1, kTd, dtd, taup, beta, p0, mumin;
+  int dof;
 };
 
 struct Smem {
@@ -78,6 +83,9 @@ struct Smem {
   int flag;
   int next_sys;
   int work;
+  double mcum;  // cell scale accumulated since the last list build
+  float alpha;  // CSVR momentum scale of the coming step
+  float mu;     // barostat scale of this step
 };
 
 
@@ -128,6 +136,53 @@ __device__ inline int cell_of_point(const SysParams &p, float x, float y, float 
   cy = cell_coord(f[1], p.coff[1], p.cscale[1], p.nc[1]);
   cz = cell_coord(f[2], p.coff[2], p.cscale[2], p.nc[2]);
   return (cz * p.nc[1] + cy) * p.nc[0] + cx;
+}
+
+// Cell-dependent parameters from p.L and p.rl (one thread): inverse, image
+// margins m = rl / width per axis, image layers K = ceil(m) and the cell grid
+// over the extended region [-0.5 - m, 0.5 + m).
+__device__ void set_cell(SysParams &p) {
+  const float A = p.L[0], B = p.L[1], C = p.L[2], D = p.L[3], E = p.L[4], F = p.L[5];
+  p.inv[0] = 1.0f / A;
+  p.inv[2] = 1.0f / C;
+  p.inv[5] = 1.0f / F;
+  p.inv[1] = -(B * p.inv[0]) / C;
+  p.inv[4] = -(E * p.inv[2]) / F;
+  p.inv[3] = -((D * p.inv[0]) + (E * p.inv[1])) / F;
+  const float rl = p.rl;
+  const float vol = fabsf(A * C * F);
+  const float c0 = C * F, c1 = B * F, c2 = B * E - C * D;
+  const float w[3] = {vol / sqrtf(c0 * c0 + c1 * c1 + c2 * c2),
+                      vol / sqrtf((A * F) * (A * F) + (A * E) * (A * E)), vol / fabsf(A * C)};
+  int ncell = 1;
+  for (int d = 0; d < 3; ++d) {
+    p.m[d] = rl / w[d];
+    p.K[d] = (int)ceilf(p.m[d]);
+    p.ext[d] = 1.0f + 2.0f * p.m[d];
+    p.nc[d] = max(1, (int)floorf(p.ext[d] * w[d] / rl));
+    ncell *= p.nc[d];
+  }
+  while (ncell > kMaxCells) {
+    int am = 0;
+    for (int d = 1; d < 3; ++d)
+      if (p.nc[d] > p.nc[am]) am = d;
+    p.nc[am] = (p.nc[am] + 1) / 2;
+    ncell = p.nc[0] * p.nc[1] * p.nc[2];
+  }
+  for (int d = 0; d < 3; ++d) {
+    p.coff[d] = 0.5f + p.m[d];
+    p.cscale[d] = (float)p.nc[d] / p.ext[d];
+  }
+}
+
+__device__ inline void set_shift_vectors(Smem &sm) {
+  for (int c = threadIdx.x; c < kShiftCount; c += blockDim.x) {
+    const int ox = c / 25 - 2, oy = (c / 5) % 5 - 2, oz = c % 5 - 2;
+    const float f[3] = {(float)ox, (float)oy, (float)oz};
+    float x, y, z;
+    cart_of(sm.p, f, x, y, z);
+    sm.shift_vec[c] = make_float4(x, y, z, 0.f);
+  }
 }
 
 // Lanes serving one atom: the smallest power of two (<= 16) that still gives
@@ -524,6 +579,48 @@ __device__ __forceinline__ void forces_dispatch(Smem &sm, int n, int nsp, int tp
     compute_forces<ENERGY, VIRIAL, false>(sm, n, nsp, tpa, nl, rc2, sig2, a4, pe, wv);
 }
 
+static_assert(sizeof(Smem) <= 227 * 1024, "fused MD shared memory above the per-CTA limit");
+
+// Key offsets that separate the system-level draws (CSVR R1, the barostat's R)
+// and the chi-squared normals from the per-atom Langevin noise.
+constexpr uint64_t kSysSeed = 0x6a09e667f3bcc909ull;
+constexpr uint64_t kChiSeed = 0xbb67ae8584caa73bull;
+
+// CSVR scale of the coming step (CSVRStep, integrators.py:519-596), all threads
+// call it: R2 ~ chi^2(N_dof - 1) is the sum of N_dof - 1 squared standard
+// normals, drawn in groups of four across the block; thread 0 draws R1 and forms
+// alpha^2 = c1 + c2 (R1^2 + R2) + 2 R1 sqrt(c1 c2), c1 = exp(-dt / tau_T),
+// c2 = (1 - c1) K_target / (K N_dof), in float64.  A system with no thermal
+// degrees of freedom or no kinetic energy keeps alpha = 1 (the reference's
+// formula divides by zero there).
+__device__ void csvr_alpha(Smem &sm, double ke, uint64_t seed, int sys, uint64_t counter) {
+  const SysParams &p = sm.p;
+  const int cnt = p.dof - 1;
+  float acc = 0.f;
+  for (int g = threadIdx.x; 4 * g < cnt; g += blockDim.x) {
+    float z[4];
+    normal4(seed ^ kChiSeed, ((uint64_t)sys << 20) | (uint64_t)g, counter, z);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (4 * g + k < cnt) acc = fmaf(z[k], z[k], acc);
+  }
+  const double r2 = block_sum((double)acc, sm.red);
+  if (threadIdx.x == 0) {
+    float z[4];
+    normal4(seed ^ kSysSeed, (uint64_t)sys, counter, z);
+    double alpha = 1.0;
+    if (p.dof > 0 && ke > 0.0) {
+      const double r1 = z[0];
+      const double c1 = p.csvr_c1;
+      const double c2 = (1.0 - c1) * (0.5 * p.dof * p.kTd) / (ke * p.dof);
+      const double a2 = c1 + c2 * (r1 * r1 + (cnt > 0 ? r2 : 0.0)) + 2.0 * r1 * sqrt(c1 * c2);
+      alpha = sqrt(fmax(a2, 0.0));
+    }
+    sm.alpha = (float)alpha;
+  }
+  __syncthreads();
+}
+
 template <int INTEGRATOR>
 __global__ void __launch_bounds__(kThreads, 1)
 md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
@@ -561,57 +658,42 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
     // ---- per-system parameters, computed once into shared memory
     SysParams &p = sm.p;
     if (tid == 0) {
-      for (int k = 0; k < 6; ++k) p.L[k] = a.tril[6 * (int64_t)s + k];
-      const float A = p.L[0], B = p.L[1], C = p.L[2], D = p.L[3], E = p.L[4], F = p.L[5];
-      p.inv[0] = 1.0f / A;
-      p.inv[2] = 1.0f / C;
-      p.inv[5] = 1.0f / F;
-      p.inv[1] = -(B * p.inv[0]) / C;
-      p.inv[4] = -(E * p.inv[2]) / F;
-      p.inv[3] = -((D * p.inv[0]) + (E * p.inv[1])) / F;
+      if (INTEGRATOR == 3) {
+        for (int k = 0; k < 6; ++k) p.Ld[k] = a.cell[6 * (int64_t)s + k];
+      } else {
+        for (int k = 0; k < 6; ++k) p.Ld[k] = (double)a.tril[6 * (int64_t)s + k];
+      }
+      for (int k = 0; k < 6; ++k) p.L[k] = (float)p.Ld[k];
       const float rc = a.cutoff[s], skin = a.skin[s], rl = rc + skin;
+      p.rc = rc;
+      p.rl = rl;
       p.rc2 = rc * rc;
       p.rl2 = rl * rl;
       p.half_skin = 0.5f * skin;
-      const float vol = fabsf(A * C * F);
-      const float c0 = C * F, c1 = B * F, c2 = B * E - C * D;
-      const float w[3] = {vol / sqrtf(c0 * c0 + c1 * c1 + c2 * c2),
-                          vol / sqrtf((A * F) * (A * F) + (A * E) * (A * E)), vol / fabsf(A * C)};
-      int ncell = 1;
-      for (int d = 0; d < 3; ++d) {
-        p.m[d] = rl / w[d];
-        p.K[d] = (int)ceilf(p.m[d]);
-        p.ext[d] = 1.0f + 2.0f * p.m[d];
-        p.nc[d] = max(1, (int)floorf(p.ext[d] * w[d] / rl));
-        ncell *= p.nc[d];
-      }
-      while (ncell > kMaxCells) {
-        int am = 0;
-        for (int d = 1; d < 3; ++d)
-          if (p.nc[d] > p.nc[am]) am = d;
-        p.nc[am] = (p.nc[am] + 1) / 2;
-        ncell = p.nc[0] * p.nc[1] * p.nc[2];
-      }
-      for (int d = 0; d < 3; ++d) {
-        p.coff[d] = 0.5f + p.m[d];
-        p.cscale[d] = (float)p.nc[d] / p.ext[d];
-      }
+      set_cell(p);
       p.dt = a.dt[s];
       p.c1 = expf(-a.friction[s] * p.dt);
       p.c2 = sqrtf(a.kT[s] * (1.0f - p.c1 * p.c1));
+      if (INTEGRATOR >= 2) {
+        p.dtd = (double)p.dt;
+        p.kTd = (double)a.kT[s];
+        p.csvr_c1 = exp(-p.dtd / a.thermostat_tau[s]);
+        p.dof = 3 * n - 3;
+      }
+      if (INTEGRATOR == 3) {
+        p.taup = a.barostat_tau[s];
+        p.beta = a.compressibility[s];
+        p.p0 = a.target_pressure[s];
+        p.mumin = a.min_scale[s];
+      }
+      sm.mcum = 1.0;
     }
     __syncthreads();
     if (p.K[0] > 2 || p.K[1] > 2 || p.K[2] > 2) {
       if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
       continue;
     }
-    for (int c = tid; c < kShiftCount; c += nt) {
-      const int ox = c / 25 - 2, oy = (c / 5) % 5 - 2, oz = c % 5 - 2;
-      const float f[3] = {(float)ox, (float)oy, (float)oz};
-      float x, y, z;
-      cart_of(p, f, x, y, z);
-      sm.shift_vec[c] = make_float4(x, y, z, 0.f);
-    }
+    set_shift_vectors(sm);
     int bad_species = 0;
     for (int i = tid; i < n; i += nt) {
       const float4 qv = gpos[a0 + i];
@@ -636,6 +718,12 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
     // hot scalars in registers
     const float rc2 = p.rc2, dt = p.dt, hdt = 0.5f * p.dt, c1 = p.c1, c2 = p.c2;
     const float half_skin = p.half_skin;
+    // list-validity threshold on the distance travelled (in the frame of the last
+    // build): with the cell scaled by m since that build, a pair missing from the
+    // list is at least m (rc + skin - 2 d) apart, so the list holds while
+    // d <= (rc + skin - rc / m) / 2 (skin / 2 at m = 1)
+    float thr = half_skin, inv_mcum = 1.0f;
+    double mcum = 1.0;
     float wv[6] = {0, 0, 0, 0, 0, 0};
     double pe = 0.0;
     if (!a.forces_valid) {
@@ -645,20 +733,34 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
       __syncthreads();
     }
+    if (INTEGRATOR >= 2 && a.n_steps > 0) {
+      float ke = 0.f;
+      for (int i = tid; i < n; i += nt) {
+        const float4 m = sm.mom[i];
+        ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
+      }
+      csvr_alpha(sm, block_sum((double)ke, sm.red + 36), a.seed, s, a.step0);
+    }
     for (int step = 0; step < a.n_steps && ok; ++step) {
       const bool last = step == a.n_steps - 1;
       const bool want_e = last || a.trace_pe != nullptr || a.trace_ke != nullptr;
-      // ---- B A (O A)
+      // ---- (CSVR) B A (O A)
+      const float alpha = INTEGRATOR >= 2 ? sm.alpha : 1.0f;
       if (tid == 0) sm.work = 0;
       int moved_far = 0;
       for (int i = tid; i < n; i += nt) {
         float4 x = sm.pos[i], m = sm.mom[i], f = sm.frc[i];
         const float inv_m = 1.0f / m.w;
+        if (INTEGRATOR >= 2) {
+          m.x = __fmul_rn(m.x, alpha);
+          m.y = __fmul_rn(m.y, alpha);
+          m.z = __fmul_rn(m.z, alpha);
+        }
         m.x = fmaf(f.x, hdt, m.x);
         m.y = fmaf(f.y, hdt, m.y);
         m.z = fmaf(f.z, hdt, m.z);
         float dx, dy, dz;
-        if (INTEGRATOR == 0) {
+        if (INTEGRATOR != 1) {
           const float sc = inv_m * dt;
           dx = m.x * sc;
           dy = m.y * sc;
@@ -681,8 +783,12 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         x.x += dx;
         x.y += dy;
         x.z += dz;
-        f.w += sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
-        moved_far |= f.w > half_skin;
+        const float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+        if (INTEGRATOR == 3)
+          f.w = fmaf(len, inv_mcum, f.w);
+        else
+          f.w += len;
+        moved_far |= f.w > thr;
         sm.pos[i] = x;
         sm.mom[i] = m;
         sm.frc[i] = f;
@@ -693,6 +799,9 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         if (tid == 0 && a.rebuilds != nullptr) a.rebuilds[s] += 1;
         ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s, prof, scratch);
         if (!ok) break;
+        mcum = 1.0;
+        thr = half_skin;
+        inv_mcum = 1.0f;
         if (tid == 0) sm.work = 0;
         __syncthreads();
       } else {
@@ -702,15 +811,22 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
       prof_add(prof, 2, t0);
       // ---- forces
       pe = 0.0;
-      if (last && a.virial != nullptr)
+      if (INTEGRATOR == 3) {
+        // the barostat needs the pair virial at every step
+#pragma unroll
+        for (int k = 0; k < 6; ++k) wv[k] = 0.f;
+        forces_dispatch<false, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+      } else if (last && a.virial != nullptr) {
         forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
-      else if (want_e)
+      } else if (want_e) {
         forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
-      else
+      } else {
         forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+      }
       __syncthreads();
       prof_add(prof, 3, t0);
-      // ---- B (and kinetic energy when recorded)
+      // ---- B (and kinetic energy when recorded or needed by the thermostat)
+      const bool need_ke = want_e || INTEGRATOR >= 2;
       float ke = 0.f;
       for (int i = tid; i < n; i += nt) {
         float4 m = sm.mom[i];
@@ -719,11 +835,80 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         m.y = fmaf(f.y, hdt, m.y);
         m.z = fmaf(f.z, hdt, m.z);
         sm.mom[i] = m;
-        if (want_e) ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
+        if (need_ke) ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
+      }
+      const double ke_tot = need_ke ? block_sum((double)ke, sm.red + 36) : 0.0;
+      if (INTEGRATOR == 3) {
+        // ---- stochastic cell rescaling (integrators.py:710-789): pressure from the
+        // kinetic energy and the pair virial, P = (2 K - Tr W) / 3V, then
+        // d eps = dt / tau_P beta (P - P0) + sqrt(2 kT beta dt / (tau_P V)) R and
+        // mu = exp(d eps / 3) clipped to [mu_min, 1 / mu_min] scale cell and positions
+        double w6[6];
+        for (int k = 0; k < 6; ++k) w6[k] = block_sum((double)wv[k], sm.red);
+        if (tid == 0) {
+          const double vol = fabs(p.Ld[0] * p.Ld[2] * p.Ld[5]);
+          const double prs = (2.0 * ke_tot - (w6[0] + w6[2] + w6[5])) / (3.0 * vol);
+          float z[4];
+          normal4(a.seed ^ kSysSeed, (uint64_t)s, a.step0 + (uint64_t)step, z);
+          const double deps = p.dtd / p.taup * p.beta * (prs - p.p0) +
+                              sqrt(2.0 * p.kTd * p.beta * p.dtd / (p.taup * vol)) * (double)z[1];
+          const double mu = fmin(fmax(exp(deps / 3.0), p.mumin), 1.0 / p.mumin);
+          for (int k = 0; k < 6; ++k) {
+            p.Ld[k] *= mu;
+            p.L[k] = (float)p.Ld[k];
+          }
+          set_cell(p);
+          sm.mu = (float)mu;
+          sm.work = 0;
+        }
+        __syncthreads();
+        if (p.K[0] > 2 || p.K[1] > 2 || p.K[2] > 2) {
+          if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
+          ok = false;
+          break;
+        }
+        set_shift_vectors(sm);
+        const float mu = sm.mu;
+        mcum *= (double)mu;
+        inv_mcum = (float)(1.0 / mcum);
+        thr = mcum == 1.0 ? half_skin : 0.5f * (p.rl - p.rc * inv_mcum);
+        int far = 0;
+        for (int i = tid; i < n; i += nt) {
+          float4 x = sm.pos[i];
+          x.x = __fmul_rn(x.x, mu);
+          x.y = __fmul_rn(x.y, mu);
+          x.z = __fmul_rn(x.z, mu);
+          sm.pos[i] = x;
+          far |= sm.frc[i].w > thr;
+        }
+        if (__syncthreads_or(far)) {
+          if (tid == 0 && a.rebuilds != nullptr) a.rebuilds[s] += 1;
+          ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s, prof, scratch);
+          if (!ok) break;
+          mcum = 1.0;
+          thr = half_skin;
+          inv_mcum = 1.0f;
+          if (tid == 0) sm.work = 0;
+          __syncthreads();
+        } else {
+          update_ghosts(sm, n);
+          __syncthreads();
+        }
+        // ---- forces at the rescaled positions (the next step's first kick)
+        pe = 0.0;
+        if (last && a.virial != nullptr) {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) wv[k] = 0.f;
+          forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        } else if (want_e) {
+          forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        } else {
+          forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        }
+        __syncthreads();
       }
       if (want_e) {
         const double pe_tot = block_sum(pe, sm.red);
-        const double ke_tot = block_sum((double)ke, sm.red + 36);
         if (tid == 0) {
           if (a.trace_pe) a.trace_pe[(int64_t)step * a.n_systems + s] = pe_tot;
           if (a.trace_ke) a.trace_ke[(int64_t)step * a.n_systems + s] = ke_tot;
@@ -733,6 +918,7 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
           }
         }
       }
+      if (INTEGRATOR >= 2 && !last) csvr_alpha(sm, ke_tot, a.seed, s, a.step0 + (uint64_t)step + 1);
       prof_add(prof, 4, t0);
     }
     if (!ok) continue;
@@ -788,7 +974,7 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         fwt[k] = block_sum((double)fw[k], sm.red + 36);
         __syncthreads();
       }
-      const double A = p.L[0], B = p.L[1], C = p.L[2], D = p.L[3], E = p.L[4], F = p.L[5];
+      const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
       double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
       Li[1][0] = -(B * Li[0][0]) / C;
       Li[2][1] = -(E * Li[1][1]) / F;
@@ -808,6 +994,8 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         }
       }
     }
+    if (INTEGRATOR == 3 && tid == 0)
+      for (int k = 0; k < 6; ++k) a.cell[6 * (int64_t)s + k] = p.Ld[k];
     prof_add(prof, 5, t0);
     __syncthreads();
   }
@@ -817,6 +1005,16 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
 }  // namespace kups
 
 using namespace kups;
+
+template <int INTEGRATOR>
+static cudaError_t launch_md(const kups_md_args &a, int ctas, int threads, size_t smem, uint32_t *nl,
+                             int *queue, kups_status *status, cudaStream_t stream) {
+  cudaError_t e = cudaFuncSetAttribute(md_lj_kernel<INTEGRATOR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  md_lj_kernel<INTEGRATOR><<<ctas, threads, smem, stream>>>(a, nl, queue, status);
+  return cudaSuccess;
+}
 
 extern "C" int32_t kups_lj_md_max_atoms(void) { return kMaxAtoms; }
 
@@ -835,7 +1033,12 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
   if (a == nullptr || a->n_systems < 0 || a->n_steps < 0 || a->n_species <= 0 ||
       a->n_species > kMaxSpecies || a->neighbor_capacity <= 0 || a->neighbor_capacity > 4096 ||
       a->neighbor_capacity % 16 != 0 ||
-      (a->integrator != 0 && a->integrator != 1))
+      a->integrator < 0 || a->integrator > 3)
+    return KUPS_ERR_INVALID;
+  if (a->integrator >= 2 && a->thermostat_tau == nullptr) return KUPS_ERR_INVALID;
+  if (a->integrator == 3 && (a->target_pressure == nullptr || a->barostat_tau == nullptr ||
+                             a->compressibility == nullptr || a->min_scale == nullptr ||
+                             a->cell == nullptr))
     return KUPS_ERR_INVALID;
   if (ws_bytes < kups_lj_md_workspace_bytes(a)) return KUPS_ERR_INVALID;
   if (a->n_systems == 0) return KUPS_OK;
@@ -849,12 +1052,11 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
   uint32_t *nl = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(queue) + 256);
   KUPS_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(int), stream));
   const size_t smem = sizeof(Smem);
-  if (a->integrator == 0) {
-    KUPS_CUDA_TRY(cudaFuncSetAttribute(md_lj_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    md_lj_kernel<0><<<ctas, threads, smem, stream>>>(*a, nl, queue, status);
-  } else {
-    KUPS_CUDA_TRY(cudaFuncSetAttribute(md_lj_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    md_lj_kernel<1><<<ctas, threads, smem, stream>>>(*a, nl, queue, status);
+  switch (a->integrator) {
+    case 0: KUPS_CUDA_TRY(launch_md<0>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
+    case 1: KUPS_CUDA_TRY(launch_md<1>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
+    case 2: KUPS_CUDA_TRY(launch_md<2>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
+    default: KUPS_CUDA_TRY(launch_md<3>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
   }
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

@@ -1,17 +1,19 @@
 """Fused Lennard-Jones molecular dynamics behind kUPS's ``Propagator`` interface.
 
 Mirrors ``Propagator.__call__(key, state) -> state`` (src/kups/core/propagator.py:84-121)
-for the propagators built by ``make_velocity_verlet_step`` and
-``make_baoab_langevin_step`` (src/kups/md/integrators.py:273-318, 405-455)
-around the Lennard-Jones potential, as ``make_md_propagator`` wires them
+for the propagators built by ``make_velocity_verlet_step``,
+``make_baoab_langevin_step``, ``make_csvr_step`` and ``make_csvr_npt_step``
+(src/kups/md/integrators.py:273-318, 405-455, 598-640, 801-890) around the
+Lennard-Jones potential, as ``make_md_propagator`` wires them
 (src/kups/application/md/simulation.py:74-119).  One call runs
 ``steps_per_call`` steps of every system in one persistent CUDA launch
 (``kups_lj_md_run``).
 
 State layout: the reference's particle table (float64 positions, momenta,
 masses, species, system index; ``MDParticles``, application/md/data.py:31-65)
-and system table (lattice ``tril``, time step, temperature, friction;
-``MDSystems``, :68-106).  Inside, atoms are packed once into float4 arrays
+and system table (lattice ``tril``, time step, temperature, friction, CSVR and
+barostat constants; ``MDSystems``, :68-106).  The NPT integrator scales the cell:
+the returned state carries the new ``tril``.  Inside, atoms are packed once into float4 arrays
 grouped by system (``PackedMD``); repeated calls on a ``PackedMD`` keep the
 state on the device.  Capacity overflows restore the state from a backup and
 retry with the size the kernel reported, as ``ResetOnErrorPropagator``
@@ -35,7 +37,8 @@ from .neighborlist import _stream, new_status, read_status
 from .potential import LennardJonesParameters
 from .units import BOLTZMANN_CONSTANT
 
-INTEGRATORS = {"velocity_verlet": 0, "vv": 0, "nve": 0, "baoab": 1, "baoab_langevin": 1, "nvt": 1}
+INTEGRATORS = {"verlet": 0, "velocity_verlet": 0, "vv": 0, "nve": 0, "baoab": 1, "baoab_langevin": 1, "nvt": 1,
+               "csvr": 2, "csvr_npt": 3, "npt": 3}
 
 
 @dataclass
@@ -58,6 +61,11 @@ class MDSystems:
     kinetic_energy: torch.Tensor | None = None
     unitcell_gradients: torch.Tensor | None = None  # dE/dtril [S, 6]
     pressure: torch.Tensor | None = None  # instantaneous pressure [S] (energy / length^3)
+    thermostat_time_constant: torch.Tensor | None = None  # [S] CSVR tau_T (internal time)
+    target_pressure: torch.Tensor | None = None  # [S] P0 (energy / length^3)
+    pressure_coupling_time: torch.Tensor | None = None  # [S] tau_P (internal time)
+    compressibility: torch.Tensor | None = None  # [S] beta (length^3 / energy)
+    minimum_scale_factor: torch.Tensor | None = None  # [S] barostat clip
 
 
 @dataclass
@@ -96,6 +104,12 @@ class PackedMD:
     pressure: torch.Tensor | None = None
     rebuilds: torch.Tensor | None = None  # int32 [S], accumulated list builds (optional)
     profile: torch.Tensor | None = None  # int64 [10], cycles per kernel phase (optional)
+    cell: torch.Tensor | None = None  # float64 [S, 6]: the cell the barostat scales
+    thermostat_tau: torch.Tensor | None = None  # float64 [S] (CSVR, NPT)
+    target_pressure: torch.Tensor | None = None  # float64 [S] (NPT)
+    barostat_tau: torch.Tensor | None = None
+    compressibility: torch.Tensor | None = None
+    min_scale: torch.Tensor | None = None
 
     @property
     def n_atoms(self) -> int:
@@ -105,8 +119,17 @@ class PackedMD:
     def n_systems(self) -> int:
         return self.sys_offset.shape[0] - 1
 
-    def clone_dynamic(self) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
-        return self.pos4.clone(), self.mom4.clone(), self.frc4.clone()
+    def clone_dynamic(self) -> tuple:
+        return (self.pos4.clone(), self.mom4.clone(), self.frc4.clone(),
+                self.cell.clone() if self.cell is not None else None)
+
+    def restore_dynamic(self, backup) -> None:
+        self.pos4.copy_(backup[0])
+        self.mom4.copy_(backup[1])
+        self.frc4.copy_(backup[2])
+        if backup[3] is not None:
+            self.cell.copy_(backup[3])
+            self.tril32.copy_(backup[3])
 
 
 def lj_table(params: LennardJonesParameters) -> torch.Tensor:
@@ -146,17 +169,21 @@ def pack(state: MDState) -> PackedMD:
     vol = (tril[:, 0] * tril[:, 2] * tril[:, 5]).abs()
     dens = float((counts.to(torch.float64) / vol).max()) if s > 0 else 0.0
     kT = torch.as_tensor(sy.temperature, dtype=torch.float64).to(dev) * BOLTZMANN_CONSTANT
+    f64 = lambda x: None if x is None else torch.as_tensor(x, dtype=torch.float64).to(dev).reshape(-1).expand(s).contiguous()
     return PackedMD(
         pos4=pos4, mom4=mom4, frc4=frc4, perm=perm32, sys_offset=sys_offset.to(torch.int32).contiguous(),
         order=order.to(torch.int32).contiguous(), tril32=tril.to(torch.float32).contiguous(),
         cutoff=f32(state.lj_parameters.cutoff), skin=f32(state.skin), dt=f32(sy.time_step), kT=f32(kT),
         friction=f32(sy.friction_coefficient), lj_table=lj_table(state.lj_parameters),
         n_species=int(state.lj_parameters.sigma.shape[0]), max_atoms=int(counts.max()) if s > 0 else 0,
-        max_density=dens, forces_valid=p.forces is not None,
+        max_density=dens, forces_valid=p.forces is not None, cell=tril.clone().contiguous(),
+        thermostat_tau=f64(sy.thermostat_time_constant), target_pressure=f64(sy.target_pressure),
+        barostat_tau=f64(sy.pressure_coupling_time), compressibility=f64(sy.compressibility),
+        min_scale=f64(sy.minimum_scale_factor),
     )
 
 
-def unpack(packed: PackedMD, state: MDState) -> MDState:
+def unpack(packed: PackedMD, state: MDState, integrator: int = 0) -> MDState:
     """Packed device arrays -> a new reference-layout state (kups_md_unpack)."""
     lib = _lib.load()
     n = packed.n_atoms
@@ -169,6 +196,8 @@ def unpack(packed: PackedMD, state: MDState) -> MDState:
     parts = replace(state.particles, positions=pos, momenta=mom, forces=frc)
     systems = replace(state.systems, potential_energy=packed.energy, kinetic_energy=packed.kinetic,
                       unitcell_gradients=packed.virial, pressure=packed.pressure)
+    if packed.cell is not None and integrator == INTEGRATORS["csvr_npt"]:
+        systems = replace(systems, tril=packed.cell.clone())
     return replace(state, particles=parts, systems=systems)
 
 
@@ -198,7 +227,7 @@ class FusedLennardJonesMD:
     def __call__(self, key, state: MDState) -> MDState:
         packed = pack(state)
         self.run_packed(packed, self.steps_per_call, key_to_seed(key), state.step)
-        out = unpack(packed, state)
+        out = unpack(packed, state, INTEGRATORS[self.integrator])
         return replace(out, step=state.step + self.steps_per_call)
 
     def capacity_for(self, packed: PackedMD) -> int:
@@ -235,6 +264,17 @@ class FusedLennardJonesMD:
         a.neighbor_capacity = self.capacity_for(packed)
         a.seed, a.step0 = int(seed) & (2**64 - 1), int(step0)
         a.n_ctas, a.block_threads = self.n_ctas, self.block_threads
+        if a.integrator >= 2:
+            need = ["thermostat_tau"] + (["target_pressure", "barostat_tau", "compressibility", "min_scale"]
+                                         if a.integrator == 3 else [])
+            missing = [k for k in need if getattr(packed, k) is None]
+            if missing:
+                raise ValueError(f"integrator {self.integrator!r} needs the system fields {missing}")
+            a.thermostat_tau = packed.thermostat_tau.data_ptr()
+            if a.integrator == 3:
+                a.target_pressure, a.barostat_tau = packed.target_pressure.data_ptr(), packed.barostat_tau.data_ptr()
+                a.compressibility, a.min_scale = packed.compressibility.data_ptr(), packed.min_scale.data_ptr()
+                a.cell = packed.cell.data_ptr()
         return a
 
     def workspace(self, a: _lib.MdArgs) -> torch.Tensor:
@@ -252,6 +292,8 @@ class FusedLennardJonesMD:
         rc = _lib.load().kups_lj_md_run(C.byref(a), ws.data_ptr(), ws.numel(), status.data_ptr(), _stream())
         _lib.check(rc, "kups_lj_md_run")
         packed.forces_valid = True
+        if a.integrator == 3:
+            packed.tril32.copy_(packed.cell)
         return status
 
     def run_packed(self, packed: PackedMD, n_steps: int, seed: int = 0, step0: int = 0, trace: bool = False,
@@ -269,9 +311,7 @@ class FusedLennardJonesMD:
             if status.code == _lib.KUPS_OK:
                 return (tpe, tke) if trace else None
             if status.code == _lib.KUPS_ERR_CAPACITY and status.detail == _lib.KUPS_CAP_NEIGHBORS:
-                packed.pos4.copy_(backup[0])
-                packed.mom4.copy_(backup[1])
-                packed.frc4.copy_(backup[2])
+                packed.restore_dynamic(backup)
                 packed.forces_valid = valid0
                 self.neighbor_capacity = int(math.ceil(status.required * 1.25 / 16.0) * 16)
                 continue
@@ -287,3 +327,15 @@ def make_velocity_verlet_step(steps_per_call: int = 1, **kw) -> FusedLennardJone
 def make_baoab_langevin_step(steps_per_call: int = 1, **kw) -> FusedLennardJonesMD:
     """BAOAB Langevin (NVT) with the LJ force as derivative computation (integrators.py:405-455)."""
     return FusedLennardJonesMD("baoab", steps_per_call, **kw)
+
+
+def make_csvr_step(steps_per_call: int = 1, **kw) -> FusedLennardJonesMD:
+    """CSVR thermostat then velocity Verlet (NVT; integrators.py:598-640); needs
+    ``MDSystems.thermostat_time_constant``."""
+    return FusedLennardJonesMD("csvr", steps_per_call, **kw)
+
+
+def make_csvr_npt_step(steps_per_call: int = 1, **kw) -> FusedLennardJonesMD:
+    """CSVR, velocity Verlet, stochastic cell rescaling and the forces again (NPT;
+    integrators.py:801-890); needs the thermostat and barostat system fields."""
+    return FusedLennardJonesMD("csvr_npt", steps_per_call, **kw)
