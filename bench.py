@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-gcmc", action="store_true", help="skip the GCMC plain / learned-proposal section")
     ap.add_argument("--no-ewald", action="store_true", help="skip the LJ + Ewald MD (ionic melt) section")
+    ap.add_argument("--no-ensembles", action="store_true", help="skip the BAOAB / CSVR / NPT comparison")
     ap.add_argument("--gcmc-replicas", type=int, default=1024)
     ap.add_argument("--strong", action="store_true",
                     help="split one --systems batch across the ranks (cost-balanced contiguous ranges) "
@@ -333,6 +334,8 @@ def run_ours(a):
         rate, cores, sample = cpu_baseline(a.systems, a.cpu_seconds, 1)
         line["cpu_baseline"] = {"value": rate, "unit": "atom-steps/s", "cores": cores, "kind": "port",
                                 "sample": sample}
+    if rank == 0 and not a.no_ensembles:
+        line["ensembles"] = run_ensembles(a, W, torch)
     if rank == 0 and not a.no_ewald:
         line["argon_nvt"] = run_argon(a, torch)
         line["lj_ewald_md"] = run_ewald_md(a)
@@ -342,6 +345,47 @@ def run_ours(a):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_ensembles(a, W, torch, steps=200):
+    """The same batched workload under each thermostat / barostat of the fused kernel, one
+    persistent launch of `steps` steps each after 10 warm-up steps: BAOAB, CSVR (tau_T 100 fs)
+    and CSVR + stochastic cell rescaling (P0 1 bar, tau_P 1 ps, beta 2e-4 / bar, mu within
+    [0.99, 1 / 0.99]; two force evaluations per step, as the reference's NPT step does)."""
+    from kups_gb300 import md
+    from kups_gb300.units import FEMTO_SECOND
+
+    bar = 6.241509074e-7  # eV / A^3
+    out = {"workload": "the headline batched workload", "steps_per_launch": steps, "ms_per_step": {},
+           "atom_steps_per_s": {}}
+    for name, make in (("baoab", md.make_baoab_langevin_step), ("csvr", md.make_csvr_step),
+                       ("csvr_npt", md.make_csvr_npt_step)):
+        state = state_from_workload(W, torch)
+        S = W.n_systems
+        full = lambda v: torch.full((S,), float(v), dtype=torch.float64, device="cuda")
+        state.systems.thermostat_time_constant = full(100 * FEMTO_SECOND)
+        state.systems.target_pressure = full(bar)
+        state.systems.pressure_coupling_time = full(1000 * FEMTO_SECOND)
+        state.systems.compressibility = full(2e-4 / bar)
+        state.systems.minimum_scale_factor = full(0.99)
+        prop = make()
+        packed = md.pack(state)
+        prop.run_packed(packed, 10, seed=5, step0=0)
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        st = prop.launch(packed, steps, seed=5, step0=10, virial=False)
+        t1.record()
+        torch.cuda.synchronize()
+        from kups_gb300 import _lib
+        from kups_gb300.neighborlist import read_status
+
+        _lib.raise_status(read_status(st))
+        ms = t0.elapsed_time(t1) / steps
+        out["ms_per_step"][name] = ms
+        out["atom_steps_per_s"][name] = W.n_atoms / (ms / 1e3)
+        del packed, prop
+    return out
 
 
 def run_argon(a, torch):

@@ -57,8 +57,12 @@ struct SysParams {
   float dt, c1, c2;
   float rc, rl;
   double Ld[6];   // the cell in float64 (the barostat scales it)
-  // CSVR (integrators 2, 3) and stochastic cell rescaling (integrator 3)
-  double csvr_c1, kTd, dtd, taup, beta, p0, mumin;
+  // CSVR (integrators 2, 3) and stochastic cell rescaling (integrator 3), set
+  // up in float64 once per system and used in float32 per step
+  float csvr_c1, csvr_omc1;  // exp(-dt / tau_T), 1 - exp(-dt / tau_T)
+  float kTf;
+  float scr_a, scr_b, p0f;   // dt / tau_P beta, 2 kT beta dt / tau_P, P0
+  double mumin, mumax;
   int dof;
 };
 
@@ -83,9 +87,10 @@ struct Smem {
   int flag;
   int next_sys;
   int work;
-  double mcum;  // cell scale accumulated since the last list build
   float alpha;  // CSVR momentum scale of the coming step
   float mu;     // barostat scale of this step
+  float red_f[12 * 32];  // per-warp partials of block_sums
+  double red_d[12];
 };
 
 
@@ -350,7 +355,6 @@ __device__ __noinline__ bool rebuild(Smem &sm, const SysParams &p, int n, int tp
   }
   __syncthreads();
   prof_add(prof, 7, tp);
-  prof_add(prof, 8, tp);
   // 3. Verlet list, row-major: a warp takes one x-row of cells and walks its
   //    (cell-sorted, hence contiguous) atoms 32 at a time, one lane per atom;
   //    the candidates of a chunk are the contiguous atom and ghost ranges of
@@ -586,37 +590,103 @@ static_assert(sizeof(Smem) <= 227 * 1024, "fused MD shared memory above the per-
 constexpr uint64_t kSysSeed = 0x6a09e667f3bcc909ull;
 constexpr uint64_t kChiSeed = 0xbb67ae8584caa73bull;
 
-// CSVR scale of the coming step (CSVRStep, integrators.py:519-596), all threads
-// call it: R2 ~ chi^2(N_dof - 1) is the sum of N_dof - 1 squared standard
-// normals, drawn in groups of four across the block; thread 0 draws R1 and forms
-// alpha^2 = c1 + c2 (R1^2 + R2) + 2 R1 sqrt(c1 c2), c1 = exp(-dt / tau_T),
-// c2 = (1 - c1) K_target / (K N_dof), in float64.  A system with no thermal
-// degrees of freedom or no kinetic energy keeps alpha = 1 (the reference's
-// formula divides by zero there).
-__device__ void csvr_alpha(Smem &sm, double ke, uint64_t seed, int sys, uint64_t counter) {
-  const SysParams &p = sm.p;
-  const int cnt = p.dof - 1;
-  float acc = 0.f;
-  for (int g = threadIdx.x; 4 * g < cnt; g += blockDim.x) {
-    float z[4];
-    normal4(seed ^ kChiSeed, ((uint64_t)sys << 20) | (uint64_t)g, counter, z);
+// Block-wide sums of N floats, returned to every thread in float64: each warp
+// adds in float, then warp 0 adds the warp partials in float64 (FP64 issue is
+// scarce on this part, so only 32 x N double additions are made).  Contains
+// two __syncthreads().
+template <int N>
+__device__ inline void block_sums(const float (&v)[N], Smem &sm, double (&out)[N]) {
+  static_assert(N <= 12, "block_sums scratch holds 12 values");
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (4 * g + k < cnt) acc = fmaf(z[k], z[k], acc);
+  for (int k = 0; k < N; ++k) {
+    float x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sm.red_f[k * 32 + wid] = x;
   }
-  const double r2 = block_sum((double)acc, sm.red);
-  if (threadIdx.x == 0) {
-    float z[4];
-    normal4(seed ^ kSysSeed, (uint64_t)sys, counter, z);
-    double alpha = 1.0;
-    if (p.dof > 0 && ke > 0.0) {
-      const double r1 = z[0];
-      const double c1 = p.csvr_c1;
-      const double c2 = (1.0 - c1) * (0.5 * p.dof * p.kTd) / (ke * p.dof);
-      const double a2 = c1 + c2 * (r1 * r1 + (cnt > 0 ? r2 : 0.0)) + 2.0 * r1 * sqrt(c1 * c2);
-      alpha = sqrt(fmax(a2, 0.0));
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const double x = warp_sum(lane < nw ? (double)sm.red_f[k * 32 + lane] : 0.0);
+      if (lane == 0) sm.red_d[k] = x;
     }
-    sm.alpha = (float)alpha;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) out[k] = sm.red_d[k];
+}
+
+// One standard normal (Box-Muller on two words) and one uniform in (0, 1] from
+// one Philox block.
+__device__ inline void normal_uniform(uint64_t seed, uint64_t stream, uint64_t counter, float &z, float &u) {
+  U4 c{(uint32_t)counter, (uint32_t)(counter >> 32), (uint32_t)stream, (uint32_t)(stream >> 32)};
+  const U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  z = sqrtf(-2.0f * logf(u01_open0(r.x))) * cospif(2.0f * u01_open0(r.y));
+  u = u01_open0(r.z);
+}
+
+// Gamma(a, 1) for a >= 1 by Marsaglia and Tsang's squeeze-and-reject method
+// ("A simple method for generating gamma variables", ACM TOMS 26, 2000):
+// d = a - 1/3, c = 1 / sqrt(9 d); for x ~ N(0, 1), y = c x > -1, v = (1 + y)^3
+// and u ~ U(0, 1), accept d v when u < 1 - 0.0331 x^4 or
+// ln u < x^2 / 2 + d (1 - v + ln v).  With d c^2 = 1/9 the right-hand side is
+// 3 d (ln(1 + y) - y + y^2 / 2 - y^3 / 3) = 3 d sum_{k >= 4} (-1)^(k+1) y^k / k,
+// summed as a series for |y| <= 1/4 (no cancellation in float32) and directly
+// above.  Each trial takes its own Philox block (stream | trial); acceptance is
+// above 95 % per trial, and after 64 rejected trials (probability below 1e-80)
+// the mean a is returned.  One thread, float32 (FP64 is scarce on this part).
+__device__ float gamma_mt(float a, uint64_t seed, uint64_t stream, uint64_t counter) {
+  const float d = a - (1.0f / 3.0f), c = rsqrtf(9.0f * d);
+  for (int t = 0; t < 64; ++t) {
+    float x, u;
+    normal_uniform(seed, (stream << 6) | (uint64_t)t, counter, x, u);
+    const float y = c * x;
+    if (y <= -1.0f) continue;
+    const float v = (1.0f + y) * (1.0f + y) * (1.0f + y);
+    const float x2 = x * x;
+    if (u < 1.0f - 0.0331f * x2 * x2) return d * v;
+    float h;
+    if (fabsf(y) <= 0.25f) {
+      // sum_{k=4}^{19} (-1)^(k+1) y^k / k, Horner in y from the top term
+      float acc = 0.0f;
+#pragma unroll
+      for (int k = 19; k >= 4; --k) acc = fmaf(acc, y, ((k & 1) ? 1.0f : -1.0f) / (float)k);
+      const float y2 = y * y;
+      h = acc * (y2 * y2);
+    } else {
+      h = log1pf(y) - y + 0.5f * y * y - y * y * y * (1.0f / 3.0f);
+    }
+    if (logf(u) < 3.0f * d * h) return d * v;
+  }
+  return a;
+}
+
+// CSVR scale of the coming step (CSVRStep, integrators.py:519-596); all threads
+// call it, thread 0 works: R1 ~ N(0, 1), R2 ~ chi^2(N_dof - 1) = 2 Gamma((N_dof - 1) / 2)
+// and alpha^2 = c1 + c2 (R1^2 + R2) + 2 R1 sqrt(c1 c2), c1 = exp(-dt / tau_T),
+// c2 = (1 - c1) K_target / (K N_dof), in float64.  N_dof = 3 N - 3, so
+// N_dof - 1 >= 2 whenever N >= 2; a single atom (no thermal degrees of freedom)
+// or a system at rest keeps alpha = 1 (the reference's formula divides by zero
+// there).
+__device__ void csvr_alpha(Smem &sm, double ke, uint64_t seed, int sys, uint64_t counter) {
+  if (threadIdx.x == 0) {
+    const SysParams &p = sm.p;
+    float alpha = 1.0f;
+    if (p.dof > 0 && ke > 0.0) {
+      float z[4];
+      normal4(seed ^ kSysSeed, (uint64_t)sys, counter, z);
+      const float r1 = z[0];
+      const float r2 = 2.0f * gamma_mt(0.5f * (float)(p.dof - 1), seed ^ kChiSeed, (uint64_t)sys, counter);
+      const float c1 = p.csvr_c1;
+      // c2 = (1 - c1) K_target / (K N_dof) with K_target = N_dof kT / 2
+      const float c2 = p.csvr_omc1 * (0.5f * p.kTf) / (float)ke;
+      const float a2 = c1 + c2 * (r1 * r1 + r2) + 2.0f * r1 * sqrtf(c1 * c2);
+      alpha = sqrtf(fmaxf(a2, 0.0f));
+    }
+    sm.alpha = alpha;
   }
   __syncthreads();
 }
@@ -675,18 +745,20 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
       p.c1 = expf(-a.friction[s] * p.dt);
       p.c2 = sqrtf(a.kT[s] * (1.0f - p.c1 * p.c1));
       if (INTEGRATOR >= 2) {
-        p.dtd = (double)p.dt;
-        p.kTd = (double)a.kT[s];
-        p.csvr_c1 = exp(-p.dtd / a.thermostat_tau[s]);
+        const double x = -(double)p.dt / a.thermostat_tau[s];
+        p.csvr_c1 = (float)exp(x);
+        p.csvr_omc1 = (float)-expm1(x);
+        p.kTf = a.kT[s];
         p.dof = 3 * n - 3;
       }
       if (INTEGRATOR == 3) {
-        p.taup = a.barostat_tau[s];
-        p.beta = a.compressibility[s];
-        p.p0 = a.target_pressure[s];
+        const double ratio = (double)p.dt / a.barostat_tau[s] * a.compressibility[s];
+        p.scr_a = (float)ratio;
+        p.scr_b = (float)(2.0 * (double)a.kT[s] * ratio);
+        p.p0f = (float)a.target_pressure[s];
         p.mumin = a.min_scale[s];
+        p.mumax = 1.0 / a.min_scale[s];
       }
-      sm.mcum = 1.0;
     }
     __syncthreads();
     if (p.K[0] > 2 || p.K[1] > 2 || p.K[2] > 2) {
@@ -739,7 +811,10 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         const float4 m = sm.mom[i];
         ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
       }
-      csvr_alpha(sm, block_sum((double)ke, sm.red + 36), a.seed, s, a.step0);
+      const float kv[1] = {ke};
+      double kt[1];
+      block_sums<1>(kv, sm, kt);
+      csvr_alpha(sm, kt[0], a.seed, s, a.step0);
     }
     for (int step = 0; step < a.n_steps && ok; ++step) {
       const bool last = step == a.n_steps - 1;
@@ -837,22 +912,35 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
         sm.mom[i] = m;
         if (need_ke) ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
       }
-      const double ke_tot = need_ke ? block_sum((double)ke, sm.red + 36) : 0.0;
+      double ke_tot = 0.0;
+      double w6[6];
+      if (INTEGRATOR == 3) {
+        const float v[7] = {ke, wv[0], wv[1], wv[2], wv[3], wv[4], wv[5]};
+        double r[7];
+        block_sums<7>(v, sm, r);
+        ke_tot = r[0];
+        for (int k = 0; k < 6; ++k) w6[k] = r[k + 1];
+      } else if (need_ke) {
+        const float v[1] = {ke};
+        double r[1];
+        block_sums<1>(v, sm, r);
+        ke_tot = r[0];
+      }
+      prof_add(prof, 4, t0);
       if (INTEGRATOR == 3) {
         // ---- stochastic cell rescaling (integrators.py:710-789): pressure from the
         // kinetic energy and the pair virial, P = (2 K - Tr W) / 3V, then
         // d eps = dt / tau_P beta (P - P0) + sqrt(2 kT beta dt / (tau_P V)) R and
         // mu = exp(d eps / 3) clipped to [mu_min, 1 / mu_min] scale cell and positions
-        double w6[6];
-        for (int k = 0; k < 6; ++k) w6[k] = block_sum((double)wv[k], sm.red);
         if (tid == 0) {
-          const double vol = fabs(p.Ld[0] * p.Ld[2] * p.Ld[5]);
-          const double prs = (2.0 * ke_tot - (w6[0] + w6[2] + w6[5])) / (3.0 * vol);
+          // float32 on the one thread (FP64 is scarce); mu = 1 + expm1(d eps / 3)
+          // keeps mu - 1 to float32 relative precision, the cell stays float64
+          const float vol = fabsf(p.L[0] * p.L[2] * p.L[5]);
+          const float prs = (float)(2.0 * ke_tot - (w6[0] + w6[2] + w6[5])) / (3.0f * vol);
           float z[4];
           normal4(a.seed ^ kSysSeed, (uint64_t)s, a.step0 + (uint64_t)step, z);
-          const double deps = p.dtd / p.taup * p.beta * (prs - p.p0) +
-                              sqrt(2.0 * p.kTd * p.beta * p.dtd / (p.taup * vol)) * (double)z[1];
-          const double mu = fmin(fmax(exp(deps / 3.0), p.mumin), 1.0 / p.mumin);
+          const float deps = p.scr_a * (prs - p.p0f) + sqrtf(p.scr_b / vol) * z[1];
+          const double mu = fmin(fmax(1.0 + (double)expm1f(deps * (1.0f / 3.0f)), p.mumin), p.mumax);
           for (int k = 0; k < 6; ++k) {
             p.Ld[k] *= mu;
             p.L[k] = (float)p.Ld[k];
@@ -862,6 +950,7 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
           sm.work = 0;
         }
         __syncthreads();
+        prof_add(prof, 8, t0);
         if (p.K[0] > 2 || p.K[1] > 2 || p.K[2] > 2) {
           if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
           ok = false;
@@ -894,6 +983,7 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
           update_ghosts(sm, n);
           __syncthreads();
         }
+        prof_add(prof, 2, t0);
         // ---- forces at the rescaled positions (the next step's first kick)
         pe = 0.0;
         if (last && a.virial != nullptr) {
@@ -906,6 +996,7 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
           forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
         }
         __syncthreads();
+        prof_add(prof, 3, t0);
       }
       if (want_e) {
         const double pe_tot = block_sum(pe, sm.red);
@@ -918,8 +1009,11 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
           }
         }
       }
-      if (INTEGRATOR >= 2 && !last) csvr_alpha(sm, ke_tot, a.seed, s, a.step0 + (uint64_t)step + 1);
       prof_add(prof, 4, t0);
+      if (INTEGRATOR >= 2 && !last) {
+        csvr_alpha(sm, ke_tot, a.seed, s, a.step0 + (uint64_t)step + 1);
+        prof_add(prof, 8, t0);
+      }
     }
     if (!ok) continue;
     if (a.n_steps == 0) {
@@ -958,22 +1052,16 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
     if (a.virial != nullptr) {
       // X_ab = sum_c (L^-1)_{ca} W_cb ; W symmetric from wv = [xx, yx, yy, zx, zy, zz]
       double W[3][3];
-      double acc[6];
-      for (int k = 0; k < 6; ++k) {
-        acc[k] = block_sum((double)wv[k], sm.red);
-        __syncthreads();
-      }
+      const float v[12] = {wv[0], wv[1], wv[2], wv[3], wv[4], wv[5], fw[0], fw[1], fw[2], fw[3], fw[4], fw[5]};
+      double r[12];
+      block_sums<12>(v, sm, r);
+      const double *acc = r, *fwt = r + 6;
       W[0][0] = acc[0];
       W[1][0] = W[0][1] = acc[1];
       W[1][1] = acc[2];
       W[2][0] = W[0][2] = acc[3];
       W[2][1] = W[1][2] = acc[4];
       W[2][2] = acc[5];
-      double fwt[6];
-      for (int k = 0; k < 6; ++k) {
-        fwt[k] = block_sum((double)fw[k], sm.red + 36);
-        __syncthreads();
-      }
       const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
       double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
       Li[1][0] = -(B * Li[0][0]) / C;
