@@ -391,6 +391,10 @@ typedef struct kups_gcmc_args {
                                    (blocks start on multiples of 32) the fractional centre and
                                    per-axis half extents; used when every cell width is at
                                    least twice the cutoffs, to skip groups beyond the cutoff */
+  double *obs_sums;             /* [S, 5] in/out or NULL: after every step adds U, N, U N, N^2
+                                   and U^2 (U = energy[s], N = n_mol[s]): the block sums behind
+                                   the reference's per-step energy / loading / heat-of-adsorption
+                                   analysis (application/mcmc/analysis.py:82-158) */
   float move_cum[3];
   float pad0;
   double coulomb_k;

@@ -66,7 +66,7 @@ class GcmcArgs(C.Structure):
         ("width_max", C.c_void_p), ("history", C.c_void_p), ("history_index", C.c_void_p),
         ("attempted", C.c_void_p), ("accepted", C.c_void_p), ("proposals", C.c_void_p), ("out_delta", C.c_void_p),
         ("proposal_node", C.c_void_p), ("proposal_cdf", C.c_void_p), ("workspace", C.c_void_p),
-        ("fw_group", C.c_void_p),
+        ("fw_group", C.c_void_p), ("obs_sums", C.c_void_p),
         ("move_cum", C.c_float * 3), ("pad0", C.c_float), ("coulomb_k", C.c_double), ("seed", C.c_uint64),
         ("step0", C.c_uint64), ("n_systems", C.c_int32), ("max_mol", C.c_int32), ("atoms_per_mol", C.c_int32),
         ("n_species", C.c_int32), ("n_kvecs", C.c_int32), ("n_steps", C.c_int32), ("history_len", C.c_int32),

@@ -340,6 +340,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
     }
   }
   const bool learned = a.proposal_node != nullptr;
+  double ob[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // thread 0: this launch's U, N, U N, N^2, U^2 sums
   for (int step = 0; step < a.n_steps; ++step) {
     const uint64_t ctr = a.step0 + (uint64_t)step;
     // ---------------------------------------------------------------- proposal (thread 0)
@@ -740,9 +741,19 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
         if (ub > 0.f) nv = fminf(nv, ub);
         if (fabsf(avg - target) > tol) a.width[s * 4 + sched] = nv;
       }
+      if (a.obs_sums != nullptr) {
+        const double u = a.energy[s], nm = (double)a.n_mol[s];
+        ob[0] += u;
+        ob[1] += nm;
+        ob[2] += __dmul_rn(u, nm);  // rounded products, as the reference's float64 series hold them
+        ob[3] += __dmul_rn(nm, nm);
+        ob[4] += __dmul_rn(u, u);
+      }
     }
     __syncthreads();
   }
+  if (tid == 0 && a.obs_sums != nullptr)
+    for (int k = 0; k < 5; ++k) a.obs_sums[5 * (int64_t)s + k] += ob[k];
 }
 
 }  // namespace

@@ -212,6 +212,8 @@ class GCMC:
         self.fw_count = i32(setup.fw_count)
         self.guest = torch.zeros((s, setup.max_mol, apm, 4), dtype=torch.float32, device=dev)
         self.n_mol = torch.zeros(s, dtype=torch.int32, device=dev)
+        # per-step U, N, U N, N^2, U^2 sums the kernel adds to (kups_gcmc_args.obs_sums)
+        self.obs = torch.zeros((s, 5), dtype=torch.float64, device=dev)
         self.motif = f32(np.concatenate([setup.motif_positions, sp_bits(setup.motif_species)[:, None]], 1))
         self.motif_q = f32(setup.motif_charges)
         msc = np.bincount(setup.motif_species, minlength=T).astype(float)
@@ -301,6 +303,7 @@ class GCMC:
         a.out_delta = out_delta.data_ptr() if out_delta is not None else None
         a.workspace = self.ws.data_ptr()
         a.fw_group = self.fw_group.data_ptr() if self.fw_group is not None else None
+        a.obs_sums = self.obs.data_ptr()
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid
@@ -412,6 +415,25 @@ class GCMC:
         O = torch.as_tensor(np.array(off, np.int32), device="cuda")
         _, _, _, sk, _ = ewald_recip(P, Q, O, int(np.diff(off).max()), self.tril, self.kn, self.alpha, grad_tril=False)
         self.sk.copy_(sk)
+
+    def run_blocks(self, n_blocks: int, block_steps: int) -> np.ndarray:
+        """n_blocks launches of block_steps steps; returns the per-block sums of U, N, U N, N^2
+        and U^2 of every system, [n_blocks, S, 5] float64, read back once at the end (the
+        sums behind analyze_mcmc's per-step series, application/mcmc/analysis.py:82-158)."""
+        out = torch.empty((n_blocks,) + tuple(self.obs.shape), dtype=torch.float64, device=self.obs.device)
+        for b in range(n_blocks):
+            self.obs.zero_()
+            self.launch(block_steps)
+            out[b].copy_(self.obs)
+        self.check()
+        return out.cpu().numpy()
+
+    def analyze(self, block_sums, block_steps: int, n_blocks: int | None = None) -> dict:
+        """Energy, loading and heat of adsorption (mean, SEM over blocks) per system from
+        run_blocks' sums (analysis.gcmc_block_analysis)."""
+        from .analysis import gcmc_block_analysis
+
+        return gcmc_block_analysis(block_sums, block_steps, self.setup.temperature, n_blocks)
 
     def statistics(self):
         att = self.attempted.cpu().numpy()

@@ -25,6 +25,9 @@ import torch
 
 from . import _lib
 from .neighborlist import _stream, new_status, read_status
+from .units import BOLTZMANN_CONSTANT, KILO_JOULE, MOL
+
+EV_TO_KJ_PER_MOL = MOL / KILO_JOULE
 
 
 def gemm(a: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None, bias=None, act: int = 0,
@@ -202,26 +205,24 @@ class LearnedInsertionProposal:
 
 
 def _timed_run(mc, steps, block):
-    """Runs ``steps`` MC steps in blocks; returns device ms, accepted/attempted per move kind
-    and the per-block mean loading [blocks, S] (loading sampled every 100 steps)."""
+    """Runs ``steps`` MC steps in launches of ``block`` steps; returns device ms (the whole
+    sequence), accepted/attempted per move kind and the kernel's per-block sums of U, N, U N,
+    N^2, U^2 of every system [blocks, S, 5] (every step counted, one read-back at the end)."""
     att0, acc0 = mc.attempted.clone(), mc.accepted.clone()
-    loads, ms = [], 0.0
-    sample = min(100, block)
-    for _ in range(steps // block):
-        acc_load = torch.zeros_like(mc.n_mol, dtype=torch.float64)
-        for _ in range(block // sample):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            mc.launch(sample)
-            e1.record()
-            torch.cuda.synchronize()
-            ms += e0.elapsed_time(e1)
-            acc_load += mc.n_mol.to(torch.float64)
-        loads.append((acc_load / (block // sample)).cpu().numpy())
+    nb = steps // block
+    sums = torch.empty((nb,) + tuple(mc.obs.shape), dtype=torch.float64, device=mc.obs.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for b in range(nb):
+        mc.obs.zero_()
+        mc.launch(block)
+        sums[b].copy_(mc.obs)
+    e1.record()
+    torch.cuda.synchronize()
     mc.check()
     att = (mc.attempted - att0).sum(0).cpu().numpy()
     acc = (mc.accepted - acc0).sum(0).cpu().numpy()
-    return ms, att, acc, np.array(loads)
+    return e0.elapsed_time(e1), att, acc, sums.cpu().numpy()
 
 
 def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, train_steps=3000, batch=16384,
@@ -260,8 +261,18 @@ def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, 
     for tag, proposal in (("plain", None), ("learned", net)):
         run = mc.clone(seed=seed + 3)
         run.use_proposal(proposal)
-        ms, att, acc, loads = _timed_run(run, prod_steps, block)
+        ms, att, acc, sums = _timed_run(run, prod_steps, block)
+        m = sums / block  # block means of U, N, U N, N^2, U^2 per system
+        loads = m[..., 1]
         g = loads.reshape(len(loads), groups, S // groups).mean(2)  # [blocks, groups]
+        # heat of adsorption per block and pressure group, cov(U, N) / var(N) - kT with the
+        # within-block covariances pooled over the group's replicas (a single replica's N can
+        # stay constant for a whole block in the condensed channel)
+        cov = (m[..., 2] - m[..., 0] * m[..., 1]).reshape(len(m), groups, S // groups).mean(2)
+        var = (m[..., 3] - m[..., 1] ** 2).reshape(len(m), groups, S // groups).mean(2)
+        kt = np.asarray(setup.temperature, np.float64).reshape(groups, S // groups).mean(1) * BOLTZMANN_CONSTANT
+        with np.errstate(invalid="ignore", divide="ignore"):
+            qg = (cov / var - kt[None, :]) * EV_TO_KJ_PER_MOL
         out[tag] = {
             "ms_per_step": ms / prod_steps,
             "accepted_insertions_per_s": float(acc[3] / ms * 1e3),
@@ -273,6 +284,8 @@ def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, 
             "loading_se": (g.std(0, ddof=1) / np.sqrt(len(g))).tolist(),
             "loading_all": float(loads.mean()),
             "loading_all_se": float(loads.mean(1).std(ddof=1) / np.sqrt(len(loads))),
+            "heat_of_adsorption_kj_mol": qg.mean(0).tolist(),
+            "heat_of_adsorption_se": (qg.std(0, ddof=1) / np.sqrt(len(qg))).tolist(),
         }
     lp, ll = np.array(out["plain"]["loading"]), np.array(out["learned"]["loading"])
     sp, sl = np.array(out["plain"]["loading_se"]), np.array(out["learned"]["loading_se"])

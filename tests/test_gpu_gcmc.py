@@ -353,3 +353,41 @@ def test_host_group_skipping_changes_nothing(kind):
         outs.append(mc.evaluate([gcmc.MOVES.index(kind)] * 4, mols, news))
     np.testing.assert_array_equal(outs[0], outs[1])
     assert np.all(np.isfinite(outs[0]))
+
+
+# ----------------------------------------------------------------------------- device observables
+def test_device_block_sums_equal_the_per_step_series():
+    """kups_gcmc_run's per-step U, N, U N, N^2, U^2 sums equal, bit for bit, the sums of the
+    per-step series read after one-step launches of an identical sampler (same seed: the step
+    counter keys the random numbers, so launch length does not change the trajectory); the
+    block analysis equals the oracle's analysis of that series (application/mcmc/analysis.py)."""
+    from kups_gb300 import gcmc
+    from oracle import analysis as oan
+
+    setup = small_setup(n_sys=4, seed=2)
+    setup.log_activity = np.full(4, -6.0)
+    a, b = gcmc.GCMC(setup, seed=5), gcmc.GCMC(setup, seed=5)
+    block, nb = 20, 6
+    u_series, n_series = [], []
+    for _ in range(block * nb):
+        a.launch(1)
+        u_series.append(a.energy.cpu().numpy().copy())
+        n_series.append(a.n_mol.cpu().numpy().astype(float))
+    a.check()
+    sums = b.run_blocks(nb, block)
+    u, n = np.array(u_series), np.array(n_series)
+    assert n.max() > 0 and np.ptp(n) > 0
+    for k in range(nb):
+        exp = np.zeros((4, 5))
+        for t in range(k * block, (k + 1) * block):
+            for s in range(4):
+                exp[s] += [u[t, s], n[t, s], u[t, s] * n[t, s], n[t, s] * n[t, s], u[t, s] * u[t, s]]
+        np.testing.assert_array_equal(sums[k], exp)
+    res = b.analyze(sums, block, n_blocks=3)
+    for s in range(4):
+        ref = oan.analyze_single_system(u[:, s], n[:, s], setup.temperature[s], 3)
+        np.testing.assert_allclose(res["energy"].mean[s], ref["energy"][0], rtol=1e-12)
+        np.testing.assert_allclose(res["loading"].mean[s], ref["loading"][0][0], rtol=1e-12)
+        if np.isfinite(ref["heat_of_adsorption"][0][0]):
+            np.testing.assert_allclose(res["heat_of_adsorption"].mean[s], ref["heat_of_adsorption"][0][0],
+                                       rtol=1e-9)
