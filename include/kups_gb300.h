@@ -302,6 +302,35 @@ int32_t kups_pair_edges(const double *positions, const int32_t *system, const in
                         void *stream);
 
 /* ------------------------------------------------------------------------
+ * Bonded edge-set potentials — replace the energies of
+ * src/kups/potential/classical/harmonic.py:83-163, morse.py:142-171,
+ * cosine_angle.py:152-221, dihedral.py:214-273 and inversion.py:136-209 on the
+ * HyperGraph of an EdgeSetGraphConstructor (potential/common/graph.py:289-361),
+ * with the jax.vjp gradient of PotentialFromEnergy (common/energy.py:264-355).
+ *   kind  order  params per species tuple (row-major table [T^order, params])
+ *   0     2      harmonic bond   x0, k:             k (r - x0)^2
+ *   1     2      Morse bond      r0, D, alpha:      D (1 - exp(-alpha (r - r0)))^2
+ *   2     3      harmonic angle  theta0 [deg], k:   k (theta - theta0)^2, theta at atom 0
+ *   3     3      cosine angle    theta0 [rad], K, linear_tol (UFF cosine form)
+ *   4     4      dihedral        V, n, phi0:        V/2 (1 - cos(n phi0) cos(n phi))
+ *   5     4      inversion       omega0, k          (UFF, atom 0 the centre)
+ *   edges  i32 [n_edges, order]; shifts i32 [n_edges, order - 1, 3]: integer image
+ *          shifts of atoms 1.. relative to atom 0 (Edges.shifts)
+ *   energy f64 [n_systems], grad f64 [n_particles, 3], grad_tril f64 [n_systems, 6]
+ *          (may be NULL): ADDED to (zero them first), so several terms can share
+ *          one buffer; an edge belongs to the system of its atom 0.
+ * Float64 arithmetic; an edge with an index or species out of range records
+ * KUPS_ERR_INVALID (first offending edge) and is skipped. */
+int32_t kups_bonded_order(int32_t kind);
+int32_t kups_bonded_param_count(int32_t kind);
+int32_t kups_bonded_edges(int32_t kind, const double *positions, const int32_t *system,
+                          const int32_t *species, int64_t n_particles, const double *tril,
+                          int32_t n_systems, const int32_t *edges, const int32_t *shifts,
+                          int64_t n_edges, const double *params, int32_t n_species,
+                          double *energy, double *grad, double *grad_tril, kups_status *status,
+                          void *stream);
+
+/* ------------------------------------------------------------------------
  * Integrator building blocks on the float64 particle table (systems larger
  * than kups_lj_md_max_atoms, Ewald MD): MomentumStep (p -= dE/dx * dt * scale),
  * PositionStep + MinimumImageConventionFlow (r += p/m * dt * scale, wrapped

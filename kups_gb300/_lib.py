@@ -113,6 +113,9 @@ SIGNATURES = {
     "kups_lj_tail_correction": (_I32, [_P, _P, _I32, _P, _P, _P, _P, _I32, _P, _P, _P, _P, _P]),
     "kups_gemm_bf16": (_I32, [_P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64, _I64, _P, _I32, _I64,
                                _I64, _P, _P, _I32, _I64, _I64, _I32, _I32, _I32, C.c_float, C.c_float, _I32, _I32, _P, _P]),
+    "kups_bonded_order": (_I32, [_I32]),
+    "kups_bonded_param_count": (_I32, [_I32]),
+    "kups_bonded_edges": (_I32, [_I32, _P, _P, _P, _I64, _P, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P, _P, _P]),
     "kups_pair_edges": (_I32, [_P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
 }
 

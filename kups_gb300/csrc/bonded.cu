@@ -1,0 +1,312 @@
+// Bonded edge-set potentials: energy, dE/dx and dE/dtril over an edge list of
+// order D (bonds 2, angles 3, dihedrals and inversions 4).
+//
+// Replaces the energies of src/kups/potential/classical/ harmonic.py:83-163
+// (harmonic bond, harmonic angle), morse.py:142-171, cosine_angle.py:152-221,
+// dihedral.py:214-273 and inversion.py:136-209 evaluated on the HyperGraph of an
+// EdgeSetGraphConstructor (src/kups/potential/common/graph.py:289-361), with the
+// gradient PotentialFromEnergy takes by jax.vjp with respect to
+// PositionAndUnitCell (src/kups/potential/common/energy.py:264-355).
+//
+// One thread per edge (i_0, ..., i_{D-1}) with integer image shifts s_m:
+//   v_m = x_{i_m} - x_{i_0} + s_m @ L  (Edges.difference_vectors,
+//   src/kups/core/neighborlist.py:164-204), E_e(v_1 .. v_{D-1}) with the
+//   parameter row of the edge's species tuple, g_m = dE_e/dv_m analytic, then
+//   dE/dx_{i_m} += g_m, dE/dx_{i_0} -= sum_m g_m, dE/dL_ab += sum_m s_ma g_mb,
+//   E_s += E_e for the system of i_0.  Float64 throughout (the edge counts of
+//   bonded terms are small next to pair lists); per-system sums are warp-
+//   aggregated atomics, per-atom gradients float64 atomics.
+// Angle derivatives: d cos t / dv1 = v2 / (r1 r2) - cos t v1 / r1^2 (and 1 <-> 2).
+// Dihedral: phi = atan2(|b2| b1 . (b2 x b3), (b1 x b2) . (b2 x b3)) with
+// b1 = x_j - x_i, b2 = x_k - x_j, b3 = x_l - x_k, m = b1 x b2, n = b2 x b3; its
+// position derivatives are the closed forms of Blondel and Karplus (J. Comput.
+// Chem. 17, 1132, 1996): dphi/dx_i = -|b2| m / |m|^2, dphi/dx_l = |b2| n / |n|^2,
+// dphi/dx_j = -(1 + p) dphi/dx_i + q dphi/dx_l, dphi/dx_k = p dphi/dx_i - (1 + q) dphi/dx_l,
+// p = b1.b2 / |b2|^2, q = b3.b2 / |b2|^2.  Inversion: derivatives of
+// sin w = (v1 . n / (|n| + eps)) / (|v1| + eps), n = v2 x v3, with the
+// reference's 1e-10 regularisers kept.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace kups {
+namespace {
+
+constexpr double kEps = 1e-10;
+
+__device__ inline void cross3(const double a[3], const double b[3], double c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ inline double dot3(const double a[3], const double b[3]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+template <int KIND>
+struct Kind;
+template <>
+struct Kind<0> { static constexpr int order = 2, params = 2; };  // harmonic bond: x0, k
+template <>
+struct Kind<1> { static constexpr int order = 2, params = 3; };  // Morse: r0, D, alpha
+template <>
+struct Kind<2> { static constexpr int order = 3, params = 2; };  // harmonic angle: theta0 (deg), k
+template <>
+struct Kind<3> { static constexpr int order = 3, params = 3; };  // cosine angle: theta0 (rad), k, linear_tol
+template <>
+struct Kind<4> { static constexpr int order = 4, params = 3; };  // dihedral: V, n, phi0
+template <>
+struct Kind<5> { static constexpr int order = 4, params = 2; };  // inversion: omega0, k
+
+// Energy of one edge and g[m] = dE/dv_{m+1}.
+template <int KIND>
+__device__ double edge_energy_grad(const double (*v)[3], const double *p, double (*g)[3]) {
+  if (KIND == 0 || KIND == 1) {
+    const double r = sqrt(dot3(v[0], v[0]));
+    double e, dedr;
+    if (KIND == 0) {
+      e = (r - p[0]) * (r - p[0]) * p[1];
+      dedr = 2.0 * p[1] * (r - p[0]);
+    } else {
+      const double x = exp(-p[2] * (r - p[0]));
+      e = p[1] * (1.0 - x) * (1.0 - x);
+      dedr = 2.0 * p[1] * (1.0 - x) * p[2] * x;
+    }
+    const double f = r > 0.0 ? dedr / r : 0.0;
+    for (int a = 0; a < 3; ++a) g[0][a] = f * v[0][a];
+    return e;
+  } else if (KIND == 2 || KIND == 3) {
+    const double r1 = sqrt(dot3(v[0], v[0])), r2 = sqrt(dot3(v[1], v[1]));
+    const double c = dot3(v[0], v[1]) / (r1 * r2);
+    double e, dedc;
+    if (KIND == 2) {
+      // the reference takes arccos of the unclipped cosine; clamping keeps
+      // round-off above 1 from turning a straight angle into NaN
+      const double cc = fmin(fmax(c, -1.0), 1.0);
+      const double th = acos(cc) * (180.0 / M_PI);
+      e = (th - p[0]) * (th - p[0]) * p[1];
+      dedc = -2.0 * p[1] * (th - p[0]) * (180.0 / M_PI) / sqrt(fmax(1.0 - cc * cc, 1e-30));
+    } else {
+      const double cc = fmin(fmax(c, -1.0), 1.0);
+      const double th0 = p[0], k = p[1];
+      if (fabs(th0 - M_PI) < p[2]) {
+        e = k * (1.0 + cc);
+        dedc = k;
+      } else {
+        const double s2 = sin(th0) * sin(th0), ct0 = cos(th0);
+        const double c2 = 1.0 / (4.0 * fmax(s2, 1e-10));
+        const double c1 = -4.0 * c2 * ct0, c0 = c2 * (2.0 * ct0 * ct0 + 1.0);
+        e = k * (c0 + c1 * cc + c2 * (2.0 * cc * cc - 1.0));
+        dedc = k * (c1 + 4.0 * c2 * cc);
+      }
+      if (fabs(c) > 1.0) dedc = 0.0;  // clipped: no gradient
+    }
+    const double i12 = 1.0 / (r1 * r2);
+    for (int a = 0; a < 3; ++a) {
+      g[0][a] = dedc * (v[1][a] * i12 - c * v[0][a] / (r1 * r1));
+      g[1][a] = dedc * (v[0][a] * i12 - c * v[1][a] / (r2 * r2));
+    }
+    return e;
+  } else if (KIND == 4) {
+    double b1[3], b2[3], b3[3];
+    for (int a = 0; a < 3; ++a) {
+      b1[a] = v[0][a];
+      b2[a] = v[1][a] - v[0][a];
+      b3[a] = v[2][a] - v[1][a];
+    }
+    double m[3], n[3];
+    cross3(b1, b2, m);
+    cross3(b2, b3, n);
+    const double mm = dot3(m, m), nn = dot3(n, n), lb = sqrt(dot3(b2, b2));
+    const double lm = sqrt(mm), ln = sqrt(nn);
+    double n1[3], n2[3], bn[3], x[3];
+    for (int a = 0; a < 3; ++a) {
+      n1[a] = m[a] / (lm + kEps);
+      n2[a] = n[a] / (ln + kEps);
+      bn[a] = b2[a] / (lb + kEps);
+    }
+    cross3(n1, n2, x);
+    const double phi = atan2(dot3(x, bn), dot3(n1, n2));
+    const double V = p[0], per = p[1], phi0 = p[2];
+    const double e = 0.5 * V * (1.0 - cos(per * phi0) * cos(per * phi));
+    const double dedphi = 0.5 * V * cos(per * phi0) * per * sin(per * phi);
+    if (mm > 0.0 && nn > 0.0 && lb > 0.0) {
+      const double pp = dot3(b1, b2) / (lb * lb), qq = dot3(b3, b2) / (lb * lb);
+      for (int a = 0; a < 3; ++a) {
+        const double di = -lb / mm * m[a], dl = lb / nn * n[a];
+        g[0][a] = dedphi * (-(1.0 + pp) * di + qq * dl);
+        g[1][a] = dedphi * (pp * di - (1.0 + qq) * dl);
+        g[2][a] = dedphi * dl;
+      }
+    } else {
+      for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 3; ++a) g[k][a] = 0.0;
+    }
+    return e;
+  } else {
+    double n[3];
+    cross3(v[1], v[2], n);
+    const double ln = sqrt(dot3(n, n)), la = sqrt(dot3(v[0], v[0]));
+    const double an = dot3(v[0], n);
+    const double s_raw = an / (ln + kEps) / (la + kEps);
+    const double s = fmin(fmax(s_raw, -1.0), 1.0);
+    const double w = asin(s);
+    const double om0 = p[0], k = p[1];
+    const bool sp2 = fabs(om0) < 1e-6;
+    const double s2 = sin(om0) * sin(om0), cw0 = cos(om0);
+    const double c2 = sp2 ? 0.0 : 1.0 / (4.0 * (s2 > 1e-10 ? s2 : 1.0));
+    const double c1 = sp2 ? -1.0 : -4.0 * c2 * cw0;
+    const double c0 = sp2 ? 1.0 : c2 * (2.0 * cw0 * cw0 + 1.0);
+    const double ks = sp2 ? k : k / fmax(c0 + c1 + c2, 1e-10);
+    const double e = ks * (c0 + c1 * cos(w) + c2 * cos(2.0 * w));
+    const double dedw = ks * (-c1 * sin(w) - 2.0 * c2 * sin(2.0 * w));
+    const double deds = fabs(s_raw) <= 1.0 ? dedw / sqrt(fmax(1.0 - s * s, 1e-30)) : 0.0;
+    // ds/dv1 and ds/dn; dn/dv2 (x) and dn/dv3 (x) through the cross product
+    double wv[3], t[3];
+    const double inv_la = 1.0 / (la + kEps), inv_ln = 1.0 / (ln + kEps);
+    for (int a = 0; a < 3; ++a) {
+      const double nu = n[a] * inv_ln;
+      g[0][a] = deds * (nu * inv_la - (an * inv_ln) * inv_la * inv_la / (la > 0.0 ? la : 1.0) * v[0][a]);
+      wv[a] = (v[0][a] * inv_ln - an * inv_ln * inv_ln / (ln > 0.0 ? ln : 1.0) * n[a]) * inv_la;
+    }
+    cross3(v[2], wv, t);
+    for (int a = 0; a < 3; ++a) g[1][a] = deds * t[a];
+    cross3(wv, v[1], t);
+    for (int a = 0; a < 3; ++a) g[2][a] = deds * t[a];
+    return e;
+  }
+}
+
+template <int KIND>
+__global__ void bonded_kernel(const double *pos, const int32_t *system, const int32_t *species, int64_t n,
+                              const double *tril, int32_t n_sys, const int32_t *edges, const int32_t *shifts,
+                              int64_t n_edges, const double *params, int32_t nsp, double *energy, double *grad,
+                              double *grad_tril, kups_status *status) {
+  constexpr int D = Kind<KIND>::order, P = Kind<KIND>::params;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int sys = -1;
+  double en = 0.0, dl[6] = {0, 0, 0, 0, 0, 0};
+  if (e < n_edges) {
+    int idx[D];
+    bool ok = true;
+    int64_t row = 0;
+    for (int d = 0; d < D; ++d) {
+      idx[d] = edges[(int64_t)D * e + d];
+      ok &= idx[d] >= 0 && idx[d] < n;
+    }
+    if (ok) {
+      for (int d = 0; d < D; ++d) {
+        const int t = species[idx[d]];
+        ok &= t >= 0 && t < nsp;
+        row = row * nsp + t;
+      }
+    }
+    const int s0 = ok ? system[idx[0]] : -1;
+    if (!ok || s0 < 0 || s0 >= n_sys) {
+      status_error(status, KUPS_ERR_INVALID, e);
+    } else {
+      sys = s0;
+      const Tril64 L = load_tril64(tril + 6 * (int64_t)s0);
+      double v[D - 1][3], sh[D - 1][3], g[D - 1][3];
+      for (int m = 0; m < D - 1; ++m) {
+        for (int a = 0; a < 3; ++a) sh[m][a] = shifts[((int64_t)(D - 1) * e + m) * 3 + a];
+        double sL[3];
+        row_times_tril64(sh[m], L, sL);
+        for (int a = 0; a < 3; ++a) v[m][a] = pos[3 * (int64_t)idx[m + 1] + a] - pos[3 * (int64_t)idx[0] + a] + sL[a];
+      }
+      en = edge_energy_grad<KIND>(v, params + row * P, g);
+      bool finite = isfinite(en);
+      for (int m = 0; m < D - 1; ++m)
+        for (int a = 0; a < 3; ++a) finite &= isfinite(g[m][a]);
+      if (!finite) status_error(status, KUPS_ERR_NONFINITE, e);
+      for (int m = 0; m < D - 1; ++m) {
+        for (int a = 0; a < 3; ++a) {
+          atomicAdd(&grad[3 * (int64_t)idx[m + 1] + a], g[m][a]);
+          atomicAdd(&grad[3 * (int64_t)idx[0] + a], -g[m][a]);
+        }
+        dl[0] += sh[m][0] * g[m][0];
+        dl[1] += sh[m][1] * g[m][0];
+        dl[2] += sh[m][1] * g[m][1];
+        dl[3] += sh[m][2] * g[m][0];
+        dl[4] += sh[m][2] * g[m][1];
+        dl[5] += sh[m][2] * g[m][2];
+      }
+    }
+  }
+  add_system(energy, 1, 0, sys, en);
+  if (grad_tril != nullptr)
+    for (int k = 0; k < 6; ++k) add_system(grad_tril, 6, k, sys, dl[k]);
+}
+
+template <int KIND>
+cudaError_t launch_bonded(const double *pos, const int32_t *system, const int32_t *species, int64_t n,
+                          const double *tril, int32_t s, const int32_t *edges, const int32_t *shifts,
+                          int64_t n_edges, const double *params, int32_t nsp, double *energy, double *grad,
+                          double *grad_tril, kups_status *status, cudaStream_t stream) {
+  const unsigned grid = (unsigned)((n_edges + 127) / 128);
+  bonded_kernel<KIND><<<grid, 128, 0, stream>>>(pos, system, species, n, tril, s, edges, shifts, n_edges, params,
+                                                nsp, energy, grad, grad_tril, status);
+  return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace kups
+
+using namespace kups;
+
+extern "C" int32_t kups_bonded_order(int32_t kind) {
+  switch (kind) {
+    case 0: return Kind<0>::order;
+    case 1: return Kind<1>::order;
+    case 2: return Kind<2>::order;
+    case 3: return Kind<3>::order;
+    case 4: return Kind<4>::order;
+    case 5: return Kind<5>::order;
+    default: return -1;
+  }
+}
+
+extern "C" int32_t kups_bonded_param_count(int32_t kind) {
+  switch (kind) {
+    case 0: return Kind<0>::params;
+    case 1: return Kind<1>::params;
+    case 2: return Kind<2>::params;
+    case 3: return Kind<3>::params;
+    case 4: return Kind<4>::params;
+    case 5: return Kind<5>::params;
+    default: return -1;
+  }
+}
+
+extern "C" int32_t kups_bonded_edges(int32_t kind, const double *positions, const int32_t *system,
+                                     const int32_t *species, int64_t n_particles, const double *tril,
+                                     int32_t n_systems, const int32_t *edges, const int32_t *shifts, int64_t n_edges,
+                                     const double *params, int32_t n_species, double *energy, double *grad,
+                                     double *grad_tril, kups_status *status, void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (kind < 0 || kind > 5 || n_particles < 0 || n_systems < 0 || n_edges < 0 || n_species <= 0 ||
+      n_species > 1024)
+    return KUPS_ERR_INVALID;
+  if (n_edges == 0) return KUPS_OK;
+  if (positions == nullptr || system == nullptr || species == nullptr || tril == nullptr || edges == nullptr ||
+      shifts == nullptr || params == nullptr || energy == nullptr || grad == nullptr || status == nullptr)
+    return KUPS_ERR_INVALID;
+  cudaError_t err;
+  switch (kind) {
+#define KUPS_BONDED_CASE(K)                                                                                      \
+  case K:                                                                                                        \
+    err = launch_bonded<K>(positions, system, species, n_particles, tril, n_systems, edges, shifts, n_edges,     \
+                           params, n_species, energy, grad, grad_tril, status, stream);                          \
+    break;
+    KUPS_BONDED_CASE(0)
+    KUPS_BONDED_CASE(1)
+    KUPS_BONDED_CASE(2)
+    KUPS_BONDED_CASE(3)
+    KUPS_BONDED_CASE(4)
+    default:
+      err = launch_bonded<5>(positions, system, species, n_particles, tril, n_systems, edges, shifts, n_edges,
+                             params, n_species, energy, grad, grad_tril, status, stream);
+#undef KUPS_BONDED_CASE
+  }
+  return err == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}

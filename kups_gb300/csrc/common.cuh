@@ -152,6 +152,19 @@ __device__ inline float warp_sum(float v) {
   return v;
 }
 
+// arr[sys * stride + comp] += v from every lane of a full warp (sys < 0: nothing);
+// one atomic per warp when the whole warp works on one system.
+__device__ inline void add_system(double *arr, int stride, int comp, int sys, double v) {
+  const unsigned full = 0xffffffffu;
+  const int s0 = __shfl_sync(full, sys, 0);
+  if (__all_sync(full, sys == s0)) {
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0 && sys >= 0) atomicAdd(&arr[(int64_t)sys * stride + comp], v);
+  } else if (sys >= 0) {
+    atomicAdd(&arr[(int64_t)sys * stride + comp], v);
+  }
+}
+
 // Block-wide sum of a double; every thread gets the result.  `scratch` holds
 // at least 33 doubles; the call contains two __syncthreads().
 __device__ inline double block_sum(double v, double *scratch) {

@@ -28,18 +28,6 @@ __device__ inline void lj_pair(R r2, R sig, R eps, R rc2, R &e, R &dedr2) {
   }
 }
 
-__device__ inline void add_system(double *arr, int stride, int comp, int sys, double v) {
-  // Warp-aggregated when the whole warp works on one system.
-  const unsigned full = 0xffffffffu;
-  const int s0 = __shfl_sync(full, sys, 0);
-  if (__all_sync(full, sys == s0)) {
-    v = warp_sum(v);
-    if ((threadIdx.x & 31) == 0 && sys >= 0) atomicAdd(&arr[(int64_t)sys * stride + comp], v);
-  } else if (sys >= 0) {
-    atomicAdd(&arr[(int64_t)sys * stride + comp], v);
-  }
-}
-
 __global__ void lj_edges_kernel(const double *pos, const int32_t *system, const int32_t *species,
                                 int64_t n, const double *tril, const double *cutoffs, int32_t s,
                                 const double *sigma, const double *epsilon, int32_t nsp,

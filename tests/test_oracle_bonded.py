@@ -1,0 +1,116 @@
+"""Bonded-term oracle against the reference's known answers
+(test/potential/test_harmonic.py, test/potential/classical/test_{morse,cosine_angle,
+dihedral,inversion}.py) and its gradients against total-energy finite differences (CPU)."""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle import bonded as ob
+
+BOX = np.array([[20.0, 0, 20.0, 0, 0, 20.0]])
+
+
+def energy(kind, pos, row, order):
+    T = 1
+    table = np.asarray(row, np.float64).reshape((T,) * order + (-1,)).reshape(1, -1)
+    e, _, _ = ob.bonded(kind, pos, np.zeros(len(pos), int), np.zeros(len(pos), int), BOX, table, T,
+                        np.arange(order)[None], np.zeros((1, order - 1, 3)))
+    return e[0]
+
+
+def dihedral_positions(phi):
+    """i, j, k fixed; l rotated about the j-k axis by phi - pi from its trans position."""
+    i, j, k = np.zeros(3), np.array([1.0, 0, 0]), np.array([1.5, 1.0, 0])
+    axis = (k - j) / np.linalg.norm(k - j)
+    t = np.array([2.5, 1.0, 0]) - k
+    a = phi - np.pi
+    rot = t * np.cos(a) + np.cross(axis, t) * np.sin(a) + axis * axis.dot(t) * (1 - np.cos(a))
+    return np.stack([i, j, k, k + rot])
+
+
+def test_dihedral_known_answers():
+    assert energy("dihedral", dihedral_positions(np.pi), [2.0, 3.0, np.pi], 4) == pytest.approx(0.0, abs=1e-10)
+    assert energy("dihedral", dihedral_positions(0.0), [2.0, 3.0, np.pi], 4) == pytest.approx(2.0, abs=1e-10)
+    assert energy("dihedral", dihedral_positions(np.pi / 2), [2.0, 3.0, np.pi], 4) == pytest.approx(1.0, abs=1e-10)
+    for phi0_deg, n in [(180, 3), (180, 2), (0, 6), (60, 3)]:
+        phi0 = math.radians(phi0_deg)
+        assert energy("dihedral", dihedral_positions(phi0), [2.0, n, phi0], 4) == pytest.approx(0.0, abs=1e-10)
+
+
+def test_cosine_angle_known_answers():
+    for deg, exp in ((90, (0.25, 0.0, 0.25)), (120, (0.5, 2 / 3, 1 / 3))):
+        np.testing.assert_allclose(ob.cosine_coefficients(math.radians(deg)), exp, atol=1e-12)
+    for deg in (90, 120, 180):
+        t = math.radians(deg)
+        pos = np.array([[0, 0, 0], [1.0, 0, 0], [math.cos(t), math.sin(t), 0]])
+        assert energy("cosine_angle", pos, [t, 3.0, math.radians(5)], 3) == pytest.approx(0.0, abs=1e-10)
+
+
+def inversion_positions(h):
+    return np.array([[0.0, 0.0, h], [1.0, 0.0, 0.0], [-0.5, 0.866025, 0.0], [-0.5, -0.866025, 0.0]])
+
+
+def inversion_omega(h):
+    rji, rjk, rjl = np.array([1.0, 0, -h]), np.array([-0.5, 0.866025, -h]), np.array([-0.5, -0.866025, -h])
+    n = np.cross(rjk, rjl)
+    return np.arcsin(np.clip(rji.dot(n / np.linalg.norm(n)) / np.linalg.norm(rji), -1, 1))
+
+
+def test_inversion_known_answers():
+    assert energy("inversion", inversion_positions(0.0), [0.0, 10.0], 4) == pytest.approx(0.0, abs=1e-10)
+    assert energy("inversion", inversion_positions(0.2), [0.0, 10.0], 4) == pytest.approx(
+        10.0 * (1 - math.cos(inversion_omega(0.2))), rel=1e-7)
+    w0 = math.radians(30.0)
+    assert energy("inversion", inversion_positions(0.0), [w0, 22.0], 4) == pytest.approx(22.0, rel=1e-9)
+    c2 = 1 / (4 * math.sin(w0) ** 2)
+    c1, c0 = -4 * c2 * math.cos(w0), c2 * (2 * math.cos(w0) ** 2 + 1)
+    w = inversion_omega(0.3)
+    exp = 10.0 / (c0 + c1 + c2) * (c0 + c1 * math.cos(w) + c2 * math.cos(2 * w))
+    assert energy("inversion", inversion_positions(0.3), [w0, 10.0], 4) == pytest.approx(exp, rel=1e-7)
+
+
+def test_two_body_and_harmonic_angle_known_answers():
+    pos = np.array([[0, 0, 0], [1.7, 0, 0.0]])
+    assert energy("harmonic_bond", pos, [1.2, 3.0], 2) == pytest.approx((1.7 - 1.2) ** 2 * 3.0)
+    assert energy("morse_bond", pos, [1.2, 2.0, 1.5], 2) == pytest.approx(2.0 * (1 - math.exp(-1.5 * 0.5)) ** 2)
+    pos = np.array([[0, 0, 0], [1.0, 0, 0], [0, 2.0, 0]])
+    assert energy("harmonic_angle", pos, [109.5, 0.02], 3) == pytest.approx((90.0 - 109.5) ** 2 * 0.02)
+
+
+@pytest.mark.parametrize("kind", list(ob.KINDS))
+def test_oracle_gradients_match_total_energy_differences(kind):
+    """dE/dx and dE/dtril (Cartesian positions fixed) of the oracle against central
+    differences of the total energy in positions and in tril, with image shifts."""
+    rng = np.random.default_rng(1)
+    _, order = ob.KINDS[kind]
+    T, N, E = 2, 12, 10
+    tril = np.array([[7.0, 0.8, 6.5, -0.6, 0.9, 7.5]])
+    pos = rng.uniform(0, 6, (N, 3))
+    edges = np.array([rng.choice(N, order, replace=False) for _ in range(E)])
+    shifts = rng.integers(-1, 2, (E, order - 1, 3))
+    npar = {"harmonic_bond": 2, "morse_bond": 3, "harmonic_angle": 2, "cosine_angle": 3, "dihedral": 3,
+            "inversion": 2}[kind]
+    table = rng.uniform(0.5, 2.0, (T**order, npar))
+    if kind == "cosine_angle":
+        table[:, 2] = math.radians(5)
+    species = rng.integers(0, T, N)
+    sysi = np.zeros(N, int)
+    e, g, gt = ob.bonded(kind, pos, sysi, species, tril, table, T, edges, shifts)
+    h = 1e-6
+    for i in range(N):
+        for a in range(3):
+            p1, p2 = pos.copy(), pos.copy()
+            p1[i, a] += h
+            p2[i, a] -= h
+            fd = (ob.bonded(kind, p1, sysi, species, tril, table, T, edges, shifts)[0][0]
+                  - ob.bonded(kind, p2, sysi, species, tril, table, T, edges, shifts)[0][0]) / (2 * h)
+            assert fd == pytest.approx(g[i, a], rel=1e-5, abs=1e-6 * max(1.0, np.abs(g).max()))
+    for k in range(6):
+        t1, t2 = tril.copy(), tril.copy()
+        t1[0, k] += h
+        t2[0, k] -= h
+        fd = (ob.bonded(kind, pos, sysi, species, t1, table, T, edges, shifts)[0][0]
+              - ob.bonded(kind, pos, sysi, species, t2, table, T, edges, shifts)[0][0]) / (2 * h)
+        assert fd == pytest.approx(gt[0, k], rel=1e-5, abs=1e-6 * max(1.0, np.abs(gt).max()))
