@@ -193,7 +193,7 @@ __device__ inline void set_shift_vectors(Smem &sm) {
 // Lanes serving one atom: the smallest power of two (<= 16) that still gives
 // every thread of the block an atom-lane to work on.
 __device__ inline int choose_tpa(int n, int threads) {
-  int t = 1;
+  int t = 2;
   while (t < 16 && n * t < threads) t <<= 1;
   return t;
 }
@@ -355,31 +355,54 @@ __device__ __noinline__ bool rebuild(Smem &sm, const SysParams &p, int n, int tp
   }
   __syncthreads();
   prof_add(prof, 7, tp);
-  // 3. Verlet list, row-major: a warp takes one x-row of cells and walks its
-  //    (cell-sorted, hence contiguous) atoms 32 at a time, one lane per atom;
-  //    the candidates of a chunk are the contiguous atom and ghost ranges of
-  //    the 3 x 3 neighbour rows over the x-range of the chunk's cells plus one
-  //    cell either side, read once per warp (shared-memory broadcast).  Hits
-  //    of 32 candidates are gathered in a per-lane bit mask, then appended in
-  //    candidate order (deterministic), four per 8-byte store.
+  // 3. Verlet list.  Work unit: a chunk of up to 32 consecutive (cell-sorted)
+  //    atoms of one x-row of cells, one lane per atom (a system's atoms fill
+  //    only the central rows of the extended grid, so whole rows as units left
+  //    warps idle); sm.bin_b[r] holds the exclusive prefix of the rows' chunk
+  //    counts.  The candidates of a chunk are the contiguous atom and ghost
+  //    ranges of the 3 x 3 neighbour rows over the x-range of the chunk's cells
+  //    plus one cell either side, read once per warp (shared-memory broadcast).
+  //    Hits of 32 candidates are gathered in a per-lane bit mask, then appended
+  //    in candidate order (deterministic), four per 8-byte store.
   const int lane = threadIdx.x & 31;
   const int ltpa = __ffs(tpa) - 1;
   const uint32_t sent = (uint32_t)n_items;
   const int n_rows = p.nc[1] * p.nc[2];
+  uint16_t *rowp = sm.bin_b;
+  {
+    int carry = 0;
+    for (int r0 = 0; r0 < n_rows; r0 += nt) {
+      const int r = r0 + tid;
+      const int v = r < n_rows ? (sm.cell_start[(r + 1) * p.nc[0]] - sm.cell_start[r * p.nc[0]] + 31) >> 5 : 0;
+      int tot;
+      const int ex = block_exclusive_scan<int>(v, sm.iscan, &tot);
+      __syncthreads();
+      if (r < n_rows) rowp[r] = (uint16_t)(carry + ex);
+      carry += tot;
+    }
+    if (tid == 0) rowp[n_rows] = (uint16_t)carry;
+    __syncthreads();
+  }
+  const int n_chunks = rowp[n_rows];
   int my_max = 0;
   while (true) {
     int unit = 0;
     if (lane == 0) unit = atomicAdd(&sm.work, 1);
     unit = __shfl_sync(0xffffffffu, unit, 0);
-    if (unit >= n_rows) break;
-    const int cy = unit % p.nc[1], cz = unit / p.nc[1];
-    const int rowc = unit * p.nc[0];
+    if (unit >= n_chunks) break;
+    int row = 0, hi = n_rows - 1;  // the last row with rowp[row] <= unit (empty rows share it)
+    while (row < hi) {
+      const int mid = (row + hi + 1) >> 1;
+      if (rowp[mid] <= unit) row = mid; else hi = mid - 1;
+    }
+    const int cy = row % p.nc[1], cz = row / p.nc[1];
+    const int rowc = row * p.nc[0];
     const int ab = sm.cell_start[rowc], ae = sm.cell_start[rowc + p.nc[0]];
-    if (ae == ab) continue;
     const int z0 = max(cz - 1, 0), z1 = min(cz + 1, p.nc[2] - 1);
     const int y0 = max(cy - 1, 0), y1 = min(cy + 1, p.nc[1] - 1);
     const float rl2 = p.rl2;
-    for (int a0 = ab; a0 < ae; a0 += 32) {
+    {
+      const int a0 = ab + (unit - rowp[row]) * 32;
       // x-range of the chunk's cells (cells of a row are consecutive)
       const int last = min(a0 + 32, ae) - 1;
       int cfirst = 0, clast = 0;
