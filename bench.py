@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-gcmc", action="store_true", help="skip the GCMC plain / learned-proposal section")
     ap.add_argument("--no-ewald", action="store_true", help="skip the LJ + Ewald MD (ionic melt) section")
     ap.add_argument("--no-ensembles", action="store_true", help="skip the BAOAB / CSVR / NPT comparison")
+    ap.add_argument("--no-autotune", action="store_true", help="library-default launch shape for the MD kernel")
     ap.add_argument("--gcmc-replicas", type=int, default=1024)
     ap.add_argument("--strong", action="store_true",
                     help="split one --systems batch across the ranks (cost-balanced contiguous ranges) "
@@ -227,6 +228,13 @@ def run_ours(a):
     state = state_from_workload(W, torch)
     prop = md.make_baoab_langevin_step()
     packed = md.pack(state)
+    tuned = None
+    if not a.no_autotune:
+        from kups_gb300.autotune import autotune_md
+
+        # launch shape picked on a copy of the state (restored after every trial); untimed
+        tuned = autotune_md(prop, packed)
+    a.tuned = (prop.block_threads, prop.min_lanes_per_atom)
     # warm-up (includes the first list build and force evaluation)
     prop.run_packed(packed, max(a.warmup, 3), seed=11, step0=0)
     torch.cuda.synchronize()
@@ -298,6 +306,11 @@ def run_ours(a):
             "systems_per_gpu": W.n_systems,
             "atoms_per_gpu": W.n_atoms,
             "steps_per_launch": chunks[0],
+            "launch_shape": {"block_threads": prop.block_threads or 1024,
+                             "min_lanes_per_atom": prop.min_lanes_per_atom or 2,
+                             "chosen_by": "kups_gb300.autotune.autotune_md" if tuned else "library default",
+                             "candidates_ms_per_step": ([[bt, ml, ms] for bt, ml, ms in tuned.table]
+                                                        if tuned else None)},
             "l2": "inputs larger than L2 (state 4.4M atoms x 48 B + Verlet lists)",
             "parallelism": (f"systems split over {world} ranks by cost (contiguous ranges), no collective"
                             if a.strong else f"replicas x{world} (independent systems, no collective)"),
@@ -369,6 +382,7 @@ def run_ensembles(a, W, torch, steps=200):
         state.systems.compressibility = full(2e-4 / bar)
         state.systems.minimum_scale_factor = full(0.99)
         prop = make()
+        prop.block_threads, prop.min_lanes_per_atom = getattr(a, "tuned", (0, 0))
         packed = md.pack(state)
         prop.run_packed(packed, 10, seed=5, step0=0)
         torch.cuda.synchronize()
@@ -396,6 +410,11 @@ def run_argon(a, torch):
     W = workloads.argon_fcc()
     prop = md.make_baoab_langevin_step()
     packed = md.pack(state_from_workload(W, torch))
+    shape = None
+    if not a.no_autotune:
+        from kups_gb300.autotune import autotune_md
+
+        shape = autotune_md(prop, packed, steps=100)
     prop.run_packed(packed, 20, seed=3, step0=0)
     torch.cuda.synchronize()
     steps = 1000
@@ -406,7 +425,9 @@ def run_argon(a, torch):
     torch.cuda.synchronize()
     ms = t0.elapsed_time(t1)
     return {"workload": "argon NVT: 864 atoms (6x6x6 fcc, a 5.74 A), rc 8.5 A + 1 A skin, BAOAB dt 2 fs, 94.4 K",
-            "us_per_step": ms / steps * 1e3, "value": W.n_atoms * steps / (ms / 1e3), "unit": "atom-steps/s"}
+            "us_per_step": ms / steps * 1e3, "value": W.n_atoms * steps / (ms / 1e3), "unit": "atom-steps/s",
+            "launch_shape": {"block_threads": prop.block_threads or 1024, "min_lanes_per_atom": prop.min_lanes_per_atom or 2,
+                             "chosen_by": "kups_gb300.autotune.autotune_md" if shape else "library default"}}
 
 
 def run_ewald_md(a):
@@ -495,6 +516,7 @@ def run_e2e(a, W, torch):
     out_frc = torch.empty_like(out_pos).pin_memory()
     out_e = torch.empty(W.n_systems, dtype=torch.float64).pin_memory()
     prop = md.make_baoab_langevin_step(steps_per_call=a.e2e_chunk)
+    prop.block_threads, prop.min_lanes_per_atom = getattr(a, "tuned", (0, 0))
 
     def one_call(i):
         p = host.particles

@@ -185,6 +185,10 @@ typedef struct kups_md_args {
   uint64_t step0;
   int32_t n_ctas;            /* 0 = one per SM */
   int32_t block_threads;     /* 0 = library default */
+  int32_t min_lanes_per_atom; /* lanes sharing one atom's Verlet list in the force phase:
+                                 at least this many (1, 2 or 4; 0 = library default 2),
+                                 more for small systems so every thread has work */
+  int32_t pad_md;
   /* integrator 2 = CSVR (CSVRStep + velocity Verlet, md/integrators.py:469-640),
    * integrator 3 = CSVR + stochastic cell rescaling (make_csvr_npt_step, :641-890).
    * Per-system R1, R2 and the barostat's R are independent draws (the reference

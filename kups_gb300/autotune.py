@@ -1,0 +1,101 @@
+"""Launch-shape autotuner of the fused Lennard-Jones MD kernel.
+
+The fused kernel's throughput depends on two launch choices that no formula fixes well
+across workloads: threads per CTA (one CTA per SM owns one system at a time; more threads
+hide more shared-memory latency but lengthen the barrier tails of small systems) and the
+minimum number of lanes that share one atom's Verlet list in the force phase (more lanes
+give finer work units at the end of a phase, fewer lanes fewer shuffle reductions).
+``autotune_md`` times every candidate on a copy of the caller's packed state (the state is
+restored after each trial, so tuning does not advance the simulation), keeps the fastest,
+and caches it per workload signature (system count, largest system, densest system, cutoff
+and skin, integrator), in memory and optionally in a JSON file.  Results of the tuned and
+untuned kernels are the same up to float32 summation order.
+"""
+
+from __future__ import annotations
+
+import json
+import math
+import os
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib
+from .neighborlist import read_status
+
+BLOCK_THREADS = (512, 640, 768, 896, 1024)
+MIN_LANES = (1, 2, 4)
+
+_CACHE: dict[str, dict] = {}
+
+
+@dataclass
+class TunedShape:
+    block_threads: int
+    min_lanes_per_atom: int
+    ms_per_step: float
+    table: list  # [(block_threads, min_lanes, ms_per_step)] of every candidate
+
+
+def signature(packed, prop) -> str:
+    counts = (packed.sys_offset[1:] - packed.sys_offset[:-1]).to(torch.float64)
+    return json.dumps({
+        "systems": int(packed.n_systems), "max_atoms": int(packed.max_atoms),
+        "density": round(float(packed.max_density), 4), "mean_atoms": round(float(counts.mean()), 1),
+        "cutoff": round(float(packed.cutoff.max()), 3), "skin": round(float(packed.skin.max()), 3),
+        "integrator": prop.integrator,
+    }, sort_keys=True)
+
+
+def _time(prop, packed, steps, seed):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    st = prop.launch(packed, steps, seed=seed, step0=0, virial=False)
+    e1.record()
+    torch.cuda.synchronize()
+    status = read_status(st)
+    return e0.elapsed_time(e1) / steps, status
+
+
+def autotune_md(prop, packed, steps: int = 40, cache_file: str | None = None,
+                block_threads=BLOCK_THREADS, min_lanes=MIN_LANES) -> TunedShape:
+    """Time each (block_threads, min_lanes_per_atom) candidate for `steps` steps after one
+    untimed launch of the same length (list builds and caches warm), set the fastest on
+    `prop` and return it.  `packed` is left as it was."""
+    key = signature(packed, prop)
+    if key not in _CACHE and cache_file and os.path.exists(cache_file):
+        with open(cache_file) as f:
+            _CACHE.update(json.load(f))
+    if key in _CACHE:
+        c = _CACHE[key]
+        prop.block_threads, prop.min_lanes_per_atom = c["block_threads"], c["min_lanes_per_atom"]
+        return TunedShape(c["block_threads"], c["min_lanes_per_atom"], c["ms_per_step"], c["table"])
+    backup = packed.clone_dynamic()
+    valid0 = packed.forces_valid
+    saved = (prop.block_threads, prop.min_lanes_per_atom)
+    table = []
+    best = (math.inf, None)
+    for bt in block_threads:
+        for ml in min_lanes:
+            prop.block_threads, prop.min_lanes_per_atom = bt, ml
+            _, st0 = _time(prop, packed, steps, seed=1)
+            ms, st1 = _time(prop, packed, steps, seed=2)
+            packed.restore_dynamic(backup)
+            packed.forces_valid = valid0
+            if st0.code != _lib.KUPS_OK or st1.code != _lib.KUPS_OK:
+                table.append((bt, ml, None))
+                continue
+            table.append((bt, ml, ms))
+            if ms < best[0]:
+                best = (ms, (bt, ml))
+    if best[1] is None:
+        prop.block_threads, prop.min_lanes_per_atom = saved
+        raise _lib.KupsError("no launch shape ran without a device error")
+    prop.block_threads, prop.min_lanes_per_atom = best[1]
+    _CACHE[key] = {"block_threads": best[1][0], "min_lanes_per_atom": best[1][1], "ms_per_step": best[0],
+                   "table": table}
+    if cache_file:
+        with open(cache_file, "w") as f:
+            json.dump(_CACHE, f, indent=1)
+    return TunedShape(best[1][0], best[1][1], best[0], table)

@@ -192,8 +192,8 @@ __device__ inline void set_shift_vectors(Smem &sm) {
 
 // Lanes serving one atom: the smallest power of two (<= 16) that still gives
 // every thread of the block an atom-lane to work on.
-__device__ inline int choose_tpa(int n, int threads) {
-  int t = 2;
+__device__ inline int choose_tpa(int n, int threads, int min_lanes) {
+  int t = min_lanes;
   while (t < 16 && n * t < threads) t <<= 1;
   return t;
 }
@@ -803,7 +803,7 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
       if (tid == 0) status_error(status, KUPS_ERR_INVALID, s);
       continue;
     }
-    const int tpa = choose_tpa(n, nt);
+    const int tpa = choose_tpa(n, nt, a.min_lanes_per_atom);
     bool ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s, prof, scratch);
     if (tid == 0) sm.work = 0;
     __syncthreads();
@@ -1159,15 +1159,22 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
   const int ctas = a->n_ctas > 0 ? a->n_ctas : sms;
   const int threads = a->block_threads > 0 ? a->block_threads : kThreads;
   if (threads % 32 != 0 || threads > kThreads || threads < 64) return KUPS_ERR_INVALID;
+  const int lanes = a->min_lanes_per_atom;
+  // at most 4: the list layout strides groups of `tpa` units and neighbor_capacity / 4 is only
+  // guaranteed to be a multiple of 4 (8 or 16 lanes arise only for systems below 256 atoms,
+  // whose lists stay inside the CTA's slice for any capacity)
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4) return KUPS_ERR_INVALID;
+  kups_md_args args = *a;
+  if (args.min_lanes_per_atom == 0) args.min_lanes_per_atom = 2;
   int *queue = reinterpret_cast<int *>(((uintptr_t)workspace + 255) & ~uintptr_t(255));
   uint32_t *nl = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(queue) + 256);
   KUPS_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(int), stream));
   const size_t smem = sizeof(Smem);
   switch (a->integrator) {
-    case 0: KUPS_CUDA_TRY(launch_md<0>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
-    case 1: KUPS_CUDA_TRY(launch_md<1>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
-    case 2: KUPS_CUDA_TRY(launch_md<2>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
-    default: KUPS_CUDA_TRY(launch_md<3>(*a, ctas, threads, smem, nl, queue, status, stream)); break;
+    case 0: KUPS_CUDA_TRY(launch_md<0>(args, ctas, threads, smem, nl, queue, status, stream)); break;
+    case 1: KUPS_CUDA_TRY(launch_md<1>(args, ctas, threads, smem, nl, queue, status, stream)); break;
+    case 2: KUPS_CUDA_TRY(launch_md<2>(args, ctas, threads, smem, nl, queue, status, stream)); break;
+    default: KUPS_CUDA_TRY(launch_md<3>(args, ctas, threads, smem, nl, queue, status, stream)); break;
   }
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

@@ -222,6 +222,7 @@ class FusedLennardJonesMD:
     neighbor_capacity: int | None = None
     n_ctas: int = 0
     block_threads: int = 0
+    min_lanes_per_atom: int = 0  # 0: library default; kups_gb300.autotune picks one per workload
     _ws: torch.Tensor | None = field(default=None, repr=False)
 
     def __call__(self, key, state: MDState) -> MDState:
@@ -264,6 +265,7 @@ class FusedLennardJonesMD:
         a.neighbor_capacity = self.capacity_for(packed)
         a.seed, a.step0 = int(seed) & (2**64 - 1), int(step0)
         a.n_ctas, a.block_threads = self.n_ctas, self.block_threads
+        a.min_lanes_per_atom = self.min_lanes_per_atom
         if a.integrator >= 2:
             need = ["thermostat_tau"] + (["target_pressure", "barostat_tau", "compressibility", "min_scale"]
                                          if a.integrator == 3 else [])
