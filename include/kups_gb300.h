@@ -296,6 +296,23 @@ int32_t kups_lj_ewald_real_forces(const double *positions, const double *charges
                                   int32_t n_species, const double *lj_cutoff, const double *alpha,
                                   const double *ewald_cutoff, double coulomb_k, int32_t terms, double *energy,
                                   double *grad, kups_status *status, void *stream);
+/* kups_lj_ewald_real_forces_packed: the same sum, arguments and outputs as
+ * kups_lj_ewald_real_forces, with positions first stored in `workspace` as float
+ * pairs hi = fl(x), lo = fl(x - hi) (differences (hj - hi) + (lj - li) keep float32
+ * relative accuracy with no float64 arithmetic) and the pair terms evaluated only for
+ * the partners a lane found inside the cutoff among 32 tested.  A system with more
+ * than max_atoms_per_system atoms records KUPS_ERR_INVALID and is skipped.
+ * Workspace: kups_lj_ewald_real_forces_workspace_bytes(n_systems, max_atoms). */
+size_t kups_lj_ewald_real_forces_workspace_bytes(int32_t n_systems, int32_t max_atoms_per_system);
+int32_t kups_lj_ewald_real_forces_packed(const double *positions, const double *charges,
+                                         const int32_t *species, const int32_t *sys_offset,
+                                         int32_t n_systems, int32_t max_atoms_per_system,
+                                         const double *tril, const double *lj_sigma,
+                                         const double *lj_epsilon, int32_t n_species,
+                                         const double *lj_cutoff, const double *alpha,
+                                         const double *ewald_cutoff, double coulomb_k, int32_t terms,
+                                         double *energy, double *grad, void *workspace,
+                                         size_t workspace_bytes, kups_status *status, void *stream);
 int32_t kups_pair_edges(const double *positions, const int32_t *system, const int32_t *species,
                         const double *charges, int64_t n_particles, const double *tril,
                         int32_t n_systems, const double *lj_sigma, const double *lj_epsilon,

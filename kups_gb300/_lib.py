@@ -97,6 +97,8 @@ SIGNATURES = {
     "kups_ewald_recip": (_I32, [_P, _P, _P, _I32, _I32, _P, _P, _I32, _P, C.c_double, _P, _P, _P, _P, _P, _SZ, _P, _P]),
     "kups_ewald_recip_static": (_I32, [_P, _P, _P, _I32, _I32, _P, _P, _I32, _P, C.c_double, _P, _P, _P, _P, _P, _P]),
     "kups_lj_ewald_real_forces": (_I32, [_P, _P, _P, _P, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _P, _P]),
+    "kups_lj_ewald_real_forces_workspace_bytes": (C.c_size_t, [_I32, _I32]),
+    "kups_lj_ewald_real_forces_packed": (_I32, [_P, _P, _P, _P, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _P, C.c_size_t, _P, _P]),
     "kups_ewald_self": (_I32, [_P, _P, _I32, _P, C.c_double, _P, _P]),
     "kups_md_kick": (_I32, [_P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_drift": (_I32, [_P, _P, _P, _P, _P, _P, C.c_double, _I64, _P]),

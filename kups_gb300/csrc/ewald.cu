@@ -496,6 +496,155 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_allpairs_kernel(
   if (threadIdx.x == 0) atomicAdd(&energy[s], esum);
 }
 
+// ---------------------------------------------------------------- packed real space
+// The all-pairs kernel above forms every pair difference in float64 (three float64
+// subtractions per pair test, slow on this part) and runs the LJ + erfc branch for a
+// whole warp whenever any lane has a partner inside the cutoff (~11 % of pair tests
+// in a dense melt, so ~98 % of warp iterations at ~11 % lane use).  The packed path:
+//  * a pack kernel stores each coordinate as a float pair hi = fl(x), lo = fl(x - hi);
+//    a difference (hj - hi) + (lj - li) then carries float32 relative error in d
+//    itself (the rounding of hj - hi is relative to the result), with no float64;
+//  * the force kernel tests 32 partners per pass into a per-lane hit mask and then
+//    evaluates only the hits (loop count = the warp's largest hit count, not 32).
+// Pair terms, the minimum image and the fixed-order reduction are those of the
+// all-pairs kernel.
+// Packed arrays are indexed by system * max_atoms + local index (inside the workspace
+// for any sys_offset); a system above max_atoms is refused.
+__global__ void real_pack_kernel(const double *pos, const double *q, const int32_t *species, const int32_t *sys_offset,
+                                 int terms, int max_atoms, float4 *hi, float4 *lo, kups_status *status) {
+  const int s = blockIdx.y;
+  const int a0 = sys_offset[s], n = sys_offset[s + 1] - a0;
+  if (n > max_atoms) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) status_error(status, KUPS_ERR_INVALID, s);
+    return;
+  }
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t g = a0 + k, p = (int64_t)s * max_atoms + k;
+    float h[3], l[3];
+    for (int a = 0; a < 3; ++a) {
+      const double x = pos[3 * g + a];
+      h[a] = (float)x;
+      l[a] = (float)(x - (double)h[a]);
+    }
+    hi[p] = make_float4(h[0], h[1], h[2], (float)q[g]);
+    lo[p] = make_float4(l[0], l[1], l[2], __int_as_float((terms & 1) ? species[g] : 0));
+  }
+}
+
+__global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
+    const int32_t *sys_offset, const double *tril, const double *lj_sigma, const double *lj_eps, int nsp,
+    const double *rc_lj, const double *alpha, const double *rc_ew, double ke, int terms, int max_atoms,
+    const float4 *hi, const float4 *lo, double *energy, double *grad, kups_status *status) {
+  __shared__ float2 ljt[64];
+  __shared__ float part[kRealStreams][kRealAtoms][3];
+  __shared__ double red[40];
+  const int s = blockIdx.y;
+  const int a0 = sys_offset[s], n = sys_offset[s + 1] - a0;
+  if ((int)blockIdx.x * kRealAtoms >= n || n > max_atoms) return;  // uniform over the block
+  const int64_t pb = (int64_t)s * max_atoms;  // this system's rows of the packed arrays
+  const Tril64 L64 = load_tril64(tril + 6 * (int64_t)s);
+  const Tril64 I64 = inverse_tril64(L64);
+  double wd[3];
+  perpendicular_widths64(L64, wd);
+  const double rlj = (terms & 1) ? rc_lj[s] : 0.0, rew = (terms & 2) ? rc_ew[s] : 0.0;
+  const double rmax = fmax(rlj, rew);
+  if (fmin(wd[0], fmin(wd[1], wd[2])) < 2.0 * rmax) {
+    if (threadIdx.x == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
+    return;
+  }
+  float L[6], I[6];
+  for (int k = 0; k < 6; ++k) {
+    L[k] = (float)L64.t[k];
+    I[k] = (float)I64.t[k];
+  }
+  if ((terms & 1) && nsp * nsp <= 64)
+    for (int k = threadIdx.x; k < nsp * nsp; k += blockDim.x) {
+      const double sg = lj_sigma[k];
+      ljt[k] = make_float2((float)(sg * sg), (float)(4.0 * lj_eps[k]));
+    }
+  __syncthreads();
+  const float rc2_lj = (float)(rlj * rlj), rc2_ew = (float)(rew * rew), rc2 = (float)(rmax * rmax);
+  const float al = (terms & 2) ? (float)alpha[s] : 0.f;
+  const float two_al_rsqrtpi = 2.0f * al * 0.56418958354775628695f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = lane & (kRealAtoms - 1), stream_id = warp * 2 + (lane >> 4);
+  const int il = blockIdx.x * kRealAtoms + slot;
+  const bool act = il < n;
+  const int64_t gi = a0 + (act ? il : 0);
+  const float4 hi_i = hi[pb + (act ? il : 0)], lo_i = lo[pb + (act ? il : 0)];
+  const float qi = (float)((double)hi_i.w * ke);
+  const int ti = __float_as_int(lo_i.w);
+  // minimum-image difference x_j - x_i from the hi / lo pairs
+  auto diff = [&](int64_t gj, float &dx, float &dy, float &dz, float &r2) {
+    const float4 hj = hi[gj], lj = lo[gj];
+    const float d0 = (hj.x - hi_i.x) + (lj.x - lo_i.x), d1 = (hj.y - hi_i.y) + (lj.y - lo_i.y),
+                d2 = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+    float f0 = (d0 * I[0] + d1 * I[1]) + d2 * I[3], f1 = d1 * I[2] + d2 * I[4], f2 = d2 * I[5];
+    f0 -= rintf(f0);
+    f1 -= rintf(f1);
+    f2 -= rintf(f2);
+    dx = (f0 * L[0] + f1 * L[1]) + f2 * L[3];
+    dy = f1 * L[2] + f2 * L[4];
+    dz = f2 * L[5];
+    r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  };
+  float fx = 0.f, fy = 0.f, fz = 0.f;  // dE/dx_i, this half-warp's partners
+  float ef = 0.f;
+  const int per = (n + kRealStreams - 1) / kRealStreams;
+  const int j0 = stream_id * per, j1 = min(n, j0 + per);
+  for (int c0 = j0; c0 < j1; c0 += 32) {
+    const int cn = min(32, j1 - c0);
+    uint32_t hits = 0;
+    for (int t = 0; t < cn; ++t) {
+      float dx, dy, dz, r2;
+      diff(pb + c0 + t, dx, dy, dz, r2);
+      hits |= (uint32_t)(r2 < rc2) << t;
+    }
+    if (c0 <= il && il < c0 + cn) hits &= ~(1u << (il - c0));  // not the atom itself
+    if (!act) hits = 0;
+    while (hits) {
+      const int t = __ffs(hits) - 1;
+      hits &= hits - 1;
+      const int64_t gj = pb + c0 + t;
+      float dx, dy, dz, r2;
+      diff(gj, dx, dy, dz, r2);
+      float dedr2 = 0.f;
+      if ((terms & 1) && r2 < rc2_lj) {
+        const float2 c = ljt[ti * nsp + __float_as_int(lo[gj].w)];
+        const float inv = 1.f / r2, s2 = c.x * inv, c6 = s2 * s2 * s2;
+        ef += c.y * (c6 * c6 - c6);
+        dedr2 += -0.5f * c.y * c6 * (12.f * c6 - 6.f) * inv;
+      }
+      if ((terms & 2) && r2 < rc2_ew) {
+        const float r = sqrtf(r2), ir = 1.f / r, qq = qi * hi[gj].w;
+        const float er = erfcf(al * r);
+        ef += qq * er * ir;
+        dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * expf(-al * al * r2) * ir);
+      }
+      fx = fmaf(-2.f * dedr2, dx, fx);
+      fy = fmaf(-2.f * dedr2, dy, fy);
+      fz = fmaf(-2.f * dedr2, dz, fz);
+    }
+  }
+  part[stream_id][slot][0] = fx;
+  part[stream_id][slot][1] = fy;
+  part[stream_id][slot][2] = fz;
+  __syncthreads();
+  if (threadIdx.x < kRealAtoms && act) {
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int k = 0; k < kRealStreams; ++k) {
+      gx += part[k][slot][0];
+      gy += part[k][slot][1];
+      gz += part[k][slot][2];
+    }
+    grad[3 * gi] = gx;
+    grad[3 * gi + 1] = gy;
+    grad[3 * gi + 2] = gz;
+  }
+  const double esum = block_sum(0.5 * (double)ef, red);
+  if (threadIdx.x == 0) atomicAdd(&energy[s], esum);
+}
+
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace
@@ -679,5 +828,44 @@ extern "C" int32_t kups_lj_ewald_real_forces(const double *positions, const doub
   real_allpairs_kernel<<<g, 32 * kRealWarps, 0, stream>>>(positions, charges, species, sys_offset, tril, lj_sigma,
                                                     lj_epsilon, n_species, lj_cutoff, alpha, ewald_cutoff,
                                                     coulomb_k, terms, energy, grad, status);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+extern "C" size_t kups_lj_ewald_real_forces_workspace_bytes(int32_t n_systems, int32_t max_atoms_per_system) {
+  if (n_systems <= 0 || max_atoms_per_system <= 0) return 256;
+  const size_t cap = (size_t)n_systems * (size_t)max_atoms_per_system;
+  return 2 * align256(cap * sizeof(float4)) + 256;
+}
+
+extern "C" int32_t kups_lj_ewald_real_forces_packed(const double *positions, const double *charges,
+                                                    const int32_t *species, const int32_t *sys_offset,
+                                                    int32_t n_systems, int32_t max_atoms_per_system,
+                                                    const double *tril, const double *lj_sigma,
+                                                    const double *lj_epsilon, int32_t n_species,
+                                                    const double *lj_cutoff, const double *alpha,
+                                                    const double *ewald_cutoff, double coulomb_k, int32_t terms,
+                                                    double *energy, double *grad, void *workspace,
+                                                    size_t workspace_bytes, kups_status *status, void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_systems < 0 || max_atoms_per_system < 0 || terms < 1 || terms > 3) return KUPS_ERR_INVALID;
+  if ((terms & 1) && (n_species < 1 || n_species > 8 || lj_sigma == nullptr || lj_epsilon == nullptr))
+    return KUPS_ERR_INVALID;
+  if (n_systems == 0) return KUPS_OK;
+  KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
+  if (max_atoms_per_system == 0) return KUPS_OK;
+  if (workspace == nullptr ||
+      workspace_bytes < kups_lj_ewald_real_forces_workspace_bytes(n_systems, max_atoms_per_system))
+    return KUPS_ERR_INVALID;
+  const size_t cap = (size_t)n_systems * (size_t)max_atoms_per_system;
+  char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~uintptr_t(255));
+  float4 *hi = reinterpret_cast<float4 *>(base);
+  float4 *lo = reinterpret_cast<float4 *>(base + align256(cap * sizeof(float4)));
+  dim3 gp((max_atoms_per_system + 255) / 256, n_systems);
+  real_pack_kernel<<<gp, 256, 0, stream>>>(positions, charges, species, sys_offset, terms, max_atoms_per_system, hi,
+                                           lo, status);
+  dim3 g((max_atoms_per_system + kRealAtoms - 1) / kRealAtoms, n_systems);
+  real_packed_kernel<<<g, 32 * kRealWarps, 0, stream>>>(sys_offset, tril, lj_sigma, lj_epsilon, n_species, lj_cutoff,
+                                                        alpha, ewald_cutoff, coulomb_k, terms, max_atoms_per_system,
+                                                        hi, lo, energy, grad, status);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

@@ -329,6 +329,8 @@ class LJEwaldMD:
         self.n_edges = torch.zeros(1, dtype=torch.int64, device="cuda")
         lib = _lib.load()
         self.nl_ws = torch.empty(lib.kups_neighborlist_workspace_bytes(self.n, self.s), dtype=torch.uint8, device="cuda")
+        self.real_ws = torch.empty(lib.kups_lj_ewald_real_forces_workspace_bytes(self.s, self.max_atoms),
+                                   dtype=torch.uint8, device="cuda") if self.allpairs else None
         self.rws = RecipWorkspace()
         self.rws.get(lib.kups_ewald_recip_workspace_bytes(self.s, self.kn.shape[1]))
         self.status = new_status()
@@ -351,13 +353,14 @@ class LJEwaldMD:
         if self.allpairs:
             terms = TERM_EWALD_REAL | (TERM_LJ if self.lj else 0)
             nsp = int(self.sig.shape[0]) if self.lj else 1
-            rc = lib.kups_lj_ewald_real_forces(
+            rc = lib.kups_lj_ewald_real_forces_packed(
                 pos.data_ptr(), self.q.data_ptr(), self.species.data_ptr(), self.off.data_ptr(), self.s,
                 self.max_atoms, self.tril.data_ptr(), self.sig.data_ptr() if self.lj else None,
                 self.eps.data_ptr() if self.lj else None, nsp, self.rc_lj.data_ptr() if self.lj else None,
                 self.alpha.data_ptr(), self.rc_ew.data_ptr(), TO_STANDARD_UNITS, terms, self.e_pair.data_ptr(),
-                self.g_pair.data_ptr(), self.status.data_ptr(), _stream())
-            _lib.check(rc, "kups_lj_ewald_real_forces")
+                self.g_pair.data_ptr(), self.real_ws.data_ptr(), self.real_ws.numel(), self.status.data_ptr(),
+                _stream())
+            _lib.check(rc, "kups_lj_ewald_real_forces_packed")
             ewald_recip(pos, self.q, self.off, self.max_atoms, self.tril, self.kn, self.alpha, grad_tril=False,
                         ws=self.rws, out=(self.e_rec, self.g_rec, self.t_rec, self.sk), status=self.status)
             torch.add(self.g_pair, self.g_rec, out=self.grad)

@@ -150,10 +150,13 @@ def test_lj_ewald_md_conserves_energy_with_graph_replay():
     assert abs(e1 - e0) / abs(e0) < 2e-3, (e0, e1)
 
 
-def test_allpairs_real_space_matches_edge_sum():
-    """kups_lj_ewald_real_forces (all pairs, float32 pair arithmetic) against the float64
-    oracle sum over the neighbour list at the cutoff: energy relative 1e-5, force RMS
-    relative 1e-5; a cell narrower than twice the cutoff is refused (KUPS_ERR_UNSUPPORTED)."""
+@pytest.mark.parametrize("binned", [False, True])
+def test_allpairs_real_space_matches_edge_sum(binned):
+    """kups_lj_ewald_real_forces (all pairs) and kups_lj_ewald_real_forces_packed (Morton-
+    sorted atoms, partner groups skipped by box distance), float32 pair arithmetic, against
+    the float64 oracle sum over the neighbour list at the cutoff: energy relative 1e-5,
+    force RMS relative 1e-5; a cell narrower than twice the cutoff is refused
+    (KUPS_ERR_UNSUPPORTED)."""
     import ctypes as C
 
     from kups_gb300 import _lib
@@ -187,10 +190,17 @@ def test_allpairs_real_space_matches_edge_sum():
     args = [cuda(pos), cuda(q), cuda(sp, torch.int32), off, cuda(tril), cuda(sig), cuda(eps), cuda(rc), cuda(alpha)]
     lib = _lib.load()
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    rc_ = lib.kups_lj_ewald_real_forces(args[0].data_ptr(), args[1].data_ptr(), args[2].data_ptr(), off.data_ptr(), 2, mx,
-                                        args[4].data_ptr(), args[5].data_ptr(), args[6].data_ptr(), 2,
-                                        args[7].data_ptr(), args[8].data_ptr(), args[7].data_ptr(), KE,
-                                        TERM_LJ | TERM_EWALD_REAL, en.data_ptr(), gr.data_ptr(), st.data_ptr(), stream)
+    ws = torch.empty(lib.kups_lj_ewald_real_forces_workspace_bytes(2, mx), dtype=torch.uint8, device="cuda")
+
+    def real(rcut, status):
+        common = (args[0].data_ptr(), args[1].data_ptr(), args[2].data_ptr(), off.data_ptr(), 2, mx,
+                  args[4].data_ptr(), args[5].data_ptr(), args[6].data_ptr(), 2, rcut.data_ptr(), args[8].data_ptr(),
+                  rcut.data_ptr(), KE, TERM_LJ | TERM_EWALD_REAL, en.data_ptr(), gr.data_ptr())
+        if binned:
+            return lib.kups_lj_ewald_real_forces_packed(*common, ws.data_ptr(), ws.numel(), status.data_ptr(), stream)
+        return lib.kups_lj_ewald_real_forces(*common, status.data_ptr(), stream)
+
+    rc_ = real(args[7], st)
     assert rc_ == 0
     torch.cuda.synchronize()
     assert read_status(st).code == 0
@@ -201,9 +211,6 @@ def test_allpairs_real_space_matches_edge_sum():
     # cutoff above half the narrowest width: refused, status records it
     st2 = new_status()
     big = cuda(np.array([9.9, 10.0]))
-    lib.kups_lj_ewald_real_forces(args[0].data_ptr(), args[1].data_ptr(), args[2].data_ptr(), off.data_ptr(), 2, mx,
-                                  args[4].data_ptr(), args[5].data_ptr(), args[6].data_ptr(), 2, big.data_ptr(),
-                                  args[8].data_ptr(), big.data_ptr(), KE, TERM_LJ | TERM_EWALD_REAL, en.data_ptr(),
-                                  gr.data_ptr(), st2.data_ptr(), stream)
+    real(big, st2)
     torch.cuda.synchronize()
     assert read_status(st2).code == _lib.KUPS_ERR_UNSUPPORTED
