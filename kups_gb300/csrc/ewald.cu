@@ -538,25 +538,37 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
   __shared__ float2 ljt[64];
   __shared__ float part[kRealStreams][kRealAtoms][3];
   __shared__ double red[40];
+  __shared__ uint16_t queue[kRealWarps][32 * 32];  // per warp: hits of one pass (half << 9 | slot << 5 | t)
   const int s = blockIdx.y;
   const int a0 = sys_offset[s], n = sys_offset[s + 1] - a0;
   if ((int)blockIdx.x * kRealAtoms >= n || n > max_atoms) return;  // uniform over the block
   const int64_t pb = (int64_t)s * max_atoms;  // this system's rows of the packed arrays
-  const Tril64 L64 = load_tril64(tril + 6 * (int64_t)s);
-  const Tril64 I64 = inverse_tril64(L64);
-  double wd[3];
-  perpendicular_widths64(L64, wd);
-  const double rlj = (terms & 1) ? rc_lj[s] : 0.0, rew = (terms & 2) ? rc_ew[s] : 0.0;
-  const double rmax = fmax(rlj, rew);
-  if (fmin(wd[0], fmin(wd[1], wd[2])) < 2.0 * rmax) {
-    if (threadIdx.x == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
-    return;
+  // cell, inverse and widths once per block (float64 is scarce on this part)
+  __shared__ float cellf[12];
+  __shared__ int refused;
+  if (threadIdx.x == 0) {
+    const Tril64 L64 = load_tril64(tril + 6 * (int64_t)s);
+    const Tril64 I64 = inverse_tril64(L64);
+    double wd[3];
+    perpendicular_widths64(L64, wd);
+    const double rmax = fmax((terms & 1) ? rc_lj[s] : 0.0, (terms & 2) ? rc_ew[s] : 0.0);
+    refused = fmin(wd[0], fmin(wd[1], wd[2])) < 2.0 * rmax;
+    if (refused) status_error(status, KUPS_ERR_UNSUPPORTED, s);
+    for (int k = 0; k < 6; ++k) {
+      cellf[k] = (float)L64.t[k];
+      cellf[6 + k] = (float)I64.t[k];
+    }
   }
+  __syncthreads();
+  if (refused) return;
   float L[6], I[6];
   for (int k = 0; k < 6; ++k) {
-    L[k] = (float)L64.t[k];
-    I[k] = (float)I64.t[k];
+    L[k] = cellf[k];
+    I[k] = cellf[6 + k];
   }
+  const double rlj = (terms & 1) ? rc_lj[s] : 0.0, rew = (terms & 2) ? rc_ew[s] : 0.0;
+  const double rmax = fmax(rlj, rew);
+  const float kef = (float)ke;
   if ((terms & 1) && nsp * nsp <= 64)
     for (int k = threadIdx.x; k < nsp * nsp; k += blockDim.x) {
       const double sg = lj_sigma[k];
@@ -572,8 +584,6 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
   const bool act = il < n;
   const int64_t gi = a0 + (act ? il : 0);
   const float4 hi_i = hi[pb + (act ? il : 0)], lo_i = lo[pb + (act ? il : 0)];
-  const float qi = (float)((double)hi_i.w * ke);
-  const int ti = __float_as_int(lo_i.w);
   // minimum-image difference x_j - x_i from the hi / lo pairs
   auto diff = [&](int64_t gj, float &dx, float &dy, float &dz, float &r2) {
     const float4 hj = hi[gj], lj = lo[gj];
@@ -588,47 +598,79 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
     dz = f2 * L[5];
     r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
   };
-  float fx = 0.f, fy = 0.f, fz = 0.f;  // dE/dx_i, this half-warp's partners
+  for (int k = threadIdx.x; k < kRealStreams * kRealAtoms * 3; k += blockDim.x) (&part[0][0][0])[k] = 0.f;
+  __syncthreads();
   float ef = 0.f;
   const int per = (n + kRealStreams - 1) / kRealStreams;
   const int j0 = stream_id * per, j1 = min(n, j0 + per);
-  for (int c0 = j0; c0 < j1; c0 += 32) {
-    const int cn = min(32, j1 - c0);
+  const int j0h[2] = {(warp * 2) * per, (warp * 2 + 1) * per};  // chunk starts of the warp's two streams
+  uint16_t *wq = queue[warp];
+  const int passes = (per + 31) / 32;  // the same for both half-warps of a warp
+  for (int pass = 0; pass < passes; ++pass) {
+    const int c0 = j0 + pass * 32;
+    const int cn = max(0, min(32, j1 - c0));
     uint32_t hits = 0;
-    for (int t = 0; t < cn; ++t) {
-      float dx, dy, dz, r2;
-      diff(pb + c0 + t, dx, dy, dz, r2);
-      hits |= (uint32_t)(r2 < rc2) << t;
+#pragma unroll 4
+    for (int t = 0; t < 32; ++t) {
+      if (t < cn) {  // four independent partner loads in flight
+        float dx, dy, dz, r2;
+        diff(pb + c0 + t, dx, dy, dz, r2);
+        hits |= (uint32_t)(r2 < rc2) << t;
+      }
     }
-    if (c0 <= il && il < c0 + cn) hits &= ~(1u << (il - c0));  // not the atom itself
+    if (cn > 0 && c0 <= il && il < c0 + cn) hits &= ~(1u << (il - c0));  // not the atom itself
     if (!act) hits = 0;
+    // append this lane's hits to the warp's queue (exclusive prefix of the counts)
+    const int cnt = __popc(hits);
+    int off = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, off, o);
+      if (lane >= o) off += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, off, 31);
+    off -= cnt;
+    const uint16_t tag = (uint16_t)(((lane >> 4) << 9) | (slot << 5));
     while (hits) {
       const int t = __ffs(hits) - 1;
       hits &= hits - 1;
-      const int64_t gj = pb + c0 + t;
-      float dx, dy, dz, r2;
-      diff(gj, dx, dy, dz, r2);
+      wq[off++] = tag | (uint16_t)t;
+    }
+    __syncwarp();
+    // every lane takes queued pairs until the queue is empty
+    for (int e = lane; e < total; e += 32) {
+      const int code = wq[e];
+      const int h = code >> 9, sl = (code >> 5) & 15, t = code & 31;
+      const int64_t ii = pb + blockIdx.x * kRealAtoms + sl;
+      const int64_t gj = pb + j0h[h] + pass * 32 + t;
+      const float4 hi_a = hi[ii], lo_a = lo[ii], hj = hi[gj], lj = lo[gj];
+      const float d0 = (hj.x - hi_a.x) + (lj.x - lo_a.x), d1 = (hj.y - hi_a.y) + (lj.y - lo_a.y),
+                  d2 = (hj.z - hi_a.z) + (lj.z - lo_a.z);
+      float f0 = (d0 * I[0] + d1 * I[1]) + d2 * I[3], f1 = d1 * I[2] + d2 * I[4], f2 = d2 * I[5];
+      f0 -= rintf(f0);
+      f1 -= rintf(f1);
+      f2 -= rintf(f2);
+      const float dx = (f0 * L[0] + f1 * L[1]) + f2 * L[3], dy = f1 * L[2] + f2 * L[4], dz = f2 * L[5];
+      const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
       float dedr2 = 0.f;
       if ((terms & 1) && r2 < rc2_lj) {
-        const float2 c = ljt[ti * nsp + __float_as_int(lo[gj].w)];
+        const float2 c = ljt[__float_as_int(lo_a.w) * nsp + __float_as_int(lj.w)];
         const float inv = 1.f / r2, s2 = c.x * inv, c6 = s2 * s2 * s2;
         ef += c.y * (c6 * c6 - c6);
         dedr2 += -0.5f * c.y * c6 * (12.f * c6 - 6.f) * inv;
       }
       if ((terms & 2) && r2 < rc2_ew) {
-        const float r = sqrtf(r2), ir = 1.f / r, qq = qi * hi[gj].w;
+        const float r = sqrtf(r2), ir = 1.f / r, qq = (hi_a.w * kef) * hj.w;
         const float er = erfcf(al * r);
         ef += qq * er * ir;
         dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * expf(-al * al * r2) * ir);
       }
-      fx = fmaf(-2.f * dedr2, dx, fx);
-      fy = fmaf(-2.f * dedr2, dy, fy);
-      fz = fmaf(-2.f * dedr2, dz, fz);
+      float *pp = part[warp * 2 + h][sl];
+      atomicAdd(pp, -2.f * dedr2 * dx);
+      atomicAdd(pp + 1, -2.f * dedr2 * dy);
+      atomicAdd(pp + 2, -2.f * dedr2 * dz);
     }
+    __syncwarp();
   }
-  part[stream_id][slot][0] = fx;
-  part[stream_id][slot][1] = fy;
-  part[stream_id][slot][2] = fz;
   __syncthreads();
   if (threadIdx.x < kRealAtoms && act) {
     float gx = 0.f, gy = 0.f, gz = 0.f;

@@ -8,6 +8,8 @@
 //                c1 = exp(-gamma dt)            (StochasticStep, :330-401); eta from
 //                Philox4x32-10 keyed by (seed, particle), counter = step.
 // Forces are F = -grad (the potential's dE/dx).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace kups {
@@ -52,6 +54,21 @@ __global__ void thermostat_kernel(double *mom, const double *mass, const int32_t
 }
 
 }  // namespace
+// Threads per block for a per-atom float64 kernel: 256 once there are enough atoms to
+// fill every SM, fewer (down to one warp) below that, so that a small system's atoms
+// spread over all SMs instead of queueing on the float64 units of a few.
+inline unsigned atom_block(int64_t n) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const int64_t per = (n + sms - 1) / sms;
+  return (unsigned)std::min<int64_t>(256, std::max<int64_t>(32, (per + 31) / 32 * 32));
+}
+
 }  // namespace kups
 
 using namespace kups;
@@ -60,7 +77,7 @@ extern "C" int32_t kups_md_kick(double *momenta, const double *grad, const int32
                                 const double *dt, double scale, int64_t n, void *stream) {
   if (n < 0) return KUPS_ERR_INVALID;
   if (n == 0) return KUPS_OK;
-  kick_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(momenta, grad, system, dt,
+  kick_kernel<<<(unsigned)((n + atom_block(n) - 1) / atom_block(n)), atom_block(n), 0, (cudaStream_t)stream>>>(momenta, grad, system, dt,
                                                                              scale, n);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
@@ -70,7 +87,7 @@ extern "C" int32_t kups_md_drift(double *positions, const double *momenta, const
                                  double scale, int64_t n, void *stream) {
   if (n < 0) return KUPS_ERR_INVALID;
   if (n == 0) return KUPS_OK;
-  drift_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(positions, momenta, masses,
+  drift_kernel<<<(unsigned)((n + atom_block(n) - 1) / atom_block(n)), atom_block(n), 0, (cudaStream_t)stream>>>(positions, momenta, masses,
                                                                               system, dt, tril, scale, n);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
@@ -80,7 +97,7 @@ extern "C" int32_t kups_md_thermostat(double *momenta, const double *masses, con
                                       uint64_t seed, uint64_t step, int64_t n, void *stream) {
   if (n < 0) return KUPS_ERR_INVALID;
   if (n == 0) return KUPS_OK;
-  thermostat_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+  thermostat_kernel<<<(unsigned)((n + atom_block(n) - 1) / atom_block(n)), atom_block(n), 0, (cudaStream_t)stream>>>(
       momenta, masses, system, dt, kT, friction, seed, step, n);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
