@@ -123,7 +123,7 @@ __device__ inline float2 cmul(float2 a, float2 b) {
 // chunk in float32, then adds it to S in float64.
 __global__ void structure_factor_kernel(const double *pos, const double *q, const int32_t *sys_offset,
                                         const int32_t *kn, int32_t nk, const RecipSys *sysp,
-                                        double *sk) {
+                                        double *sk, double *grad) {
   __shared__ float2 tab[kAtomsPerChunk][3 * kTab];
   __shared__ float qs[kAtomsPerChunk];
   const int s = blockIdx.z;
@@ -138,6 +138,9 @@ __global__ void structure_factor_kernel(const double *pos, const double *q, cons
     frac64(P.inv, r, f);
     fill_tables(tab[t], f);
     qs[t] = (float)q[c0 + t];
+    // the force kernel adds its k-range partials into grad: zero this chunk's rows first
+    if (blockIdx.x == 0 && grad != nullptr)
+      for (int a = 0; a < 3; ++a) grad[3 * (int64_t)(c0 + t) + a] = 0.0;
   }
   __syncthreads();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,7 +222,8 @@ __global__ void recip_energy_kernel(const int32_t *kn, int32_t nk, const double 
 // staged through shared memory), plus the sum_i f_ia F_ib part of dE/dL.
 __global__ void recip_force_kernel(const double *pos, const double *q, const int32_t *sys_offset,
                                    const int32_t *kn, int32_t nk, const RecipSys *sysp,
-                                   const Coef *coef, double ke, double *grad, double *dtril) {
+                                   const Coef *coef, double ke, double *grad, double *dtril,
+                                   int kblocks_per_split) {
   __shared__ float2 tab[kAtomsPerChunk][3 * kTab];
   __shared__ float4 kc[kKPerBlock];  // (P S_c, P S_s, -, -) as float
   __shared__ int4 kni[kKPerBlock];
@@ -241,7 +245,10 @@ __global__ void recip_force_kernel(const double *pos, const double *q, const int
   __syncthreads();
   // gradient in fractional components: dE/df_a = sum_k 2 K q P 2 pi n_a (Ss c - Sc s)
   float g0 = 0.f, g1 = 0.f, g2 = 0.f;
-  for (int kb = 0; kb < nk; kb += kKPerBlock) {
+  // this block's share of the k vectors (blockIdx.z); partials are added into grad
+  const int kbeg = blockIdx.z * kblocks_per_split * kKPerBlock;
+  const int kfin = min(nk, kbeg + kblocks_per_split * kKPerBlock);
+  for (int kb = kbeg; kb < kfin; kb += kKPerBlock) {
     __syncthreads();
     for (int j = threadIdx.x; j < kKPerBlock; j += blockDim.x) {
       if (kb + j < nk) {
@@ -256,7 +263,7 @@ __global__ void recip_force_kernel(const double *pos, const double *q, const int
     }
     __syncthreads();
     if (atom < na) {
-      const int kend = min(kKPerBlock, nk - kb);
+      const int kend = min(kKPerBlock, kfin - kb);
       for (int j = sub; j < kend; j += 4) {
         const int4 n3 = kni[j];
         const float2 e = cmul(cmul(tab[atom][n3.x + kMaxM], tab[atom][kTab + n3.y + kMaxM]),
@@ -285,9 +292,15 @@ __global__ void recip_force_kernel(const double *pos, const double *q, const int
     const double *iv = P.inv;
     const double gr[3] = {df[0] * iv[0], df[0] * iv[1] + df[1] * iv[2],
                           df[0] * iv[3] + df[1] * iv[4] + df[2] * iv[5]};
-    grad[3 * (int64_t)i] = gr[0];
-    grad[3 * (int64_t)i + 1] = gr[1];
-    grad[3 * (int64_t)i + 2] = gr[2];
+    if (kblocks_per_split > 0) {  // k-range partials; the structure-factor kernel zeroed grad
+      atomicAdd(&grad[3 * (int64_t)i], gr[0]);
+      atomicAdd(&grad[3 * (int64_t)i + 1], gr[1]);
+      atomicAdd(&grad[3 * (int64_t)i + 2], gr[2]);
+    } else {  // no k vectors (no structure-factor launch): write the zero gradient
+      grad[3 * (int64_t)i] = gr[0];
+      grad[3 * (int64_t)i + 1] = gr[1];
+      grad[3 * (int64_t)i + 2] = gr[2];
+    }
     // fractional coordinates of atom i (recomputed: the table owner is lane `atom`)
     const double r[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
     double fi[3];
@@ -689,6 +702,17 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+inline int recip_sm_count() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
 }  // namespace
 }  // namespace kups
 
@@ -721,17 +745,27 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
   if (n_kvecs > 0 && chunks > 0) {
     dim3 g((n_kvecs + kKPerBlock - 1) / kKPerBlock, chunks, n_systems);
     structure_factor_kernel<<<g, kKPerBlock, 0, stream>>>(positions, charges, sys_offset, kvec_n,
-                                                          n_kvecs, sysp, structure_factor);
+                                                          n_kvecs, sysp, structure_factor, grad);
   }
   KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
   if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * (size_t)n_systems, stream));
   recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 255) / 256), n_systems), 256, 0, stream>>>(
       kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, grad_tril);
-  if (chunks > 0) {
-    dim3 g(chunks, n_systems);
+  if (chunks > 0 && n_kvecs > 0) {
+    // enough k splits that the launch holds about 16 warps per SM
+    const int kblocks = (n_kvecs + kKPerBlock - 1) / kKPerBlock;
+    const int want = std::max(1, (16 * recip_sm_count()) / std::max(1, 4 * chunks * n_systems));
+    const int splits = std::min(kblocks, want);
+    const int per = (kblocks + splits - 1) / splits;
+    dim3 g(chunks, n_systems, (kblocks + per - 1) / per);
     recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
                                                              n_kvecs, sysp, coef, coulomb_k, grad,
-                                                             grad_tril);
+                                                             grad_tril, per);
+  } else if (chunks > 0) {
+    dim3 g(chunks, n_systems, 1);
+    recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
+                                                             n_kvecs, sysp, coef, coulomb_k, grad,
+                                                             grad_tril, 0);
   }
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
@@ -799,17 +833,27 @@ extern "C" int32_t kups_ewald_recip_static(const double *positions, const double
   if (n_kvecs > 0 && chunks > 0) {
     dim3 g((n_kvecs + kKPerBlock - 1) / kKPerBlock, chunks, n_systems);
     structure_factor_kernel<<<g, kKPerBlock, 0, stream>>>(positions, charges, sys_offset, kvec_n,
-                                                          n_kvecs, sysp, structure_factor);
+                                                          n_kvecs, sysp, structure_factor, grad);
   }
   KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
   if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * (size_t)n_systems, stream));
   recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 255) / 256), n_systems), 256, 0, stream>>>(
       kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, grad_tril);
-  if (chunks > 0) {
-    dim3 g(chunks, n_systems);
+  if (chunks > 0 && n_kvecs > 0) {
+    // enough k splits that the launch holds about 16 warps per SM
+    const int kblocks = (n_kvecs + kKPerBlock - 1) / kKPerBlock;
+    const int want = std::max(1, (16 * recip_sm_count()) / std::max(1, 4 * chunks * n_systems));
+    const int splits = std::min(kblocks, want);
+    const int per = (kblocks + splits - 1) / splits;
+    dim3 g(chunks, n_systems, (kblocks + per - 1) / per);
     recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
                                                              n_kvecs, sysp, coef, coulomb_k, grad,
-                                                             grad_tril);
+                                                             grad_tril, per);
+  } else if (chunks > 0) {
+    dim3 g(chunks, n_systems, 1);
+    recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
+                                                             n_kvecs, sysp, coef, coulomb_k, grad,
+                                                             grad_tril, 0);
   }
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
