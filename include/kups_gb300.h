@@ -300,8 +300,10 @@ int32_t kups_lj_ewald_real_forces(const double *positions, const double *charges
  * kups_lj_ewald_real_forces, with positions first stored in `workspace` as float
  * pairs hi = fl(x), lo = fl(x - hi) (differences (hj - hi) + (lj - li) keep float32
  * relative accuracy with no float64 arithmetic) and the pair terms evaluated only for
- * the partners a lane found inside the cutoff among 32 tested.  A system with more
- * than max_atoms_per_system atoms records KUPS_ERR_INVALID and is skipped.
+ * the partners a lane found inside the cutoff among 32 tested.  terms & 8 adds the
+ * energy and gradient onto the caller's (e.g. the reciprocal-space result) instead
+ * of writing them.  A system with more than max_atoms_per_system atoms records
+ * KUPS_ERR_INVALID and is skipped.
  * Workspace: kups_lj_ewald_real_forces_workspace_bytes(n_systems, max_atoms). */
 size_t kups_lj_ewald_real_forces_workspace_bytes(int32_t n_systems, int32_t max_atoms_per_system);
 int32_t kups_lj_ewald_real_forces_packed(const double *positions, const double *charges,

@@ -692,9 +692,15 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
       gy += part[k][slot][1];
       gz += part[k][slot][2];
     }
-    grad[3 * gi] = gx;
-    grad[3 * gi + 1] = gy;
-    grad[3 * gi + 2] = gz;
+    if (terms & 8) {  // add onto the caller's gradient (this block owns atom gi)
+      grad[3 * gi] += gx;
+      grad[3 * gi + 1] += gy;
+      grad[3 * gi + 2] += gz;
+    } else {
+      grad[3 * gi] = gx;
+      grad[3 * gi + 1] = gy;
+      grad[3 * gi + 2] = gz;
+    }
   }
   const double esum = block_sum(0.5 * (double)ef, red);
   if (threadIdx.x == 0) atomicAdd(&energy[s], esum);
@@ -749,7 +755,8 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
   }
   KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
   if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * (size_t)n_systems, stream));
-  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 255) / 256), n_systems), 256, 0, stream>>>(
+  // one warp per block: the per-k float64 exp and divisions spread over many SMs
+  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 31) / 32), n_systems), 32, 0, stream>>>(
       kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, grad_tril);
   if (chunks > 0 && n_kvecs > 0) {
     // enough k splits that the launch holds about 16 warps per SM
@@ -837,7 +844,8 @@ extern "C" int32_t kups_ewald_recip_static(const double *positions, const double
   }
   KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
   if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * (size_t)n_systems, stream));
-  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 255) / 256), n_systems), 256, 0, stream>>>(
+  // one warp per block: the per-k float64 exp and divisions spread over many SMs
+  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 31) / 32), n_systems), 32, 0, stream>>>(
       kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, grad_tril);
   if (chunks > 0 && n_kvecs > 0) {
     // enough k splits that the launch holds about 16 warps per SM
@@ -933,11 +941,11 @@ extern "C" int32_t kups_lj_ewald_real_forces_packed(const double *positions, con
                                                     double *energy, double *grad, void *workspace,
                                                     size_t workspace_bytes, kups_status *status, void *stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
-  if (n_systems < 0 || max_atoms_per_system < 0 || terms < 1 || terms > 3) return KUPS_ERR_INVALID;
+  if (n_systems < 0 || max_atoms_per_system < 0 || (terms & ~11) != 0 || (terms & 3) == 0) return KUPS_ERR_INVALID;
   if ((terms & 1) && (n_species < 1 || n_species > 8 || lj_sigma == nullptr || lj_epsilon == nullptr))
     return KUPS_ERR_INVALID;
   if (n_systems == 0) return KUPS_OK;
-  KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
+  if (!(terms & 8)) KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
   if (max_atoms_per_system == 0) return KUPS_OK;
   if (workspace == nullptr ||
       workspace_bytes < kups_lj_ewald_real_forces_workspace_bytes(n_systems, max_atoms_per_system))

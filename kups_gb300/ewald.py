@@ -29,6 +29,7 @@ from .potential import PositionAndUnitCell, PotentialOut
 from .units import BOLTZMANN_CONSTANT, TO_STANDARD_UNITS
 
 TERM_LJ, TERM_EWALD_REAL, TERM_VACUUM = 1, 2, 4
+TERM_ACCUMULATE = 8  # kups_lj_ewald_real_forces_packed: add onto energy / grad
 
 
 # ----------------------------------------------------------------------------- host-side setup
@@ -353,18 +354,17 @@ class LJEwaldMD:
         if self.allpairs:
             terms = TERM_EWALD_REAL | (TERM_LJ if self.lj else 0)
             nsp = int(self.sig.shape[0]) if self.lj else 1
+            # reciprocal space writes energy and grad; real space adds onto them
+            ewald_recip(pos, self.q, self.off, self.max_atoms, self.tril, self.kn, self.alpha, grad_tril=False,
+                        ws=self.rws, out=(self.energy, self.grad, self.t_rec, self.sk), status=self.status)
             rc = lib.kups_lj_ewald_real_forces_packed(
                 pos.data_ptr(), self.q.data_ptr(), self.species.data_ptr(), self.off.data_ptr(), self.s,
                 self.max_atoms, self.tril.data_ptr(), self.sig.data_ptr() if self.lj else None,
                 self.eps.data_ptr() if self.lj else None, nsp, self.rc_lj.data_ptr() if self.lj else None,
-                self.alpha.data_ptr(), self.rc_ew.data_ptr(), TO_STANDARD_UNITS, terms, self.e_pair.data_ptr(),
-                self.g_pair.data_ptr(), self.real_ws.data_ptr(), self.real_ws.numel(), self.status.data_ptr(),
-                _stream())
+                self.alpha.data_ptr(), self.rc_ew.data_ptr(), TO_STANDARD_UNITS, terms | TERM_ACCUMULATE,
+                self.energy.data_ptr(), self.grad.data_ptr(), self.real_ws.data_ptr(), self.real_ws.numel(),
+                self.status.data_ptr(), _stream())
             _lib.check(rc, "kups_lj_ewald_real_forces_packed")
-            ewald_recip(pos, self.q, self.off, self.max_atoms, self.tril, self.kn, self.alpha, grad_tril=False,
-                        ws=self.rws, out=(self.e_rec, self.g_rec, self.t_rec, self.sk), status=self.status)
-            torch.add(self.g_pair, self.g_rec, out=self.grad)
-            torch.add(self.e_pair, self.e_rec, out=self.energy)
             self.energy.add_(self.e_self)
             return
         rc = lib.kups_neighborlist_build(pos.data_ptr(), self.system.data_ptr(), self.incl.data_ptr(),

@@ -208,6 +208,18 @@ def test_allpairs_real_space_matches_edge_sum(binned):
     g = gl + ge
     rms = np.sqrt(np.mean((gr.cpu().numpy() - g) ** 2) / np.mean(g**2))
     assert rms < 1e-5, rms
+    if binned:  # terms & 8: added onto the caller's energy and gradient
+        e1, g1 = en.clone(), gr.clone()
+        en.fill_(1.0)
+        gr.fill_(1.0)
+        lib.kups_lj_ewald_real_forces_packed(
+            args[0].data_ptr(), args[1].data_ptr(), args[2].data_ptr(), off.data_ptr(), 2, mx, args[4].data_ptr(),
+            args[5].data_ptr(), args[6].data_ptr(), 2, args[7].data_ptr(), args[8].data_ptr(), args[7].data_ptr(),
+            KE, TERM_LJ | TERM_EWALD_REAL | 8, en.data_ptr(), gr.data_ptr(), ws.data_ptr(), ws.numel(),
+            st.data_ptr(), stream)
+        torch.cuda.synchronize()
+        torch.testing.assert_close(en - 1.0, e1, rtol=1e-12, atol=1e-9)
+        torch.testing.assert_close(gr - 1.0, g1, rtol=1e-6, atol=1e-9)
     # cutoff above half the narrowest width: refused, status records it
     st2 = new_status()
     big = cuda(np.array([9.9, 10.0]))
