@@ -434,7 +434,7 @@ def run_ewald_md(a):
     """LJ + Ewald NVE MD of the ionic melt: 2000 (+1 e) + 2000 (-1 e) ions in a 40 A cube,
     LB-mixed LJ (0.1 / 0.15 kcal/mol, 2.35 / 4.40 A), rc 12 A, alpha 0.3, |n| <= 8 k vectors
     in the reference's half-space layout, dt 1 fs, velocity Verlet; one step is captured
-    once as a CUDA graph and replayed.  Device-timed over 500 steps after 20."""
+    once as a CUDA graph and replayed.  Device-timed over 1000 steps after 20."""
     import torch
 
     from kups_gb300 import ewald, workloads
@@ -448,7 +448,7 @@ def run_ewald_md(a):
     sim.run(20)
     torch.cuda.synchronize()
     e0 = float((sim.energy + sim.kinetic_energy()).item())
-    steps = 500
+    steps = 1000
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0.record()
     sim.run(steps)
@@ -461,7 +461,28 @@ def run_ewald_md(a):
     return {"workload": f"ionic melt: {n} ions, 40 A cube, LJ + Ewald (alpha 0.3, rc 12 A, |n| <= 8), NVE dt 1 fs",
             "value": n * steps / (ms / 1e3), "unit": "atom-steps/s", "ms_per_step": ms / steps, "steps": steps,
             "relative_energy_change": (e1 - e0) / abs(e0),
-            "real_space": "all pairs, no list" if sim.allpairs else "neighbour list every step"}
+            "real_space": ("all pairs (float hi/lo positions, per-warp hit queue), no list" if sim.allpairs
+                           else "neighbour list every step"),
+            "fp32_roofline": ewald_fp32_roofline(W, n * steps / (ms / 1e3))}
+
+
+def ewald_fp32_roofline(W, atom_steps_per_s):
+    """FP32 work per atom-step of the LJ + Ewald step: half-list pairs within the cutoff x 70 flop
+    (LJ 30 + erfc / exp 40) plus, per k vector, about 10 flop for the structure factor and 10 for
+    the force (two complex products and the accumulation); peak derived from the SM count and
+    the maximum SM clock (152 x 128 lanes x 2 flop x 2070 MHz on GB300)."""
+    import torch
+
+    n = len(W.charges)
+    vol = abs(float(np.prod(np.asarray(W.tril).reshape(-1, 6)[0, [0, 2, 5]])))
+    n_half = 4.0 / 3.0 * math.pi * W.cutoff**3 * n / vol / 2.0
+    n_k = int(np.asarray(W.kvec_n).shape[1])
+    flop = n_half * 70.0 + n_k * 20.0
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    peak = sms * 128 * 2 * 2070e6 / 1e12
+    achieved = atom_steps_per_s * flop / 1e12
+    return {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "flop_per_atom_step": flop, "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x 2070 MHz"}
 
 
 def run_gcmc(a):
