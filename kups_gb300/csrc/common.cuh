@@ -183,6 +183,25 @@ __device__ inline double block_sum(double v, double *scratch) {
   return r;
 }
 
+// Block-wide sum of per-thread float partials, returned to every thread as a double:
+// warps add in float, warp 0 adds the warp partials in double (float64 issue is
+// scarce on this part, so a double shuffle tree over the whole block is avoided).
+// `scratch` holds at least 33 doubles; two __syncthreads() inside.
+__device__ inline double block_sum_f(float v, double *scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  if (lane == 0) scratch[wid] = (double)v;
+  __syncthreads();
+  if (wid == 0) {
+    double s = lane < nw ? scratch[lane] : 0.0;
+    s = warp_sum(s);
+    if (lane == 0) scratch[32] = s;
+  }
+  __syncthreads();
+  return scratch[32];
+}
+
 // Block-wide exclusive scan; returns this thread's exclusive prefix and writes
 // the block total to *total.  `scratch` holds at least 32 T; two
 // __syncthreads() inside, and the caller syncs before reusing `scratch`.

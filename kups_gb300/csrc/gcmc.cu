@@ -309,6 +309,8 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
   const float ke = (float)a.coulomb_k;
   const double kT = a.kT[s];
   const double volume = fabs(a.tril[6 * (int64_t)s] * a.tril[6 * (int64_t)s + 2] * a.tril[6 * (int64_t)s + 5]);
+  const double inv_kT = 1.0 / kT;
+  const double lnfv = a.log_activity[s] + log(volume);  // ln(f V / kT), once per launch
   const int fw0 = a.fw_start[s], fwn = a.fw_count[s];
   float4 *gpos = reinterpret_cast<float4 *>(a.guest_pos) + (int64_t)s * a.max_mol * apm;
   const float4 *motif = reinterpret_cast<const float4 *>(a.motif_pos);
@@ -608,7 +610,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
       e_acc += sign * pair_images(Lf, fa, fb, __float_as_int(pa.w), __float_as_int(pb.w), sh.q[ia] * sh.q[ib], lj,
                                   nsp, li, ei, alpha, ke, true);
     }
-    const double de_real = block_sum((double)e_acc, red);
+    const double de_real = block_sum_f(e_acc, red);
     // ---------------------------------------------------------------- reciprocal space
     // per-k terms in float32 (|term| <~ 15 eV: ~1e-6 eV rounding each), the k sum of a
     // thread in float32, the block sum and S(k) itself in float64
@@ -645,7 +647,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
       de_rec_f = fmaf(pkk.x, fmaf(2.f, fmaf(sck.x, dc, sck.y * ds), fmaf(dc, dc, ds * ds)), de_rec_f);
     }
     __syncthreads();
-    const double de_rec = block_sum((double)de_rec_f, red) * a.coulomb_k;
+    const double de_rec = block_sum_f(de_rec_f, red) * a.coulomb_k;
     // ---------------------------------------------------------------- acceptance (thread 0)
     if (tid == 0) {
       double de = de_real + de_rec;
@@ -667,10 +669,10 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
           de += tail_energy(c1, nsp, tc) - tail_energy(c0, nsp, tc);
         }
       }
-      double logp = -de / kT + sh.ln_ratio;
+      double logp = -de * inv_kT + sh.ln_ratio;
       if (n_new != n_old) {
-        const double lnfv = a.log_activity[s] + log(volume);
-        logp += (n_new - n_old) * lnfv + lgamma((double)n_old + 1.0) - lgamma((double)n_new + 1.0);
+        // ln n_old! - ln n_new! for n_new = n_old +- 1 is -ln n_new (insert) or +ln n_old (delete)
+        logp += (n_new - n_old) * lnfv + (n_new > n_old ? -log((double)n_new) : log((double)n_old));
       }
       const U4 r4 = rng4(a.seed, 1 + (uint64_t)s, 8 * ctr + 4);
       const double u = ((double)(r4.w >> 8) + 1.0) * (1.0 / 16777216.0);  // (0, 1]
