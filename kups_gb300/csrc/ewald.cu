@@ -665,14 +665,15 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
       const float dx = (f0 * L[0] + f1 * L[1]) + f2 * L[3], dy = f1 * L[2] + f2 * L[4], dz = f2 * L[5];
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
       float dedr2 = 0.f;
+      const float ir = rsqrtf(r2);  // a few ulp; one MUFU op instead of IEEE sqrt and divisions
       if ((terms & 1) && r2 < rc2_lj) {
         const float2 c = ljt[__float_as_int(lo_a.w) * nsp + __float_as_int(lj.w)];
-        const float inv = 1.f / r2, s2 = c.x * inv, c6 = s2 * s2 * s2;
+        const float inv = ir * ir, s2 = c.x * inv, c6 = s2 * s2 * s2;
         ef += c.y * (c6 * c6 - c6);
         dedr2 += -0.5f * c.y * c6 * (12.f * c6 - 6.f) * inv;
       }
       if ((terms & 2) && r2 < rc2_ew) {
-        const float r = sqrtf(r2), ir = 1.f / r, qq = (hi_a.w * kef) * hj.w;
+        const float r = r2 * ir, qq = (hi_a.w * kef) * hj.w;
         const float er = erfcf(al * r);
         ef += qq * er * ir;
         dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * expf(-al * al * r2) * ir);

@@ -145,16 +145,19 @@ __device__ inline void qrot(const float q[4], const float v[3], float o[3]) {
 __device__ inline float pair_u(float r2, int ti, int tj, float qq, const float2 *lj, int nsp,
                                const ImgCfg &lj_img, const ImgCfg &ew_img, float alpha, float ke,
                                bool in_lj, bool in_ew) {
+  // one reciprocal square root serves both terms (a few ulp; IEEE division and square
+  // root would each cost a multi-instruction sequence per pair)
+  const float ir = rsqrtf(r2);
   float e = 0.f;
   if (in_lj && r2 < lj_img.rc2) {
     const float2 c = lj[ti * nsp + tj];
-    const float s2 = c.x / r2;
+    const float s2 = c.x * (ir * ir);
     const float c6 = s2 * s2 * s2;
     e += c.y * (c6 * c6 - c6);
   }
   if (in_ew && r2 < ew_img.rc2 && qq != 0.f) {
-    const float r = sqrtf(r2);
-    e += ke * qq * erfcf(alpha * r) / r;
+    const float r = r2 * ir;
+    e += ke * qq * erfcf(alpha * r) * ir;
   }
   return e;
 }
