@@ -101,3 +101,31 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_host_side_validation_of_newer_entry_points():
+    """Arguments the library refuses before touching the device: an unknown bonded kind, an
+    unknown MD integrator, a CSVR / NPT call without its thermostat or cell buffers, lanes per
+    atom other than 1, 2 or 4, and undefined real-space term bits."""
+    import ctypes as C
+
+    from kups_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.kups_bonded_order(2) == 3 and lib.kups_bonded_param_count(4) == 3
+    assert lib.kups_bonded_order(6) == -1
+    assert lib.kups_bonded_edges(6, None, None, None, 0, None, 0, None, None, 1, None, 1, None, None, None, None,
+                                 None) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_bonded_edges(0, None, None, None, 0, None, 0, None, None, 0, None, 1, None, None, None, None,
+                                 None) == _lib.KUPS_OK  # no edges: nothing to do
+    a = _lib.MdArgs()
+    a.n_systems, a.n_species, a.n_steps, a.neighbor_capacity = 1, 1, 1, 64
+    for integrator, fields in ((4, {}), (2, {}), (3, {"thermostat_tau": 8})):
+        a.integrator = integrator
+        for k, v in fields.items():
+            setattr(a, k, v)
+        assert lib.kups_lj_md_run(C.byref(a), None, 0, None, None) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_lj_ewald_real_forces_packed(None, None, None, None, 1, 1, None, None, None, 1, None, None, None,
+                                                1.0, 4, None, None, None, 0, None, None) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_lj_ewald_real_forces_packed(None, None, None, None, 1, 1, None, None, None, 1, None, None, None,
+                                                1.0, 2 | 16, None, None, None, 0, None, None) == _lib.KUPS_ERR_INVALID
