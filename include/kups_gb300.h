@@ -315,6 +315,11 @@ int32_t kups_lj_ewald_real_forces_packed(const double *positions, const double *
                                          const double *ewald_cutoff, double coulomb_k, int32_t terms,
                                          double *energy, double *grad, void *workspace,
                                          size_t workspace_bytes, kups_status *status, void *stream);
+/* kups_erfc_eval: out[i] = erfc(x[i]) for x >= 0 (float32) by the library's pair-term
+ * erfc, the Chebyshev-fitted formula of Numerical Recipes in C (2nd ed., section 6.2),
+ * fractional error below 1.2e-7 in exact arithmetic; exposed so its accuracy can be
+ * checked against a float64 erfc. */
+int32_t kups_erfc_eval(const float *x, int64_t n, float *out, void *stream);
 int32_t kups_pair_edges(const double *positions, const int32_t *system, const int32_t *species,
                         const double *charges, int64_t n_particles, const double *tril,
                         int32_t n_systems, const double *lj_sigma, const double *lj_epsilon,

@@ -152,6 +152,27 @@ __device__ inline float warp_sum(float v) {
   return v;
 }
 
+// erfc(x) for x >= 0 by the Chebyshev-fitted formula of Numerical Recipes in C, 2nd ed.,
+// section 6.2 ("erfcc"): t = 1 / (1 + x / 2), erfc(x) = t exp(-x^2 + P(t)) with a degree-9
+// polynomial P; fractional error below 1.2e-7 everywhere in exact arithmetic (float32
+// evaluation adds a few ulp plus |x^2| * 2^-24 through the exponential).  One reciprocal,
+// nine FMAs and one fast exponential.
+__device__ __forceinline__ float erfc_cheb(float x) {
+  float t;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(t) : "f"(fmaf(0.5f, x, 1.0f)));  // 1 ulp
+  float p = 0.17087277f;
+  p = fmaf(p, t, -0.82215223f);
+  p = fmaf(p, t, 1.48851587f);
+  p = fmaf(p, t, -1.13520398f);
+  p = fmaf(p, t, 0.27886807f);
+  p = fmaf(p, t, -0.18628806f);
+  p = fmaf(p, t, 0.09678418f);
+  p = fmaf(p, t, 0.37409196f);
+  p = fmaf(p, t, 1.00002368f);
+  p = fmaf(p, t, -1.26551223f);
+  return t * __expf(fmaf(-x, x, p));
+}
+
 // arr[sys * stride + comp] += v from every lane of a full warp (sys < 0: nothing);
 // one atomic per warp when the whole warp works on one system.
 __device__ inline void add_system(double *arr, int stride, int comp, int sys, double v) {

@@ -674,9 +674,9 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
       }
       if ((terms & 2) && r2 < rc2_ew) {
         const float r = r2 * ir, qq = (hi_a.w * kef) * hj.w;
-        const float er = erfcf(al * r);
+        const float er = erfc_cheb(al * r);
         ef += qq * er * ir;
-        dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * expf(-al * al * r2) * ir);
+        dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * __expf(-al * al * r2) * ir);
       }
       float *pp = part[warp * 2 + h][sl];
       atomicAdd(pp, -2.f * dedr2 * dx);
@@ -962,5 +962,21 @@ extern "C" int32_t kups_lj_ewald_real_forces_packed(const double *positions, con
   real_packed_kernel<<<g, 32 * kRealWarps, 0, stream>>>(sys_offset, tril, lj_sigma, lj_epsilon, n_species, lj_cutoff,
                                                         alpha, ewald_cutoff, coulomb_k, terms, max_atoms_per_system,
                                                         hi, lo, energy, grad, status);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+namespace kups {
+namespace {
+__global__ void erfc_eval_kernel(const float *x, int64_t n, float *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = erfc_cheb(x[i]);
+}
+}  // namespace
+}  // namespace kups
+
+extern "C" int32_t kups_erfc_eval(const float *x, int64_t n, float *out, void *stream) {
+  if (n < 0) return KUPS_ERR_INVALID;
+  if (n == 0) return KUPS_OK;
+  erfc_eval_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, n, out);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

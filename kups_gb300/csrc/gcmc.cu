@@ -157,7 +157,7 @@ __device__ inline float pair_u(float r2, int ti, int tj, float qq, const float2 
   }
   if (in_ew && r2 < ew_img.rc2 && qq != 0.f) {
     const float r = r2 * ir;
-    e += ke * qq * erfcf(alpha * r) * ir;
+    e += ke * qq * erfc_cheb(alpha * r) * ir;
   }
   return e;
 }
