@@ -425,20 +425,30 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_allpairs_kernel(
   const int s = blockIdx.y;
   const int a0 = sys_offset[s], n = sys_offset[s + 1] - a0;
   if ((int)blockIdx.x * kRealAtoms >= n) return;  // uniform over the block
-  const Tril64 L64 = load_tril64(tril + 6 * (int64_t)s);
-  const Tril64 I64 = inverse_tril64(L64);
-  double w[3];
-  perpendicular_widths64(L64, w);
+  // cell, inverse and widths once per block (float64 is scarce on this part)
+  __shared__ float cellf[12];
+  __shared__ int refused;
+  if (threadIdx.x == 0) {
+    const Tril64 L64 = load_tril64(tril + 6 * (int64_t)s);
+    const Tril64 I64 = inverse_tril64(L64);
+    double w[3];
+    perpendicular_widths64(L64, w);
+    const double rm = fmax((terms & 1) ? rc_lj[s] : 0.0, (terms & 2) ? rc_ew[s] : 0.0);
+    refused = fmin(w[0], fmin(w[1], w[2])) < 2.0 * rm;
+    if (refused) status_error(status, KUPS_ERR_UNSUPPORTED, s);
+    for (int k = 0; k < 6; ++k) {
+      cellf[k] = (float)L64.t[k];
+      cellf[6 + k] = (float)I64.t[k];
+    }
+  }
+  __syncthreads();
+  if (refused) return;
   const double rlj = (terms & 1) ? rc_lj[s] : 0.0, rew = (terms & 2) ? rc_ew[s] : 0.0;
   const double rmax = fmax(rlj, rew);
-  if (fmin(w[0], fmin(w[1], w[2])) < 2.0 * rmax) {
-    if (threadIdx.x == 0) status_error(status, KUPS_ERR_UNSUPPORTED, s);
-    return;
-  }
   float L[6], I[6];
   for (int k = 0; k < 6; ++k) {
-    L[k] = (float)L64.t[k];
-    I[k] = (float)I64.t[k];
+    L[k] = cellf[k];
+    I[k] = cellf[6 + k];
   }
   if ((terms & 1) && nsp * nsp <= 64)
     for (int k = threadIdx.x; k < nsp * nsp; k += blockDim.x) {
@@ -473,17 +483,18 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_allpairs_kernel(
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     if (r2 >= rc2 || j == il || !act) continue;
     float dedr2 = 0.f;  // dE/d(r^2) of the pair
+    const float ir = rsqrtf(r2);
     if ((terms & 1) && r2 < rc2_lj) {
       const float2 c = ljt[ti * nsp + species[gj]];
-      const float inv = 1.f / r2, s2 = c.x * inv, c6 = s2 * s2 * s2;
+      const float inv = ir * ir, s2 = c.x * inv, c6 = s2 * s2 * s2;
       ef += c.y * (c6 * c6 - c6);
       dedr2 += -0.5f * c.y * c6 * (12.f * c6 - 6.f) * inv;
     }
     if ((terms & 2) && r2 < rc2_ew) {
-      const float r = sqrtf(r2), ir = 1.f / r, qq = qi * (float)q[gj];
-      const float er = erfcf(al * r);
+      const float r = r2 * ir, qq = qi * (float)q[gj];
+      const float er = erfc_cheb(al * r);
       ef += qq * er * ir;
-      dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * expf(-al * al * r2) * ir);
+      dedr2 += 0.5f * ir * qq * (-er * ir * ir - two_al_rsqrtpi * __expf(-al * al * r2) * ir);
     }
     // d = x_j - x_i: dE/dx_i = -2 dE/d(r^2) d for this ordered pair (both halves)
     fx = fmaf(-2.f * dedr2, dx, fx);
