@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-ewald", action="store_true", help="skip the LJ + Ewald MD (ionic melt) section")
     ap.add_argument("--no-ensembles", action="store_true", help="skip the BAOAB / CSVR / NPT comparison")
     ap.add_argument("--no-autotune", action="store_true", help="library-default launch shape for the MD kernel")
+    ap.add_argument("--no-bonded", action="store_true", help="skip the bonded-term and local-MLIAP timings")
     ap.add_argument("--gcmc-replicas", type=int, default=1024)
     ap.add_argument("--strong", action="store_true",
                     help="split one --systems batch across the ranks (cost-balanced contiguous ranges) "
@@ -352,6 +353,9 @@ def run_ours(a):
     if rank == 0 and not a.no_ewald:
         line["argon_nvt"] = run_argon(a, torch)
         line["lj_ewald_md"] = run_ewald_md(a)
+    if rank == 0 and not a.no_bonded:
+        line["bonded"] = run_bonded(a)
+        line["local_mliap"] = run_mliap(a)
     if rank == 0 and not a.no_gcmc:
         line["gcmc"] = run_gcmc(a)
     if rank == 0:
@@ -400,6 +404,121 @@ def run_ensembles(a, W, torch, steps=200):
         out["atom_steps_per_s"][name] = W.n_atoms / (ms / 1e3)
         del packed, prop
     return out
+
+
+def _chains(n_systems=2048, n_per=256, seed=7):
+    """Seeded chain molecules: a random walk of 1.5 A steps per system in a 40 A cube."""
+    rng = np.random.default_rng(seed)
+    steps = rng.normal(size=(n_systems, n_per, 3))
+    steps *= 1.5 / np.linalg.norm(steps, axis=-1, keepdims=True)
+    pos = np.cumsum(steps, axis=1) + rng.uniform(0, 40, (n_systems, 1, 3))
+    return pos.reshape(-1, 3), np.repeat(np.arange(n_systems), n_per), n_per
+
+
+def run_bonded(a, reps=20):
+    """Bonded terms on 2048 chain molecules of 256 atoms (524 288 atoms): harmonic bonds, harmonic
+    angles, dihedrals and inversions along each chain (about 5.2e5 edges of each kind), two
+    species, one kups_bonded_edges launch per kind, summed into one energy / gradient / cell-
+    gradient buffer.  Algorithmic bytes per edge: indices 4 B and species 4 B per atom, shifts
+    12 B per non-first atom, float64 positions 24 B read and gradient 24 B added per atom, the
+    parameter row; timed over `reps` evaluations."""
+    import torch
+
+    from kups_gb300 import bonded
+
+    pos, system, n_per = _chains()
+    S = int(system.max()) + 1
+    species = (np.arange(len(pos)) % 2).astype(np.int32)
+    tril = np.tile([40.0, 0, 40.0, 0, 0, 40.0], (S, 1))
+    base = (np.arange(S) * n_per)[:, None]
+    idx = lambda offs, lo, hi: (base + np.arange(lo, hi)[None, :])[..., None] + np.asarray(offs)
+    T = 2
+    terms = [
+        bonded.BondedTerm(bonded.HarmonicBondParameters(("A", "B"), np.full((T, T), 1.5), np.full((T, T), 2.0)),
+                          idx([0, 1], 0, n_per - 1).reshape(-1, 2)),
+        bonded.BondedTerm(bonded.HarmonicAngleParameters(("A", "B"), np.full((T,) * 3, 109.5), np.full((T,) * 3, 0.01)),
+                          idx([0, -1, 1], 1, n_per - 1).reshape(-1, 3)),
+        bonded.BondedTerm(bonded.DihedralParameters(("A", "B"), np.full((T,) * 4, 0.1), np.full((T,) * 4, 3.0),
+                                                    np.full((T,) * 4, np.pi)), idx([0, 1, 2, 3], 0, n_per - 3).reshape(-1, 4)),
+        bonded.BondedTerm(bonded.InversionParameters(("A", "B"), np.zeros((T,) * 4), np.full((T,) * 4, 0.05)),
+                          idx([0, -1, 1, 2], 1, n_per - 2).reshape(-1, 4)),
+    ]
+    bonded.evaluate(terms, pos, system, species, tril)  # warm-up, status checked
+    from kups_gb300 import _lib
+    from kups_gb300.neighborlist import new_status, read_status
+
+    dev = "cuda"
+    p = torch.as_tensor(pos, device=dev)
+    sy = torch.as_tensor(system, device=dev, dtype=torch.int32)
+    sp = torch.as_tensor(species, device=dev, dtype=torch.int32)
+    tr = torch.as_tensor(tril, device=dev)
+    energy = torch.zeros(S, dtype=torch.float64, device=dev)
+    grad = torch.zeros_like(p)
+    gtril = torch.zeros((S, 6), dtype=torch.float64, device=dev)
+    status = new_status()
+
+    def timed():
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            for t in terms:  # energies and gradients add up across terms and repetitions
+                t.add_to(p, sy, sp, tr, energy, grad, gtril, status)
+        e1.record()
+        torch.cuda.synchronize()
+        _lib.raise_status(read_status(status))
+        return e0.elapsed_time(e1) / reps
+
+    ms = timed()
+    for t in terms:
+        t.fp32 = True
+    ms32 = timed()
+    lib = _lib.load()
+    n_edges = sum(t._edges.shape[0] for t in terms)
+    nbytes = sum(t._edges.shape[0] * (t.order * (4 + 4 + 24 + 24) + 12 * (t.order - 1)
+                                     + 8 * lib.kups_bonded_param_count(t.parameters.kind)) for t in terms)
+    peak, kind = measured_peak()
+    gbs, gbs32 = nbytes / (ms / 1e3) / 1e9, nbytes / (ms32 / 1e3) / 1e9
+    return {"workload": f"{S} chains x {n_per} atoms: bonds, angles, dihedrals, inversions ({n_edges} edges)",
+            "ms_per_evaluation": ms, "edges_per_s": n_edges / (ms / 1e3),
+            "ms_per_evaluation_fp32": ms32, "edges_per_s_fp32": n_edges / (ms32 / 1e3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "peak_source": kind, "note": "float64 atomics into the gradient, four launches per "
+                                                      "evaluation, buffers allocated once"},
+            "roofline_fp32": {"bound": "hbm", "achieved": gbs32, "peak": peak, "unit": "GB/s",
+                              "frac": gbs32 / peak, "peak_source": kind,
+                              "note": "per-edge arithmetic in float32, sums in float64"}}
+
+
+def run_mliap(a, reps=10):
+    """Local MLIAP energy and forces (the reference's test model: embedding 0.1, message
+    h_j / (|d| + 1), linear readout) on 256 argon-like systems of 500 atoms at rc 5 A: graph by
+    kups_neighborlist_build, model and gradients in torch."""
+    import torch
+
+    from kups_gb300 import mliap, workloads
+
+    W = workloads.batched_uneven_lj(n_systems=256, n_min=500, n_max=500, seed=3)
+    emb = torch.full((3, 4), 0.1, dtype=torch.float64, device="cuda")
+    w = torch.full((4, 1), 0.1, dtype=torch.float64, device="cuda")
+    pot = mliap.LocalMLIAP(lambda z: emb[z], lambda h1, h2, d: h2 / (d.norm(dim=-1, keepdim=True) + 1.0),
+                           lambda h, m: ((h + m) @ w).squeeze(-1))
+    pos = torch.as_tensor(W.positions, device="cuda")
+    z = torch.zeros(W.n_atoms, dtype=torch.int64, device="cuda")
+    sy = torch.as_tensor(W.system, device="cuda")
+    tr = torch.as_tensor(W.tril, device="cuda")
+    cut = np.full(W.n_systems, 5.0)
+    pot.energy(pos, z, sy, tr, cut)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        res = pot.energy(pos, z, sy, tr, cut)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return {"workload": f"{W.n_systems} systems x 500 atoms, rc 5 A, reference test model", "ms_per_evaluation": ms,
+            "atoms_per_s": W.n_atoms / (ms / 1e3), "note": "energy + dE/dx + dE/dtril; graph on the device, model in torch"}
 
 
 def run_argon(a, torch):

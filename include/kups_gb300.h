@@ -347,16 +347,18 @@ int32_t kups_pair_edges(const double *positions, const int32_t *system, const in
  *   energy f64 [n_systems], grad f64 [n_particles, 3], grad_tril f64 [n_systems, 6]
  *          (may be NULL): ADDED to (zero them first), so several terms can share
  *          one buffer; an edge belongs to the system of its atom 0.
- * Float64 arithmetic; an edge with an index or species out of range records
- * KUPS_ERR_INVALID (first offending edge) and is skipped. */
+ * Difference vectors and all sums in float64; the per-edge energy and gradient in
+ * float64, or in float32 when fp32 != 0 (float32 relative error, about 1e-6 on the
+ * energies; float64 is slow on this part).  An edge with an index or species out of
+ * range records KUPS_ERR_INVALID (first offending edge) and is skipped. */
 int32_t kups_bonded_order(int32_t kind);
 int32_t kups_bonded_param_count(int32_t kind);
 int32_t kups_bonded_edges(int32_t kind, const double *positions, const int32_t *system,
                           const int32_t *species, int64_t n_particles, const double *tril,
                           int32_t n_systems, const int32_t *edges, const int32_t *shifts,
                           int64_t n_edges, const double *params, int32_t n_species,
-                          double *energy, double *grad, double *grad_tril, kups_status *status,
-                          void *stream);
+                          double *energy, double *grad, double *grad_tril, int32_t fp32,
+                          kups_status *status, void *stream);
 
 /* ------------------------------------------------------------------------
  * Integrator building blocks on the float64 particle table (systems larger

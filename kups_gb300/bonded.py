@@ -113,6 +113,7 @@ class BondedTerm:
     parameters: object
     edges: np.ndarray
     shifts: np.ndarray | None = None
+    fp32: bool = False  # per-edge arithmetic in float32 (sums and differences stay float64)
 
     def __post_init__(self):
         lib = _lib.load()
@@ -135,7 +136,7 @@ class BondedTerm:
             self.parameters.kind, positions.data_ptr(), system.data_ptr(), species.data_ptr(), positions.shape[0],
             tril.data_ptr(), tril.shape[0], self._edges.data_ptr(), self._shifts.data_ptr(), self._edges.shape[0],
             self._table.data_ptr(), self.n_species, energy.data_ptr(), grad.data_ptr(),
-            grad_tril.data_ptr() if grad_tril is not None else None, status.data_ptr(), _stream())
+            grad_tril.data_ptr() if grad_tril is not None else None, int(self.fp32), status.data_ptr(), _stream())
         _lib.check(rc, "kups_bonded_edges")
 
 

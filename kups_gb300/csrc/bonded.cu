@@ -13,9 +13,14 @@
 //   src/kups/core/neighborlist.py:164-204), E_e(v_1 .. v_{D-1}) with the
 //   parameter row of the edge's species tuple, g_m = dE_e/dv_m analytic, then
 //   dE/dx_{i_m} += g_m, dE/dx_{i_0} -= sum_m g_m, dE/dL_ab += sum_m s_ma g_mb,
-//   E_s += E_e for the system of i_0.  Float64 throughout (the edge counts of
-//   bonded terms are small next to pair lists); per-system sums are warp-
-//   aggregated atomics, per-atom gradients float64 atomics.
+//   E_s += E_e for the system of i_0.  Difference vectors in float64; the
+//   edge's arithmetic in float64, or in float32 with fp32 (this part issues
+//   about 2 float64 FMA per cycle per SM, so the float64 angles, square roots
+//   and trigonometry bound the float64 mode); per-system sums are warp-
+//   aggregated float64 atomics, per-atom gradients float64 atomics.  The float32
+//   mode takes angles as atan2 of cross and dot products and the cosine-angle and
+//   inversion energies in factored forms, equal to the reference's in exact
+//   arithmetic but without its cancellations, which float32 would amplify.
 // Angle derivatives: d cos t / dv1 = v2 / (r1 r2) - cos t v1 / r1^2 (and 1 <-> 2).
 // Dihedral: phi = atan2(|b2| b1 . (b2 x b3), (b1 x b2) . (b2 x b3)) with
 // b1 = x_j - x_i, b2 = x_k - x_j, b3 = x_l - x_k, m = b1 x b2, n = b2 x b3; its
@@ -34,12 +39,14 @@ namespace {
 
 constexpr double kEps = 1e-10;
 
-__device__ inline void cross3(const double a[3], const double b[3], double c[3]) {
+template <typename R>
+__device__ inline void cross3(const R a[3], const R b[3], R c[3]) {
   c[0] = a[1] * b[2] - a[2] * b[1];
   c[1] = a[2] * b[0] - a[0] * b[2];
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
-__device__ inline double dot3(const double a[3], const double b[3]) {
+template <typename R>
+__device__ inline R dot3(const R a[3], const R b[3]) {
   return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
 
@@ -59,115 +66,197 @@ template <>
 struct Kind<5> { static constexpr int order = 4, params = 2; };  // inversion: omega0, k
 
 // Energy of one edge and g[m] = dE/dv_{m+1}.
-template <int KIND>
-__device__ double edge_energy_grad(const double (*v)[3], const double *p, double (*g)[3]) {
+template <int KIND, typename R>
+__device__ R edge_energy_grad(const R (*v)[3], const R *p, R (*g)[3]) {
   if (KIND == 0 || KIND == 1) {
-    const double r = sqrt(dot3(v[0], v[0]));
-    double e, dedr;
+    const R r = sqrt(dot3(v[0], v[0]));
+    R e, dedr;
     if (KIND == 0) {
       e = (r - p[0]) * (r - p[0]) * p[1];
-      dedr = 2.0 * p[1] * (r - p[0]);
+      dedr = R(2.0) * p[1] * (r - p[0]);
     } else {
-      const double x = exp(-p[2] * (r - p[0]));
-      e = p[1] * (1.0 - x) * (1.0 - x);
-      dedr = 2.0 * p[1] * (1.0 - x) * p[2] * x;
+      const R x = exp(-p[2] * (r - p[0]));
+      e = p[1] * (R(1.0) - x) * (R(1.0) - x);
+      dedr = R(2.0) * p[1] * (R(1.0) - x) * p[2] * x;
     }
-    const double f = r > 0.0 ? dedr / r : 0.0;
+    const R f = r > R(0.0) ? dedr / r : R(0.0);
     for (int a = 0; a < 3; ++a) g[0][a] = f * v[0][a];
     return e;
+  } else if ((KIND == 2 || KIND == 3) && sizeof(R) == 4) {
+    // float32: theta = atan2(|v1 x v2|, v1 . v2) and the derivatives through
+    // v1 x (v1 x v2), which keep float32 digits near 0 and pi where acos and
+    // 1 / sqrt(1 - cos^2) lose them
+    R cr[3], t1[3], t2[3];
+    cross3(v[0], v[1], cr);
+    cross3(v[0], cr, t1);
+    cross3(v[1], cr, t2);
+    const R sn = sqrt(dot3(cr, cr)), cs = dot3(v[0], v[1]);
+    const R r1s = dot3(v[0], v[0]), r2s = dot3(v[1], v[1]);
+    R e, f1, f2;  // g[0] = f1 * v1 x (v1 x v2), g[1] = f2 * v2 x (v1 x v2)
+    if (KIND == 2) {
+      const R th = atan2(sn, cs) * (R(180.0) / R(M_PI));
+      e = (th - p[0]) * (th - p[0]) * p[1];
+      const R f = sn > R(0.0) ? R(2.0) * p[1] * (th - p[0]) * (R(180.0) / R(M_PI)) / sn : R(0.0);
+      f1 = f / r1s;
+      f2 = -f / r2s;
+    } else {
+      // k (c0 + c1 c + c2 (2c^2 - 1)) = 2 k c2 (c - cos theta0)^2
+      const R r12 = sqrt(r1s * r2s), c = cs / r12;
+      const R cc = fmin(fmax(c, -R(1.0)), R(1.0));
+      const R th0 = p[0], k = p[1];
+      R dedc;
+      if (fabs(th0 - R(M_PI)) < p[2]) {
+        e = k * (R(1.0) + cc);
+        dedc = k;
+      } else {
+        const R c2 = R(1.0) / (R(4.0) * fmax(sin(th0) * sin(th0), R(1e-10))), d = cc - cos(th0);
+        e = R(2.0) * k * c2 * d * d;
+        dedc = R(4.0) * k * c2 * d;
+      }
+      if (fabs(c) > R(1.0)) dedc = R(0.0);
+      f1 = -dedc / (r1s * r12);
+      f2 = dedc / (r2s * r12);
+    }
+    for (int a = 0; a < 3; ++a) {
+      g[0][a] = f1 * t1[a];
+      g[1][a] = f2 * t2[a];
+    }
+    return e;
   } else if (KIND == 2 || KIND == 3) {
-    const double r1 = sqrt(dot3(v[0], v[0])), r2 = sqrt(dot3(v[1], v[1]));
-    const double c = dot3(v[0], v[1]) / (r1 * r2);
-    double e, dedc;
+    const R r1 = sqrt(dot3(v[0], v[0])), r2 = sqrt(dot3(v[1], v[1]));
+    const R c = dot3(v[0], v[1]) / (r1 * r2);
+    R e, dedc;
     if (KIND == 2) {
       // the reference takes arccos of the unclipped cosine; clamping keeps
       // round-off above 1 from turning a straight angle into NaN
-      const double cc = fmin(fmax(c, -1.0), 1.0);
-      const double th = acos(cc) * (180.0 / M_PI);
+      const R cc = fmin(fmax(c, -R(1.0)), R(1.0));
+      const R th = acos(cc) * (R(180.0) / R(M_PI));
       e = (th - p[0]) * (th - p[0]) * p[1];
-      dedc = -2.0 * p[1] * (th - p[0]) * (180.0 / M_PI) / sqrt(fmax(1.0 - cc * cc, 1e-30));
+      dedc = -R(2.0) * p[1] * (th - p[0]) * (R(180.0) / R(M_PI)) / sqrt(fmax(R(1.0) - cc * cc, R(1e-30)));
     } else {
-      const double cc = fmin(fmax(c, -1.0), 1.0);
-      const double th0 = p[0], k = p[1];
-      if (fabs(th0 - M_PI) < p[2]) {
-        e = k * (1.0 + cc);
+      const R cc = fmin(fmax(c, -R(1.0)), R(1.0));
+      const R th0 = p[0], k = p[1];
+      if (fabs(th0 - R(M_PI)) < p[2]) {
+        e = k * (R(1.0) + cc);
         dedc = k;
       } else {
-        const double s2 = sin(th0) * sin(th0), ct0 = cos(th0);
-        const double c2 = 1.0 / (4.0 * fmax(s2, 1e-10));
-        const double c1 = -4.0 * c2 * ct0, c0 = c2 * (2.0 * ct0 * ct0 + 1.0);
-        e = k * (c0 + c1 * cc + c2 * (2.0 * cc * cc - 1.0));
-        dedc = k * (c1 + 4.0 * c2 * cc);
+        const R s2 = sin(th0) * sin(th0), ct0 = cos(th0);
+        const R c2 = R(1.0) / (R(4.0) * fmax(s2, R(1e-10)));
+        const R c1 = -R(4.0) * c2 * ct0, c0 = c2 * (R(2.0) * ct0 * ct0 + R(1.0));
+        e = k * (c0 + c1 * cc + c2 * (R(2.0) * cc * cc - R(1.0)));
+        dedc = k * (c1 + R(4.0) * c2 * cc);
       }
-      if (fabs(c) > 1.0) dedc = 0.0;  // clipped: no gradient
+      if (fabs(c) > R(1.0)) dedc = R(0.0);  // clipped: no gradient
     }
-    const double i12 = 1.0 / (r1 * r2);
+    const R i12 = R(1.0) / (r1 * r2);
     for (int a = 0; a < 3; ++a) {
       g[0][a] = dedc * (v[1][a] * i12 - c * v[0][a] / (r1 * r1));
       g[1][a] = dedc * (v[0][a] * i12 - c * v[1][a] / (r2 * r2));
     }
     return e;
   } else if (KIND == 4) {
-    double b1[3], b2[3], b3[3];
+    R b1[3], b2[3], b3[3];
     for (int a = 0; a < 3; ++a) {
       b1[a] = v[0][a];
       b2[a] = v[1][a] - v[0][a];
       b3[a] = v[2][a] - v[1][a];
     }
-    double m[3], n[3];
+    R m[3], n[3];
     cross3(b1, b2, m);
     cross3(b2, b3, n);
-    const double mm = dot3(m, m), nn = dot3(n, n), lb = sqrt(dot3(b2, b2));
-    const double lm = sqrt(mm), ln = sqrt(nn);
-    double n1[3], n2[3], bn[3], x[3];
+    const R mm = dot3(m, m), nn = dot3(n, n), lb = sqrt(dot3(b2, b2));
+    const R lm = sqrt(mm), ln = sqrt(nn);
+    R n1[3], n2[3], bn[3], x[3];
     for (int a = 0; a < 3; ++a) {
-      n1[a] = m[a] / (lm + kEps);
-      n2[a] = n[a] / (ln + kEps);
-      bn[a] = b2[a] / (lb + kEps);
+      n1[a] = m[a] / (lm + R(kEps));
+      n2[a] = n[a] / (ln + R(kEps));
+      bn[a] = b2[a] / (lb + R(kEps));
     }
     cross3(n1, n2, x);
-    const double phi = atan2(dot3(x, bn), dot3(n1, n2));
-    const double V = p[0], per = p[1], phi0 = p[2];
-    const double e = 0.5 * V * (1.0 - cos(per * phi0) * cos(per * phi));
-    const double dedphi = 0.5 * V * cos(per * phi0) * per * sin(per * phi);
-    if (mm > 0.0 && nn > 0.0 && lb > 0.0) {
-      const double pp = dot3(b1, b2) / (lb * lb), qq = dot3(b3, b2) / (lb * lb);
+    const R phi = atan2(dot3(x, bn), dot3(n1, n2));
+    const R V = p[0], per = p[1], phi0 = p[2];
+    const R e = R(0.5) * V * (R(1.0) - cos(per * phi0) * cos(per * phi));
+    const R dedphi = R(0.5) * V * cos(per * phi0) * per * sin(per * phi);
+    if (mm > R(0.0) && nn > R(0.0) && lb > R(0.0)) {
+      const R pp = dot3(b1, b2) / (lb * lb), qq = dot3(b3, b2) / (lb * lb);
       for (int a = 0; a < 3; ++a) {
-        const double di = -lb / mm * m[a], dl = lb / nn * n[a];
-        g[0][a] = dedphi * (-(1.0 + pp) * di + qq * dl);
-        g[1][a] = dedphi * (pp * di - (1.0 + qq) * dl);
+        const R di = -lb / mm * m[a], dl = lb / nn * n[a];
+        g[0][a] = dedphi * (-(R(1.0) + pp) * di + qq * dl);
+        g[1][a] = dedphi * (pp * di - (R(1.0) + qq) * dl);
         g[2][a] = dedphi * dl;
       }
     } else {
       for (int k = 0; k < 3; ++k)
-        for (int a = 0; a < 3; ++a) g[k][a] = 0.0;
+        for (int a = 0; a < 3; ++a) g[k][a] = R(0.0);
     }
     return e;
-  } else {
-    double n[3];
+  } else if (sizeof(R) == 4) {
+    // float32 inversion: w = atan2(v1 . n, |v1 x n|), n = v2 x v3, and the
+    // energy in the cancellation-free form
+    //   ks (c0 + c1 cos w + c2 cos 2w) = 8 ks c2 X^2, X = sin((w + w0)/2) sin((w - w0)/2),
+    //   c0 + c1 + c2 = 8 c2 sin^4(w0 / 2)
+    // dw/dv1 = (|u1| n - (v1 . n) n x u1 / |u1|) / (|n| |v1|)^2,
+    // dw/dn = (|u1| v1 + (v1 . n) v1 x u1 / |u1|) / (|n| |v1|)^2, u1 = v1 x n
+    R n[3], u[3], nu[3], vu[3];
     cross3(v[1], v[2], n);
-    const double ln = sqrt(dot3(n, n)), la = sqrt(dot3(v[0], v[0]));
-    const double an = dot3(v[0], n);
-    const double s_raw = an / (ln + kEps) / (la + kEps);
-    const double s = fmin(fmax(s_raw, -1.0), 1.0);
-    const double w = asin(s);
-    const double om0 = p[0], k = p[1];
-    const bool sp2 = fabs(om0) < 1e-6;
-    const double s2 = sin(om0) * sin(om0), cw0 = cos(om0);
-    const double c2 = sp2 ? 0.0 : 1.0 / (4.0 * (s2 > 1e-10 ? s2 : 1.0));
-    const double c1 = sp2 ? -1.0 : -4.0 * c2 * cw0;
-    const double c0 = sp2 ? 1.0 : c2 * (2.0 * cw0 * cw0 + 1.0);
-    const double ks = sp2 ? k : k / fmax(c0 + c1 + c2, 1e-10);
-    const double e = ks * (c0 + c1 * cos(w) + c2 * cos(2.0 * w));
-    const double dedw = ks * (-c1 * sin(w) - 2.0 * c2 * sin(2.0 * w));
-    const double deds = fabs(s_raw) <= 1.0 ? dedw / sqrt(fmax(1.0 - s * s, 1e-30)) : 0.0;
-    // ds/dv1 and ds/dn; dn/dv2 (x) and dn/dv3 (x) through the cross product
-    double wv[3], t[3];
-    const double inv_la = 1.0 / (la + kEps), inv_ln = 1.0 / (ln + kEps);
+    cross3(v[0], n, u);
+    cross3(n, u, nu);
+    cross3(v[0], u, vu);
+    const R nn = dot3(n, n), la2 = dot3(v[0], v[0]), an = dot3(v[0], n), lu = sqrt(dot3(u, u));
+    const R w = atan2(an, lu);
+    const R om0 = p[0], k = p[1];
+    const R den = nn * la2;
+    const R sw = den > R(0.0) ? an * rsqrt(den) : R(0.0);
+    R e, dedw;
+    if (fabs(om0) < R(1e-6)) {
+      const R h = sin(R(0.5) * w);
+      e = R(2.0) * k * h * h;  // k (1 - cos w)
+      dedw = k * sw;
+    } else {
+      const R s2 = sin(om0) * sin(om0), h0 = sin(R(0.5) * om0);
+      const R c2 = R(1.0) / (R(4.0) * (s2 > R(1e-10) ? s2 : R(1.0)));
+      const R ks = k / fmax(R(8.0) * c2 * h0 * h0 * h0 * h0, R(1e-10));
+      const R X = sin(R(0.5) * (w + om0)) * sin(R(0.5) * (w - om0));
+      e = R(8.0) * ks * c2 * X * X;
+      dedw = R(8.0) * ks * c2 * X * sw;
+    }
+    const R f = den > R(0.0) ? dedw / den : R(0.0);
+    const R q = lu > R(0.0) ? an / lu : R(0.0);
+    R G[3], t[3];
     for (int a = 0; a < 3; ++a) {
-      const double nu = n[a] * inv_ln;
-      g[0][a] = deds * (nu * inv_la - (an * inv_ln) * inv_la * inv_la / (la > 0.0 ? la : 1.0) * v[0][a]);
-      wv[a] = (v[0][a] * inv_ln - an * inv_ln * inv_ln / (ln > 0.0 ? ln : 1.0) * n[a]) * inv_la;
+      g[0][a] = f * (lu * n[a] - q * nu[a]);
+      G[a] = f * (lu * v[0][a] + q * vu[a]);
+    }
+    cross3(v[2], G, t);
+    for (int a = 0; a < 3; ++a) g[1][a] = t[a];
+    cross3(G, v[1], t);
+    for (int a = 0; a < 3; ++a) g[2][a] = t[a];
+    return e;
+  } else {
+    R n[3];
+    cross3(v[1], v[2], n);
+    const R ln = sqrt(dot3(n, n)), la = sqrt(dot3(v[0], v[0]));
+    const R an = dot3(v[0], n);
+    const R s_raw = an / (ln + R(kEps)) / (la + R(kEps));
+    const R s = fmin(fmax(s_raw, -R(1.0)), R(1.0));
+    const R w = asin(s);
+    const R om0 = p[0], k = p[1];
+    const bool sp2 = fabs(om0) < R(1e-6);
+    const R s2 = sin(om0) * sin(om0), cw0 = cos(om0);
+    const R c2 = sp2 ? R(0.0) : R(1.0) / (R(4.0) * (s2 > R(1e-10) ? s2 : R(1.0)));
+    const R c1 = sp2 ? -R(1.0) : -R(4.0) * c2 * cw0;
+    const R c0 = sp2 ? R(1.0) : c2 * (R(2.0) * cw0 * cw0 + R(1.0));
+    const R ks = sp2 ? k : k / fmax(c0 + c1 + c2, R(1e-10));
+    const R e = ks * (c0 + c1 * cos(w) + c2 * cos(R(2.0) * w));
+    const R dedw = ks * (-c1 * sin(w) - R(2.0) * c2 * sin(R(2.0) * w));
+    const R deds = fabs(s_raw) <= R(1.0) ? dedw / sqrt(fmax(R(1.0) - s * s, R(1e-30))) : R(0.0);
+    // ds/dv1 and ds/dn; dn/dv2 (x) and dn/dv3 (x) through the cross product
+    R wv[3], t[3];
+    const R inv_la = R(1.0) / (la + R(kEps)), inv_ln = R(1.0) / (ln + R(kEps));
+    for (int a = 0; a < 3; ++a) {
+      const R nu = n[a] * inv_ln;
+      g[0][a] = deds * (nu * inv_la - (an * inv_ln) * inv_la * inv_la / (la > R(0.0) ? la : R(1.0)) * v[0][a]);
+      wv[a] = (v[0][a] * inv_ln - an * inv_ln * inv_ln / (ln > R(0.0) ? ln : R(1.0)) * n[a]) * inv_la;
     }
     cross3(v[2], wv, t);
     for (int a = 0; a < 3; ++a) g[1][a] = deds * t[a];
@@ -177,7 +266,7 @@ __device__ double edge_energy_grad(const double (*v)[3], const double *p, double
   }
 }
 
-template <int KIND>
+template <int KIND, typename R>
 __global__ void bonded_kernel(const double *pos, const int32_t *system, const int32_t *species, int64_t n,
                               const double *tril, int32_t n_sys, const int32_t *edges, const int32_t *shifts,
                               int64_t n_edges, const double *params, int32_t nsp, double *energy, double *grad,
@@ -207,22 +296,26 @@ __global__ void bonded_kernel(const double *pos, const int32_t *system, const in
     } else {
       sys = s0;
       const Tril64 L = load_tril64(tril + 6 * (int64_t)s0);
-      double v[D - 1][3], sh[D - 1][3], g[D - 1][3];
+      // difference vectors in float64 (positions are float64), then the edge's arithmetic in R
+      R v[D - 1][3], g[D - 1][3], pr[P];
+      double sh[D - 1][3];
       for (int m = 0; m < D - 1; ++m) {
         for (int a = 0; a < 3; ++a) sh[m][a] = shifts[((int64_t)(D - 1) * e + m) * 3 + a];
         double sL[3];
         row_times_tril64(sh[m], L, sL);
-        for (int a = 0; a < 3; ++a) v[m][a] = pos[3 * (int64_t)idx[m + 1] + a] - pos[3 * (int64_t)idx[0] + a] + sL[a];
+        for (int a = 0; a < 3; ++a)
+          v[m][a] = (R)(pos[3 * (int64_t)idx[m + 1] + a] - pos[3 * (int64_t)idx[0] + a] + sL[a]);
       }
-      en = edge_energy_grad<KIND>(v, params + row * P, g);
+      for (int k = 0; k < P; ++k) pr[k] = (R)params[row * P + k];
+      en = (double)edge_energy_grad<KIND, R>(v, pr, g);
       bool finite = isfinite(en);
       for (int m = 0; m < D - 1; ++m)
         for (int a = 0; a < 3; ++a) finite &= isfinite(g[m][a]);
       if (!finite) status_error(status, KUPS_ERR_NONFINITE, e);
       for (int m = 0; m < D - 1; ++m) {
         for (int a = 0; a < 3; ++a) {
-          atomicAdd(&grad[3 * (int64_t)idx[m + 1] + a], g[m][a]);
-          atomicAdd(&grad[3 * (int64_t)idx[0] + a], -g[m][a]);
+          atomicAdd(&grad[3 * (int64_t)idx[m + 1] + a], (double)g[m][a]);
+          atomicAdd(&grad[3 * (int64_t)idx[0] + a], -(double)g[m][a]);
         }
         dl[0] += sh[m][0] * g[m][0];
         dl[1] += sh[m][1] * g[m][0];
@@ -238,13 +331,13 @@ __global__ void bonded_kernel(const double *pos, const int32_t *system, const in
     for (int k = 0; k < 6; ++k) add_system(grad_tril, 6, k, sys, dl[k]);
 }
 
-template <int KIND>
+template <int KIND, typename R>
 cudaError_t launch_bonded(const double *pos, const int32_t *system, const int32_t *species, int64_t n,
                           const double *tril, int32_t s, const int32_t *edges, const int32_t *shifts,
                           int64_t n_edges, const double *params, int32_t nsp, double *energy, double *grad,
                           double *grad_tril, kups_status *status, cudaStream_t stream) {
   const unsigned grid = (unsigned)((n_edges + 127) / 128);
-  bonded_kernel<KIND><<<grid, 128, 0, stream>>>(pos, system, species, n, tril, s, edges, shifts, n_edges, params,
+  bonded_kernel<KIND, R><<<grid, 128, 0, stream>>>(pos, system, species, n, tril, s, edges, shifts, n_edges, params,
                                                 nsp, energy, grad, grad_tril, status);
   return cudaGetLastError();
 }
@@ -282,7 +375,7 @@ extern "C" int32_t kups_bonded_edges(int32_t kind, const double *positions, cons
                                      const int32_t *species, int64_t n_particles, const double *tril,
                                      int32_t n_systems, const int32_t *edges, const int32_t *shifts, int64_t n_edges,
                                      const double *params, int32_t n_species, double *energy, double *grad,
-                                     double *grad_tril, kups_status *status, void *stream_) {
+                                     double *grad_tril, int32_t fp32, kups_status *status, void *stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
   if (kind < 0 || kind > 5 || n_particles < 0 || n_systems < 0 || n_edges < 0 || n_species <= 0 ||
       n_species > 1024)
@@ -292,21 +385,27 @@ extern "C" int32_t kups_bonded_edges(int32_t kind, const double *positions, cons
       shifts == nullptr || params == nullptr || energy == nullptr || grad == nullptr || status == nullptr)
     return KUPS_ERR_INVALID;
   cudaError_t err;
-  switch (kind) {
-#define KUPS_BONDED_CASE(K)                                                                                      \
-  case K:                                                                                                        \
-    err = launch_bonded<K>(positions, system, species, n_particles, tril, n_systems, edges, shifts, n_edges,     \
-                           params, n_species, energy, grad, grad_tril, status, stream);                          \
+  switch (kind * 2 + (fp32 ? 1 : 0)) {
+#define KUPS_BONDED_CASE(K, R)                                                                                   \
+  case 2 * K + (sizeof(R) == 4 ? 1 : 0):                                                                         \
+    err = launch_bonded<K, R>(positions, system, species, n_particles, tril, n_systems, edges, shifts, n_edges,  \
+                              params, n_species, energy, grad, grad_tril, status, stream);                       \
     break;
-    KUPS_BONDED_CASE(0)
-    KUPS_BONDED_CASE(1)
-    KUPS_BONDED_CASE(2)
-    KUPS_BONDED_CASE(3)
-    KUPS_BONDED_CASE(4)
-    default:
-      err = launch_bonded<5>(positions, system, species, n_particles, tril, n_systems, edges, shifts, n_edges,
-                             params, n_species, energy, grad, grad_tril, status, stream);
+    KUPS_BONDED_CASE(0, double)
+    KUPS_BONDED_CASE(0, float)
+    KUPS_BONDED_CASE(1, double)
+    KUPS_BONDED_CASE(1, float)
+    KUPS_BONDED_CASE(2, double)
+    KUPS_BONDED_CASE(2, float)
+    KUPS_BONDED_CASE(3, double)
+    KUPS_BONDED_CASE(3, float)
+    KUPS_BONDED_CASE(4, double)
+    KUPS_BONDED_CASE(4, float)
+    KUPS_BONDED_CASE(5, double)
+    KUPS_BONDED_CASE(5, float)
 #undef KUPS_BONDED_CASE
+    default:
+      return KUPS_ERR_INVALID;
   }
   return err == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

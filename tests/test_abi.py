@@ -114,9 +114,9 @@ def test_host_side_validation_of_newer_entry_points():
     lib = _lib.load()
     assert lib.kups_bonded_order(2) == 3 and lib.kups_bonded_param_count(4) == 3
     assert lib.kups_bonded_order(6) == -1
-    assert lib.kups_bonded_edges(6, None, None, None, 0, None, 0, None, None, 1, None, 1, None, None, None, None,
+    assert lib.kups_bonded_edges(6, None, None, None, 0, None, 0, None, None, 1, None, 1, None, None, None, 0, None,
                                  None) == _lib.KUPS_ERR_INVALID
-    assert lib.kups_bonded_edges(0, None, None, None, 0, None, 0, None, None, 0, None, 1, None, None, None, None,
+    assert lib.kups_bonded_edges(0, None, None, None, 0, None, 0, None, None, 0, None, 1, None, None, None, 1, None,
                                  None) == _lib.KUPS_OK  # no edges: nothing to do
     a = _lib.MdArgs()
     a.n_systems, a.n_species, a.n_steps, a.neighbor_capacity = 1, 1, 1, 64

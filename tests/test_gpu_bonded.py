@@ -74,6 +74,23 @@ def test_bonded_kernel_matches_oracle(kind):
     np.testing.assert_allclose(gt, gtr, rtol=0, atol=1e-6 * np.abs(gtr).max())
 
 
+@pytest.mark.parametrize("kind", list(ob.KINDS))
+def test_bonded_fp32_mode_within_float32_tolerance(kind):
+    """fp32 != 0: the per-edge arithmetic in float32, so energies to 2e-5 of the largest
+    per-system energy (a few hundred edges of float32 rounding each) and gradients to 2e-4 of
+    the largest component (angles near 0 or pi amplify the rounding of the cosine)."""
+    from kups_gb300 import bonded
+
+    rng = np.random.default_rng(ob.KINDS[kind][0] + 7)
+    pos, system, species, tril, edges, shifts, table, T, order = random_case(kind, rng)
+    term = bonded.BondedTerm(params_object(kind, table, T, order), edges, shifts, fp32=True)
+    e, g, gt = (x.cpu().numpy() for x in bonded.evaluate([term], pos, system, species, tril))
+    er, gr, gtr = ob.bonded(kind, pos, system, species, tril, table, T, edges, shifts)
+    np.testing.assert_allclose(e, er, rtol=0, atol=2e-5 * np.abs(er).max())
+    np.testing.assert_allclose(g, gr, rtol=0, atol=2e-4 * np.abs(gr).max())
+    np.testing.assert_allclose(gt, gtr, rtol=0, atol=2e-4 * np.abs(gtr).max())
+
+
 def test_terms_add_into_one_buffer():
     from kups_gb300 import bonded
 
