@@ -356,6 +356,7 @@ def run_ours(a):
     if rank == 0 and not a.no_bonded:
         line["bonded"] = run_bonded(a)
         line["local_mliap"] = run_mliap(a)
+        line["virial_observables"] = run_observables(a)
     if rank == 0 and not a.no_gcmc:
         line["gcmc"] = run_gcmc(a)
     if rank == 0:
@@ -488,6 +489,66 @@ def run_bonded(a, reps=20):
             "roofline_fp32": {"bound": "hbm", "achieved": gbs32, "peak": peak, "unit": "GB/s",
                               "frac": gbs32 / peak, "peak_source": kind,
                               "note": "per-edge arithmetic in float32, sums in float64"}}
+
+
+def run_observables(a, reps=20):
+    """kups_virial_stress with every output (atomic, molecular and lattice stress, kinetic energy,
+    pressure) on 64 systems of 8000 three-atom molecules (1 536 000 atoms, positions wrapped atom
+    by atom).  Algorithmic bytes per atom: positions, dU/dx and momenta 24 B each, mass 8 B,
+    system and group 4 B each (88 B, each array read once); timed over `reps` calls with the
+    buffers allocated once."""
+    import torch
+
+    from kups_gb300 import _lib
+    from kups_gb300.neighborlist import _stream, new_status, read_status
+
+    S, n_mol = 64, 8000
+    rng = np.random.default_rng(9)
+    tril = np.tile([45.0, 1.0, 44.0, -2.0, 0.5, 46.0], (S, 1))
+    n = S * n_mol * 3
+    sysi = np.repeat(np.arange(S), n_mol * 3)
+    frac = np.repeat(rng.uniform(-0.5, 0.5, (S * n_mol, 3)), 3, axis=0) + rng.normal(scale=0.02, size=(n, 3))
+    frac = (frac + 0.5) % 1.0 - 0.5
+    L = np.zeros((S, 3, 3))
+    L[:, [0, 1, 1, 2, 2, 2], [0, 0, 1, 0, 1, 2]] = tril
+    dev = "cuda"
+    t = lambda x, dt=torch.float64: torch.as_tensor(x, dtype=dt, device=dev).contiguous()
+    pos, grad, mom = t(np.einsum("na,nab->nb", frac, L[sysi])), t(rng.normal(size=(n, 3))), t(rng.normal(size=(n, 3)))
+    mass, sy, grp = t(rng.uniform(1, 16, n)), t(sysi, torch.int32), t(np.arange(n) // 3, torch.int32)
+    tr, gt = t(tril), t(rng.normal(size=(S, 6)))
+    outs = [torch.empty(S * 9, dtype=torch.float64, device=dev) for _ in range(3)]
+    ke, pr = torch.empty(S, dtype=torch.float64, device=dev), torch.empty(S, dtype=torch.float64, device=dev)
+    lib = _lib.load()
+    G = S * n_mol
+    wsb = lib.kups_virial_stress_workspace_bytes(S, G)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    status = new_status()
+
+    def call():
+        _lib.check(lib.kups_virial_stress(pos.data_ptr(), grad.data_ptr(), sy.data_ptr(), n, tr.data_ptr(),
+                                          gt.data_ptr(), S, grp.data_ptr(), G, mom.data_ptr(), mass.data_ptr(),
+                                          outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(),
+                                          ke.data_ptr(), pr.data_ptr(), ws.data_ptr(), wsb, status.data_ptr(),
+                                          _stream()), "kups_virial_stress")
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    _lib.raise_status(read_status(status))
+    ms = e0.elapsed_time(e1) / reps
+    peak, kind = measured_peak()
+    gbs = n * 88 / (ms / 1e3) / 1e9
+    return {"workload": f"{S} systems x {n_mol} three-atom molecules ({n} atoms), all outputs", "ms_per_call": ms,
+            "atoms_per_s": n / (ms / 1e3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "peak_source": kind, "note": "float64 throughout; molecular centres take three extra "
+                                                      "passes (anchor, minimum-image sums, centre)"}}
 
 
 def run_mliap(a, reps=10):

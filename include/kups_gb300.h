@@ -377,6 +377,38 @@ int32_t kups_md_thermostat(double *momenta, const double *masses, const int32_t 
                            uint64_t seed, uint64_t step, int64_t n_particles, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Virial observables per system — replaces stress_via_virial_theorem,
+ * molecular_stress_via_virial_theorem and stress_via_lattice_vector_gradients
+ * (src/kups/observables/stress.py:64-118, 139-190), particle_kinetic_energy summed
+ * per system and instantaneous_pressure (src/kups/md/observables.py:17-61).
+ *
+ *   stress            sigma_ab = -(sum_i r_ia g_ib + (L^T G)_ab) / V
+ *   molecular_stress  -(sym(sum_i w_i (x) g_i) + L^T G) / V, sym(A) = (A + A^T) / 2,
+ *                     w_i = r_i - wrap(r_i - R_g), R_g the wrapped centre of the
+ *                     atom's group (RASPA convention)
+ *   lattice_stress    -G / V
+ *   kinetic           sum_i |p_i|^2 / (2 m_i)
+ *   pressure          2 K / (3 V) + Tr(stress) / 3 (K = 0 when momenta is NULL)
+ * g = dU/dx f64 [n_particles, 3], G = dU/dL from grad_tril f64 [n_systems, 6]
+ * (NULL: zero), V = |L00 L11 L22| of each system (the reference divides the
+ * molecular stress of every system by the first system's volume, stress.py:114).
+ * Outputs f64 [n_systems, 9] (row-major 3x3) or [n_systems]; each may be NULL.
+ * group i32 [n_particles] in [0, n_groups) is read only for molecular_stress;
+ * momenta f64 [n_particles, 3] and masses f64 [n_particles] may be NULL unless
+ * kinetic is asked for.  A particle with a system or group out of range records
+ * KUPS_ERR_INVALID and is skipped.  Workspace:
+ * kups_virial_stress_workspace_bytes(n_systems, molecular_stress ? n_groups : 0).
+ * ------------------------------------------------------------------------ */
+size_t kups_virial_stress_workspace_bytes(int32_t n_systems, int32_t n_groups);
+int32_t kups_virial_stress(const double *positions, const double *grad, const int32_t *system,
+                           int64_t n_particles, const double *tril, const double *grad_tril,
+                           int32_t n_systems, const int32_t *group, int32_t n_groups,
+                           const double *momenta, const double *masses, double *stress,
+                           double *molecular_stress, double *lattice_stress, double *kinetic,
+                           double *pressure, void *workspace, size_t workspace_bytes,
+                           kups_status *status, void *stream);
+
+/* ------------------------------------------------------------------------
  * Batched grand-canonical Monte Carlo of one rigid molecule species in rigid
  * frameworks (LJ + Ewald + LJ tail correction, muVT ensemble) — replaces
  * MCMCPropagator.__call__ with the moves of make_gcmc_mcmc_propagator

@@ -103,6 +103,9 @@ SIGNATURES = {
     "kups_md_kick": (_I32, [_P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_drift": (_I32, [_P, _P, _P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_thermostat": (_I32, [_P, _P, _P, _P, _P, _P, C.c_uint64, C.c_uint64, _I64, _P]),
+    "kups_virial_stress_workspace_bytes": (C.c_size_t, [_I32, _I32]),
+    "kups_virial_stress": (_I32, [_P, _P, _P, _I64, _P, _P, _I32, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P,
+                                  C.c_size_t, _P, _P]),
     "kups_gcmc_run": (_I32, [C.POINTER(GcmcArgs), _P, _P]),
     "kups_mlp_workspace_bytes": (_SZ, [_I64]),
     "kups_mlp_init": (_I32, [_P, C.c_uint64, _P]),

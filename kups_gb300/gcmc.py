@@ -439,3 +439,85 @@ class GCMC:
         att = self.attempted.cpu().numpy()
         acc = self.accepted.cpu().numpy()
         return {m: (int(att[:, i].sum()), int(acc[:, i].sum())) for i, m in enumerate(MOVES)}
+
+    # ------------------------------------------------------------------ stress of the guests
+    def guest_table(self):
+        """The guests as a particle table, grouped by system: positions f64 [A, 3] (the
+        float32 state widened), charges, species, system and group (molecule index) [A]."""
+        st = self.setup
+        apm = len(st.motif_charges)
+        keep = torch.arange(self.guest.shape[1], device="cuda")[None, :] < self.n_mol[:, None]
+        pos = self.guest[..., :3][keep].reshape(-1, 3).to(torch.float64).contiguous()
+        m = pos.shape[0] // apm
+        sysi = torch.repeat_interleave(torch.arange(st.n_systems, device="cuda", dtype=torch.int32),
+                                       (self.n_mol * apm).to(torch.int64))
+        group = torch.repeat_interleave(torch.arange(m, device="cuda", dtype=torch.int32), apm)
+        sp = torch.as_tensor(np.asarray(st.motif_species, np.int32), device="cuda").repeat(m)
+        q = torch.as_tensor(np.asarray(st.motif_charges, np.float64), device="cuda").repeat(m)
+        return pos, q, sp, sysi, group
+
+    def guest_potential(self, positions, charges, species, system, group, tril=None):
+        """Energy [S], dU/dx [A, 3] and dU/dtril [S, 6] of the guests alone (the guest-only
+        state of mcmc_rigid.py:389-424): LJ and Ewald with each molecule's own pairs left out
+        of the neighbour list, the excluded pairs' real-space minus vacuum Coulomb
+        correction, and the LJ tail of the guest species counts (an energy c / V whose cell
+        gradient is -U / L_aa on the diagonal)."""
+        from .ewald import EwaldParameters, EwaldParticles, LJEwaldPotential
+        from .potential import lennard_jones_tail_correction
+
+        st = self.setup
+        tr = torch.as_tensor(st.tril if tril is None else tril, dtype=torch.float64, device="cuda").reshape(-1, 6)
+        apm = len(st.motif_charges)
+        m = positions.shape[0] // apm
+        a, b = np.nonzero(~np.eye(apm, dtype=bool))
+        xe = (torch.arange(m, device="cuda", dtype=torch.int32)[:, None, None] * apm
+              + torch.as_tensor(np.stack([a, b], 1), dtype=torch.int32, device="cuda")[None]).reshape(-1, 2)
+        L = torch.zeros((tr.shape[0], 3, 3), dtype=torch.float64, device="cuda")
+        L[:, [0, 1, 1, 2, 2, 2], [0, 0, 1, 0, 1, 2]] = tr
+        frac = torch.einsum("ni,nij->nj", positions, torch.linalg.inv(L)[system.to(torch.int64)])
+        xs = torch.round(frac[xe[:, 0].long()] - frac[xe[:, 1].long()]).to(torch.int32).contiguous()
+        prm = EwaldParameters(torch.as_tensor(st.alpha), torch.as_tensor(st.rc_ew), torch.as_tensor(st.kvec_n))
+        pot = LJEwaldPotential(prm, st.sigma, st.epsilon, st.rc_lj, exclusion_edges=(xe.contiguous(), xs))
+        out = pot(EwaldParticles(positions, charges, system, species, exclusion=group), tr)
+        energy, grad, gtril = out.total_energies, out.gradients.positions, out.gradients.unitcell
+        if st.tail_correction and positions.shape[0]:
+            et, _ = lennard_jones_tail_correction(species, system, tr, st.sigma, st.epsilon, st.rc_lj)
+            dt = torch.zeros_like(gtril)
+            dt[:, 0], dt[:, 2], dt[:, 5] = -et / tr[:, 0], -et / tr[:, 2], -et / tr[:, 5]
+            energy, gtril = energy + et, gtril + dt
+        return energy, grad, gtril
+
+    def guest_stress(self) -> dict:
+        """The rigid-MC app's stress record (``make_guest_stress``, mcmc_rigid.py:385-436;
+        ``StressResult``, application/mcmc/data.py:170-175) for the current state, each
+        [S, 3, 3] float64: ``potential`` the molecular virial stress (RASPA convention) of the
+        guest-only energy and gradients; ``tail_correction`` P_tail I with P_tail of the full
+        state (host and guests); ``ideal_gas`` N_mol k_B T / V I.  Their sum is the stress the
+        reference's analysis block-averages (application/mcmc/analysis.py:186-190)."""
+        from .observables import ideal_gas_pressure, virial_observables
+        from .potential import lennard_jones_tail_correction
+
+        st = self.setup
+        S = st.n_systems
+        pos, q, sp, sysi, group = self.guest_table()
+        eye = torch.eye(3, dtype=torch.float64, device="cuda")
+        if pos.shape[0]:
+            _, grad, gtril = self.guest_potential(pos, q, sp, sysi, group)
+            potential = virial_observables(pos, grad, sysi, st.tril, gtril, group=group,
+                                           n_groups=pos.shape[0] // len(st.motif_charges),
+                                           molecular=True)["molecular_stress"]
+        else:
+            potential = torch.zeros((S, 3, 3), dtype=torch.float64, device="cuda")
+        if st.tail_correction:
+            fw_sp = [np.asarray(st.fw_species[a:a + n]) for a, n in zip(st.fw_start, st.fw_count)]
+            guests = sp.cpu().numpy()
+            counts = (self.n_mol.cpu().numpy() * len(st.motif_charges)).tolist()
+            offs = np.concatenate([[0], np.cumsum(counts)])
+            full_sp = np.concatenate([np.concatenate([fw_sp[s], guests[offs[s]:offs[s + 1]]]) for s in range(S)])
+            full_sys = np.concatenate([np.full(len(fw_sp[s]) + counts[s], s) for s in range(S)])
+            _, p_tail = lennard_jones_tail_correction(full_sp, full_sys, st.tril, st.sigma, st.epsilon, st.rc_lj)
+        else:
+            p_tail = torch.zeros(S, dtype=torch.float64, device="cuda")
+        p_ideal = ideal_gas_pressure(self.n_mol.to(torch.float64), st.temperature, st.tril)
+        return {"potential": potential, "tail_correction": p_tail[:, None, None] * eye,
+                "ideal_gas": p_ideal[:, None, None] * eye}

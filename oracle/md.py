@@ -84,12 +84,13 @@ def baoab(pos, mom, forces, masses, system, species, tril, sigma, epsilon, cutof
 
 
 def virial_stress(pos, grad, system, tril, dtril):
-    """Cauchy stress per system, -(sum_i dU/dr_i (x) r_i + h^T dU/dh) / V
-    (observables/stress.py:70-82); h^T dU/dh uses the lower-triangular dU/dtril."""
+    """Cauchy stress per system, sigma_ab = -(sum_i r_ia dU/dr_ib + (h^T dU/dh)_ab) / V
+    (observables/stress.py:70-82: ``position_gradients[:, None] * positions[..., None]``
+    puts the position on the first index); h^T dU/dh uses the lower-triangular dU/dtril."""
     sysi = np.asarray(system)
     tril = np.asarray(tril, np.float64)
     out = np.zeros((tril.shape[0], 3, 3))
-    np.add.at(out, sysi, np.asarray(grad)[:, :, None] * np.asarray(pos)[:, None, :])
+    np.add.at(out, sysi, np.asarray(pos)[:, :, None] * np.asarray(grad)[:, None, :])
     for s in range(tril.shape[0]):
         L = lattice_from_tril(tril[s])
         G = lattice_from_tril(np.asarray(dtril)[s])

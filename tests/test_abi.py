@@ -129,3 +129,25 @@ def test_host_side_validation_of_newer_entry_points():
                                                 1.0, 4, None, None, None, 0, None, None) == _lib.KUPS_ERR_INVALID
     assert lib.kups_lj_ewald_real_forces_packed(None, None, None, None, 1, 1, None, None, None, 1, None, None, None,
                                                 1.0, 2 | 16, None, None, None, 0, None, None) == _lib.KUPS_ERR_INVALID
+
+
+def test_host_side_validation_of_the_virial_observables():
+    """kups_virial_stress refuses negative sizes, a kinetic energy without momenta, a
+    molecular stress without groups and a short workspace; no systems is a no-op."""
+    from kups_gb300 import _lib
+
+    lib = _lib.load()
+    ws = lib.kups_virial_stress_workspace_bytes(2, 3)
+    assert ws >= 8 * 19 * 2 + 8 * 4 * 3 + 4 * 3 and lib.kups_virial_stress_workspace_bytes(-1, 0) == 0
+    args = lambda **kw: [kw.get(k) for k in ("pos", "grad", "sys")] + [kw.get("n", 0), kw.get("tril"), None,
+                                                                       kw.get("S", 0), kw.get("group"), kw.get("G", 0),
+                                                                       kw.get("mom"), kw.get("mass"), None,
+                                                                       kw.get("mol"), None, kw.get("kin"), None,
+                                                                       kw.get("ws"), kw.get("wsb", 0), None, None]
+    fake = 256  # never dereferenced: every call below is refused (or a no-op) on the host
+    assert lib.kups_virial_stress(*args(n=-1)) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_virial_stress(*args(S=1)) == _lib.KUPS_ERR_INVALID  # no cell
+    assert lib.kups_virial_stress(*args(S=1, tril=fake, kin=fake, wsb=1 << 20, ws=fake)) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_virial_stress(*args(S=1, tril=fake, mol=fake, wsb=1 << 20, ws=fake)) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_virial_stress(*args(S=1, tril=fake, wsb=16, ws=fake)) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_virial_stress(*args()) == _lib.KUPS_OK

@@ -391,3 +391,54 @@ def test_device_block_sums_equal_the_per_step_series():
         if np.isfinite(ref["heat_of_adsorption"][0][0]):
             np.testing.assert_allclose(res["heat_of_adsorption"].mean[s], ref["heat_of_adsorption"][0][0],
                                        rtol=1e-9)
+
+
+def test_guest_stress_is_the_volume_derivative_of_the_guest_energy():
+    """GCMC.guest_stress (mcmc_rigid.py:385-436) on molecules that straddle the cell faces:
+    Tr(potential) / 3 equals -dU/dV of the guest-only energy (LJ + Ewald with the intramolecular
+    exclusion + LJ tail) when the cell scales and every molecule moves rigidly with its centre
+    (central differences, relative step 1e-6); the potential part is the oracle's molecular
+    virial stress of the same gradients; the tail and ideal-gas parts are the oracle's formulas."""
+    from kups_gb300 import gcmc
+    from oracle import lennard_jones as olj
+    from oracle import observables as oobs
+
+    setup = small_setup(n_sys=2, rc=5.0)
+    L = ouc.lattice_from_tril(setup.tril[0])
+    rng = np.random.default_rng(21)
+    mpos = co2_template()[0]
+    guests = [wrapped(np.concatenate([random_molecule(rng, L, mpos) for _ in range(n)]), setup.tril[0])
+              for n in (7, 5)]
+    mc = gcmc.GCMC(setup, seed=1)
+    mc.set_guests(guests)
+    res = {k: v.cpu().numpy() for k, v in mc.guest_stress().items()}
+    pos, q, sp, sysi, grp = mc.guest_table()
+    _, g, gt = mc.guest_potential(pos, q, sp, sysi, grp)
+    p, s, gr = pos.cpu().numpy(), sysi.cpu().numpy(), grp.cpu().numpy()
+    G = int(gr.max()) + 1
+    mol = oobs.molecular_virial_stress(p, g.cpu().numpy(), s, gr, G, setup.tril, gt.cpu().numpy())
+    scale = np.abs(mol).max()
+    np.testing.assert_allclose(res["potential"], mol, rtol=0, atol=1e-10 * scale)
+
+    com, _ = oobs.group_centres(p, gr, G, s, setup.tril)
+    w = p - ouc.wrap(p - com[gr], setup.tril[s])
+
+    def energy(eps):
+        pe = torch.as_tensor(p + eps * w, device="cuda")
+        return mc.guest_potential(pe, q, sp, sysi, grp, tril=setup.tril * (1 + eps))[0].cpu().numpy()
+
+    h = 1e-6
+    dU = (energy(h) - energy(-h)) / (2 * h)
+    p_fd = -dU / (3 * ouc.volume(setup.tril))
+    p_virial = np.trace(res["potential"], axis1=1, axis2=2) / 3
+    np.testing.assert_allclose(p_virial, p_fd, rtol=0, atol=1e-5 * scale)
+
+    counts = np.zeros((2, setup.sigma.shape[0]))
+    for i, n in enumerate((7, 5)):
+        np.add.at(counts[i], setup.fw_species, 1)
+        np.add.at(counts[i], np.tile(setup.motif_species, n), 1)
+    pt = olj.tail_correction_pressure(counts, setup.tril, setup.sigma, setup.epsilon, setup.rc_lj,
+                                      setup.epsilon > 0)
+    np.testing.assert_allclose(res["tail_correction"], pt[:, None, None] * np.eye(3), rtol=1e-10, atol=1e-300)
+    pi = oobs.ideal_gas_pressure([7, 5], setup.temperature, setup.tril)
+    np.testing.assert_allclose(res["ideal_gas"], pi[:, None, None] * np.eye(3), rtol=1e-12, atol=1e-300)
