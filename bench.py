@@ -474,6 +474,40 @@ def run_bonded(a, reps=20):
     for t in terms:
         t.fp32 = True
     ms32 = timed()
+    for t in terms:
+        t.fp32 = False
+    # MC energy change of one moved atom per chain (all systems in one call per term)
+    rng = np.random.default_rng(4)
+    ch = torch.as_tensor((np.arange(S) * n_per + rng.integers(0, n_per, S)).astype(np.int32), device=dev)
+    newp = (p[ch.long()] + torch.as_tensor(rng.normal(scale=0.2, size=(S, 3)), device=dev)).contiguous()
+    delta = torch.zeros(S, dtype=torch.float64, device=dev)
+    dws = torch.empty(_lib.load().kups_bonded_delta_workspace_bytes(p.shape[0]), dtype=torch.uint8, device=dev)
+    def delta_all():
+        for t in terms:
+            t.add_delta(p, sy, sp, tr, ch, newp, None, delta, dws, status)
+
+    def timed_delta(run):
+        run()
+        torch.cuda.synchronize()
+        d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d0.record()
+        for _ in range(reps):
+            run()
+        d1.record()
+        torch.cuda.synchronize()
+        _lib.raise_status(read_status(status))
+        return d0.elapsed_time(d1) / reps
+
+    ms_delta_eager = timed_delta(delta_all)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        delta_all()  # warm-up on the capturing stream
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        delta_all()  # every launch of the four terms (memset, slot table, edge scan) in one graph
+    ms_delta = timed_delta(graph.replay)
     lib = _lib.load()
     n_edges = sum(t._edges.shape[0] for t in terms)
     nbytes = sum(t._edges.shape[0] * (t.order * (4 + 4 + 24 + 24) + 12 * (t.order - 1)
@@ -483,6 +517,9 @@ def run_bonded(a, reps=20):
     return {"workload": f"{S} chains x {n_per} atoms: bonds, angles, dihedrals, inversions ({n_edges} edges)",
             "ms_per_evaluation": ms, "edges_per_s": n_edges / (ms / 1e3),
             "ms_per_evaluation_fp32": ms32, "edges_per_s_fp32": n_edges / (ms32 / 1e3),
+            "mc_delta": {"ms_per_call": ms_delta, "ms_per_call_eager": ms_delta_eager, "moved_atoms": S,
+                         "note": "one moved atom per chain, four terms, every edge scanned for a moved atom; "
+                                 "ms_per_call replays the four calls from a CUDA graph, eager is host-launched"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "peak_source": kind, "note": "float64 atomics into the gradient, four launches per "
                                                       "evaluation, buffers allocated once"},

@@ -360,6 +360,30 @@ int32_t kups_bonded_edges(int32_t kind, const double *positions, const int32_t *
                           double *energy, double *grad, double *grad_tril, int32_t fp32,
                           kups_status *status, void *stream);
 
+/* MC energy change of a bonded term for a patch of moved particles — replaces the
+ * old-graph / new-graph pair of LocalGraphSumComposer over an EdgeSetGraphConstructor
+ * with a probe (src/kups/potential/common/graph.py:336-361, 412-450).
+ *   delta[s] += sum over edges with an atom in `changed` of E_e(new) - E_e(old), the
+ *   edge's system being that of its atom 0 (zero delta first; terms add up).
+ *   changed       i32 [n_changed] distinct particle indices (all systems in one call)
+ *   new_positions f64 [n_changed, 3]
+ *   new_image     i32 [n_changed, 3] or NULL: the lattice offset n with
+ *                 new_position = unwrapped - n @ L when the move wrapped the atom; an
+ *                 edge's shifts become s_m + n_{m+1} - n_0, as the reference's probe
+ *                 rewrites the edge data
+ * Positions are not modified.  Workspace: kups_bonded_delta_workspace_bytes(n_particles).
+ * Other arguments as kups_bonded_edges; a changed index out of range records
+ * KUPS_ERR_INVALID (first_bad = its position in `changed`). */
+size_t kups_bonded_delta_workspace_bytes(int64_t n_particles);
+int32_t kups_bonded_delta(int32_t kind, const double *positions, const int32_t *system,
+                          const int32_t *species, int64_t n_particles, const double *tril,
+                          int32_t n_systems, const int32_t *edges, const int32_t *shifts,
+                          int64_t n_edges, const double *params, int32_t n_species,
+                          const int32_t *changed, const double *new_positions,
+                          const int32_t *new_image, int64_t n_changed, double *delta, int32_t fp32,
+                          void *workspace, size_t workspace_bytes, kups_status *status,
+                          void *stream);
+
 /* ------------------------------------------------------------------------
  * Integrator building blocks on the float64 particle table (systems larger
  * than kups_lj_md_max_atoms, Ewald MD): MomentumStep (p -= dE/dx * dt * scale),

@@ -139,6 +139,17 @@ class BondedTerm:
             grad_tril.data_ptr() if grad_tril is not None else None, int(self.fp32), status.data_ptr(), _stream())
         _lib.check(rc, "kups_bonded_edges")
 
+    def add_delta(self, positions, system, species, tril, changed, new_positions, new_image, delta, workspace, status):
+        """delta[s] += E(new) - E(old) over this term's edges that touch a changed particle."""
+        ws_bytes = workspace.numel()
+        rc = _lib.load().kups_bonded_delta(
+            self.parameters.kind, positions.data_ptr(), system.data_ptr(), species.data_ptr(), positions.shape[0],
+            tril.data_ptr(), tril.shape[0], self._edges.data_ptr(), self._shifts.data_ptr(), self._edges.shape[0],
+            self._table.data_ptr(), self.n_species, changed.data_ptr(), new_positions.data_ptr(),
+            new_image.data_ptr() if new_image is not None else None, changed.shape[0], delta.data_ptr(),
+            int(self.fp32), workspace.data_ptr(), ws_bytes, status.data_ptr(), _stream())
+        _lib.check(rc, "kups_bonded_delta")
+
 
 def evaluate(terms, positions, system, species, tril):
     """Sum of bonded terms: (energy [S], dE/dx [N, 3], dE/dtril [S, 6]), float64 device tensors."""
@@ -156,3 +167,26 @@ def evaluate(terms, positions, system, species, tril):
         t.add_to(pos, sysi, spc, tr, energy, grad, grad_tril, status)
     _lib.raise_status(read_status(status))
     return energy, grad, grad_tril
+
+
+def delta_energy(terms, positions, system, species, tril, changed, new_positions, new_image=None):
+    """MC energy change [S] of a sum of bonded terms when the particles `changed` move to
+    `new_positions` (the old-graph / new-graph difference of the reference's
+    LocalGraphSumComposer, potential/common/graph.py:412-450); ``new_image`` [k, 3] gives the
+    lattice offset n of each moved atom whose new position was wrapped (new = unwrapped - n @ L)."""
+    dev = "cuda"
+    pos = torch.as_tensor(positions, dtype=torch.float64, device=dev).contiguous()
+    sysi = torch.as_tensor(system, device=dev).to(torch.int32).contiguous()
+    spc = torch.as_tensor(species, device=dev).to(torch.int32).contiguous()
+    tr = torch.as_tensor(tril, dtype=torch.float64, device=dev).contiguous()
+    ch = torch.as_tensor(changed, device=dev).to(torch.int32).contiguous()
+    npos = torch.as_tensor(new_positions, dtype=torch.float64, device=dev).reshape(-1, 3).contiguous()
+    img = (torch.as_tensor(new_image, device=dev).to(torch.int32).reshape(-1, 3).contiguous()
+           if new_image is not None else None)
+    delta = torch.zeros(tr.shape[0], dtype=torch.float64, device=dev)
+    ws = torch.empty(_lib.load().kups_bonded_delta_workspace_bytes(pos.shape[0]), dtype=torch.uint8, device=dev)
+    status = new_status()
+    for t in terms:
+        t.add_delta(pos, sysi, spc, tr, ch, npos, img, delta, ws, status)
+    _lib.raise_status(read_status(status))
+    return delta

@@ -118,6 +118,13 @@ def test_host_side_validation_of_newer_entry_points():
                                  None) == _lib.KUPS_ERR_INVALID
     assert lib.kups_bonded_edges(0, None, None, None, 0, None, 0, None, None, 0, None, 1, None, None, None, 1, None,
                                  None) == _lib.KUPS_OK  # no edges: nothing to do
+    assert lib.kups_bonded_delta(6, None, None, None, 0, None, 0, None, None, 1, None, 1, None, None, None, 1, None,
+                                 0, None, 0, None, None) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_bonded_delta(0, None, None, None, 0, None, 0, None, None, 1, None, 1, None, None, None, 0, None,
+                                 0, None, 0, None, None) == _lib.KUPS_OK  # nothing moved
+    assert lib.kups_bonded_delta(0, 8, 8, 8, 2, 8, 1, 8, 8, 1, 8, 1, 8, 8, None, 1, 8, 0, 8, 4, 8,
+                                 None) == _lib.KUPS_ERR_INVALID  # workspace too small (nothing dereferenced)
+    assert lib.kups_bonded_delta_workspace_bytes(10) >= 40
     a = _lib.MdArgs()
     a.n_systems, a.n_species, a.n_steps, a.neighbor_capacity = 1, 1, 1, 64
     for integrator, fields in ((4, {}), (2, {}), (3, {"thermostat_tau": 8})):

@@ -137,3 +137,73 @@ def test_out_of_range_edge_is_reported():
     with pytest.raises(_lib.KupsError):
         bonded.evaluate([term], np.zeros((2, 3)) + [[0, 0, 0], [1.0, 0, 0]], np.zeros(2, np.int32),
                         np.zeros(2, np.int32), np.array([[10.0, 0, 10.0, 0, 0, 10.0]]))
+
+
+def _moved(rng, pos, system, tril, n_changed):
+    """Distinct moved atoms, small displacements, new positions wrapped into the cell with
+    their lattice offsets (new = unwrapped - n @ L)."""
+    from oracle.unitcell import lattice_from_tril, to_fractional
+
+    ch = rng.choice(len(pos), n_changed, replace=False)
+    L = lattice_from_tril(tril[system[ch]])
+    hop = rng.integers(-1, 2, (n_changed, 3)).astype(float)  # some moves land in a neighbouring cell
+    unwrapped = pos[ch] + rng.normal(scale=0.3, size=(n_changed, 3)) + np.einsum("ka,kab->kb", hop, L)
+    f = to_fractional(unwrapped, tril[system[ch]])
+    n = np.floor(f + 0.5).astype(np.int64)
+    new = unwrapped - np.einsum("ka,kab->kb", n.astype(float), L)
+    return ch, new, n
+
+
+@pytest.mark.parametrize("kind", list(ob.KINDS))
+@pytest.mark.parametrize("fp32", [False, True])
+def test_mc_delta_matches_the_oracle_energy_difference(kind, fp32):
+    """kups_bonded_delta (old-graph / new-graph difference over the affected edges,
+    graph.py:336-361, 412-450) against the oracle's total energies before and after the move,
+    with wrapped moves rewriting the edge shifts; relative 1e-9 (float64 per-edge arithmetic)
+    or 2e-5 (float32) of the largest total energy."""
+    from kups_gb300 import bonded
+
+    rng = np.random.default_rng(ob.KINDS[kind][0] + 31)
+    pos, system, species, tril, edges, shifts, table, T, order = random_case(kind, rng)
+    ch, new, n = _moved(rng, pos, system, tril, 25)
+    term = bonded.BondedTerm(params_object(kind, table, T, order), edges, shifts, fp32=fp32)
+    d = bonded.delta_energy([term], pos, system, species, tril, ch, new, n).cpu().numpy()
+    img = np.zeros((len(pos), 3), np.int64)
+    img[ch] = n
+    pos_new = pos.copy()
+    pos_new[ch] = new
+    shifts_new = shifts + img[edges[:, 1:]] - img[edges[:, :1]]
+    e0 = ob.bonded(kind, pos, system, species, tril, table, T, edges, shifts)[0]
+    e1 = ob.bonded(kind, pos_new, system, species, tril, table, T, edges, shifts_new)[0]
+    tol = (2e-5 if fp32 else 1e-9) * np.abs(e0).max()
+    np.testing.assert_allclose(d, e1 - e0, rtol=0, atol=tol)
+    assert np.any(n != 0)  # some moves wrapped
+
+
+def test_mc_delta_of_null_and_lattice_moves_is_zero():
+    from oracle.unitcell import lattice_from_tril
+
+    from kups_gb300 import bonded
+
+    rng = np.random.default_rng(2)
+    pos, system, species, tril, edges, shifts, table, T, order = random_case("dihedral", rng)
+    term = bonded.BondedTerm(params_object("dihedral", table, T, order), edges, shifts)
+    ch = rng.choice(len(pos), 30, replace=False)
+    d = bonded.delta_energy([term], pos, system, species, tril, ch, pos[ch]).cpu().numpy()
+    assert np.abs(d).max() < 1e-12
+    n = rng.integers(-2, 3, (30, 3))
+    L = lattice_from_tril(tril[system[ch]])
+    moved = pos[ch] - np.einsum("ka,kab->kb", n.astype(float), L)  # the same atoms, other images
+    d = bonded.delta_energy([term], pos, system, species, tril, ch, moved, n).cpu().numpy()
+    e0 = ob.bonded("dihedral", pos, system, species, tril, table, T, edges, shifts)[0]
+    assert np.abs(d).max() < 1e-9 * np.abs(e0).max()
+
+
+def test_mc_delta_reports_a_bad_index():
+    from kups_gb300 import _lib, bonded
+
+    term = bonded.BondedTerm(bonded.HarmonicBondParameters(("A",), np.ones((1, 1)), np.ones((1, 1))),
+                             np.array([[0, 1]]))
+    with pytest.raises(_lib.KupsError):
+        bonded.delta_energy([term], np.zeros((2, 3)) + [[0, 0, 0], [1.0, 0, 0]], np.zeros(2, np.int32),
+                            np.zeros(2, np.int32), np.array([[10.0, 0, 10.0, 0, 0, 10.0]]), [5], [[0.0, 0, 0]])
