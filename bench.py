@@ -508,6 +508,16 @@ def run_bonded(a, reps=20):
     with torch.cuda.graph(graph):
         delta_all()  # every launch of the four terms (memset, slot table, edge scan) in one graph
     ms_delta = timed_delta(graph.replay)
+    for t in terms:
+        t.fp32 = True
+    delta_all()
+    torch.cuda.synchronize()
+    graph32 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph32):
+        delta_all()
+    ms_delta32 = timed_delta(graph32.replay)
+    for t in terms:
+        t.fp32 = False
     lib = _lib.load()
     n_edges = sum(t._edges.shape[0] for t in terms)
     nbytes = sum(t._edges.shape[0] * (t.order * (4 + 4 + 24 + 24) + 12 * (t.order - 1)
@@ -517,9 +527,11 @@ def run_bonded(a, reps=20):
     return {"workload": f"{S} chains x {n_per} atoms: bonds, angles, dihedrals, inversions ({n_edges} edges)",
             "ms_per_evaluation": ms, "edges_per_s": n_edges / (ms / 1e3),
             "ms_per_evaluation_fp32": ms32, "edges_per_s_fp32": n_edges / (ms32 / 1e3),
-            "mc_delta": {"ms_per_call": ms_delta, "ms_per_call_eager": ms_delta_eager, "moved_atoms": S,
-                         "note": "one moved atom per chain, four terms, every edge scanned for a moved atom; "
-                                 "ms_per_call replays the four calls from a CUDA graph, eager is host-launched"},
+            "mc_delta": {"ms_per_call": ms_delta, "ms_per_call_fp32": ms_delta32, "ms_per_call_eager": ms_delta_eager,
+                         "moved_atoms": S,
+                         "note": "one moved atom per chain, four terms, each moved atom's edges from the incidence "
+                                 "lists; ms_per_call replays the four calls from a CUDA graph, eager is "
+                                 "host-launched"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "peak_source": kind, "note": "float64 atomics into the gradient, four launches per "
                                                       "evaluation, buffers allocated once"},

@@ -371,6 +371,11 @@ int32_t kups_bonded_edges(int32_t kind, const double *positions, const int32_t *
  *                 new_position = unwrapped - n @ L when the move wrapped the atom; an
  *                 edge's shifts become s_m + n_{m+1} - n_0, as the reference's probe
  *                 rewrites the edge data
+ *   incidence_offsets i64 [n_particles + 1], incidence_edges i32 [...] or both NULL:
+ *                 the edges of particle i are incidence_edges[incidence_offsets[i] ..
+ *                 incidence_offsets[i + 1]), each listed once; with them each changed
+ *                 particle walks its own edges (an edge with several changed particles is
+ *                 taken by the one earliest in `changed`), without them every edge is scanned
  * Positions are not modified.  Workspace: kups_bonded_delta_workspace_bytes(n_particles).
  * Other arguments as kups_bonded_edges; a changed index out of range records
  * KUPS_ERR_INVALID (first_bad = its position in `changed`). */
@@ -379,6 +384,7 @@ int32_t kups_bonded_delta(int32_t kind, const double *positions, const int32_t *
                           const int32_t *species, int64_t n_particles, const double *tril,
                           int32_t n_systems, const int32_t *edges, const int32_t *shifts,
                           int64_t n_edges, const double *params, int32_t n_species,
+                          const int64_t *incidence_offsets, const int32_t *incidence_edges,
                           const int32_t *changed, const double *new_positions,
                           const int32_t *new_image, int64_t n_changed, double *delta, int32_t fp32,
                           void *workspace, size_t workspace_bytes, kups_status *status,

@@ -123,8 +123,8 @@ SIGNATURES = {
     "kups_bonded_param_count": (_I32, [_I32]),
     "kups_bonded_edges": (_I32, [_I32, _P, _P, _P, _I64, _P, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P, _I32, _P, _P]),
     "kups_bonded_delta_workspace_bytes": (_SZ, [_I64]),
-    "kups_bonded_delta": (_I32, [_I32, _P, _P, _P, _I64, _P, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P, _I64, _P, _I32,
-                                 _P, _SZ, _P, _P]),
+    "kups_bonded_delta": (_I32, [_I32, _P, _P, _P, _I64, _P, _I32, _P, _P, _I64, _P, _I32, _P, _P, _P, _P, _P, _I64,
+                                 _P, _I32, _P, _SZ, _P, _P]),
     "kups_erfc_eval": (_I32, [_P, _I64, _P, _P]),
     "kups_pair_edges": (_I32, [_P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
 }

@@ -139,13 +139,35 @@ class BondedTerm:
             grad_tril.data_ptr() if grad_tril is not None else None, int(self.fp32), status.data_ptr(), _stream())
         _lib.check(rc, "kups_bonded_edges")
 
-    def add_delta(self, positions, system, species, tril, changed, new_positions, new_image, delta, workspace, status):
-        """delta[s] += E(new) - E(old) over this term's edges that touch a changed particle."""
+    def incidence(self, n_particles):
+        """Atom -> edge lists (CSR: offsets int64 [n + 1], edge ids int32), each (atom, edge)
+        pair once; built on the device once per particle count (the edge set is fixed)."""
+        cache = getattr(self, "_incidence", None)
+        if cache is not None and cache[0] == n_particles:
+            return cache[1], cache[2]
+        E = self._edges.shape[0]
+        atoms = self._edges.reshape(-1).to(torch.int64)
+        eid = torch.arange(E, device="cuda", dtype=torch.int64).repeat_interleave(self.order)
+        ok = (atoms >= 0) & (atoms < n_particles)
+        key = torch.unique(atoms[ok] * max(E, 1) + eid[ok])
+        atom = key // max(E, 1)
+        offsets = torch.zeros(n_particles + 1, dtype=torch.int64, device="cuda")
+        offsets[1:] = torch.cumsum(torch.bincount(atom, minlength=n_particles), 0)
+        edges = (key % max(E, 1)).to(torch.int32).contiguous()
+        self._incidence = (n_particles, offsets, edges)
+        return offsets, edges
+
+    def add_delta(self, positions, system, species, tril, changed, new_positions, new_image, delta, workspace, status,
+                  use_incidence=True):
+        """delta[s] += E(new) - E(old) over this term's edges that touch a changed particle
+        (through the incidence lists, or by scanning every edge)."""
         ws_bytes = workspace.numel()
+        off, inc = self.incidence(positions.shape[0]) if use_incidence else (None, None)
         rc = _lib.load().kups_bonded_delta(
             self.parameters.kind, positions.data_ptr(), system.data_ptr(), species.data_ptr(), positions.shape[0],
             tril.data_ptr(), tril.shape[0], self._edges.data_ptr(), self._shifts.data_ptr(), self._edges.shape[0],
-            self._table.data_ptr(), self.n_species, changed.data_ptr(), new_positions.data_ptr(),
+            self._table.data_ptr(), self.n_species, off.data_ptr() if off is not None else None,
+            inc.data_ptr() if inc is not None else None, changed.data_ptr(), new_positions.data_ptr(),
             new_image.data_ptr() if new_image is not None else None, changed.shape[0], delta.data_ptr(),
             int(self.fp32), workspace.data_ptr(), ws_bytes, status.data_ptr(), _stream())
         _lib.check(rc, "kups_bonded_delta")
@@ -169,7 +191,7 @@ def evaluate(terms, positions, system, species, tril):
     return energy, grad, grad_tril
 
 
-def delta_energy(terms, positions, system, species, tril, changed, new_positions, new_image=None):
+def delta_energy(terms, positions, system, species, tril, changed, new_positions, new_image=None, use_incidence=True):
     """MC energy change [S] of a sum of bonded terms when the particles `changed` move to
     `new_positions` (the old-graph / new-graph difference of the reference's
     LocalGraphSumComposer, potential/common/graph.py:412-450); ``new_image`` [k, 3] gives the
@@ -187,6 +209,6 @@ def delta_energy(terms, positions, system, species, tril, changed, new_positions
     ws = torch.empty(_lib.load().kups_bonded_delta_workspace_bytes(pos.shape[0]), dtype=torch.uint8, device=dev)
     status = new_status()
     for t in terms:
-        t.add_delta(pos, sysi, spc, tr, ch, npos, img, delta, ws, status)
+        t.add_delta(pos, sysi, spc, tr, ch, npos, img, delta, ws, status, use_incidence)
     _lib.raise_status(read_status(status))
     return delta

@@ -351,13 +351,70 @@ __global__ void changed_slot_kernel(const int32_t *changed, int64_t n_changed, i
 // new_pos[slot[d]]; its wrap image n_d (new position = unwrapped - n_d @ L) moves the
 // edge's shifts to s_m + n_{m+1} - n_0, which keeps each difference vector on the same
 // image (the edge data the reference's probe updates).
+// E_e(new) - E_e(old) of edge e whose atoms idx[] have slots sl[] (-1: not moved);
+// returns the edge's system, or -1 (status recorded) for an invalid species or system.
+template <int KIND, typename R>
+__device__ int edge_delta(int64_t e, const int *idx, const int *sl, const double *pos, const int32_t *system,
+                          const int32_t *species, const double *tril, int32_t n_sys, const int32_t *shifts,
+                          const double *params, int32_t nsp, const double *new_pos, const int32_t *new_image,
+                          double &de, kups_status *status) {
+  constexpr int D = Kind<KIND>::order, P = Kind<KIND>::params;
+  bool ok = true;
+  int64_t row = 0;
+  for (int d = 0; d < D; ++d) {
+    const int t = species[idx[d]];
+    ok &= t >= 0 && t < nsp;
+    row = row * nsp + t;
+  }
+  const int s0 = system[idx[0]];
+  if (!ok || s0 < 0 || s0 >= n_sys) {
+    status_error(status, KUPS_ERR_INVALID, e);
+    return -1;
+  }
+  const Tril64 L = load_tril64(tril + 6 * (int64_t)s0);
+  double x_old[D][3], x_new[D][3], img[D][3];
+  for (int d = 0; d < D; ++d)
+    for (int a = 0; a < 3; ++a) {
+      x_old[d][a] = pos[3 * (int64_t)idx[d] + a];
+      x_new[d][a] = sl[d] >= 0 ? new_pos[3 * (int64_t)sl[d] + a] : x_old[d][a];
+      img[d][a] = (sl[d] >= 0 && new_image) ? (double)new_image[3 * (int64_t)sl[d] + a] : 0.0;
+    }
+  R v_old[D - 1][3], v_new[D - 1][3], g[D - 1][3], pr[P];
+  for (int m = 0; m < D - 1; ++m) {
+    double sh[3], sh_new[3], sL[3], sL_new[3];
+    for (int a = 0; a < 3; ++a) {
+      sh[a] = shifts[((int64_t)(D - 1) * e + m) * 3 + a];
+      sh_new[a] = sh[a] + img[m + 1][a] - img[0][a];
+    }
+    row_times_tril64(sh, L, sL);
+    row_times_tril64(sh_new, L, sL_new);
+    for (int a = 0; a < 3; ++a) {
+      v_old[m][a] = (R)(x_old[m + 1][a] - x_old[0][a] + sL[a]);
+      v_new[m][a] = (R)(x_new[m + 1][a] - x_new[0][a] + sL_new[a]);
+    }
+  }
+  for (int k = 0; k < P; ++k) pr[k] = (R)params[row * P + k];
+  const double e_new = (double)edge_energy_grad<KIND, R>(v_new, pr, g);
+  const double e_old = (double)edge_energy_grad<KIND, R>(v_old, pr, g);
+  de = e_new - e_old;
+  if (!isfinite(de)) status_error(status, KUPS_ERR_NONFINITE, e);
+  return s0;
+}
+
+// delta[s] += E_e(new) - E_e(old) over the edges with at least one changed atom: the
+// old graph (weight -1) and new graph (weight +1) of LocalGraphSumComposer
+// (src/kups/potential/common/graph.py:412-450) restricted, as EdgeSetGraphConstructor's
+// probe path restricts them (:336-361), to the affected edges.  A changed atom d takes
+// new_pos[slot[d]]; its wrap image n_d (new position = unwrapped - n_d @ L) moves the
+// edge's shifts to s_m + n_{m+1} - n_0, which keeps each difference vector on the same
+// image (the edge data the reference's probe updates).  This form scans every edge.
 template <int KIND, typename R>
 __global__ void bonded_delta_kernel(const double *pos, const int32_t *system, const int32_t *species, int64_t n,
                                     const double *tril, int32_t n_sys, const int32_t *edges, const int32_t *shifts,
                                     int64_t n_edges, const double *params, int32_t nsp, const int32_t *slot,
                                     const double *new_pos, const int32_t *new_image, double *delta,
                                     kups_status *status) {
-  constexpr int D = Kind<KIND>::order, P = Kind<KIND>::params;
+  constexpr int D = Kind<KIND>::order;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
   double de = 0.0;
@@ -373,51 +430,60 @@ __global__ void bonded_delta_kernel(const double *pos, const int32_t *system, co
         sl[d] = slot[idx[d]];
         touched |= sl[d] >= 0;
       }
-    if (!ok) {
+    if (!ok)
       status_error(status, KUPS_ERR_INVALID, e);
-    } else if (touched) {
-      int64_t row = 0;
-      for (int d = 0; d < D; ++d) {
-        const int t = species[idx[d]];
-        ok &= t >= 0 && t < nsp;
-        row = row * nsp + t;
-      }
-      const int s0 = system[idx[0]];
-      if (!ok || s0 < 0 || s0 >= n_sys) {
-        status_error(status, KUPS_ERR_INVALID, e);
-      } else {
-        const Tril64 L = load_tril64(tril + 6 * (int64_t)s0);
-        double x_old[D][3], x_new[D][3], img[D][3];
-        for (int d = 0; d < D; ++d)
-          for (int a = 0; a < 3; ++a) {
-            x_old[d][a] = pos[3 * (int64_t)idx[d] + a];
-            x_new[d][a] = sl[d] >= 0 ? new_pos[3 * (int64_t)sl[d] + a] : x_old[d][a];
-            img[d][a] = (sl[d] >= 0 && new_image) ? (double)new_image[3 * (int64_t)sl[d] + a] : 0.0;
-          }
-        R v_old[D - 1][3], v_new[D - 1][3], g[D - 1][3], pr[P];
-        for (int m = 0; m < D - 1; ++m) {
-          double sh[3], sh_new[3], sL[3], sL_new[3];
-          for (int a = 0; a < 3; ++a) {
-            sh[a] = shifts[((int64_t)(D - 1) * e + m) * 3 + a];
-            sh_new[a] = sh[a] + img[m + 1][a] - img[0][a];
-          }
-          row_times_tril64(sh, L, sL);
-          row_times_tril64(sh_new, L, sL_new);
-          for (int a = 0; a < 3; ++a) {
-            v_old[m][a] = (R)(x_old[m + 1][a] - x_old[0][a] + sL[a]);
-            v_new[m][a] = (R)(x_new[m + 1][a] - x_new[0][a] + sL_new[a]);
-          }
-        }
-        for (int k = 0; k < P; ++k) pr[k] = (R)params[row * P + k];
-        const double e_new = (double)edge_energy_grad<KIND, R>(v_new, pr, g);
-        const double e_old = (double)edge_energy_grad<KIND, R>(v_old, pr, g);
-        de = e_new - e_old;
-        if (!isfinite(de)) status_error(status, KUPS_ERR_NONFINITE, e);
-        sys = s0;
-      }
-    }
+    else if (touched)
+      sys = edge_delta<KIND, R>(e, idx, sl, pos, system, species, tril, n_sys, shifts, params, nsp, new_pos,
+                                new_image, de, status);
   }
   add_system(delta, 1, 0, sys, de);
+}
+
+// The same sum through the atom -> edge incidence lists: changed atom k's edges are
+// split over kDeltaSplit consecutive threads (edge j to thread j mod kDeltaSplit), so
+// that a batch of a few thousand moved atoms spreads over every SM; an edge with
+// several changed atoms belongs to the one earliest in `changed`.
+constexpr int kDeltaSplit = 4;
+template <int KIND, typename R>
+__global__ void bonded_delta_incident_kernel(const double *pos, const int32_t *system, const int32_t *species,
+                                             int64_t n, const double *tril, int32_t n_sys, const int32_t *edges,
+                                             const int32_t *shifts, int64_t n_edges, const double *params,
+                                             int32_t nsp, const int32_t *changed, int64_t n_changed,
+                                             const int64_t *inc_offsets, const int32_t *inc_edges,
+                                             const int32_t *slot, const double *new_pos, const int32_t *new_image,
+                                             double *delta, kups_status *status) {
+  constexpr int D = Kind<KIND>::order;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = t / kDeltaSplit;
+  if (k >= n_changed) return;
+  const int32_t i = changed[k];
+  if (i < 0 || i >= n) return;  // recorded by changed_slot_kernel
+  for (int64_t q = inc_offsets[i] + t % kDeltaSplit; q < inc_offsets[i + 1]; q += kDeltaSplit) {
+    const int64_t e = inc_edges[q];
+    if (e < 0 || e >= n_edges) {
+      status_error(status, KUPS_ERR_INVALID, e);
+      continue;
+    }
+    int idx[D], sl[D];
+    bool ok = true, mine = true;
+    for (int d = 0; d < D; ++d) {
+      idx[d] = edges[(int64_t)D * e + d];
+      ok &= idx[d] >= 0 && idx[d] < n;
+    }
+    if (!ok) {
+      status_error(status, KUPS_ERR_INVALID, e);
+      continue;
+    }
+    for (int d = 0; d < D; ++d) {
+      sl[d] = slot[idx[d]];
+      mine &= sl[d] < 0 || sl[d] >= k;
+    }
+    if (!mine) continue;
+    double de = 0.0;
+    const int s = edge_delta<KIND, R>(e, idx, sl, pos, system, species, tril, n_sys, shifts, params, nsp, new_pos,
+                                      new_image, de, status);
+    if (s >= 0) atomicAdd(&delta[s], de);
+  }
 }
 
 template <int KIND, typename R>
@@ -506,7 +572,8 @@ extern "C" size_t kups_bonded_delta_workspace_bytes(int64_t n_particles) {
 extern "C" int32_t kups_bonded_delta(int32_t kind, const double *positions, const int32_t *system,
                                      const int32_t *species, int64_t n_particles, const double *tril,
                                      int32_t n_systems, const int32_t *edges, const int32_t *shifts, int64_t n_edges,
-                                     const double *params, int32_t n_species, const int32_t *changed,
+                                     const double *params, int32_t n_species, const int64_t *incidence_offsets,
+                                     const int32_t *incidence_edges, const int32_t *changed,
                                      const double *new_positions, const int32_t *new_image, int64_t n_changed,
                                      double *delta, int32_t fp32, void *workspace, size_t workspace_bytes,
                                      kups_status *status, void *stream_) {
@@ -525,13 +592,21 @@ extern "C" int32_t kups_bonded_delta(int32_t kind, const double *positions, cons
   KUPS_CUDA_TRY(cudaMemsetAsync(slot, 0xff, sizeof(int32_t) * (size_t)n_particles, stream));  // -1
   changed_slot_kernel<<<(unsigned)((n_changed + 127) / 128), 128, 0, stream>>>(changed, n_changed, n_particles, slot,
                                                                               status);
+  if ((incidence_offsets == nullptr) != (incidence_edges == nullptr)) return KUPS_ERR_INVALID;
+  const bool incident = incidence_offsets != nullptr;
   const unsigned grid = (unsigned)((n_edges + 127) / 128);
+  const unsigned grid_k = (unsigned)((n_changed * kDeltaSplit + 63) / 64);
   switch (kind * 2 + (fp32 ? 1 : 0)) {
-#define KUPS_DELTA_CASE(K, R)                                                                                   \
-  case 2 * K + (sizeof(R) == 4 ? 1 : 0):                                                                        \
-    bonded_delta_kernel<K, R><<<grid, 128, 0, stream>>>(positions, system, species, n_particles, tril, n_systems, \
-                                                        edges, shifts, n_edges, params, n_species, slot,          \
-                                                        new_positions, new_image, delta, status);                \
+#define KUPS_DELTA_CASE(K, R)                                                                                     \
+  case 2 * K + (sizeof(R) == 4 ? 1 : 0):                                                                          \
+    if (incident)                                                                                                 \
+      bonded_delta_incident_kernel<K, R><<<grid_k, 64, 0, stream>>>(                                              \
+          positions, system, species, n_particles, tril, n_systems, edges, shifts, n_edges, params, n_species,    \
+          changed, n_changed, incidence_offsets, incidence_edges, slot, new_positions, new_image, delta, status); \
+    else                                                                                                          \
+      bonded_delta_kernel<K, R><<<grid, 128, 0, stream>>>(positions, system, species, n_particles, tril,          \
+                                                          n_systems, edges, shifts, n_edges, params, n_species,   \
+                                                          slot, new_positions, new_image, delta, status);         \
     break;
     KUPS_DELTA_CASE(0, double)
     KUPS_DELTA_CASE(0, float)

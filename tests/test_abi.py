@@ -118,12 +118,13 @@ def test_host_side_validation_of_newer_entry_points():
                                  None) == _lib.KUPS_ERR_INVALID
     assert lib.kups_bonded_edges(0, None, None, None, 0, None, 0, None, None, 0, None, 1, None, None, None, 1, None,
                                  None) == _lib.KUPS_OK  # no edges: nothing to do
-    assert lib.kups_bonded_delta(6, None, None, None, 0, None, 0, None, None, 1, None, 1, None, None, None, 1, None,
-                                 0, None, 0, None, None) == _lib.KUPS_ERR_INVALID
-    assert lib.kups_bonded_delta(0, None, None, None, 0, None, 0, None, None, 1, None, 1, None, None, None, 0, None,
-                                 0, None, 0, None, None) == _lib.KUPS_OK  # nothing moved
-    assert lib.kups_bonded_delta(0, 8, 8, 8, 2, 8, 1, 8, 8, 1, 8, 1, 8, 8, None, 1, 8, 0, 8, 4, 8,
-                                 None) == _lib.KUPS_ERR_INVALID  # workspace too small (nothing dereferenced)
+    delta_args = lambda kind, n_changed, ws_bytes, ptr=None, inc=None: (
+        [kind, ptr, ptr, ptr, 2, ptr, 1, ptr, ptr, 1, ptr, 1, inc, inc, ptr, ptr, None, n_changed, ptr, 0, ptr,
+         ws_bytes, ptr, None])
+    assert lib.kups_bonded_delta(*delta_args(6, 1, 0)) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_bonded_delta(*delta_args(0, 0, 0)) == _lib.KUPS_OK  # nothing moved
+    # nothing below is dereferenced: each call is refused on the host
+    assert lib.kups_bonded_delta(*delta_args(0, 1, 4, ptr=8)) == _lib.KUPS_ERR_INVALID  # workspace too small
     assert lib.kups_bonded_delta_workspace_bytes(10) >= 40
     a = _lib.MdArgs()
     a.n_systems, a.n_species, a.n_steps, a.neighbor_capacity = 1, 1, 1, 64

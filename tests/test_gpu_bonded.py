@@ -155,8 +155,8 @@ def _moved(rng, pos, system, tril, n_changed):
 
 
 @pytest.mark.parametrize("kind", list(ob.KINDS))
-@pytest.mark.parametrize("fp32", [False, True])
-def test_mc_delta_matches_the_oracle_energy_difference(kind, fp32):
+@pytest.mark.parametrize("fp32,use_incidence", [(False, True), (True, True), (False, False)])
+def test_mc_delta_matches_the_oracle_energy_difference(kind, fp32, use_incidence):
     """kups_bonded_delta (old-graph / new-graph difference over the affected edges,
     graph.py:336-361, 412-450) against the oracle's total energies before and after the move,
     with wrapped moves rewriting the edge shifts; relative 1e-9 (float64 per-edge arithmetic)
@@ -167,7 +167,7 @@ def test_mc_delta_matches_the_oracle_energy_difference(kind, fp32):
     pos, system, species, tril, edges, shifts, table, T, order = random_case(kind, rng)
     ch, new, n = _moved(rng, pos, system, tril, 25)
     term = bonded.BondedTerm(params_object(kind, table, T, order), edges, shifts, fp32=fp32)
-    d = bonded.delta_energy([term], pos, system, species, tril, ch, new, n).cpu().numpy()
+    d = bonded.delta_energy([term], pos, system, species, tril, ch, new, n, use_incidence).cpu().numpy()
     img = np.zeros((len(pos), 3), np.int64)
     img[ch] = n
     pos_new = pos.copy()
