@@ -16,8 +16,10 @@
 //   E_s += E_e for the system of i_0.  Difference vectors in float64; the
 //   edge's arithmetic in float64, or in float32 with fp32 (this part issues
 //   about 2 float64 FMA per cycle per SM, so the float64 angles, square roots
-//   and trigonometry bound the float64 mode); per-system sums are warp-
-//   aggregated float64 atomics, per-atom gradients float64 atomics.  The float32
+//   and trigonometry bound the float64 mode); per-system sums are warp sums (in
+//   float in the float32 mode) added by one float64 atomic per warp, per-atom
+//   gradients float64 atomics (atom 0's summed over the edge first), and the
+//   image term s @ L is formed only for non-zero shifts.  The float32
 //   mode takes angles as atan2 of cross and dot products and the cosine-angle and
 //   inversion energies in factored forms, equal to the reference's in exact
 //   arithmetic but without its cancellations, which float32 would amplify.
@@ -266,6 +268,19 @@ __device__ R edge_energy_grad(const R (*v)[3], const R *p, R (*g)[3]) {
   }
 }
 
+// add_system for a float or double value: the warp's sum in R, added to the float64 array.
+template <typename R>
+__device__ inline void add_system_r(double *arr, int stride, int comp, int sys, R v) {
+  const unsigned full = 0xffffffffu;
+  const int s0 = __shfl_sync(full, sys, 0);
+  if (__all_sync(full, sys == s0)) {
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0 && sys >= 0) atomicAdd(&arr[(int64_t)sys * stride + comp], (double)v);
+  } else if (sys >= 0) {
+    atomicAdd(&arr[(int64_t)sys * stride + comp], (double)v);
+  }
+}
+
 template <int KIND, typename R>
 __global__ void bonded_kernel(const double *pos, const int32_t *system, const int32_t *species, int64_t n,
                               const double *tril, int32_t n_sys, const int32_t *edges, const int32_t *shifts,
@@ -274,7 +289,7 @@ __global__ void bonded_kernel(const double *pos, const int32_t *system, const in
   constexpr int D = Kind<KIND>::order, P = Kind<KIND>::params;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int sys = -1;
-  double en = 0.0, dl[6] = {0, 0, 0, 0, 0, 0};
+  R en = R(0.0), dl[6] = {R(0.0), R(0.0), R(0.0), R(0.0), R(0.0), R(0.0)};
   if (e < n_edges) {
     int idx[D];
     bool ok = true;
@@ -298,37 +313,44 @@ __global__ void bonded_kernel(const double *pos, const int32_t *system, const in
       const Tril64 L = load_tril64(tril + 6 * (int64_t)s0);
       // difference vectors in float64 (positions are float64), then the edge's arithmetic in R
       R v[D - 1][3], g[D - 1][3], pr[P];
-      double sh[D - 1][3];
+      int sh[D - 1][3];
+      const double *x0 = pos + 3 * (int64_t)idx[0];
       for (int m = 0; m < D - 1; ++m) {
         for (int a = 0; a < 3; ++a) sh[m][a] = shifts[((int64_t)(D - 1) * e + m) * 3 + a];
-        double sL[3];
-        row_times_tril64(sh[m], L, sL);
-        for (int a = 0; a < 3; ++a)
-          v[m][a] = (R)(pos[3 * (int64_t)idx[m + 1] + a] - pos[3 * (int64_t)idx[0] + a] + sL[a]);
+        // s @ L only for a non-zero shift (zero adds nothing: same result)
+        double sL[3] = {0.0, 0.0, 0.0};
+        if (sh[m][0] | sh[m][1] | sh[m][2]) {
+          const double shd[3] = {(double)sh[m][0], (double)sh[m][1], (double)sh[m][2]};
+          row_times_tril64(shd, L, sL);
+        }
+        for (int a = 0; a < 3; ++a) v[m][a] = (R)(pos[3 * (int64_t)idx[m + 1] + a] - x0[a] + sL[a]);
       }
       for (int k = 0; k < P; ++k) pr[k] = (R)params[row * P + k];
-      en = (double)edge_energy_grad<KIND, R>(v, pr, g);
+      en = edge_energy_grad<KIND, R>(v, pr, g);
       bool finite = isfinite(en);
       for (int m = 0; m < D - 1; ++m)
         for (int a = 0; a < 3; ++a) finite &= isfinite(g[m][a]);
       if (!finite) status_error(status, KUPS_ERR_NONFINITE, e);
+      R g0[3] = {R(0.0), R(0.0), R(0.0)};  // atom 0 takes -sum_m g_m in one atomic per axis
       for (int m = 0; m < D - 1; ++m) {
         for (int a = 0; a < 3; ++a) {
           atomicAdd(&grad[3 * (int64_t)idx[m + 1] + a], (double)g[m][a]);
-          atomicAdd(&grad[3 * (int64_t)idx[0] + a], -(double)g[m][a]);
+          g0[a] -= g[m][a];
         }
-        dl[0] += sh[m][0] * g[m][0];
-        dl[1] += sh[m][1] * g[m][0];
-        dl[2] += sh[m][1] * g[m][1];
-        dl[3] += sh[m][2] * g[m][0];
-        dl[4] += sh[m][2] * g[m][1];
-        dl[5] += sh[m][2] * g[m][2];
+        dl[0] += R(sh[m][0]) * g[m][0];
+        dl[1] += R(sh[m][1]) * g[m][0];
+        dl[2] += R(sh[m][1]) * g[m][1];
+        dl[3] += R(sh[m][2]) * g[m][0];
+        dl[4] += R(sh[m][2]) * g[m][1];
+        dl[5] += R(sh[m][2]) * g[m][2];
       }
+      for (int a = 0; a < 3; ++a) atomicAdd(&grad[3 * (int64_t)idx[0] + a], (double)g0[a]);
     }
   }
-  add_system(energy, 1, 0, sys, en);
+  // warp sums in R (float32 mode: float, the warp total added in float64), one atomic per warp
+  add_system_r<R>(energy, 1, 0, sys, en);
   if (grad_tril != nullptr)
-    for (int k = 0; k < 6; ++k) add_system(grad_tril, 6, k, sys, dl[k]);
+    for (int k = 0; k < 6; ++k) add_system_r<R>(grad_tril, 6, k, sys, dl[k]);
 }
 
 // slot[i] = k for the k-th changed particle, -1 for every other particle (slot preset to -1).
