@@ -52,6 +52,17 @@ __device__ inline void wrap64(const double r[3], const Tril64 &L, const Tril64 &
   row_times_tril64(f, L, out);
 }
 
+// The image the wrap takes: n = floor(f + 0.5), f = d @ L^-1 (the same rounding as
+// wrap64), so that wrap(d) = d - n @ L.  Returns false when n = 0 (wrap(d) = d up to the
+// rounding of the round trip through fractional coordinates).
+__device__ inline bool wrap_image64(const double d[3], const Tril64 &Li, double n[3]) {
+  double f[3];
+  row_times_tril64(d, Li, f);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) n[a] = floor(__dadd_rn(f[a], 0.5));
+  return n[0] != 0.0 || n[1] != 0.0 || n[2] != 0.0;
+}
+
 __device__ inline bool valid_index(int v, int n) { return v >= 0 && v < n; }
 
 // 1 / m to float64 accuracy without a float64 division: the float32 reciprocal
@@ -94,12 +105,17 @@ __global__ void group_sum_kernel(const double *pos, const int32_t *group, const 
   const int a = anchor[g];
   const Tril64 L = load_tril64(tril + 6 * (int64_t)s);
   const Tril64 Li = load_tril64(inv + 6 * (int64_t)s);
-  double d[3], w[3];
+  double d[3], img[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) d[c] = __dsub_rn(pos[3 * i + c], pos[3 * (int64_t)a + c]);
-  wrap64(d, L, Li, w);
+  if (wrap_image64(d, Li, img)) {  // wrap(d) = d - img @ L
+    double nL[3];
+    row_times_tril64(img, L, nL);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) atomicAdd(&gsum[4 * (int64_t)g + c], w[c]);
+    for (int c = 0; c < 3; ++c) d[c] = __dsub_rn(d[c], nL[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) atomicAdd(&gsum[4 * (int64_t)g + c], d[c]);
   atomicAdd(&gsum[4 * (int64_t)g + 3], 1.0);
 }
 
@@ -179,14 +195,23 @@ __global__ void __launch_bounds__(kThreads) virial_accumulate_kernel(
             Li = load_tril64(inv + 6 * (int64_t)s);
             lsys = s;
           }
-          double d[3], rel[3];
+          // w = r - wrap(r - R) = R + n @ L: the centre's image nearest the atom
+          double w[3], d[3], n[3];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) d[c] = __dsub_rn(r[c], gcentre[4 * (int64_t)gi + c]);
-          wrap64(d, L, Li, rel);
+          for (int c = 0; c < 3; ++c) {
+            w[c] = gcentre[4 * (int64_t)gi + c];
+            d[c] = __dsub_rn(r[c], w[c]);
+          }
+          if (wrap_image64(d, Li, n)) {
+            double nL[3];
+            row_times_tril64(n, L, nL);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) w[c] = __dadd_rn(w[c], nL[c]);
+          }
 #pragma unroll
           for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) v[10 + 3 * a + b] = __dsub_rn(r[a], rel[a]) * g[b];
+            for (int b = 0; b < 3; ++b) v[10 + 3 * a + b] = w[a] * g[b];
         } else {
           status_error(status, KUPS_ERR_INVALID, i);
         }
