@@ -114,3 +114,76 @@ def test_oracle_gradients_match_total_energy_differences(kind):
         fd = (ob.bonded(kind, pos, sysi, species, t1, table, T, edges, shifts)[0][0]
               - ob.bonded(kind, pos, sysi, species, t2, table, T, edges, shifts)[0][0]) / (2 * h)
         assert fd == pytest.approx(gt[0, k], rel=1e-5, abs=1e-6 * max(1.0, np.abs(gt).max()))
+
+
+def test_morse_known_answers_with_species_pairs():
+    """test/potential/classical/test_morse.py:35-133: two species with asymmetric-looking but
+    symmetric pair tables, the (A, B) pair evaluated: zero at r0, the dissociation limit D,
+    compression above extension, the closed form at r = 1, zero gradient at r0, within 5 % of
+    the harmonic bond with k = D alpha^2 near r0; MorseBondParameters.from_harmonic."""
+    from kups_gb300.bonded import MorseBondParameters
+
+    r0 = np.array([[1.5, 1.2], [1.2, 1.8]])
+    D = np.array([[2.0, 1.5], [1.5, 2.5]])
+    alpha = np.array([[2.0, 1.8], [1.8, 2.2]])
+    table = np.stack([r0, D, alpha], -1).reshape(4, 3)
+    species = np.array([0, 1])
+
+    def morse(r, kind="morse_bond", tab=table):
+        pos = np.array([[0.0, 0, 0], [r, 0, 0]])
+        e, g, _ = ob.bonded(kind, pos, np.zeros(2, int), species, BOX * 10, tab, 2, np.array([[0, 1]]),
+                            np.zeros((1, 1, 3)))
+        return e[0], g
+
+    assert morse(1.2)[0] == pytest.approx(0.0, abs=1e-10)
+    assert morse(1.5)[0] > 0
+    assert morse(100.0)[0] == pytest.approx(1.5, rel=1e-6)
+    assert morse(1.2 - 0.3)[0] > morse(1.2 + 0.3)[0]
+    assert morse(1.0)[0] == pytest.approx(1.5 * (1 - math.exp(-1.8 * (1.0 - 1.2))) ** 2, rel=1e-6)
+    np.testing.assert_allclose(morse(1.2)[1], 0.0, atol=1e-6)
+    assert np.linalg.norm(morse(1.5)[1]) > 1e-6
+    harmonic = np.stack([r0, D * alpha**2], -1).reshape(4, 2)
+    assert morse(1.21)[0] == pytest.approx(morse(1.21, "harmonic_bond", harmonic)[0], rel=0.05)
+    k = np.array([[100.0, 80.0], [80.0, 120.0]])
+    p = MorseBondParameters.from_harmonic(("A", "B"), np.array([[1.0, 1.2], [1.2, 1.5]]), k, D)
+    np.testing.assert_allclose(p.alpha, np.sqrt(k / D))
+    np.testing.assert_allclose(p.D, D)
+
+
+def _energy_grad(kind, pos, row, order, edges=None, system=None, boxes=None):
+    T = 1
+    table = np.asarray(row, np.float64).reshape(1, -1)
+    edges = np.arange(order)[None] if edges is None else np.asarray(edges)
+    system = np.zeros(len(pos), int) if system is None else np.asarray(system)
+    boxes = BOX if boxes is None else boxes
+    return ob.bonded(kind, pos, system, np.zeros(len(pos), int), boxes, table, T, edges,
+                     np.zeros((len(edges), order - 1, 3)))
+
+
+def test_remaining_cosine_angle_and_inversion_cases():
+    """test/potential/classical/test_cosine_angle.py:61-110 (zero gradient at theta0 for 90,
+    120, 180 degrees, positive energy and non-zero gradient away from it, zero force constant)
+    and test_inversion.py:140-205 (zero force constant, the three cyclic orderings of one
+    centre, two systems in one call)."""
+    def angle_pos(t):
+        return np.array([[0, 0, 0], [1.0, 0, 0], [math.cos(t), math.sin(t), 0]])
+
+    for deg, away in ((90, 60), (120, 90), (180, 90)):
+        t0 = math.radians(deg)
+        e, g, _ = _energy_grad("cosine_angle", angle_pos(t0), [t0, 3.0, math.radians(5)], 3)
+        assert e[0] == pytest.approx(0.0, abs=1e-10)
+        np.testing.assert_allclose(g, 0.0, atol=1e-6)
+        e, g, _ = _energy_grad("cosine_angle", angle_pos(math.radians(away)), [t0, 3.0, math.radians(5)], 3)
+        assert e[0] > 0 and np.linalg.norm(g) > 1e-6
+    e, _, _ = _energy_grad("cosine_angle", angle_pos(0.7), [math.pi / 2, 0.0, math.radians(5)], 3)
+    assert e[0] == pytest.approx(0.0, abs=1e-10)
+
+    e, _, _ = _energy_grad("inversion", inversion_positions(0.5), [0.0, 0.0], 4)
+    assert e[0] == pytest.approx(0.0, abs=1e-10)
+    e, _, _ = _energy_grad("inversion", inversion_positions(0.2), [0.0, 10.0], 4,
+                           edges=[[0, 1, 2, 3], [0, 2, 3, 1], [0, 3, 1, 2]])
+    assert e[0] > 0 and np.isfinite(e[0])
+    pos = np.concatenate([inversion_positions(0.0), inversion_positions(0.5)])
+    e, _, _ = _energy_grad("inversion", pos, [0.0, 10.0], 4, edges=[[0, 1, 2, 3], [4, 5, 6, 7]],
+                           system=[0] * 4 + [1] * 4, boxes=np.repeat(BOX, 2, 0))
+    assert e[0] == pytest.approx(0.0, abs=1e-10) and e[1] > 0
