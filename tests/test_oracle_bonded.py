@@ -187,3 +187,48 @@ def test_remaining_cosine_angle_and_inversion_cases():
     e, _, _ = _energy_grad("inversion", pos, [0.0, 10.0], 4, edges=[[0, 1, 2, 3], [4, 5, 6, 7]],
                            system=[0] * 4 + [1] * 4, boxes=np.repeat(BOX, 2, 0))
     assert e[0] == pytest.approx(0.0, abs=1e-10) and e[1] > 0
+
+
+def test_harmonic_species_tuple_known_answers():
+    """test/potential/test_harmonic.py:70-345: species-indexed tables (the row of an edge is
+    its atoms' species in edge order), angles at atom 0, several edges and systems."""
+    x0 = np.array([[1.5, 1.2], [1.2, 1.8]])
+    kb = np.array([[100.0, 80.0], [80.0, 120.0]])
+    bond = np.stack([x0, kb], -1).reshape(4, 2)
+    z = np.zeros
+
+    def bonds(pos, species, edges, system=None, boxes=None):
+        system = z(len(pos), int) if system is None else np.asarray(system)
+        boxes = np.array([[10.0, 0, 10.0, 0, 0, 10.0]]) if boxes is None else boxes
+        return ob.bonded("harmonic_bond", np.asarray(pos, float), system, np.asarray(species), boxes, bond, 2,
+                         np.asarray(edges), z((len(edges), 1, 3)))[0]
+
+    assert bonds([[0, 0, 0], [1.0, 0, 0]], [0, 1], [[0, 1]])[0] == pytest.approx((1.0 - 1.2) ** 2 * 80.0)
+    assert bonds([[0, 0, 0], [1.2, 0, 0]], [0, 1], [[0, 1]])[0] == pytest.approx(0.0, abs=1e-10)
+    assert bonds([[0, 0, 0], [1.5, 0, 0]], [0, 0], [[0, 1]])[0] == pytest.approx(0.0, abs=1e-10)
+    e = bonds([[0, 0, 0], [1.0, 0, 0], [2.5, 0, 0]], [0, 1, 0], [[0, 1], [1, 2]])[0]
+    assert e == pytest.approx((1.0 - 1.2) ** 2 * 80.0 + (1.5 - 1.2) ** 2 * 80.0)
+    e = bonds([[0, 0, 0], [1.0, 0, 0], [0, 0, 0], [2.0, 0, 0]], [0, 1, 0, 1], [[0, 1], [2, 3]], [0, 0, 1, 1],
+              np.tile([10.0, 0, 10.0, 0, 0, 10.0], (2, 1)))
+    np.testing.assert_allclose(e, [(1.0 - 1.2) ** 2 * 80.0, (2.0 - 1.2) ** 2 * 80.0])
+
+    theta0 = np.array([[[120.0, 90.0], [90.0, 120.0]], [[90.0, 90.0], [120.0, 90.0]]])
+    ka = np.array([[[10.0, 8.0], [12.0, 10.0]], [[8.0, 12.0], [10.0, 8.0]]])
+    angle = np.stack([theta0, ka], -1).reshape(8, 2)
+
+    def angles(pos, edges, system, boxes, tab=angle):
+        sp = np.tile([0, 1, 0], len(pos) // 3)
+        return ob.bonded("harmonic_angle", np.asarray(pos, float), np.asarray(system), sp, boxes, tab, 2,
+                         np.asarray(edges), z((len(edges), 2, 3)))[0]
+
+    box1 = np.array([[10.0, 0, 10.0, 0, 0, 10.0]])
+    base = [[1.0, 0, 0], [0, 0, 0], [1.0, 1.0, 0]]  # 90 degrees at atom 0, table entry (A, B, A) = 90
+    assert angles(base, [[0, 1, 2]], [0, 0, 0], box1)[0] == pytest.approx(0.0, abs=1e-6)
+    zero_k = np.stack([theta0, np.zeros_like(ka)], -1).reshape(8, 2)
+    assert angles(base, [[0, 1, 2]], [0, 0, 0], box1, zero_k)[0] == pytest.approx(0.0, abs=1e-10)
+    e = angles([[0, 0, 0], [1.0, 0, 0], [2.0, 0, 0]], [[0, 1, 2]], [0, 0, 0], box1)[0]
+    assert e == pytest.approx((180.0 - 90.0) ** 2 * 12.0, rel=1e-5)  # k[A, B, A] = 12
+    e = angles(base + [[1.0, 0, 0], [0, 0, 0], [1.5, 0.866, 0]], [[0, 1, 2], [3, 4, 5]], [0, 0, 0, 1, 1, 1],
+               np.repeat(box1, 2, 0))
+    theta = math.degrees(math.acos(np.dot([-1.0, 0, 0], [0.5, 0.866, 0]) / np.linalg.norm([0.5, 0.866, 0])))
+    np.testing.assert_allclose(e, [0.0, (theta - 90.0) ** 2 * 12.0], rtol=1e-6, atol=1e-9)
