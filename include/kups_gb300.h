@@ -365,7 +365,8 @@ int32_t kups_bonded_edges(int32_t kind, const double *positions, const int32_t *
  * with a probe (src/kups/potential/common/graph.py:336-361, 412-450).
  *   delta[s] += sum over edges with an atom in `changed` of E_e(new) - E_e(old), the
  *   edge's system being that of its atom 0 (zero delta first; terms add up).
- *   changed       i32 [n_changed] distinct particle indices (all systems in one call)
+ *   changed       i32 [n_changed] distinct particle indices (all systems in one call),
+ *                 n_changed < 2^31 - 1
  *   new_positions f64 [n_changed, 3]
  *   new_image     i32 [n_changed, 3] or NULL: the lattice offset n with
  *                 new_position = unwrapped - n @ L when the move wrapped the atom; an

@@ -600,8 +600,9 @@ extern "C" int32_t kups_bonded_delta(int32_t kind, const double *positions, cons
                                      double *delta, int32_t fp32, void *workspace, size_t workspace_bytes,
                                      kups_status *status, void *stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
+  // slots hold positions in `changed` as int32
   if (kind < 0 || kind > 5 || n_particles < 0 || n_systems < 0 || n_edges < 0 || n_changed < 0 ||
-      n_species <= 0 || n_species > 1024)
+      n_changed >= (int64_t)INT32_MAX || n_species <= 0 || n_species > 1024)
     return KUPS_ERR_INVALID;
   if (n_edges == 0 || n_changed == 0) return KUPS_OK;
   if (positions == nullptr || system == nullptr || species == nullptr || tril == nullptr || edges == nullptr ||

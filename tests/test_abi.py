@@ -123,6 +123,7 @@ def test_host_side_validation_of_newer_entry_points():
          ws_bytes, ptr, None])
     assert lib.kups_bonded_delta(*delta_args(6, 1, 0)) == _lib.KUPS_ERR_INVALID
     assert lib.kups_bonded_delta(*delta_args(0, 0, 0)) == _lib.KUPS_OK  # nothing moved
+    assert lib.kups_bonded_delta(*delta_args(0, 1 << 31, 0)) == _lib.KUPS_ERR_INVALID  # beyond int32 slots
     # nothing below is dereferenced: each call is refused on the host
     assert lib.kups_bonded_delta(*delta_args(0, 1, 4, ptr=8)) == _lib.KUPS_ERR_INVALID  # workspace too small
     assert lib.kups_bonded_delta_workspace_bytes(10) >= 40
