@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--no-ewald", action="store_true", help="skip the LJ + Ewald MD (ionic melt) section")
     ap.add_argument("--no-ensembles", action="store_true", help="skip the BAOAB / CSVR / NPT comparison")
     ap.add_argument("--no-autotune", action="store_true", help="library-default launch shape for the MD kernel")
-    ap.add_argument("--no-bonded", action="store_true", help="skip the bonded-term and local-MLIAP timings")
+    ap.add_argument("--no-bonded", action="store_true", help="skip the bonded-term (evaluation and MC energy change), "
+                    "virial-observable and local-MLIAP timings")
     ap.add_argument("--gcmc-replicas", type=int, default=1024)
     ap.add_argument("--strong", action="store_true",
                     help="split one --systems batch across the ranks (cost-balanced contiguous ranges) "
