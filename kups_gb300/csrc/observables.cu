@@ -294,7 +294,7 @@ extern "C" int32_t kups_virial_stress(const double *positions, const double *gra
   const bool ke = momenta != nullptr;
   if (n_particles < 0 || n_systems < 0 || n_groups < 0) return KUPS_ERR_INVALID;
   if (n_systems > 0 && !tril) return KUPS_ERR_INVALID;
-  if (n_particles > 0 && (!positions || !grad || !system)) return KUPS_ERR_INVALID;
+  if (n_particles > 0 && (!positions || !grad || !system || !status)) return KUPS_ERR_INVALID;
   if (ke && !masses) return KUPS_ERR_INVALID;
   if (kinetic && !ke) return KUPS_ERR_INVALID;
   if (mol && (!group || n_particles >= (int64_t)INT32_MAX)) return KUPS_ERR_INVALID;

@@ -159,4 +159,6 @@ def test_host_side_validation_of_the_virial_observables():
     assert lib.kups_virial_stress(*args(S=1, tril=fake, kin=fake, wsb=1 << 20, ws=fake)) == _lib.KUPS_ERR_INVALID
     assert lib.kups_virial_stress(*args(S=1, tril=fake, mol=fake, wsb=1 << 20, ws=fake)) == _lib.KUPS_ERR_INVALID
     assert lib.kups_virial_stress(*args(S=1, tril=fake, wsb=16, ws=fake)) == _lib.KUPS_ERR_INVALID
+    assert lib.kups_virial_stress(*args(n=4, pos=fake, grad=fake, sys=fake, S=1, tril=fake, wsb=1 << 20,
+                                        ws=fake)) == _lib.KUPS_ERR_INVALID  # no status word
     assert lib.kups_virial_stress(*args()) == _lib.KUPS_OK
