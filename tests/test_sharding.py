@@ -82,3 +82,45 @@ def test_two_gloo_ranks_shard_systems_and_gather(tmp_path):
     W = workloads.batched_uneven_lj(n_systems=9, n_min=20, n_max=90, seed=4)
     expected = _system_energies(W, 0, W.n_systems)
     np.testing.assert_array_equal(np.load(out), expected)
+
+
+def _system_stress(W, lo, hi):
+    from oracle import md as omd
+
+    sel = (W.system >= lo) & (W.system < hi)
+    sysi = W.system[sel] - lo
+    _, f, dt = omd.lj_forces(W.positions[sel], sysi, W.species[sel], W.tril[lo:hi], W.sigma, W.epsilon,
+                             np.full(hi - lo, W.cutoff))
+    return omd.virial_stress(W.positions[sel], -f, sysi, W.tril[lo:hi], dt)
+
+
+def _rank_stress(rank, world, port, out_path):
+    import torch.distributed as dist
+
+    from kups_gb300 import workloads
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    W = workloads.batched_uneven_lj(n_systems=7, n_min=20, n_max=80, seed=6)
+    counts = np.bincount(W.system, minlength=W.n_systems)
+    ranges = [rank_systems(counts, r, world) for r in range(world)]
+    lo, hi = ranges[rank]
+    gathered = gather_per_system(torch.as_tensor(_system_stress(W, lo, hi)), ranges, rank)
+    if rank == 0:
+        np.save(out_path, gathered.numpy())
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_gather_per_system_stress_tensors(tmp_path):
+    """Per-system [3, 3] observables (the virial stress of each rank's systems) gather in
+    system order, trailing dimensions kept."""
+    from kups_gb300 import workloads
+
+    out = str(tmp_path / "stress.npy")
+    mp.start_processes(_rank_stress, args=(2, _free_port(), out), nprocs=2, start_method="spawn", join=True)
+    W = workloads.batched_uneven_lj(n_systems=7, n_min=20, n_max=80, seed=6)
+    got = np.load(out)
+    assert got.shape == (7, 3, 3)
+    np.testing.assert_array_equal(got, _system_stress(W, 0, W.n_systems))
