@@ -472,6 +472,25 @@ typedef struct kups_gcmc_proposal {
   float pos[8][4]; /* new positions (x, y, z, species bits) of the molecule */
 } kups_gcmc_proposal;
 
+/* One record per (step, system) written when kups_gcmc_args.trace is set,
+ * at trace[step * n_systems + s]: what the step proposed and decided, so a
+ * replay can check the move generator, ln acc and the accept decision. */
+typedef struct kups_gcmc_trace {
+  int32_t kind;      /* 0 translate, 1 rotate, 2 reinsert, 3 insert, 4 delete */
+  int32_t mol;       /* molecule slot moved, inserted into or deleted (-1: none) */
+  int32_t accept;
+  int32_t n_mol;     /* molecules before the step */
+  int32_t has_old;   /* the move removes an existing molecule's old position */
+  int32_t has_new;   /* the move places a molecule (new_pos valid) */
+  float width;       /* step width of the move's scheduler when proposed */
+  int32_t pad;
+  double de;         /* energy change of the proposal */
+  double log_p;      /* ln acc (muVT + proposal ratio) */
+  double log_u;      /* ln u of the uniform in (0, 1] it was compared with */
+  double ln_ratio;   /* log proposal ratio of the learned density (0: uniform) */
+  float new_pos[8][4];
+} kups_gcmc_trace;
+
 typedef struct kups_gcmc_args {
   const void *fw_pos;           /* float4 */
   const float *fw_charge;
@@ -532,6 +551,7 @@ typedef struct kups_gcmc_args {
   int32_t proposal_grid;        /* G; with proposal_node set, insertions draw the molecule's
                                    centre (atom mean) from the grid density q and add
                                    -ln(V q) to ln acc, deletions add +ln(V q) */
+  kups_gcmc_trace *trace;       /* [n_steps, S] or NULL: per-step record of every system */
 } kups_gcmc_args;
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);

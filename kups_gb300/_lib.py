@@ -71,8 +71,14 @@ class GcmcArgs(C.Structure):
         ("move_cum", C.c_float * 3), ("pad0", C.c_float), ("coulomb_k", C.c_double), ("seed", C.c_uint64),
         ("step0", C.c_uint64), ("n_systems", C.c_int32), ("max_mol", C.c_int32), ("atoms_per_mol", C.c_int32),
         ("n_species", C.c_int32), ("n_kvecs", C.c_int32), ("n_steps", C.c_int32), ("history_len", C.c_int32),
-        ("proposal_grid", C.c_int32),
+        ("proposal_grid", C.c_int32), ("trace", C.c_void_p),
     ]
+
+
+# numpy layout of kups_gcmc_trace (one record per step and system)
+GCMC_TRACE_DTYPE = [("kind", "<i4"), ("mol", "<i4"), ("accept", "<i4"), ("n_mol", "<i4"), ("has_old", "<i4"),
+                    ("has_new", "<i4"), ("width", "<f4"), ("pad", "<i4"), ("de", "<f8"), ("log_p", "<f8"),
+                    ("log_u", "<f8"), ("ln_ratio", "<f8"), ("new_pos", "<f4", (8, 4))]
 
 
 class Mlp(C.Structure):

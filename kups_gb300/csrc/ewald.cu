@@ -720,44 +720,36 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// SM count of the current device, looked up once per device.
 inline int recip_sm_count() {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
+  constexpr int kDevices = 64;
+  static int sms[kDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  int n = dev >= 0 && dev < kDevices ? sms[dev] : 0;
+  if (n <= 0) {
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+    if (dev >= 0 && dev < kDevices) sms[dev] = n;
   }
-  return sms;
+  return n;
 }
 
-}  // namespace
-}  // namespace kups
-
-using namespace kups;
-
-extern "C" size_t kups_ewald_recip_workspace_bytes(int32_t n_systems, int32_t n_kvecs) {
+// The reciprocal-space launch sequence of kups_ewald_recip and
+// kups_ewald_recip_static: setup, structure factor, energy and forces.
+// `base` is 256-byte aligned scratch of at least recip_scratch_bytes().
+inline size_t recip_scratch_bytes(int32_t n_systems, int32_t n_kvecs) {
   return align256(sizeof(RecipSys) * (size_t)n_systems) +
-         align256(sizeof(Coef) * (size_t)n_systems * (size_t)n_kvecs) + 512;
+         align256(sizeof(Coef) * (size_t)n_systems * (size_t)n_kvecs);
 }
 
-extern "C" int32_t kups_ewald_recip(const double *positions, const double *charges,
-                                    const int32_t *sys_offset, int32_t n_systems,
-                                    int32_t max_atoms_per_system, const double *tril,
-                                    const int32_t *kvec_n, int32_t n_kvecs, const double *alpha,
-                                    double coulomb_k, double *energy, double *grad,
-                                    double *grad_tril, double *structure_factor,
-                                    void *workspace, size_t workspace_bytes, kups_status *status,
-                                    void *stream_) {
-  cudaStream_t stream = (cudaStream_t)stream_;
-  if (n_systems < 0 || n_kvecs < 0 || max_atoms_per_system < 0) return KUPS_ERR_INVALID;
-  if (workspace_bytes < kups_ewald_recip_workspace_bytes(n_systems, n_kvecs)) return KUPS_ERR_INVALID;
-  if (n_systems == 0) return KUPS_OK;
-  char *base = (char *)(((uintptr_t)workspace + 255) & ~uintptr_t(255));
+int32_t recip_launch(char *base, const double *positions, const double *charges, const int32_t *sys_offset,
+                     int32_t n_systems, int32_t max_atoms_per_system, const double *tril, const int32_t *kvec_n,
+                     int32_t n_kvecs, const double *alpha, double coulomb_k, double *energy, double *grad,
+                     double *grad_tril, double *structure_factor, kups_status *status, cudaStream_t stream) {
   RecipSys *sysp = (RecipSys *)base;
   Coef *coef = (Coef *)(base + align256(sizeof(RecipSys) * (size_t)n_systems));
-  recip_setup_kernel<<<n_systems, 256, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
-                                                                   sysp, status);
+  recip_setup_kernel<<<n_systems, 256, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs, sysp, status);
   KUPS_CUDA_TRY(cudaMemsetAsync(structure_factor, 0, sizeof(double) * 2 * (size_t)n_systems * n_kvecs, stream));
   const int chunks = (max_atoms_per_system + kAtomsPerChunk - 1) / kAtomsPerChunk;
   if (n_kvecs > 0 && chunks > 0) {
@@ -789,6 +781,32 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 
+}  // namespace
+}  // namespace kups
+
+using namespace kups;
+
+extern "C" size_t kups_ewald_recip_workspace_bytes(int32_t n_systems, int32_t n_kvecs) {
+  return recip_scratch_bytes(n_systems, n_kvecs) + 512;
+}
+
+extern "C" int32_t kups_ewald_recip(const double *positions, const double *charges,
+                                    const int32_t *sys_offset, int32_t n_systems,
+                                    int32_t max_atoms_per_system, const double *tril,
+                                    const int32_t *kvec_n, int32_t n_kvecs, const double *alpha,
+                                    double coulomb_k, double *energy, double *grad,
+                                    double *grad_tril, double *structure_factor,
+                                    void *workspace, size_t workspace_bytes, kups_status *status,
+                                    void *stream_) {
+  if (n_systems < 0 || n_kvecs < 0 || max_atoms_per_system < 0) return KUPS_ERR_INVALID;
+  if (workspace_bytes < kups_ewald_recip_workspace_bytes(n_systems, n_kvecs)) return KUPS_ERR_INVALID;
+  if (n_systems == 0) return KUPS_OK;
+  char *base = (char *)(((uintptr_t)workspace + 255) & ~uintptr_t(255));
+  return recip_launch(base, positions, charges, sys_offset, n_systems, max_atoms_per_system, tril, kvec_n,
+                      n_kvecs, alpha, coulomb_k, energy, grad, grad_tril, structure_factor, status,
+                      (cudaStream_t)stream_);
+}
+
 // ---------------------------------------------------------------------------
 // kups_ewald_recip_static: the reciprocal-space computation above with its
 // scratch (per-system cell data, then per-(system, k) coefficients) in one
@@ -800,6 +818,9 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
 // call left in it; every byte a call reads is written earlier in the same
 // call, so nothing in it has to start at zero.  Two calls whose launches
 // overlap in time (different streams, or different host threads) race on it.
+// The array lives in this file's module: every device on which any kernel of
+// this file runs holds its KUPS_EWALD_RECIP_STATIC_SCRATCH_BYTES until the
+// process exits (or the device is reset).
 namespace kups {
 namespace {
 constexpr size_t kStaticScratchBytes = KUPS_EWALD_RECIP_STATIC_SCRATCH_BYTES;
@@ -818,15 +839,12 @@ extern "C" int32_t kups_ewald_recip_static(const double *positions, const double
                                            double *grad, double *grad_tril,
                                            double *structure_factor, kups_status *status,
                                            void *stream_) {
-  cudaStream_t stream = (cudaStream_t)stream_;
   if (n_systems < 0 || n_kvecs < 0 || max_atoms_per_system < 0) return KUPS_ERR_INVALID;
   // Sizes beyond the array are refused before anything is touched.
   if ((size_t)n_systems > kStaticScratchBytes / sizeof(RecipSys)) return KUPS_ERR_CAPACITY;
   if (n_kvecs > 0 && (size_t)n_systems > kStaticScratchBytes / sizeof(Coef) / (size_t)n_kvecs)
     return KUPS_ERR_CAPACITY;
-  const size_t sys_bytes = align256(sizeof(RecipSys) * (size_t)n_systems);
-  if (sys_bytes + align256(sizeof(Coef) * (size_t)n_systems * (size_t)n_kvecs) > kStaticScratchBytes)
-    return KUPS_ERR_CAPACITY;
+  if (recip_scratch_bytes(n_systems, n_kvecs) > kStaticScratchBytes) return KUPS_ERR_CAPACITY;
   if (n_systems == 0) return KUPS_OK;
   // Once per device, with that device current: look up the array's address.
   int dev = 0;
@@ -843,39 +861,9 @@ extern "C" int32_t kups_ewald_recip_static(const double *positions, const double
     }
     base = (char *)g_static_scratch_ptr[dev];
   }
-  RecipSys *sysp = (RecipSys *)base;
-  Coef *coef = (Coef *)(base + sys_bytes);
-  recip_setup_kernel<<<n_systems, 256, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs,
-                                                                   sysp, status);
-  KUPS_CUDA_TRY(cudaMemsetAsync(structure_factor, 0, sizeof(double) * 2 * (size_t)n_systems * n_kvecs, stream));
-  const int chunks = (max_atoms_per_system + kAtomsPerChunk - 1) / kAtomsPerChunk;
-  if (n_kvecs > 0 && chunks > 0) {
-    dim3 g((n_kvecs + kKPerBlock - 1) / kKPerBlock, chunks, n_systems);
-    structure_factor_kernel<<<g, kKPerBlock, 0, stream>>>(positions, charges, sys_offset, kvec_n,
-                                                          n_kvecs, sysp, structure_factor, grad);
-  }
-  KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
-  if (grad_tril) KUPS_CUDA_TRY(cudaMemsetAsync(grad_tril, 0, sizeof(double) * 6 * (size_t)n_systems, stream));
-  // one warp per block: the per-k float64 exp and divisions spread over many SMs
-  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 31) / 32), n_systems), 32, 0, stream>>>(
-      kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, grad_tril);
-  if (chunks > 0 && n_kvecs > 0) {
-    // enough k splits that the launch holds about 16 warps per SM
-    const int kblocks = (n_kvecs + kKPerBlock - 1) / kKPerBlock;
-    const int want = std::max(1, (16 * recip_sm_count()) / std::max(1, 4 * chunks * n_systems));
-    const int splits = std::min(kblocks, want);
-    const int per = (kblocks + splits - 1) / splits;
-    dim3 g(chunks, n_systems, (kblocks + per - 1) / per);
-    recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
-                                                             n_kvecs, sysp, coef, coulomb_k, grad,
-                                                             grad_tril, per);
-  } else if (chunks > 0) {
-    dim3 g(chunks, n_systems, 1);
-    recip_force_kernel<<<g, kAtomsPerChunk * 4, 0, stream>>>(positions, charges, sys_offset, kvec_n,
-                                                             n_kvecs, sysp, coef, coulomb_k, grad,
-                                                             grad_tril, 0);
-  }
-  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+  return recip_launch(base, positions, charges, sys_offset, n_systems, max_atoms_per_system, tril, kvec_n,
+                      n_kvecs, alpha, coulomb_k, energy, grad, grad_tril, structure_factor, status,
+                      (cudaStream_t)stream_);
 }
 
 extern "C" int32_t kups_ewald_self(const double *charges, const int32_t *sys_offset,

@@ -685,6 +685,28 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc
       sh.accept = accept;
       sh.log_p = logp;
       sh.de_total = de;
+      if (a.trace != nullptr) {
+        kups_gcmc_trace &t = a.trace[(int64_t)step * a.n_systems + s];
+        t.kind = kind;
+        t.mol = mol;
+        t.accept = accept;
+        t.n_mol = n_old;
+        t.has_old = has_old;
+        t.has_new = has_new;
+        t.width = a.width[s * 4 + (kind >= 3 ? 3 : kind)];
+        t.pad = 0;
+        t.de = de;
+        t.log_p = logp;
+        t.log_u = log(u);
+        t.ln_ratio = sh.ln_ratio;
+        for (int i = 0; i < kMaxApm; ++i) {
+          const float4 p = i < apm && has_new ? sh.new_pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+          t.new_pos[i][0] = p.x;
+          t.new_pos[i][1] = p.y;
+          t.new_pos[i][2] = p.z;
+          t.new_pos[i][3] = p.w;
+        }
+      }
       sh.de_real = de_real;
       sh.de_recip = de_rec;
       if (a.out_delta != nullptr) {

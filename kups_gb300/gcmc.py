@@ -17,6 +17,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 from dataclasses import dataclass, field
+from typing import NamedTuple
 
 import numpy as np
 import torch
@@ -29,30 +30,61 @@ MOVES = ("translate", "rotate", "reinsert", "insert", "delete")
 
 
 # ----------------------------------------------------------------------------- host-side thermodynamics
-def _cubic_roots(c):
-    r = np.roots(c)
-    return r
+class LogFugacityResult(NamedTuple):
+    """ln f per component (in the pressure's unit) and the compressibility Z of the root each
+    component's fugacity was taken from (``LogFugacityResult``, src/kups/mcmc/fugacity.py:23-32)."""
+
+    log_fugacity: np.ndarray
+    compressibility: np.ndarray
 
 
-def peng_robinson_log_fugacity(pressure_pa, temperature, pc_pa, tc, omega):
-    """ln f (f in the pressure's unit) of a pure gas, gas-phase root (fugacity.py:38-127)."""
-    pr, tr = pressure_pa / pc_pa, temperature / tc
-    m = 0.37464 + 1.54226 * omega - 0.26992 * omega**2
-    sa = 1 + m * (1 - tr**0.5)
-    A = 0.45724 * pr / tr**2 * sa**2
-    B = 0.0778 * pr / tr
-    roots = _cubic_roots([1.0, B - 1.0, A - 3.0 * B**2 - 2.0 * B, -(A * B - B**2 - B**3)])
-    best = None
-    for z in roots:
-        if abs(z.imag) > 1e-12 or z.real <= B:
+def peng_robinson_log_fugacity(pressure, temperature, critical_pressure, critical_temperature, acentric_factor,
+                               composition=None, interaction=None) -> LogFugacityResult:
+    """Peng-Robinson fugacity of each component of a gas mixture (src/kups/mcmc/fugacity.py:35-193).
+
+    Reduced pressure and temperature per component, m(omega), A_i = 0.45724 Pr_i / Tr_i^2
+    (1 + m_i (1 - sqrt(Tr_i)))^2, B_i = 0.0778 Pr_i / Tr_i; mixing A = sum_ij y_i y_j (1 - k_ij)
+    sqrt(A_i A_j), B = sum_i y_i B_i; Z from the cubic Z^3 + (B - 1) Z^2 + (A - 3B^2 - 2B) Z -
+    (AB - B^2 - B^3) = 0; for each component the real root with the smallest ln phi_i (the gas
+    phase, as RASPA selects it) among roots where ln phi_i is defined (Z > B).  The pressure's
+    unit cancels in every reduced quantity, so ln f is in that unit.  Host code (once per setup).
+    """
+    pc = np.atleast_1d(np.asarray(critical_pressure, np.float64))
+    n = pc.size
+    tc = np.atleast_1d(np.asarray(critical_temperature, np.float64))
+    om = np.atleast_1d(np.asarray(acentric_factor, np.float64))
+    y = np.ones(1) if composition is None else np.atleast_1d(np.asarray(composition, np.float64))
+    kij = np.zeros((n, n)) if interaction is None else np.asarray(interaction, np.float64).reshape(n, n)
+    if y.size != n:
+        raise ValueError("composition needs one mole fraction per component")
+    p, t = float(pressure), float(temperature)
+    pr, tr = p / pc, t / tc
+    m = 0.37464 + 1.54226 * om - 0.26992 * om**2
+    sa = 1.0 + m * (1.0 - np.sqrt(tr))
+    a = 0.45724 * pr / tr**2 * sa**2
+    b = 0.0778 * pr / tr
+    aij = (1.0 - kij) * np.sqrt(np.outer(a, a))
+    bm = float(y @ b)
+    am = float(y @ aij @ y)
+    roots = np.roots([1.0, bm - 1.0, am - 3.0 * bm**2 - 2.0 * bm, -(am * bm - bm**2 - bm**3)])
+    scale = max(1.0, float(np.max(np.abs(roots))))
+    z = np.sort(roots[np.abs(roots.imag) <= 1e-10 * scale].real)
+    sq2 = math.sqrt(2.0)
+    da = 2.0 * aij @ y
+    best_phi = np.full(n, np.inf)
+    best_z = np.full(n, np.nan)
+    for zr in z:
+        if not (zr > bm and zr > 0.0):
             continue
-        z = z.real
-        sq2 = math.sqrt(2.0)
-        lnphi = (z - 1) - math.log(z - B) - A / (2 * sq2 * B) * (2.0 - 1.0) * math.log(
-            (z + (1 + sq2) * B) / (z + (1 - sq2) * B))
-        if best is None or lnphi < best:
-            best = lnphi
-    return best + math.log(pressure_pa)
+        lnphi = ((b / bm) * (zr - 1.0) - math.log(zr - bm)
+                 - am / (2.0 * sq2 * bm) * (da / am - b / bm)
+                 * math.log((zr + (1.0 + sq2) * bm) / (zr + (1.0 - sq2) * bm)))
+        better = lnphi < best_phi
+        best_phi = np.where(better, lnphi, best_phi)
+        best_z = np.where(better, zr, best_z)
+    with np.errstate(divide="ignore"):
+        ln_f = best_phi + math.log(p) + np.log(y)
+    return LogFugacityResult(ln_f, best_z)
 
 
 def lorentz_berthelot(sigma, epsilon):
@@ -282,7 +314,7 @@ class GCMC:
         _, _, _, sk, _ = ewald_recip(P, Q, O, int(np.max(st.fw_count)), self.tril, self.kn, self.alpha, grad_tril=False)
         self.sk.copy_(sk)
 
-    def args(self, n_steps, proposals=None, out_delta=None) -> _lib.GcmcArgs:
+    def args(self, n_steps, proposals=None, out_delta=None, trace=None) -> _lib.GcmcArgs:
         a = _lib.GcmcArgs()
         st = self.setup
         a.fw_pos, a.fw_charge, a.fw_start, a.fw_count = (self.fw_pos.data_ptr(), self.fw_q.data_ptr(),
@@ -304,6 +336,7 @@ class GCMC:
         a.workspace = self.ws.data_ptr()
         a.fw_group = self.fw_group.data_ptr() if self.fw_group is not None else None
         a.obs_sums = self.obs.data_ptr()
+        a.trace = trace.data_ptr() if trace is not None else None
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid
@@ -315,11 +348,21 @@ class GCMC:
         a.n_species, a.n_kvecs, a.n_steps, a.history_len = st.sigma.shape[0], st.kvec_n.shape[1], int(n_steps), 100
         return a
 
-    def launch(self, n_steps, proposals=None, out_delta=None):
-        a = self.args(n_steps, proposals, out_delta)
+    def launch(self, n_steps, proposals=None, out_delta=None, trace=None):
+        a = self.args(n_steps, proposals, out_delta, trace)
         rc = _lib.load().kups_gcmc_run(C.byref(a), self.status.data_ptr(), _stream())
         _lib.check(rc, "kups_gcmc_run")
         self.step += n_steps
+
+    def run_traced(self, n_steps: int) -> np.ndarray:
+        """n_steps steps of every system with the per-step record (``kups_gcmc_trace``): a
+        structured array [n_steps, S] of the move kind, slot, decision, molecule count,
+        energy change, ln acc, ln u, proposal log ratio, step width and proposed positions."""
+        dt = np.dtype(_lib.GCMC_TRACE_DTYPE)
+        buf = torch.zeros((n_steps * self.setup.n_systems * dt.itemsize,), dtype=torch.uint8, device="cuda")
+        self.launch(n_steps, trace=buf)
+        self.check()
+        return buf.cpu().numpy().view(dt).reshape(n_steps, self.setup.n_systems)
 
     def __call__(self, key=None, n_steps: int = 1):
         """Propagator: n_steps MC steps of every system (one launch)."""

@@ -341,3 +341,129 @@ def make_csvr_npt_step(steps_per_call: int = 1, **kw) -> FusedLennardJonesMD:
     """CSVR, velocity Verlet, stochastic cell rescaling and the forces again (NPT;
     integrators.py:801-890); needs the thermostat and barostat system fields."""
     return FusedLennardJonesMD("csvr_npt", steps_per_call, **kw)
+
+
+class LennardJonesMD64:
+    """Float64 LJ molecular dynamics: the reference's own arithmetic, step by step.
+
+    One step is the reference's propagator (``make_velocity_verlet_step`` / ``make_baoab_langevin_step``,
+    src/kups/md/integrators.py:273-318, 405-455) with its derivative computation as the reference's MD
+    application runs it (application/md/simulation.py:74-119): the neighbour list rebuilt at every step
+    (``kups_neighborlist_build``, exact float64 membership), LJ energy and gradients over the edges in
+    float64 (``kups_lj_edges``), and the float64 integrator blocks (``kups_md_kick`` / ``kups_md_drift``
+    with the wrap / ``kups_md_thermostat``).  Every launch is stream-ordered with no host
+    synchronisation; velocity-Verlet steps replay from one captured CUDA graph.  This is the float64
+    counterpart of ``FusedLennardJonesMD`` (float32 pair arithmetic), for small systems that must
+    match the reference's float64 trajectory.
+    """
+
+    def __init__(self, state: MDState, integrator: str = "baoab", avg_edges: int | None = None, seed: int = 0):
+        from .neighborlist import _f64, _i32
+
+        if INTEGRATORS[integrator] not in (0, 1):
+            raise ValueError("LennardJonesMD64 runs velocity Verlet or BAOAB")
+        self.integrator = INTEGRATORS[integrator]
+        p, sy = state.particles, state.systems
+        self.pos = _f64(p.positions).clone()
+        self.mom = _f64(p.momenta).clone()
+        self.mass = _f64(p.masses)
+        self.species = _i32(p.species)
+        self.system = _i32(p.system)
+        self.tril = _f64(sy.tril).reshape(-1, 6).contiguous()
+        s = self.tril.shape[0]
+        self.s, self.n = s, self.pos.shape[0]
+        full = lambda x: _f64(torch.as_tensor(x, dtype=torch.float64).reshape(-1).expand(s))
+        self.dt = full(sy.time_step)
+        self.kT = full(torch.as_tensor(sy.temperature, dtype=torch.float64) * BOLTZMANN_CONSTANT)
+        self.friction = full(sy.friction_coefficient)
+        prm = state.lj_parameters
+        self.cut = full(prm.cutoff)
+        self.sig, self.eps = _f64(prm.sigma), _f64(prm.epsilon)
+        self.nsp = int(self.sig.shape[0])
+        if avg_edges is None:
+            vol = float((self.tril[:, 0] * self.tril[:, 2] * self.tril[:, 5]).abs().min())
+            counts = torch.bincount(self.system.long(), minlength=s)
+            dens = float(counts.max()) / vol
+            avg_edges = int(4.0 / 3.0 * math.pi * float(self.cut.max()) ** 3 * dens * 1.5) + 32
+        self.cap = int(avg_edges) * self.n
+        dev = dict(device="cuda")
+        self.edges = torch.empty((self.cap, 2), dtype=torch.int32, **dev)
+        self.shifts = torch.empty((self.cap, 3), dtype=torch.int32, **dev)
+        self.n_edges = torch.zeros(1, dtype=torch.int64, **dev)
+        self.incl = self.system
+        self.excl = torch.arange(self.n, dtype=torch.int32, **dev)
+        lib = _lib.load()
+        self.nl_ws = torch.empty(lib.kups_neighborlist_workspace_bytes(self.n, s), dtype=torch.uint8, **dev)
+        self.energy = torch.zeros(s, dtype=torch.float64, **dev)
+        self.grad = torch.zeros((self.n, 3), dtype=torch.float64, **dev)
+        self.gtril = torch.zeros((s, 6), dtype=torch.float64, **dev)
+        self.status = new_status()
+        self.seed = int(seed)
+        self.step = int(state.step)
+        self.graph = None
+        self._forces()
+
+    def _forces(self):
+        lib = _lib.load()
+        st = _stream()
+        rc = lib.kups_neighborlist_build(self.pos.data_ptr(), self.system.data_ptr(), self.incl.data_ptr(),
+                                         self.excl.data_ptr(), self.n, self.s, self.tril.data_ptr(),
+                                         self.cut.data_ptr(), self.s, self.edges.data_ptr(), self.shifts.data_ptr(),
+                                         self.cap, self.n_edges.data_ptr(), self.nl_ws.data_ptr(), self.nl_ws.numel(),
+                                         self.status.data_ptr(), st)
+        _lib.check(rc, "kups_neighborlist_build")
+        # edges past n_edges are padded with the out-of-bounds index and skipped by the kernel
+        rc = lib.kups_lj_edges(self.pos.data_ptr(), self.system.data_ptr(), self.species.data_ptr(), self.n,
+                               self.tril.data_ptr(), self.cut.data_ptr(), self.s, self.sig.data_ptr(),
+                               self.eps.data_ptr(), self.nsp, self.edges.data_ptr(), self.shifts.data_ptr(), self.cap,
+                               self.energy.data_ptr(), self.grad.data_ptr(), self.gtril.data_ptr(), 0,
+                               self.status.data_ptr(), st)
+        _lib.check(rc, "kups_lj_edges")
+
+    def _step(self, step: int):
+        lib = _lib.load()
+        st = _stream()
+        args = (self.pos.data_ptr(), self.mom.data_ptr(), self.mass.data_ptr(), self.system.data_ptr(),
+                self.dt.data_ptr(), self.tril.data_ptr())
+        lib.kups_md_kick(self.mom.data_ptr(), self.grad.data_ptr(), self.system.data_ptr(), self.dt.data_ptr(), 0.5,
+                         self.n, st)
+        if self.integrator == 1:
+            lib.kups_md_drift(*args, 0.5, self.n, st)
+            lib.kups_md_thermostat(self.mom.data_ptr(), self.mass.data_ptr(), self.system.data_ptr(),
+                                   self.dt.data_ptr(), self.kT.data_ptr(), self.friction.data_ptr(), self.seed, step,
+                                   self.n, st)
+            lib.kups_md_drift(*args, 0.5, self.n, st)
+        else:
+            lib.kups_md_drift(*args, 1.0, self.n, st)
+        self._forces()
+        lib.kups_md_kick(self.mom.data_ptr(), self.grad.data_ptr(), self.system.data_ptr(), self.dt.data_ptr(), 0.5,
+                         self.n, st)
+
+    def run(self, n_steps: int, use_graph: bool = True):
+        """n_steps steps (the Langevin noise of step k is keyed by (seed, atom, k))."""
+        if self.integrator == 1 or not use_graph:
+            for _ in range(n_steps):
+                self._step(self.step)
+                self.step += 1
+            return
+        if self.graph is None and n_steps > 0:
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                self._step(self.step)
+            torch.cuda.current_stream().wait_stream(s)
+            self.step += 1
+            n_steps -= 1
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph):
+                self._step(0)
+        for _ in range(max(n_steps, 0)):
+            self.graph.replay()
+            self.step += 1
+
+    def check(self):
+        _lib.raise_status(read_status(self.status))
+
+    def kinetic_energy(self) -> torch.Tensor:
+        ke = 0.5 * (self.mom**2).sum(-1) / self.mass
+        return torch.zeros(self.s, dtype=torch.float64, device="cuda").index_add_(0, self.system.long(), ke)

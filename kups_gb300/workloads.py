@@ -53,6 +53,17 @@ class MDWorkload:
     def n_systems(self) -> int:
         return int(self.tril.shape[0])
 
+    def select(self, systems) -> "MDWorkload":
+        """The given systems (any order, no repeats), renumbered 0.. in that order, atoms grouped by system."""
+        systems = np.asarray(systems, np.int64)
+        parts = [np.nonzero(self.system == s)[0] for s in systems]
+        idx = np.concatenate(parts)
+        new_sys = np.repeat(np.arange(len(systems), dtype=np.int32), [len(p) for p in parts])
+        return MDWorkload(self.positions[idx], self.momenta[idx], self.masses[idx], self.species[idx], new_sys,
+                          self.tril[systems], self.temperature[systems], self.time_step[systems],
+                          self.friction[systems], self.sigma, self.epsilon, self.cutoff, self.skin,
+                          None if self.charges is None else self.charges[idx])
+
     def subset(self, lo: int, hi: int) -> "MDWorkload":
         """Systems [lo, hi) (atoms grouped by system), renumbered from 0."""
         sel = (self.system >= lo) & (self.system < hi)
@@ -265,8 +276,9 @@ def gcmc_co2_framework(n_replicas=1024, n_fw=2000, p_min_bar=0.1, p_max_bar=10.0
     kn = kvecs_from_kmax(tril, kmax)
     pressures = np.logspace(np.log10(p_min_bar), np.log10(p_max_bar), n_replicas) * 1e5
     kT = temperature * BOLTZMANN_CONSTANT
-    la = np.array([gcmc.peng_robinson_log_fugacity(p, temperature, 7.84e6, 303.75, 0.22394) + np.log(PASCAL)
-                   - np.log(kT) for p in pressures])
+    # ln(f / kT) with f from the Peng-Robinson fugacity in Pa, converted to eV / A^3
+    la = np.array([gcmc.peng_robinson_log_fugacity(p, temperature, 7.84e6, 303.75, 0.22394).log_fugacity[0]
+                   + np.log(PASCAL) - np.log(kT) for p in pressures])
     S = n_replicas
     return gcmc.GCMCSetup(
         fw_positions=fw, fw_species=fw_sp, fw_charges=q, fw_start=np.zeros(S, int), fw_count=np.full(S, n_fw),

@@ -100,30 +100,38 @@ def neighbor_list(
         if idx.size == 0:
             continue
         f = row_times_tril(pos[idx], inv[s])
-        d0 = f[:, None, :] - f[None, :, :]  # lh - rh
         inc = incl[idx]
-        seg = (inc[:, None] == inc[None, :]) & (inc[:, None] >= 0) & (inc[:, None] < n_incl)
-        same_ex = excl[idx][:, None] == excl[idx][None, :]
         rc2 = cut[s] ** 2
-        min_shift = np.round(d0)
         if np.prod(nimg[s]) == 1:
-            delta = d0 - min_shift
-            real = row_times_tril(delta, tril[s])
-            d2 = (real[..., 0] * real[..., 0] + real[..., 1] * real[..., 1]) + real[..., 2] * real[..., 2]
-            m = seg & (d2 < rc2) & ~same_ex
-            ii, jj = np.nonzero(m)
-            all_e.append(np.stack([idx[ii], idx[jj]], -1))
-            all_s.append(min_shift[ii, jj].astype(np.int64))
-        else:
-            for o in image_offsets(nimg[s]):
-                delta = d0 - o
+            # rows in blocks, so large systems stay within a few hundred MB
+            blk = max(1, 2**22 // max(1, idx.size))
+            for r0 in range(0, idx.size, blk):
+                r = slice(r0, r0 + blk)
+                d0 = f[r, None, :] - f[None, :, :]
+                seg = (inc[r, None] == inc[None, :]) & (inc[r, None] >= 0) & (inc[r, None] < n_incl)
+                same_ex = excl[idx][r, None] == excl[idx][None, :]
+                min_shift = np.round(d0)
+                delta = d0 - min_shift
                 real = row_times_tril(delta, tril[s])
                 d2 = (real[..., 0] * real[..., 0] + real[..., 1] * real[..., 1]) + real[..., 2] * real[..., 2]
-                is_min = np.all(min_shift == o, axis=-1)
-                m = seg & (d2 < rc2) & (~same_ex | ~is_min)
+                m = seg & (d2 < rc2) & ~same_ex
                 ii, jj = np.nonzero(m)
-                all_e.append(np.stack([idx[ii], idx[jj]], -1))
-                all_s.append(np.broadcast_to(o, (ii.size, 3)).astype(np.int64))
+                all_e.append(np.stack([idx[r0 + ii], idx[jj]], -1))
+                all_s.append(min_shift[ii, jj].astype(np.int64))
+            continue
+        d0 = f[:, None, :] - f[None, :, :]  # lh - rh
+        seg = (inc[:, None] == inc[None, :]) & (inc[:, None] >= 0) & (inc[:, None] < n_incl)
+        same_ex = excl[idx][:, None] == excl[idx][None, :]
+        min_shift = np.round(d0)
+        for o in image_offsets(nimg[s]):
+            delta = d0 - o
+            real = row_times_tril(delta, tril[s])
+            d2 = (real[..., 0] * real[..., 0] + real[..., 1] * real[..., 1]) + real[..., 2] * real[..., 2]
+            is_min = np.all(min_shift == o, axis=-1)
+            m = seg & (d2 < rc2) & (~same_ex | ~is_min)
+            ii, jj = np.nonzero(m)
+            all_e.append(np.stack([idx[ii], idx[jj]], -1))
+            all_s.append(np.broadcast_to(o, (ii.size, 3)).astype(np.int64))
     if not all_e:
         return np.zeros((0, 2), np.int64), np.zeros((0, 3), np.int64)
     e = np.concatenate(all_e).astype(np.int64)

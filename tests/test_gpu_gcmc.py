@@ -70,12 +70,12 @@ def wrapped(p, tril):
 
 
 @pytest.mark.parametrize("rc", [7.0, 5.0])  # 3 x 3 x 3 image offsets / minimum image (widths 10.4, 10.4, 13 A)
-@pytest.mark.parametrize("kind", ["translate", "rotate", "insert", "delete"])
+@pytest.mark.parametrize("kind", ["translate", "rotate", "reinsert", "insert", "delete"])
 def test_move_energy_change_matches_oracle(kind, rc):
     from kups_gb300 import gcmc
 
     setup = small_setup(n_sys=3, rc=rc)
-    rng = np.random.default_rng({"translate": 1, "rotate": 2, "insert": 3, "delete": 4}[kind])
+    rng = np.random.default_rng({"translate": 1, "rotate": 2, "insert": 3, "delete": 4, "reinsert": 5}[kind])
     L = ouc.lattice_from_tril(setup.tril[0])
     mpos = setup.motif_positions
     guests = [np.concatenate([wrapped(random_molecule(rng, L, mpos), setup.tril[0]) for _ in range(4)])
@@ -87,14 +87,23 @@ def test_move_energy_change_matches_oracle(kind, rc):
     for i in range(3):
         g = guests[i].reshape(4, 3, 3)
         m = int(rng.integers(0, 4))
+        # the molecule whole (atoms unwrapped against atom 0), as the kernel treats it
+        whole = g[m][0] + wrapped(g[m] - g[m][0], setup.tril[0])
         if kind == "translate":
             new = wrapped(g[m] + rng.normal(0, 0.5, 3), setup.tril[0])
         elif kind == "rotate":
             from scipy.spatial.transform import Rotation
 
-            c = g[m].mean(0)
+            c = whole.mean(0)
             R = Rotation.random(random_state=int(rng.integers(1 << 30))).as_matrix()
-            new = wrapped((g[m] - c) @ R.T + c, setup.tril[0])
+            new = wrapped((whole - c) @ R.T + c, setup.tril[0])
+        elif kind == "reinsert":
+            # full random rotation about the centre, then a uniform fractional offset
+            from scipy.spatial.transform import Rotation
+
+            c = whole.mean(0)
+            R = Rotation.random(random_state=int(rng.integers(1 << 30))).as_matrix()
+            new = wrapped((whole - c) @ R.T + c + rng.uniform(0, 1, 3) @ L, setup.tril[0])
         elif kind == "insert":
             new = wrapped(random_molecule(rng, L, mpos), setup.tril[0])
         else:
