@@ -58,6 +58,11 @@ def parse():
     ap.add_argument("--no-bonded", action="store_true", help="skip the bonded-term (evaluation and MC energy change), "
                     "virial-observable and local-MLIAP timings")
     ap.add_argument("--gcmc-replicas", type=int, default=1024)
+    ap.add_argument("--gcmc-equil", type=int, default=100000,
+                    help="GCMC equilibration steps (learned proposal) before the plain / learned production runs")
+    ap.add_argument("--gcmc-prod", type=int, default=20000, help="GCMC production steps of each sampler")
+    ap.add_argument("--no-nve-check", dest="nve_check", action="store_false",
+                    help="skip the NVE energy-conservation runs of the LJ + Ewald section")
     ap.add_argument("--strong", action="store_true",
                     help="split one --systems batch across the ranks (cost-balanced contiguous ranges) "
                          "instead of giving every rank its own batch")
@@ -654,27 +659,86 @@ def run_argon(a, torch):
     t1.record()
     torch.cuda.synchronize()
     ms = t0.elapsed_time(t1)
+    # the same system in float64 as the reference computes it: neighbour list rebuilt every step,
+    # float64 LJ over the edges and float64 integrator blocks (kups_gb300.md.LennardJonesMD64)
+    sim64 = md.LennardJonesMD64(state_from_workload(W, torch), "baoab", seed=3)
+    sim64.run(20)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    sim64.run(steps)
+    f1.record()
+    torch.cuda.synchronize()
+    sim64.check()
+    ms64 = f0.elapsed_time(f1)
     return {"workload": "argon NVT: 864 atoms (6x6x6 fcc, a 5.74 A), rc 8.5 A + 1 A skin, BAOAB dt 2 fs, 94.4 K",
             "us_per_step": ms / steps * 1e3, "value": W.n_atoms * steps / (ms / 1e3), "unit": "atom-steps/s",
+            "fp64": {"us_per_step": ms64 / steps * 1e3, "value": W.n_atoms * steps / (ms64 / 1e3),
+                     "path": "float64 step by step: neighbour list every step (rc 8.5 A), float64 LJ over the "
+                             "edges, float64 BAOAB blocks; 7 launches per step"},
             "launch_shape": {"block_threads": prop.block_threads or 1024, "min_lanes_per_atom": prop.min_lanes_per_atom or 2,
                              "chosen_by": "kups_gb300.autotune.autotune_md" if shape else "library default"}}
+
+
+def _melt_sim(W, torch, real_space="auto", integrator="velocity_verlet", positions=None, temperature=None,
+              friction=None):
+    from kups_gb300 import ewald
+
+    c = lambda x, dt=None: torch.as_tensor(np.asarray(x), dtype=dt).cuda()
+    prm = ewald.EwaldParameters(torch.tensor([W.alpha]), torch.tensor([W.cutoff]), torch.as_tensor(W.kvec_n))
+    pos = W.positions if positions is None else positions
+    parts = ewald.EwaldParticles(c(pos), c(W.charges), c(np.zeros(len(W.charges), np.int32)), c(W.species))
+    return ewald.LJEwaldMD(parts, c(W.masses), c(W.tril), prm, W.time_step, W.sigma, W.epsilon, [W.cutoff],
+                           integrator=integrator, temperature=temperature, friction=friction, real_space=real_space)
+
+
+def _against_float64(sim32, sim64, torch):
+    """Energy and force error of the float32 all-pairs step against the float64 edge path at
+    sim32's current positions (both add the same reciprocal and self terms)."""
+    sim64.p.positions.copy_(sim32.p.positions)
+    sim64._forces()
+    torch.cuda.synchronize()
+    g32, g64 = sim32.grad, sim64.grad
+    rms = float(torch.sqrt(((g32 - g64) ** 2).mean() / (g64**2).mean()))
+    e32, e64 = float(sim32.energy.item()), float(sim64.energy.item())
+    return {"force_rms_rel": rms, "energy_rel": abs(e32 - e64) / abs(e64)}
+
+
+def _nve_conservation(sim, steps, n_atoms, torch):
+    """Total energy after every step of an NVE run, judged as the reference's NVE physics check
+    does (ci/statistical/validate_nve_physics.py:29-62): slope of a linear fit per atom per step
+    (bar 1e-8 eV) and std / |mean| (bar 5e-4)."""
+    e = torch.empty(steps, dtype=torch.float64, device="cuda")
+    for k in range(steps):
+        sim.run(1)
+        e[k] = sim.energy.sum() + sim.kinetic_energy().sum()
+    sim.check()
+    e = e.cpu().numpy()
+    slope = float(np.polyfit(np.arange(steps), e, 1)[0])
+    fluct = float(e.std() / abs(e.mean()))
+    return {"steps": steps, "drift_ev_per_atom_step": abs(slope) / n_atoms, "relative_fluctuation": fluct,
+            "drift_ok": abs(slope) / n_atoms < 1e-8, "fluctuation_ok": fluct < 5e-4, "mean_total_energy_ev": float(e.mean())}
 
 
 def run_ewald_md(a):
     """LJ + Ewald NVE MD of the ionic melt: 2000 (+1 e) + 2000 (-1 e) ions in a 40 A cube,
     LB-mixed LJ (0.1 / 0.15 kcal/mol, 2.35 / 4.40 A), rc 12 A, alpha 0.3, |n| <= 8 k vectors
     in the reference's half-space layout, dt 1 fs, velocity Verlet; one step is captured
-    once as a CUDA graph and replayed.  Device-timed over 1000 steps after 20."""
+    once as a CUDA graph and replayed.  Device-timed over 1000 steps after 20.  Accuracy of the
+    float32 all-pairs real space against the float64 edge path (kups_pair_edges, itself held to
+    the float64 oracle at 1e-10) at the start and the end of the timed run; energy conservation
+    of NVE runs from a melt equilibrated with BAOAB at 1200 K, with the float32 and with the
+    float64 real space."""
     import torch
 
-    from kups_gb300 import ewald, workloads
+    from kups_gb300 import workloads
 
     W = workloads.ionic_melt()
-    c = lambda x, dt=None: torch.as_tensor(np.asarray(x), dtype=dt).cuda()
-    prm = ewald.EwaldParameters(torch.tensor([W.alpha]), torch.tensor([W.cutoff]), torch.as_tensor(W.kvec_n))
-    parts = ewald.EwaldParticles(c(W.positions), c(W.charges), c(np.zeros(len(W.charges), np.int32)), c(W.species))
-    sim = ewald.LJEwaldMD(parts, c(W.masses), c(W.tril), prm, W.time_step, W.sigma, W.epsilon, [W.cutoff])
-    sim.start(c(W.momenta))
+    sim = _melt_sim(W, torch)
+    ref = _melt_sim(W, torch, real_space="edges")
+    sim.start(torch.as_tensor(W.momenta).cuda())
+    ref.start(torch.as_tensor(W.momenta).cuda())
+    acc0 = _against_float64(sim, ref, torch)
     sim.run(20)
     torch.cuda.synchronize()
     e0 = float((sim.energy + sim.kinetic_energy()).item())
@@ -687,13 +751,33 @@ def run_ewald_md(a):
     sim.check()
     ms = t0.elapsed_time(t1)
     e1 = float((sim.energy + sim.kinetic_energy()).item())
+    acc1 = _against_float64(sim, ref, torch)
     n = len(W.charges)
-    return {"workload": f"ionic melt: {n} ions, 40 A cube, LJ + Ewald (alpha 0.3, rc 12 A, |n| <= 8), NVE dt 1 fs",
-            "value": n * steps / (ms / 1e3), "unit": "atom-steps/s", "ms_per_step": ms / steps, "steps": steps,
-            "relative_energy_change": (e1 - e0) / abs(e0),
-            "real_space": ("all pairs (float hi/lo positions, per-warp hit queue), no list" if sim.allpairs
-                           else "neighbour list every step"),
-            "fp32_roofline": ewald_fp32_roofline(W, n * steps / (ms / 1e3))}
+    out = {"workload": f"ionic melt: {n} ions, 40 A cube, LJ + Ewald (alpha 0.3, rc 12 A, |n| <= 8), NVE dt 1 fs",
+           "value": n * steps / (ms / 1e3), "unit": "atom-steps/s", "ms_per_step": ms / steps, "steps": steps,
+           "relative_energy_change_from_start": (e1 - e0) / abs(e0),
+           "real_space": ("all pairs (float hi/lo positions, per-warp hit queue), no list" if sim.allpairs
+                          else "neighbour list every step"),
+           "accuracy_vs_float64_path": {"start": acc0, "after_timed_run": acc1},
+           "fp32_roofline": ewald_fp32_roofline(W, n * steps / (ms / 1e3))}
+    if getattr(a, "nve_check", True):
+        from kups_gb300.units import FEMTO_SECOND
+
+        eq = _melt_sim(W, torch, integrator="baoab", temperature=1200.0, friction=0.01 / FEMTO_SECOND)
+        eq.start(torch.as_tensor(W.momenta).cuda())
+        eq.run(2000)
+        torch.cuda.synchronize()
+        eq.check()
+        pos_eq, mom_eq = eq.p.positions.cpu().numpy(), eq.mom.clone()
+        cons = {}
+        for tag, rs, nsteps in (("float32_all_pairs", "allpairs", 1000), ("float64_edges", "edges", 300)):
+            s2 = _melt_sim(W, torch, real_space=rs, positions=pos_eq)
+            s2.start(mom_eq)
+            cons[tag] = _nve_conservation(s2, nsteps, n, torch)
+        out["nve_energy_conservation"] = {
+            "start": "melt after 2000 BAOAB steps at 1200 K (friction 0.01 / fs) from the seeded lattice start",
+            **cons}
+    return out
 
 
 def ewald_fp32_roofline(W, atom_steps_per_s):
@@ -726,7 +810,10 @@ def run_gcmc(a):
 
     setup = workloads.gcmc_co2_framework(n_replicas=a.gcmc_replicas)
     out = learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, train_steps=3000,
-                           batch=16384, equil_steps=10000, prod_steps=5000, block=500, temper=0.5)
+                           batch=16384, equil_steps=a.gcmc_equil, prod_steps=a.gcmc_prod, block=1000, temper=0.5)
+    out["equilibration_steps"] = a.gcmc_equil
+    out["production_steps"] = a.gcmc_prod
+    out["roofline"] = gcmc_roofline(setup, out)
     out["workload"] = (f"GCMC rigid CO2 in a porous host: {a.gcmc_replicas} replicas, host 2000 atoms replicated "
                        "2x2x1 (8000), 0.1-10 bar, 298 K, Ewald alpha 0.25 rc 12 A, moves translate/rotate/"
                        "reinsert/insert/delete 1:1:1:1:1")
@@ -736,6 +823,35 @@ def run_gcmc(a):
                    "on a host that equilibrates (tests/test_gpu_gcmc.py)")
     out.pop("losses", None)
     return out
+
+
+def gcmc_roofline(setup, out):
+    """Per attempted move (one system-step), from the workload: n_cand = host + guest atoms within
+    the cutoff of one moved atom (number density x 4/3 pi rc^3); B_alg = 16 B per candidate +
+    n_k x (16 B S(k) read + 16 B write on accept + 8 B P(k)); F_alg = 6 moved positions (old and new
+    of three atoms) x n_cand x 70 flop (LJ + erfc pair term) + 6 x n_k x 28 flop (phase and
+    structure-factor update).  FP32 peak derived from the SM count and the maximum SM clock."""
+    import torch
+
+    t = np.asarray(setup.tril[0], float)
+    vol = abs(t[0] * t[2] * t[5])
+    apm = len(setup.motif_charges)
+    n_guest = float(out["plain"]["loading_all"]) * apm
+    rho = (float(setup.fw_count[0]) + n_guest) / vol
+    rc = float(max(setup.rc_lj[0], setup.rc_ew[0]))
+    n_cand = rho * 4.0 / 3.0 * math.pi * rc**3
+    n_k = int(np.asarray(setup.kvec_n).shape[1])
+    b_alg = 16.0 * n_cand + n_k * 40.0
+    f_alg = 2 * apm * n_cand * 70.0 + 2 * apm * n_k * 28.0
+    rate = float(out["plain"]["attempted_moves_per_s"])
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    peak32 = sms * 128 * 2 * 2070e6 / 1e12
+    hbm, src = measured_peak()
+    return {"bound": "fp32 issue", "unit": "TFLOP/s", "achieved": rate * f_alg / 1e12, "peak": peak32,
+            "frac": rate * f_alg / 1e12 / peak32, "flop_per_move": f_alg, "bytes_per_move": b_alg,
+            "hbm_achieved_gbs": rate * b_alg / 1e9, "hbm_peak_gbs": hbm, "hbm_frac": rate * b_alg / 1e9 / hbm,
+            "hbm_peak_source": src, "candidates_per_moved_atom": n_cand, "n_kvecs": n_k,
+            "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x 2070 MHz"}
 
 
 def state_from_workload(W, torch, device="cuda", pin=False):
@@ -757,33 +873,40 @@ def state_from_workload(W, torch, device="cuda", pin=False):
 
 
 def run_e2e(a, W, torch):
-    """Public propagator API with host buffers; H2D inputs and D2H outputs every call."""
+    """Public propagator API driven from the host: each call copies the host state (pinned) to
+    the device, runs ``FusedLennardJonesMD.__call__`` and copies the new state back, and the
+    next call starts from what came back, as a simulation loop on host buffers does.  The
+    propagator keeps its workspace between calls, so a system whose state came back unchanged
+    resumes its Verlet list (kups_md_args.reuse_lists)."""
     from kups_gb300 import md
 
     host = state_from_workload(W, torch, device="cpu", pin=True)
     n = W.n_atoms
-    out_pos = torch.empty((n, 3), dtype=torch.float64).pin_memory()
-    out_mom = torch.empty_like(out_pos).pin_memory()
-    out_frc = torch.empty_like(out_pos).pin_memory()
+    pos_h = host.particles.positions
+    mom_h = host.particles.momenta
+    frc_h = torch.zeros((n, 3), dtype=torch.float64).pin_memory()
     out_e = torch.empty(W.n_systems, dtype=torch.float64).pin_memory()
     prop = md.make_baoab_langevin_step(steps_per_call=a.e2e_chunk)
     prop.block_threads, prop.min_lanes_per_atom = getattr(a, "tuned", (0, 0))
+    have_forces = [False]
 
     def one_call(i):
         p = host.particles
         dev = md.MDState(
-            md.MDParticles(p.positions.to("cuda", non_blocking=True), p.momenta.to("cuda", non_blocking=True),
+            md.MDParticles(pos_h.to("cuda", non_blocking=True), mom_h.to("cuda", non_blocking=True),
                            p.masses.to("cuda", non_blocking=True), p.species.to("cuda", non_blocking=True),
-                           p.system.to("cuda", non_blocking=True), None),
+                           p.system.to("cuda", non_blocking=True),
+                           frc_h.to("cuda", non_blocking=True) if have_forces[0] else None),
             md.MDSystems(*(x.to("cuda", non_blocking=True) for x in (host.systems.tril, host.systems.time_step,
                                                                       host.systems.temperature,
                                                                       host.systems.friction_coefficient))),
             host.lj_parameters, skin=host.skin, step=i * a.e2e_chunk)
         out = prop([i, 1], dev)
-        out_pos.copy_(out.particles.positions, non_blocking=True)
-        out_mom.copy_(out.particles.momenta, non_blocking=True)
-        out_frc.copy_(out.particles.forces, non_blocking=True)
+        pos_h.copy_(out.particles.positions, non_blocking=True)
+        mom_h.copy_(out.particles.momenta, non_blocking=True)
+        frc_h.copy_(out.particles.forces, non_blocking=True)
         out_e.copy_(out.systems.potential_energy, non_blocking=True)
+        have_forces[0] = True
 
     one_call(0)
     torch.cuda.synchronize()
@@ -793,11 +916,12 @@ def run_e2e(a, W, torch):
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
     steps = a.e2e_calls * a.e2e_chunk
-    h2d = n * (3 * 8 * 2 + 8 + 4 + 4) + W.n_systems * 8 * 9
+    h2d = n * (3 * 8 * 3 + 8 + 4 + 4) + W.n_systems * 8 * 4
     d2h = n * 3 * 8 * 3 + W.n_systems * 8
     return {"value": n * steps / el, "unit": "atom-steps/s", "h2d_bytes_per_step": h2d / a.e2e_chunk,
             "d2h_bytes_per_step": d2h / a.e2e_chunk, "md_steps_per_call": a.e2e_chunk,
-            "api": "kups_gb300.md.FusedLennardJonesMD.__call__ (host state in pinned memory)"}
+            "api": "kups_gb300.md.FusedLennardJonesMD.__call__ (host state in pinned memory, each call "
+                   "continuing from the state the previous call returned)"}
 
 
 def run_reference(a):

@@ -122,7 +122,10 @@ int32_t kups_lj_edges(const double *positions, const int32_t *system,
  * One persistent launch runs n_steps for every system.  Each CTA takes whole
  * systems from a work queue and keeps a system's atoms, periodic-image
  * copies and cell grid in shared memory for all its steps; the Verlet list
- * (cutoff + skin, uint16 indices) lives in per-CTA workspace.  Pair
+ * (cutoff + skin, uint16 indices) lives in the workspace, one region per
+ * system, together with a per-system record (cell-sorted order, internal
+ * positions, image copies, travelled distances) that lets the next call on
+ * the same workspace resume without a list build (reuse_lists).  Pair
  * arithmetic is float32, per-system energy and virial sums float64.
  *
  * Atoms are stored sorted by system: system s owns [sys_offset[s],
@@ -188,7 +191,15 @@ typedef struct kups_md_args {
   int32_t min_lanes_per_atom; /* lanes sharing one atom's Verlet list in the force phase:
                                  at least this many (1, 2 or 4; 0 = library default 2),
                                  more for small systems so every thread has work */
-  int32_t pad_md;
+  int32_t reuse_lists;       /* 1: a system whose record in the workspace (written by the
+                                previous call on the same workspace) matches this call's inputs
+                                bit for bit (atom count, cell, cutoff, skin, lanes per atom,
+                                neighbor_capacity, and every atom's wrapped position and
+                                species) resumes with its cell-sorted order, image copies,
+                                travelled distances and Verlet list instead of rebuilding them,
+                                exactly as if the previous call had run on; 0: rebuild every
+                                system.  Every call writes the records; integrator 3 always
+                                rebuilds (the cell changes). */
   /* integrator 2 = CSVR (CSVRStep + velocity Verlet, md/integrators.py:469-640),
    * integrator 3 = CSVR + stochastic cell rescaling (make_csvr_npt_step, :641-890).
    * Per-system R1, R2 and the barostat's R are independent draws (the reference

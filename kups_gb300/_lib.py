@@ -44,7 +44,7 @@ class MdArgs(C.Structure):
         ("n_steps", C.c_int32), ("integrator", C.c_int32), ("forces_valid", C.c_int32),
         ("neighbor_capacity", C.c_int32), ("seed", C.c_uint64), ("step0", C.c_uint64),
         ("n_ctas", C.c_int32), ("block_threads", C.c_int32),
-        ("min_lanes_per_atom", C.c_int32), ("pad_md", C.c_int32),
+        ("min_lanes_per_atom", C.c_int32), ("reuse_lists", C.c_int32),
         ("thermostat_tau", C.c_void_p), ("target_pressure", C.c_void_p), ("barostat_tau", C.c_void_p),
         ("compressibility", C.c_void_p), ("min_scale", C.c_void_p), ("cell", C.c_void_p),
     ]

@@ -44,6 +44,67 @@ constexpr int kShiftCount = kShiftSide * kShiftSide * kShiftSide;
 constexpr int kThreads = 1024;
 constexpr int kScratchPerCta = 3 * kMaxAtoms > 2 * kMaxGhosts ? 3 * kMaxAtoms : 2 * kMaxGhosts;  // float4s
 
+// Per-system record kept in the workspace between calls: with it a call resumes a
+// system exactly where the previous call on the same workspace left it (same
+// cell-sorted order, internal unwrapped positions, image copies, travelled
+// distances and Verlet list) instead of rebuilding.  The record is trusted only
+// if every field below equals this call's input bit for bit and every atom's
+// internal position, wrapped as the write-back wraps it, equals the input.
+struct SysRecord {
+  int32_t valid, n, tpa, cap;
+  int32_t n_ghosts, pad0;
+  uint32_t rc, skin;
+  uint32_t tril[6];
+  uint32_t pad1[2];
+};
+static_assert(sizeof(SysRecord) == 64, "system record is 64 bytes");
+
+// Pointers into the caller's workspace (layout of md_layout below).
+struct MdWork {
+  float4 *scratch;   // [ctas][kScratchPerCta] staging of the list builds
+  SysRecord *rec;    // [S]
+  float4 *apos;      // [N] internal positions in cell-sorted slot order
+  uint32_t *ameta;   // [N] input index of the slot | neighbour count << 16
+  float *atrav;      // [N] distance travelled since the last list build
+  uint32_t *gmeta;   // [S][kMaxGhosts] image copies: source slot | shift code << 16
+  uint2 *lists;      // [N * md_units_per_atom] Verlet lists, system s from sys_offset[s] * md_units_per_atom
+};
+
+inline size_t md_align(size_t x) { return (x + 255) & ~size_t(255); }
+
+// 8-byte list units reserved per atom: capacity / 4 rounded up to a multiple of the
+// largest lane count (16), so the unit index ((u / tpa) * n + i) * tpa + u % tpa of
+// every u < capacity / 4 stays below n times this for any tpa <= 16.
+__host__ __device__ inline size_t md_units_per_atom(int capacity) {
+  return ((size_t)(capacity / 4) + 15) & ~size_t(15);
+}
+
+struct MdLayout {
+  size_t scratch, rec, apos, ameta, atrav, gmeta, lists, total;
+};
+
+// Byte offsets from the 256-byte aligned workspace base (the queue word sits at 0).
+inline MdLayout md_layout(int ctas, int64_t n_atoms, int n_systems, int capacity) {
+  MdLayout l;
+  size_t o = 256;
+  l.scratch = o;
+  o += md_align((size_t)ctas * kScratchPerCta * sizeof(float4));
+  l.rec = o;
+  o += md_align((size_t)n_systems * sizeof(SysRecord));
+  l.apos = o;
+  o += md_align((size_t)n_atoms * sizeof(float4));
+  l.ameta = o;
+  o += md_align((size_t)n_atoms * sizeof(uint32_t));
+  l.atrav = o;
+  o += md_align((size_t)n_atoms * sizeof(float));
+  l.gmeta = o;
+  o += md_align((size_t)n_systems * kMaxGhosts * sizeof(uint32_t));
+  l.lists = o;
+  o += md_align((size_t)n_atoms * md_units_per_atom(capacity) * sizeof(uint2));
+  l.total = o;
+  return l;
+}
+
 struct SysParams {
   float L[6];     // L00 L10 L11 L20 L21 L22
   float inv[6];
@@ -714,19 +775,115 @@ __device__ void csvr_alpha(Smem &sm, double ke, uint64_t seed, int sys, uint64_t
   __syncthreads();
 }
 
+// Resume system s from its record (all threads call; returns the same value in
+// every thread).  On success the shared state (cell-sorted atoms, momenta,
+// forces with travelled distances, image copies, neighbour counts) is exactly
+// what the previous call held at its last step, and the Verlet list in the
+// workspace is the one it built.  On failure nothing of the shared state is
+// relied upon: the caller loads the input and rebuilds.
+__device__ __noinline__ bool try_resume(Smem &sm, const SysParams &p, const kups_md_args &a, const MdWork &w,
+                                        int s, int a0, int n, int tpa, const float4 *gpos, const float4 *gmom,
+                                        const float4 *gfrc) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int cap = a.neighbor_capacity;
+  if (tid == 0) {
+    const SysRecord r = w.rec[s];
+    bool ok = r.valid == 1 && r.n == n && r.tpa == tpa && r.cap == cap && r.n_ghosts >= 0 &&
+              r.n_ghosts <= kMaxGhosts - 1 && r.rc == __float_as_uint(a.cutoff[s]) &&
+              r.skin == __float_as_uint(a.skin[s]);
+    for (int k = 0; k < 6; ++k) ok = ok && r.tril[k] == __float_as_uint(a.tril[6 * (int64_t)s + k]);
+    sm.flag = ok ? 1 : 0;
+    sm.n_ghosts = ok ? r.n_ghosts : 0;
+  }
+  for (int k = tid; k < kMaxAtoms / 32; k += nt) sm.cell_fill[k] = 0;  // bitmap of input indices seen
+  __syncthreads();
+  if (sm.flag == 0) return false;
+  int bad = 0;
+  for (int i = tid; i < n; i += nt) {
+    const uint32_t m = w.ameta[a0 + i];
+    const int g = (int)(m & 0xffffu), c = (int)(m >> 16);
+    if (g >= n || c > cap) {
+      bad = 1;
+      continue;
+    }
+    const uint32_t bit = 1u << (g & 31);
+    if (atomicOr(reinterpret_cast<unsigned *>(&sm.cell_fill[g >> 5]), bit) & bit) {
+      bad = 1;  // an input index claimed twice
+      continue;
+    }
+    float4 q = w.apos[a0 + i];
+    float f[3];
+    wrap_position(p, q, f);
+    const float4 in = gpos[a0 + g];
+    bad |= (__float_as_uint(q.x) != __float_as_uint(in.x)) | (__float_as_uint(q.y) != __float_as_uint(in.y)) |
+           (__float_as_uint(q.z) != __float_as_uint(in.z)) | (__float_as_uint(q.w) != __float_as_uint(in.w));
+  }
+  if (__syncthreads_or(bad)) return false;
+  const int ng = sm.n_ghosts;
+  int badg = 0;
+  for (int k = tid; k < ng; k += nt) {
+    const uint32_t m = w.gmeta[(size_t)s * kMaxGhosts + k];
+    badg |= ((int)(m & 0xffffu) >= n) | ((int)(m >> 16) >= kShiftCount);
+    sm.ghost_meta[k] = m;
+  }
+  for (int i = tid; i < n; i += nt) {
+    const uint32_t m = w.ameta[a0 + i];
+    const int g = (int)(m & 0xffffu);
+    sm.pos[i] = w.apos[a0 + i];
+    sm.gid[i] = (uint16_t)g;
+    sm.nbr_count[i] = (uint16_t)(m >> 16);
+    sm.mom[i] = gmom[a0 + g];
+    float4 F = gfrc[a0 + g];
+    F.w = w.atrav[a0 + i];
+    sm.frc[i] = F;
+  }
+  if (__syncthreads_or(badg)) return false;
+  update_ghosts(sm, n);
+  if (tid == 0) {
+    sm.pos[n + ng] = make_float4(1e15f, 1e15f, 1e15f, __int_as_float(0));  // sentinel item
+    sm.work = 0;
+  }
+  __syncthreads();
+  return true;
+}
+
+// Record of system s for the next call (all threads call).
+__device__ void save_record(const Smem &sm, const kups_md_args &a, const MdWork &w, int s, int a0, int n, int tpa,
+                            bool valid) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < n; i += nt) {
+    w.apos[a0 + i] = sm.pos[i];
+    w.ameta[a0 + i] = (uint32_t)sm.gid[i] | ((uint32_t)sm.nbr_count[i] << 16);
+    w.atrav[a0 + i] = sm.frc[i].w;
+  }
+  const int ng = sm.n_ghosts;
+  for (int k = tid; k < ng; k += nt) w.gmeta[(size_t)s * kMaxGhosts + k] = sm.ghost_meta[k];
+  if (tid == 0) {
+    SysRecord r;
+    r.valid = valid ? 1 : 0;
+    r.n = n;
+    r.tpa = tpa;
+    r.cap = a.neighbor_capacity;
+    r.n_ghosts = ng;
+    r.pad0 = 0;
+    r.rc = __float_as_uint(a.cutoff[s]);
+    r.skin = __float_as_uint(a.skin[s]);
+    for (int k = 0; k < 6; ++k) r.tril[k] = __float_as_uint(a.tril[6 * (int64_t)s + k]);
+    r.pad1[0] = r.pad1[1] = 0;
+    w.rec[s] = r;
+  }
+}
+
 template <int INTEGRATOR>
 __global__ void __launch_bounds__(kThreads, 1)
-md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
+md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
   const int tid = threadIdx.x, nt = blockDim.x;
   float4 *gpos = reinterpret_cast<float4 *>(a.pos);
   float4 *gmom = reinterpret_cast<float4 *>(a.mom);
   float4 *gfrc = reinterpret_cast<float4 *>(a.force);
-  uint2 *nl = reinterpret_cast<uint2 *>(nl_ws) + (size_t)blockIdx.x * kMaxAtoms * (a.neighbor_capacity / 4);
-  float4 *scratch = reinterpret_cast<float4 *>(reinterpret_cast<char *>(nl_ws) +
-                                               (size_t)gridDim.x * kMaxAtoms * (a.neighbor_capacity / 4) * sizeof(uint2)) +
-                    (size_t)blockIdx.x * kScratchPerCta;
+  float4 *scratch = w.scratch + (size_t)blockIdx.x * kScratchPerCta;
   unsigned long long *prof = reinterpret_cast<unsigned long long *>(a.profile);
   const int nsp = a.n_species;
   for (int k = tid; k < nsp * nsp; k += nt)
@@ -747,6 +904,11 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
       if (tid == 0) status_capacity(status, KUPS_CAP_ATOMS, n, s);
       continue;
     }
+    if ((int64_t)a0 + n > a.n_atoms || a0 < 0) {  // the workspace regions are sized by n_atoms
+      if (tid == 0) status_error(status, KUPS_ERR_INVALID, s);
+      continue;
+    }
+    uint2 *nl = w.lists + (size_t)a0 * md_units_per_atom(a.neighbor_capacity);
     long long t0 = clock64();
     // ---- per-system parameters, computed once into shared memory
     SysParams &p = sm.p;
@@ -789,26 +951,32 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
       continue;
     }
     set_shift_vectors(sm);
-    int bad_species = 0;
-    for (int i = tid; i < n; i += nt) {
-      const float4 qv = gpos[a0 + i];
-      const int t = __float_as_int(qv.w);
-      bad_species |= (t < 0) | (t >= nsp);
-      sm.pos[i] = qv;
-      sm.mom[i] = gmom[a0 + i];
-      sm.frc[i] = gfrc[a0 + i];
-      sm.gid[i] = (uint16_t)i;
-    }
-    if (__syncthreads_or(bad_species)) {
-      if (tid == 0) status_error(status, KUPS_ERR_INVALID, s);
-      continue;
-    }
     const int tpa = choose_tpa(n, nt, a.min_lanes_per_atom);
-    bool ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s, prof, scratch);
-    if (tid == 0) sm.work = 0;
-    __syncthreads();
-    if (!ok) continue;
-    if (tid == 0 && a.rebuilds != nullptr) a.rebuilds[s] += 1;
+    bool ok = true;
+    const bool resumed = INTEGRATOR != 3 && a.reuse_lists != 0 &&
+                         try_resume(sm, p, a, w, s, a0, n, tpa, gpos, gmom, gfrc);
+    if (tid == 0) w.rec[s].valid = 0;  // set again when this call has written the record
+    if (!resumed) {
+      int bad_species = 0;
+      for (int i = tid; i < n; i += nt) {
+        const float4 qv = gpos[a0 + i];
+        const int t = __float_as_int(qv.w);
+        bad_species |= (t < 0) | (t >= nsp);
+        sm.pos[i] = qv;
+        sm.mom[i] = gmom[a0 + i];
+        sm.frc[i] = gfrc[a0 + i];
+        sm.gid[i] = (uint16_t)i;
+      }
+      if (__syncthreads_or(bad_species)) {
+        if (tid == 0) status_error(status, KUPS_ERR_INVALID, s);
+        continue;
+      }
+      ok = rebuild(sm, p, n, tpa, nl, a.neighbor_capacity, status, s, prof, scratch);
+      if (tid == 0) sm.work = 0;
+      __syncthreads();
+      if (!ok) continue;
+      if (tid == 0 && a.rebuilds != nullptr) a.rebuilds[s] += 1;
+    }
     prof_add(prof, 0, t0);
     // hot scalars in registers
     const float rc2 = p.rc2, dt = p.dt, hdt = 0.5f * p.dt, c1 = p.c1, c2 = p.c2;
@@ -1107,6 +1275,7 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
     }
     if (INTEGRATOR == 3 && tid == 0)
       for (int k = 0; k < 6; ++k) a.cell[6 * (int64_t)s + k] = p.Ld[k];
+    save_record(sm, a, w, s, a0, n, tpa, INTEGRATOR != 3);
     prof_add(prof, 5, t0);
     __syncthreads();
   }
@@ -1118,12 +1287,12 @@ md_lj_kernel(kups_md_args a, uint32_t *nl_ws, int *queue, kups_status *status) {
 using namespace kups;
 
 template <int INTEGRATOR>
-static cudaError_t launch_md(const kups_md_args &a, int ctas, int threads, size_t smem, uint32_t *nl,
+static cudaError_t launch_md(const kups_md_args &a, int ctas, int threads, size_t smem, const MdWork &w,
                              int *queue, kups_status *status, cudaStream_t stream) {
   cudaError_t e = cudaFuncSetAttribute(md_lj_kernel<INTEGRATOR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
-  md_lj_kernel<INTEGRATOR><<<ctas, threads, smem, stream>>>(a, nl, queue, status);
+  md_lj_kernel<INTEGRATOR><<<ctas, threads, smem, stream>>>(a, w, queue, status);
   return cudaSuccess;
 }
 
@@ -1134,8 +1303,8 @@ extern "C" size_t kups_lj_md_workspace_bytes(const kups_md_args *a) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int ctas = a->n_ctas > 0 ? a->n_ctas : (sms > 0 ? sms : 1);
-  return 256 + (size_t)ctas * (kMaxAtoms * (size_t)(a->neighbor_capacity / 4) * sizeof(uint2) +
-                              kScratchPerCta * sizeof(float4)) + 256;
+  return md_layout(ctas, a->n_atoms < 0 ? 0 : a->n_atoms, a->n_systems < 0 ? 0 : a->n_systems,
+                   a->neighbor_capacity).total + 256;
 }
 
 extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t ws_bytes,
@@ -1166,15 +1335,25 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
   if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4) return KUPS_ERR_INVALID;
   kups_md_args args = *a;
   if (args.min_lanes_per_atom == 0) args.min_lanes_per_atom = 2;
-  int *queue = reinterpret_cast<int *>(((uintptr_t)workspace + 255) & ~uintptr_t(255));
-  uint32_t *nl = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(queue) + 256);
+  if (a->n_atoms < 0) return KUPS_ERR_INVALID;
+  char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~uintptr_t(255));
+  int *queue = reinterpret_cast<int *>(base);
+  const MdLayout l = md_layout(ctas, a->n_atoms, a->n_systems, a->neighbor_capacity);
+  MdWork w;
+  w.scratch = reinterpret_cast<float4 *>(base + l.scratch);
+  w.rec = reinterpret_cast<SysRecord *>(base + l.rec);
+  w.apos = reinterpret_cast<float4 *>(base + l.apos);
+  w.ameta = reinterpret_cast<uint32_t *>(base + l.ameta);
+  w.atrav = reinterpret_cast<float *>(base + l.atrav);
+  w.gmeta = reinterpret_cast<uint32_t *>(base + l.gmeta);
+  w.lists = reinterpret_cast<uint2 *>(base + l.lists);
   KUPS_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(int), stream));
   const size_t smem = sizeof(Smem);
   switch (a->integrator) {
-    case 0: KUPS_CUDA_TRY(launch_md<0>(args, ctas, threads, smem, nl, queue, status, stream)); break;
-    case 1: KUPS_CUDA_TRY(launch_md<1>(args, ctas, threads, smem, nl, queue, status, stream)); break;
-    case 2: KUPS_CUDA_TRY(launch_md<2>(args, ctas, threads, smem, nl, queue, status, stream)); break;
-    default: KUPS_CUDA_TRY(launch_md<3>(args, ctas, threads, smem, nl, queue, status, stream)); break;
+    case 0: KUPS_CUDA_TRY(launch_md<0>(args, ctas, threads, smem, w, queue, status, stream)); break;
+    case 1: KUPS_CUDA_TRY(launch_md<1>(args, ctas, threads, smem, w, queue, status, stream)); break;
+    case 2: KUPS_CUDA_TRY(launch_md<2>(args, ctas, threads, smem, w, queue, status, stream)); break;
+    default: KUPS_CUDA_TRY(launch_md<3>(args, ctas, threads, smem, w, queue, status, stream)); break;
   }
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

@@ -288,12 +288,13 @@ class LJEwaldMD:
     evaluated from shared-memory tiles with no stored list
     (kups_lj_ewald_real_forces); otherwise the neighbour list is rebuilt every
     step, as the reference MD application does, and the edges are evaluated by
-    kups_pair_edges.
+    kups_pair_edges in float64.  ``real_space`` forces one of the two ("allpairs",
+    "edges"; "auto" picks all pairs when it applies).
     """
 
     def __init__(self, particles: EwaldParticles, masses, tril, ewald: EwaldParameters, time_step, lj_sigma=None,
                  lj_epsilon=None, lj_cutoff=None, integrator="velocity_verlet", temperature=None, friction=None,
-                 avg_edges=None, seed=0):
+                 avg_edges=None, seed=0, real_space="auto"):
         self.p = particles
         self.n = particles.positions.shape[0]
         self.tril = _f64(tril)
@@ -320,8 +321,15 @@ class LJEwaldMD:
         vol = float((self.tril[:, 0] * self.tril[:, 2] * self.tril[:, 5]).abs().min())
         nsp = int(self.sig.shape[0]) if self.lj else 1
         grouped = bool((self.system[1:] >= self.system[:-1]).all()) if self.n > 1 else True
-        self.allpairs = grouped and nsp <= 8 and bool(
+        fits = grouped and nsp <= 8 and bool(
             (_perpendicular_widths(self.tril).min(1) >= 2.0 * self.rc_nl.cpu().numpy()).all())
+        if real_space not in ("auto", "allpairs", "edges"):
+            raise ValueError("real_space is 'auto', 'allpairs' or 'edges'")
+        if real_space == "allpairs" and not fits:
+            raise ValueError("the all-pairs real space needs systems grouped in order, at most 8 species and "
+                             "every cell width at least twice the cutoff")
+        # all pairs in float32 (no stored list) when it applies, else the float64 edge path
+        self.allpairs = fits and real_space != "edges"
         if avg_edges is None:
             avg_edges = int(4 / 3 * math.pi * float(self.rc_nl.max()) ** 3 * self.n / vol * 1.5) + 64
         self.cap = avg_edges * self.n

@@ -223,6 +223,7 @@ class FusedLennardJonesMD:
     n_ctas: int = 0
     block_threads: int = 0
     min_lanes_per_atom: int = 0  # 0: library default; kups_gb300.autotune picks one per workload
+    reuse_lists: bool = True  # resume systems whose workspace record matches the input (kups_md_args.reuse_lists)
     _ws: torch.Tensor | None = field(default=None, repr=False)
 
     def __call__(self, key, state: MDState) -> MDState:
@@ -266,6 +267,7 @@ class FusedLennardJonesMD:
         a.seed, a.step0 = int(seed) & (2**64 - 1), int(step0)
         a.n_ctas, a.block_threads = self.n_ctas, self.block_threads
         a.min_lanes_per_atom = self.min_lanes_per_atom
+        a.reuse_lists = int(bool(self.reuse_lists))
         if a.integrator >= 2:
             need = ["thermostat_tau"] + (["target_pressure", "barostat_tau", "compressibility", "min_scale"]
                                          if a.integrator == 3 else [])
@@ -282,7 +284,9 @@ class FusedLennardJonesMD:
     def workspace(self, a: _lib.MdArgs) -> torch.Tensor:
         nbytes = _lib.load().kups_lj_md_workspace_bytes(C.byref(a))
         if self._ws is None or self._ws.numel() < nbytes:
-            self._ws = torch.empty(nbytes, device="cuda", dtype=torch.uint8)
+            # the per-system records start invalid (a record is trusted only after exact checks,
+            # zeros make the first call skip them outright)
+            self._ws = torch.zeros(nbytes, device="cuda", dtype=torch.uint8)
         return self._ws
 
     def launch(self, packed: PackedMD, n_steps: int, seed: int = 0, step0: int = 0, status=None, trace_pe=None,

@@ -329,3 +329,65 @@ def test_fused_md_pressure_matches_reference_formula():
         ke = 0.5 * np.sum(mom[sel] ** 2 / W.masses[sel][:, None])
         exp.append(2 * ke / (3 * vol) + np.trace(sigma) / 3)
     np.testing.assert_allclose(got, exp, rtol=1e-4, atol=1e-4 * np.abs(exp).max())
+
+
+def _packed_copy(packed):
+    from dataclasses import replace
+
+    return replace(packed, pos4=packed.pos4.clone(), mom4=packed.mom4.clone(), frc4=packed.frc4.clone(),
+                   energy=None, kinetic=None, virial=None, pressure=None,
+                   rebuilds=torch.zeros(packed.n_systems, dtype=torch.int32, device="cuda"))
+
+
+@pytest.mark.parametrize("integrator", ["velocity_verlet", "baoab"])
+def test_fused_md_resumes_lists_across_calls(integrator):
+    """Two calls of 30 steps on one workspace give the state of one 60-step call bit for bit:
+    the second call resumes every system from the workspace record (cell-sorted order, image
+    copies, travelled distances, Verlet list) instead of rebuilding, so the list-build count
+    of the split run equals the single run's."""
+    from kups_gb300 import md
+
+    W = small_batch()
+    base = md.pack(md_state(W))
+    one, two = _packed_copy(base), _packed_copy(base)
+    md.FusedLennardJonesMD(integrator).run_packed(one, 60, seed=5, step0=0)
+    prop = md.FusedLennardJonesMD(integrator)
+    prop.run_packed(two, 30, seed=5, step0=0)
+    first = two.rebuilds.clone()
+    prop.run_packed(two, 30, seed=5, step0=30)
+    for x, y in ((one.pos4, two.pos4), (one.mom4, two.mom4), (one.frc4, two.frc4)):
+        np.testing.assert_array_equal(x.cpu().numpy(), y.cpu().numpy())
+    np.testing.assert_array_equal(one.energy.cpu().numpy(), two.energy.cpu().numpy())
+    np.testing.assert_array_equal(one.rebuilds.cpu().numpy(), two.rebuilds.cpu().numpy())
+    assert int(first.min()) >= 1  # every system built its list in the first call
+
+
+def test_fused_md_rebuilds_when_the_input_changed():
+    """A system whose positions were changed between calls (or every system, with
+    reuse_lists off) is rebuilt, and its forces still match the oracle."""
+    from kups_gb300 import md
+
+    W = small_batch()
+    packed = _packed_copy(md.pack(md_state(W)))
+    prop = md.make_velocity_verlet_step()
+    prop.run_packed(packed, 10, seed=1, step0=0)
+    off = packed.sys_offset.cpu().numpy()
+    packed.pos4[off[3], 0] += 0.01  # move one atom of system 3
+    packed.forces_valid = False
+    packed.rebuilds.zero_()
+    prop.run_packed(packed, 0, seed=1, step0=10)
+    reb = packed.rebuilds.cpu().numpy()
+    assert reb[3] == 1 and reb.sum() == 1, reb
+    pos4 = packed.pos4.cpu().numpy()
+    perm = packed.perm.cpu().numpy()
+    pos = np.empty((len(perm), 3))
+    pos[perm] = pos4[:, :3]
+    e, f, _ = oracle_forces(W, pos)
+    gf = np.empty((len(perm), 3))
+    gf[perm] = packed.frc4.cpu().numpy()[:, :3]
+    rms = np.sqrt(np.mean((gf - f) ** 2)) / np.sqrt(np.mean(f**2))
+    assert rms <= FORCE_RMS_TOL, rms
+    prop.reuse_lists = False
+    packed.rebuilds.zero_()
+    prop.run_packed(packed, 5, seed=1, step0=10)
+    assert int(packed.rebuilds.cpu().numpy().min()) >= 1

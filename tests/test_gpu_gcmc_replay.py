@@ -88,7 +88,9 @@ def _replay(rc, seed, n_steps, energy_every):
                 assert abs(r["de"] - exp) <= 2e-5 + 2e-5 * abs(exp), (t, kind, r["de"], exp)
                 n_energy += 1
             # apply the decision as the device did (deletion moves the last molecule into the slot)
-            if r["accept"]:
+            # a deletion from an empty system changes nothing (ln acc = 0 accepts it, as the
+            # reference accepts a null patch)
+            if r["accept"] and (has_old or new is not None):
                 if kind == 3:
                     state[s] = np.concatenate([state[s], dev_new[None]])
                 elif kind == 4:
@@ -109,11 +111,11 @@ def _replay(rc, seed, n_steps, energy_every):
 
 @pytest.mark.parametrize("rc", [5.0, 7.0])  # minimum image / 3 x 3 x 3 image offsets
 def test_free_running_steps_replay_exactly(rc):
-    kinds_seen, n_energy, mc = _replay(rc, seed=17 if rc == 5.0 else 23, n_steps=1200, energy_every=25)
+    kinds_seen, n_energy, mc = _replay(rc, seed=17 if rc == 5.0 else 23, n_steps=1200, energy_every=20)
     # every kind was proposed, and accepted and rejected at least once overall
     assert {k for k, _ in kinds_seen} == {0, 1, 2, 3, 4}
     assert {a for _, a in kinds_seen} == {0, 1}
-    assert n_energy >= 30
+    assert n_energy >= 25
     # the schedulers moved: 1200 steps give every displacement kind more than 100 moves
     w = mc.width.cpu().numpy()
     assert np.any(np.abs(w[:, :3] - 0.1) > 1e-3)
