@@ -348,6 +348,7 @@ def run_ours(a):
     line["fp32_roofline"] = {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                              "frac": fp32_achieved / fp32_peak, "flop_per_atom_step": flop_atom_step,
                              "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x {mhz:.0f} MHz"}
+    line["steady_state"] = steady_state(prop, packed, torch, step0, W.n_atoms)
     if not a.no_e2e:
         line["e2e"] = run_e2e(a, W, torch)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -369,6 +370,39 @@ def run_ours(a):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def steady_state(prop, packed, torch, step0, n_atoms, steps=500, traced=100):
+    """After the timed region: one launch of `steps` steps (list builds at their natural rate,
+    every Verlet list past its first use) and one launch of `traced` steps that also records the
+    potential and kinetic energy and dE/dtril of every system after every step (the reference's
+    potential returns energy and cell gradient at every step), each device-timed."""
+    from kups_gb300 import _lib
+    from kups_gb300.neighborlist import read_status
+
+    out = {}
+    for tag, n, tr in (("ms_per_step", steps, False), ("ms_per_step_with_energy_and_virial", traced, True)):
+        S = packed.n_systems
+        tpe = torch.zeros((n, S), dtype=torch.float64, device="cuda") if tr else None
+        tke = torch.zeros((n, S), dtype=torch.float64, device="cuda") if tr else None
+        tvir = torch.zeros((n, S, 6), dtype=torch.float64, device="cuda") if tr else None
+        packed.rebuilds = torch.zeros(S, dtype=torch.int32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        st = prop.launch(packed, n, seed=11, step0=step0, virial=False, trace_pe=tpe, trace_ke=tke,
+                         trace_virial=tvir)
+        e1.record()
+        torch.cuda.synchronize()
+        _lib.raise_status(read_status(st))
+        step0 += n
+        out[tag] = e0.elapsed_time(e1) / n
+        if not tr:
+            out["atom_steps_per_s"] = n_atoms / (out[tag] / 1e3)
+            out["list_builds_per_system_per_100_steps"] = float(packed.rebuilds.double().mean()) * 100.0 / n
+        packed.rebuilds = None
+    out["steps"] = steps
+    out["traced_steps"] = traced
+    return out
 
 
 def run_ensembles(a, W, torch, steps=200):

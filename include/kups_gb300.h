@@ -91,6 +91,45 @@ int32_t kups_neighborlist_build(const double *positions, const int32_t *system,
                                 void *workspace, size_t workspace_bytes,
                                 kups_status *status, void *stream);
 
+/* kups_neighborlist_build_rh replaces NearestNeighborList.__call__ with a
+ * separate rh table (src/kups/core/neighborlist.py:226-255, basic_neighborlist
+ * :743-786): directed edges (i in lh, j in rh) of the same system and inclusion
+ * label within the system's cutoff, under the image rule of the full mode with
+ * the difference lh - rh, the exclusion labels of lh and rh dropping only the
+ * minimum image (:731-735).  With rh_index_remap (rh particle j stands for lh
+ * particle remap[j], as in neighborlist_changes) a pair whose lh particle is
+ * itself remapped is kept only for i >= remap[j], and each edge (i, remap[j], s)
+ * is written with its reverse (remap[j], i, -s) (_build_segmentation_mask
+ * :505-539, _compact_edges :651-689); without it edges are (i, j), j indexing rh.
+ * Rows past n_edges are padded with max(n_lh, n_rh); overflow is reported in
+ * `status` (KUPS_CAP_EDGES, required = n_edges). */
+size_t kups_neighborlist_rh_workspace_bytes(int64_t n_lh, int64_t n_rh, int32_t n_systems);
+int32_t kups_neighborlist_build_rh(const double *lh_positions, const int32_t *lh_system,
+                                   const int32_t *lh_inclusion, const int32_t *lh_exclusion, int64_t n_lh,
+                                   const double *rh_positions, const int32_t *rh_system,
+                                   const int32_t *rh_inclusion, const int32_t *rh_exclusion, int64_t n_rh,
+                                   const int32_t *rh_index_remap, int32_t n_inclusion, const double *tril,
+                                   const double *cutoffs, int32_t n_systems, int32_t *edges, int32_t *shifts,
+                                   int64_t edge_capacity, int64_t *n_edges, void *workspace,
+                                   size_t workspace_bytes, kups_status *status, void *stream);
+
+/* kups_neighborlist_split_changes is the split step of neighborlist_changes
+ * (src/kups/core/neighborlist.py:1425-1515) applied to the edges of the combined
+ * rh call (lh = n original particles followed by the k proposed ones, rh = the
+ * old copies of the changed particles p_idx followed by the proposed ones,
+ * remap = [p_idx, n + arange(k)]): removed = edges with both ends < n; added =
+ * edges with an end >= n and no end that is a changed particle's old copy;
+ * indices n + m are rewritten to p_idx[m].  Both outputs are compacted in edge
+ * order and padded with n; n_added / n_removed receive the counts (overflow of
+ * a capacity is reported in `status`). */
+size_t kups_neighborlist_split_workspace_bytes(int64_t edge_rows, int64_t n);
+int32_t kups_neighborlist_split_changes(const int32_t *edges, const int32_t *shifts, const int64_t *n_edges,
+                                        int64_t edge_rows, int64_t n, const int32_t *p_idx, int64_t k,
+                                        int32_t *added_edges, int32_t *added_shifts, int64_t added_capacity,
+                                        int64_t *n_added, int32_t *removed_edges, int32_t *removed_shifts,
+                                        int64_t removed_capacity, int64_t *n_removed, void *workspace,
+                                        size_t workspace_bytes, kups_status *status, void *stream);
+
 /* ------------------------------------------------------------------------
  * Lennard-Jones over an edge list — replaces lennard_jones_energy
  * (src/kups/potential/classical/lennard_jones.py:149-178) together with the
@@ -211,6 +250,9 @@ typedef struct kups_md_args {
   const double *min_scale;        /* [n_systems] mu clipped to [min_scale, 1 / min_scale] */
   double *cell;                   /* [n_systems, 6] in/out (integrator 3): float64 tril of the
                                      cell, scaled by the barostat; `tril` is not read */
+  double *trace_virial;           /* [n_steps, n_systems, 6] out (may be NULL; integrators 0-2):
+                                     dE/dtril after every step, as `virial` holds it after the
+                                     last (the reference's potential returns it every step) */
 } kups_md_args;
 
 size_t kups_lj_md_workspace_bytes(const kups_md_args *args);
@@ -267,6 +309,14 @@ int32_t kups_ewald_recip(const double *positions, const double *charges,
                          double coulomb_k, double *energy, double *grad, double *grad_tril,
                          double *structure_factor, void *workspace, size_t workspace_bytes,
                          kups_status *status, void *stream);
+/* kups_ewald_recip_energy: E = K sum_k P(k) |S(k)|^2 per system from given
+ * structure factors (float64 [S, n_kvecs, 2]), the long-range energy of a
+ * cached S(k) (EwaldCache / EwaldLongRangeComposer, src/kups/potential/
+ * classical/ewald.py:86-150, 604-657); workspace as kups_ewald_recip. */
+int32_t kups_ewald_recip_energy(const double *tril, const int32_t *kvec_n, int32_t n_kvecs, const double *alpha,
+                                int32_t n_systems, double coulomb_k, const double *structure_factor,
+                                double *energy, void *workspace, size_t workspace_bytes, kups_status *status,
+                                void *stream);
 /*
  * kups_ewald_recip_static — no counterpart in the reference.  The same
  * computation and outputs as kups_ewald_recip, for callers that cannot

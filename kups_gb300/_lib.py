@@ -47,6 +47,7 @@ class MdArgs(C.Structure):
         ("min_lanes_per_atom", C.c_int32), ("reuse_lists", C.c_int32),
         ("thermostat_tau", C.c_void_p), ("target_pressure", C.c_void_p), ("barostat_tau", C.c_void_p),
         ("compressibility", C.c_void_p), ("min_scale", C.c_void_p), ("cell", C.c_void_p),
+        ("trace_virial", C.c_void_p),
     ]
 
 
@@ -93,6 +94,12 @@ SIGNATURES = {
     "kups_error_string": (C.c_char_p, [_I32]),
     "kups_neighborlist_workspace_bytes": (_SZ, [_I64, _I32]),
     "kups_neighborlist_build": (_I32, [_P, _P, _P, _P, _I64, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _SZ, _P, _P]),
+    "kups_neighborlist_rh_workspace_bytes": (_SZ, [_I64, _I64, _I32]),
+    "kups_neighborlist_build_rh": (_I32, [_P, _P, _P, _P, _I64, _P, _P, _P, _P, _I64, _P, _I32, _P, _P, _I32, _P, _P,
+                                          _I64, _P, _P, _SZ, _P, _P]),
+    "kups_neighborlist_split_workspace_bytes": (_SZ, [_I64, _I64]),
+    "kups_neighborlist_split_changes": (_I32, [_P, _P, _P, _I64, _I64, _P, _I64, _P, _P, _I64, _P, _P, _P, _I64, _P,
+                                               _P, _SZ, _P, _P]),
     "kups_lj_edges": (_I32, [_P, _P, _P, _I64, _P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _I32, _P, _P]),
     "kups_lj_md_workspace_bytes": (_SZ, [C.POINTER(MdArgs)]),
     "kups_lj_md_run": (_I32, [C.POINTER(MdArgs), _P, _SZ, _P, _P]),
@@ -101,6 +108,7 @@ SIGNATURES = {
     "kups_md_unpack": (_I32, [_P, _P, _P, _P, _I64, _P, _P, _P, _P]),
     "kups_ewald_recip_workspace_bytes": (_SZ, [_I32, _I32]),
     "kups_ewald_recip": (_I32, [_P, _P, _P, _I32, _I32, _P, _P, _I32, _P, C.c_double, _P, _P, _P, _P, _P, _SZ, _P, _P]),
+    "kups_ewald_recip_energy": (_I32, [_P, _P, _I32, _P, _I32, C.c_double, _P, _P, _P, _SZ, _P, _P]),
     "kups_ewald_recip_static": (_I32, [_P, _P, _P, _I32, _I32, _P, _P, _I32, _P, C.c_double, _P, _P, _P, _P, _P, _P]),
     "kups_lj_ewald_real_forces": (_I32, [_P, _P, _P, _P, _I32, _I32, _P, _P, _P, _I32, _P, _P, _P, C.c_double, _I32, _P, _P, _P, _P]),
     "kups_lj_ewald_real_forces_workspace_bytes": (C.c_size_t, [_I32, _I32]),

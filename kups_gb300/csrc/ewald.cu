@@ -807,6 +807,26 @@ extern "C" int32_t kups_ewald_recip(const double *positions, const double *charg
                       (cudaStream_t)stream_);
 }
 
+// Reciprocal energy from given structure factors (the energy step of the launch
+// sequence above; its scratch is the same workspace).
+extern "C" int32_t kups_ewald_recip_energy(const double *tril, const int32_t *kvec_n, int32_t n_kvecs,
+                                           const double *alpha, int32_t n_systems, double coulomb_k,
+                                           const double *structure_factor, double *energy, void *workspace,
+                                           size_t workspace_bytes, kups_status *status, void *stream_) {
+  cudaStream_t stream = (cudaStream_t)stream_;
+  if (n_systems < 0 || n_kvecs < 0) return KUPS_ERR_INVALID;
+  if (workspace_bytes < kups_ewald_recip_workspace_bytes(n_systems, n_kvecs)) return KUPS_ERR_INVALID;
+  if (n_systems == 0) return KUPS_OK;
+  char *base = (char *)(((uintptr_t)workspace + 255) & ~uintptr_t(255));
+  RecipSys *sysp = (RecipSys *)base;
+  Coef *coef = (Coef *)(base + align256(sizeof(RecipSys) * (size_t)n_systems));
+  recip_setup_kernel<<<n_systems, 256, 0, stream>>>(tril, kvec_n, n_systems, n_kvecs, sysp, status);
+  KUPS_CUDA_TRY(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)n_systems, stream));
+  recip_energy_kernel<<<dim3((unsigned)std::max(1, (n_kvecs + 31) / 32), n_systems), 32, 0, stream>>>(
+      kvec_n, n_kvecs, alpha, sysp, structure_factor, coulomb_k, coef, energy, nullptr);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------------------
 // kups_ewald_recip_static: the reciprocal-space computation above with its
 // scratch (per-system cell data, then per-(system, k) coefficients) in one

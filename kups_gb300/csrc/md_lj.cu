@@ -874,6 +874,34 @@ __device__ void save_record(const Smem &sm, const kups_md_args &a, const MdWork 
   }
 }
 
+// dE/dtril [xx, yx, yy, zx, zy, zz] of a system from block sums r[0..5] of the pair virial
+// W_cb = 1/2 sum d_c g_b (Cartesian, [xx, yx, yy, zx, zy, zz]) and r[6..11] of
+// sum_i f_i,a F_i,b over atoms (f fractional, wrapped; F the force), written by thread 0:
+// X_ab = sum_c (L^-1)_ca W_cb + sum_i f_i,a F_i,b.  Returns Tr W (every thread).
+__device__ double virial_from_sums(const SysParams &p, const double r[12], double *out) {
+  double W[3][3];
+  W[0][0] = r[0];
+  W[1][0] = W[0][1] = r[1];
+  W[1][1] = r[2];
+  W[2][0] = W[0][2] = r[3];
+  W[2][1] = W[1][2] = r[4];
+  W[2][2] = r[5];
+  const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
+  double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
+  Li[1][0] = -(B * Li[0][0]) / C;
+  Li[2][1] = -(E * Li[1][1]) / F;
+  Li[2][0] = -((D * Li[0][0]) + (E * Li[1][0])) / F;
+  const int ia[6] = {0, 1, 1, 2, 2, 2}, ib[6] = {0, 0, 1, 0, 1, 2};
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) {
+      double x = 0.0;
+      for (int c = 0; c < 3; ++c) x += Li[c][ia[k]] * W[c][ib[k]];
+      out[k] = x + r[6 + k];
+    }
+  }
+  return W[0][0] + W[1][1] + W[2][2];
+}
+
 template <int INTEGRATOR>
 __global__ void __launch_bounds__(kThreads, 1)
 md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
@@ -1007,9 +1035,10 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
       block_sums<1>(kv, sm, kt);
       csvr_alpha(sm, kt[0], a.seed, s, a.step0);
     }
+    const bool trace_v = INTEGRATOR != 3 && a.trace_virial != nullptr;
     for (int step = 0; step < a.n_steps && ok; ++step) {
       const bool last = step == a.n_steps - 1;
-      const bool want_e = last || a.trace_pe != nullptr || a.trace_ke != nullptr;
+      const bool want_e = last || a.trace_pe != nullptr || a.trace_ke != nullptr || trace_v;
       // ---- (CSVR) B A (O A)
       const float alpha = INTEGRATOR >= 2 ? sm.alpha : 1.0f;
       if (tid == 0) sm.work = 0;
@@ -1082,7 +1111,11 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) wv[k] = 0.f;
         forces_dispatch<false, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
-      } else if (last && a.virial != nullptr) {
+      } else if ((last && a.virial != nullptr) || trace_v) {
+        if (trace_v) {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) wv[k] = 0.f;
+        }
         forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
       } else if (want_e) {
         forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
@@ -1094,6 +1127,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
       // ---- B (and kinetic energy when recorded or needed by the thermostat)
       const bool need_ke = want_e || INTEGRATOR >= 2;
       float ke = 0.f;
+      float fwt[6] = {0, 0, 0, 0, 0, 0};  // sum_i f_i,a F_i,b (per-step virial record)
       for (int i = tid; i < n; i += nt) {
         float4 m = sm.mom[i];
         const float4 f = sm.frc[i];
@@ -1102,6 +1136,23 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
         m.z = fmaf(f.z, hdt, m.z);
         sm.mom[i] = m;
         if (need_ke) ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
+        if (INTEGRATOR != 3 && trace_v) {
+          float4 x = sm.pos[i];
+          float fr[3];
+          wrap_position(p, x, fr);
+          fwt[0] += fr[0] * f.x;
+          fwt[1] += fr[1] * f.x;
+          fwt[2] += fr[1] * f.y;
+          fwt[3] += fr[2] * f.x;
+          fwt[4] += fr[2] * f.y;
+          fwt[5] += fr[2] * f.z;
+        }
+      }
+      if (INTEGRATOR != 3 && trace_v) {
+        const float v[12] = {wv[0], wv[1], wv[2], wv[3], wv[4], wv[5], fwt[0], fwt[1], fwt[2], fwt[3], fwt[4], fwt[5]};
+        double r[12];
+        block_sums<12>(v, sm, r);
+        virial_from_sums(p, r, a.trace_virial + ((int64_t)step * a.n_systems + s) * 6);
       }
       double ke_tot = 0.0;
       double w6[6];
@@ -1241,36 +1292,15 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
       fw[5] += f[2] * F.z;
     }
     if (a.virial != nullptr) {
-      // X_ab = sum_c (L^-1)_{ca} W_cb ; W symmetric from wv = [xx, yx, yy, zx, zy, zz]
-      double W[3][3];
       const float v[12] = {wv[0], wv[1], wv[2], wv[3], wv[4], wv[5], fw[0], fw[1], fw[2], fw[3], fw[4], fw[5]};
       double r[12];
       block_sums<12>(v, sm, r);
-      const double *acc = r, *fwt = r + 6;
-      W[0][0] = acc[0];
-      W[1][0] = W[0][1] = acc[1];
-      W[1][1] = acc[2];
-      W[2][0] = W[0][2] = acc[3];
-      W[2][1] = W[1][2] = acc[4];
-      W[2][2] = acc[5];
-      const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
-      double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
-      Li[1][0] = -(B * Li[0][0]) / C;
-      Li[2][1] = -(E * Li[1][1]) / F;
-      Li[2][0] = -((D * Li[0][0]) + (E * Li[1][0])) / F;
-      const int ia[6] = {0, 1, 1, 2, 2, 2}, ib[6] = {0, 0, 1, 0, 1, 2};
-      if (tid == 0) {
-        for (int k = 0; k < 6; ++k) {
-          double x = 0.0;
-          for (int c = 0; c < 3; ++c) x += Li[c][ia[k]] * W[c][ib[k]];
-          a.virial[6 * (int64_t)s + k] = x + fwt[k];
-        }
-        if (a.pressure != nullptr) {
-          // sum_i dU/dr_i (x) r_i + h^T dU/dh = sum over pairs of d (x) dU/dd = W for a pair
-          // potential: P = (2 K - Tr W) / 3V
-          const double vol = fabs(A * C * F);
-          a.pressure[s] = (2.0 * a.kinetic[s] - (W[0][0] + W[1][1] + W[2][2])) / (3.0 * vol);
-        }
+      const double trw = virial_from_sums(p, r, a.virial + 6 * (int64_t)s);
+      if (tid == 0 && a.pressure != nullptr) {
+        // sum_i dU/dr_i (x) r_i + h^T dU/dh = sum over pairs of d (x) dU/dd = W for a pair
+        // potential: P = (2 K - Tr W) / 3V
+        const double vol = fabs(p.Ld[0] * p.Ld[2] * p.Ld[5]);
+        a.pressure[s] = (2.0 * a.kinetic[s] - trw) / (3.0 * vol);
       }
     }
     if (INTEGRATOR == 3 && tid == 0)
@@ -1320,6 +1350,7 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
                              a->compressibility == nullptr || a->min_scale == nullptr ||
                              a->cell == nullptr))
     return KUPS_ERR_INVALID;
+  if (a->integrator == 3 && a->trace_virial != nullptr) return KUPS_ERR_INVALID;
   if (ws_bytes < kups_lj_md_workspace_bytes(a)) return KUPS_ERR_INVALID;
   if (a->n_systems == 0) return KUPS_OK;
   int dev = 0, sms = 0;

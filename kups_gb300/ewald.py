@@ -180,6 +180,23 @@ def ewald_recip(positions, charges, sys_offset, max_atoms, tril, kvec_n, alpha, 
     return energy, grad, gtril, sk, status
 
 
+def ewald_recip_energy(tril, kvec_n, alpha, structure_factor, ws=None, status=None):
+    """K sum_k P(k) |S(k)|^2 per system from given structure factors (kups_ewald_recip_energy)."""
+    lib = _lib.load()
+    tril, al, sk = _f64(tril), _f64(alpha), _f64(structure_factor)
+    kn = _i32(kvec_n)
+    s, nk = tril.shape[0], kn.shape[1]
+    energy = torch.empty(s, dtype=torch.float64, device="cuda")
+    nbytes = lib.kups_ewald_recip_workspace_bytes(s, nk)
+    buf = (ws or RecipWorkspace()).get(nbytes)
+    status = status if status is not None else new_status()
+    rc = lib.kups_ewald_recip_energy(tril.data_ptr(), kn.data_ptr(), nk, al.data_ptr(), s, TO_STANDARD_UNITS,
+                                     sk.data_ptr(), energy.data_ptr(), buf.data_ptr(), buf.numel(), status.data_ptr(),
+                                     _stream())
+    _lib.check(rc, "kups_ewald_recip_energy")
+    return energy
+
+
 def ewald_self(charges, sys_offset, alpha, n_systems):
     lib = _lib.load()
     q, al, off = _f64(charges), _f64(alpha), _i32(sys_offset)
@@ -224,8 +241,27 @@ class EwaldParticles:
     exclusion: torch.Tensor | None = None
 
 
+@dataclass
+class LJEwaldCache:
+    """What a patched call starts from: the total energies and the structure factors S(k) of the
+    current state (``EwaldCache``, src/kups/potential/classical/ewald.py:86-120)."""
+
+    total_energies: torch.Tensor  # [S]
+    structure_factor: torch.Tensor  # [S, n_k, 2]
+
+
 class LJEwaldPotential:
-    """E = LJ (optional) + Ewald (short range + long range + self - excluded vacuum Coulomb)."""
+    """E = LJ (optional) + Ewald (short range + long range + self - excluded vacuum Coulomb).
+
+    With a ``patch`` (particles moved to new positions) the energies after the patch come from
+    the cache of the current state: the real-space terms of the removed and added edges of
+    ``neighborlist_changes`` (``LocalGraphSumComposer``, src/kups/potential/common/graph.py:419-453),
+    the intramolecular correction at the old and new positions, and the long-range energy of
+    S(k) + delta S(k) with delta S(k) the moved particles' old copies (charge -q) and new
+    positions (+q) (``_structure_factor_update``, ewald.py:442-486; ``EwaldLongRangeComposer``,
+    :604-657); no gradients.  The returned cache holds the patched energies and S(k), to be
+    kept if the move is accepted.
+    """
 
     def __init__(self, ewald: EwaldParameters, lj_sigma=None, lj_epsilon=None, lj_cutoff=None,
                  neighborlist: CellListNeighborList | None = None, exclusion_edges=None):
@@ -235,7 +271,7 @@ class LJEwaldPotential:
         self.exclusion_edges = exclusion_edges  # (edges [E,2], shifts [E,3]) intramolecular pairs
         self.ws = RecipWorkspace()
 
-    def __call__(self, particles: EwaldParticles, tril, patch=None) -> PotentialOut:
+    def __call__(self, particles: EwaldParticles, tril, patch=None, cache: LJEwaldCache | None = None) -> PotentialOut:
         tril = _f64(tril)
         s = tril.shape[0]
         alpha, rc_ew = _f64(self.ewald.alpha), _f64(self.ewald.cutoff)
@@ -247,13 +283,16 @@ class LJEwaldPotential:
             rc_lj = rc_lj.reshape(-1).expand(s).contiguous()
             rc_nl = torch.maximum(rc_nl, rc_lj)
             terms |= TERM_LJ
+        if patch is not None:
+            return self._patched(particles, tril, patch, cache, terms, sig, eps, rc_lj, alpha, rc_ew, rc_nl)
         pts = NeighborListPoints(particles.positions, particles.system, None, particles.exclusion)
         e, self.neighborlist = self.neighborlist.call_and_fix(pts, None, tril, rc_nl)
         en, g, gt = pair_edges(particles.positions, particles.system, particles.species, particles.charges, tril,
                                e.indices, e.shifts.view(-1, 3), e.n_edges, terms, sig, eps, rc_lj, alpha, rc_ew)
         off, mx = _offsets(_i32(particles.system), s)
-        el, gl, gtl, _, _ = ewald_recip(particles.positions, particles.charges, off, mx, tril,
-                                        self.ewald.reciprocal_lattice_shifts, alpha, ws=self.ws)
+        self._last_recip = ewald_recip(particles.positions, particles.charges, off, mx, tril,
+                                       self.ewald.reciprocal_lattice_shifts, alpha, ws=self.ws)
+        el, gl, gtl, _, _ = self._last_recip
         es = ewald_self(particles.charges, off, alpha, s)
         energy, grad, gtril = en + el + es, g + gl, gt + gtl
         if self.exclusion_edges is not None:
@@ -262,7 +301,47 @@ class LJEwaldPotential:
                                      xe.shape[0], TERM_EWALD_REAL | TERM_VACUUM, alpha=alpha,
                                      ewald_cutoff=torch.full_like(rc_ew, float("inf")))
             energy, grad, gtril = energy + ex, grad + gx, gtril + gtx
-        return PotentialOut(energy, PositionAndUnitCell(grad, gtril))
+        _, _, _, sk, _ = self._last_recip
+        return PotentialOut(energy, PositionAndUnitCell(grad, gtril), cache=LJEwaldCache(energy, sk))
+
+    def _patched(self, particles, tril, patch, cache, terms, sig, eps, rc_lj, alpha, rc_ew, rc_nl) -> PotentialOut:
+        from .potential import changed_edges, patched_positions
+
+        if cache is None:
+            cache = self(particles, tril).cache
+        s = tril.shape[0]
+        added, removed = changed_edges(self.neighborlist, particles.positions, particles.system, None,
+                                       particles.exclusion, tril, rc_nl, patch)
+        old = _f64(particles.positions)
+        new = patched_positions(old, patch)
+        pe = lambda pos, e: pair_edges(pos, particles.system, particles.species, particles.charges, tril, e.indices,
+                                       e.shifts.view(-1, 3), e.n_edges, terms, sig, eps, rc_lj, alpha, rc_ew,
+                                       grad_tril=False)[0]
+        de = pe(new, added) - pe(old, removed)
+        if self.exclusion_edges is not None:
+            xe, xs = self.exclusion_edges
+            inf = torch.full_like(rc_ew, float("inf"))
+            ex = lambda pos: pair_edges(pos, particles.system, None, particles.charges, tril, xe, xs, xe.shape[0],
+                                        TERM_EWALD_REAL | TERM_VACUUM, alpha=alpha, ewald_cutoff=inf,
+                                        grad_tril=False)[0]
+            de = de + ex(new) - ex(old)
+        # S(k) change: the moved particles' old copies with -q and new positions with +q, by system
+        idx = _i32(patch.indices).long()
+        q = _f64(particles.charges)[idx]
+        sysm = _i32(particles.system)[idx]
+        both_sys = torch.cat([sysm, sysm])
+        order = torch.argsort(both_sys, stable=True)
+        pos_m = torch.cat([old[idx], new[idx]])[order].contiguous()
+        q_m = torch.cat([-q, q])[order].contiguous()
+        off_m, mx = _offsets(both_sys[order], s)
+        _, _, _, dsk, _ = ewald_recip(pos_m, q_m, off_m, mx, tril, self.ewald.reciprocal_lattice_shifts, alpha,
+                                      grad_tril=False, ws=self.ws)
+        sk_new = cache.structure_factor + dsk
+        kn = self.ewald.reciprocal_lattice_shifts
+        de = de + ewald_recip_energy(tril, kn, alpha, sk_new, ws=self.ws) - ewald_recip_energy(
+            tril, kn, alpha, cache.structure_factor, ws=self.ws)
+        e_new = cache.total_energies + de
+        return PotentialOut(e_new, None, None, cache=LJEwaldCache(e_new, sk_new))
 
 
 # ----------------------------------------------------------------------------- MD

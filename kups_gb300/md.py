@@ -240,7 +240,7 @@ class FusedLennardJonesMD:
         return int(math.ceil(est / 16.0) * 16)
 
     def args(self, packed: PackedMD, n_steps: int, seed: int, step0: int, trace_pe=None, trace_ke=None,
-             virial: bool = True) -> _lib.MdArgs:
+             virial: bool = True, trace_virial=None) -> _lib.MdArgs:
         s = packed.n_systems
         if packed.energy is None:
             packed.energy = torch.zeros(s, device="cuda", dtype=torch.float64)
@@ -257,6 +257,7 @@ class FusedLennardJonesMD:
         a.pressure = packed.pressure.data_ptr() if virial and packed.pressure is not None else None
         a.trace_pe = trace_pe.data_ptr() if trace_pe is not None else None
         a.trace_ke = trace_ke.data_ptr() if trace_ke is not None else None
+        a.trace_virial = trace_virial.data_ptr() if trace_virial is not None else None
         a.rebuilds = packed.rebuilds.data_ptr() if packed.rebuilds is not None else None
         a.profile = packed.profile.data_ptr() if packed.profile is not None else None
         a.n_atoms, a.n_systems, a.n_species = packed.n_atoms, s, packed.n_species
@@ -290,9 +291,11 @@ class FusedLennardJonesMD:
         return self._ws
 
     def launch(self, packed: PackedMD, n_steps: int, seed: int = 0, step0: int = 0, status=None, trace_pe=None,
-               trace_ke=None, virial: bool = True) -> torch.Tensor:
-        """Enqueue one persistent launch (no host synchronisation)."""
-        a = self.args(packed, n_steps, seed, step0, trace_pe, trace_ke, virial)
+               trace_ke=None, virial: bool = True, trace_virial=None) -> torch.Tensor:
+        """Enqueue one persistent launch (no host synchronisation).  trace_pe / trace_ke
+        [n_steps, S] and trace_virial [n_steps, S, 6] (float64, optional) receive the potential
+        energy, kinetic energy and dE/dtril after every step."""
+        a = self.args(packed, n_steps, seed, step0, trace_pe, trace_ke, virial, trace_virial)
         ws = self.workspace(a)
         status = status if status is not None else new_status()
         rc = _lib.load().kups_lj_md_run(C.byref(a), ws.data_ptr(), ws.numel(), status.data_ptr(), _stream())

@@ -30,6 +30,37 @@ class PotentialOut:
     total_energies: torch.Tensor  # [S]
     gradients: Any = None
     hessians: Any = None
+    cache: Any = None  # what a later patched call starts from (``CachedPotential``'s cached value)
+
+
+@dataclass
+class ParticlePatch:
+    """Particles ``indices`` take ``positions`` (the ``ParticlePositionChanges`` a Monte Carlo move
+    proposes, src/kups/mcmc/moves.py:222-295; applied as a patch, src/kups/core/patch.py:37-49)."""
+
+    indices: torch.Tensor  # int [k], distinct
+    positions: torch.Tensor  # f64 [k, 3]
+
+
+def patched_positions(positions: torch.Tensor, patch: ParticlePatch) -> torch.Tensor:
+    new = _f64(positions).clone()
+    new[_i32(patch.indices).long()] = _f64(patch.positions)
+    return new
+
+
+def changed_edges(neighborlist, positions, system, inclusion, exclusion, tril, cutoffs, patch: ParticlePatch):
+    """(added, removed) edges of the patch (``neighborlist_changes``), the changed particles
+    keeping their system, inclusion and exclusion labels."""
+    from .neighborlist import neighborlist_changes
+
+    idx = _i32(patch.indices).long()
+    sysi = _i32(system)
+    incl = _i32(inclusion) if inclusion is not None else sysi
+    excl = _i32(exclusion) if exclusion is not None else torch.arange(sysi.shape[0], device="cuda",
+                                                                      dtype=torch.int32)
+    lh = NeighborListPoints(_f64(positions), sysi, incl, excl)
+    rh = NeighborListPoints(_f64(patch.positions), sysi[idx], incl[idx], excl[idx])
+    return neighborlist_changes(neighborlist, lh, patch.indices, rh, tril, cutoffs)
 
 
 @dataclass
@@ -80,18 +111,34 @@ class LennardJonesPotential:
         self.neighborlist = neighborlist or CellListNeighborList()
         self.pair_fp32 = pair_fp32
 
-    def __call__(self, state: LJState, patch=None) -> PotentialOut:
-        if patch is not None:
-            raise NotImplementedError("incremental LJ updates are served by the Monte Carlo kernels")
+    def __call__(self, state: LJState, patch: ParticlePatch | None = None, cache=None) -> PotentialOut:
+        """Energies and gradients of ``state``; with ``patch``, the energies of ``state`` after the
+        patch, E_cached - E(removed edges, old positions) + E(added edges, new positions)
+        (``LocalGraphSumComposer``, src/kups/potential/common/graph.py:419-453, over the edges of
+        ``neighborlist_changes``), no gradients.  ``cache`` is the ``cache`` of the
+        PotentialOut of ``state`` (computed here when not given)."""
         p = state.particles
         tril = _f64(as_tril(state.systems))
         s = tril.shape[0]
         prm = state.parameters
         cut = _f64(prm.cutoff.reshape(-1).expand(s))
+        if patch is not None:
+            e_old = cache if cache is not None else self(state).cache
+            added, removed = changed_edges(self.neighborlist, p.positions, p.system, p.inclusion, p.exclusion, tril,
+                                           cut, patch)
+            new_pos = patched_positions(p.positions, patch)
+            e_rm = lj_from_edges(p.positions, p.system, p.species, tril, prm.sigma, prm.epsilon, cut, removed.indices,
+                                 removed.shifts, removed.n_edges, self.pair_fp32).total_energies
+            e_add = lj_from_edges(new_pos, p.system, p.species, tril, prm.sigma, prm.epsilon, cut, added.indices,
+                                  added.shifts, added.n_edges, self.pair_fp32).total_energies
+            e_new = e_old - e_rm + e_add
+            return PotentialOut(e_new, None, None, cache=e_new)
         pts = NeighborListPoints(p.positions, p.system, p.inclusion, p.exclusion)
         edges, self.neighborlist = self.neighborlist.call_and_fix(pts, None, tril, cut)
-        return lj_from_edges(p.positions, p.system, p.species, tril, prm.sigma, prm.epsilon, cut, edges.indices,
-                             edges.shifts, edges.n_edges, self.pair_fp32)
+        out = lj_from_edges(p.positions, p.system, p.species, tril, prm.sigma, prm.epsilon, cut, edges.indices,
+                            edges.shifts, edges.n_edges, self.pair_fp32)
+        out.cache = out.total_energies
+        return out
 
 
 def lj_from_edges(positions, system, species, tril, sigma, epsilon, cutoffs, edges, shifts, n_edges,

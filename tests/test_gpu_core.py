@@ -391,3 +391,26 @@ def test_fused_md_rebuilds_when_the_input_changed():
     packed.rebuilds.zero_()
     prop.run_packed(packed, 5, seed=1, step0=10)
     assert int(packed.rebuilds.cpu().numpy().min()) >= 1
+
+
+def test_fused_md_per_step_virial_trace():
+    """trace_virial holds dE/dtril after every step: its last row is the launch's virial bit for
+    bit, and every row matches the float64 oracle at that step's positions (1e-4 relative)."""
+    from kups_gb300 import md
+
+    W = small_batch()
+    prop = md.make_velocity_verlet_step()
+    packed = md.pack(md_state(W))
+    S = W.n_systems
+    rows = []
+    for k in range(3):
+        tv = torch.zeros((2, S, 6), dtype=torch.float64, device="cuda")
+        st = prop.launch(packed, 2, seed=1, step0=2 * k, trace_virial=tv)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(tv[-1].cpu().numpy(), packed.virial.cpu().numpy())
+        pos = np.empty((packed.n_atoms, 3))
+        pos[packed.perm.cpu().numpy()] = packed.pos4.cpu().numpy()[:, :3]
+        _, _, dt = oracle_forces(W, pos)
+        np.testing.assert_allclose(tv[-1].cpu().numpy(), dt, rtol=1e-4, atol=1e-4 * np.abs(dt).max())
+        rows.append(tv[0].cpu().numpy())
+    assert all(np.isfinite(r).all() for r in rows)

@@ -304,3 +304,62 @@ def test_vv_energy_conservation_and_reversibility():
     d = uc.wrap(pos2 - pos, tril[0])
     assert np.allclose(d, 0, atol=1e-6)
     assert np.allclose(p2, -p, rtol=1e-4, atol=1e-8)
+
+
+# ----------------------------------------------------------------------------- rh subsets and changes
+def _sep_calls(pos, batch, changed, new, tril, rc):
+    from oracle import neighborlist as onl
+
+    after = pos.copy()
+    after[changed] = new
+    z = np.zeros(len(changed), int)
+    a = onl.neighbor_list_rh(after, batch, new, batch[changed] * 0 + z, tril, rc, rh_exclusion=changed,
+                             rh_index_remap=changed)
+    r = onl.neighbor_list_rh(pos, batch, pos[changed], z, tril, rc, rh_exclusion=changed, rh_index_remap=changed)
+    return a, r
+
+
+def _edge_pairs(edges):
+    return {(int(i), int(j)) for i, j in edges[0]}
+
+
+def test_neighborlist_changes_single_particle_known_answer():
+    """test/core/test_neighborlist.py:1607-1640: particle 1 moves from next to 0 to next to 2."""
+    from oracle import neighborlist as onl
+
+    pos = np.array([[0.0, 0, 0], [1.0, 0, 0], [5.0, 0, 0]])
+    tril = np.array([[10.0, 0, 10.0, 0, 0, 10.0]])
+    added, removed = onl.neighborlist_changes(pos, np.zeros(3, int), [1], [[4.5, 0, 0]], tril, [1.5])
+    assert {(0, 1), (1, 0)} <= _edge_pairs(removed) and (1, 2) not in _edge_pairs(removed)
+    assert {(1, 2), (2, 1)} <= _edge_pairs(added) and (0, 1) not in _edge_pairs(added)
+
+
+def test_neighborlist_changes_multi_system_known_answer():
+    """test/core/test_neighborlist.py:1642-1670: no edges across systems."""
+    from oracle import neighborlist as onl
+
+    pos = np.array([[0.0, 0, 0], [5.0, 0, 0], [0.0, 0, 0], [5.0, 0, 0]])
+    tril = np.array([[10.0, 0, 10.0, 0, 0, 10.0]] * 2)
+    added, _ = onl.neighborlist_changes(pos, np.array([0, 0, 1, 1]), [1], [[0.5, 0, 0]], tril, [1.5, 1.5])
+    assert {(0, 1), (1, 0)} <= _edge_pairs(added)
+    assert (1, 2) not in _edge_pairs(added) and (2, 1) not in _edge_pairs(added)
+
+
+@pytest.mark.parametrize("n,m,seed,rc", [(10, 3, 42, 3.0), (30, 5, 123, 3.0), (40, 6, 7, 6.0)])
+def test_neighborlist_changes_match_separate_calls(n, m, seed, rc):
+    """test/core/test_neighborlist.py:1553-1605, 1702-1750: the combined call's added / removed
+    edges (with shifts) equal the two separate rh calls after and before the change; rc 6 in a
+    10 A box needs periodic images."""
+    from oracle import neighborlist as onl
+
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(0, 9, (n, 3))
+    changed = rng.choice(n, m, replace=False)
+    new = rng.uniform(0, 9, (m, 3))
+    tril = np.array([[10.0, 0, 10.0, 0, 0, 10.0]])
+    batch = np.zeros(n, int)
+    added, removed = onl.neighborlist_changes(pos, batch, changed, new, tril, [rc])
+    a, r = _sep_calls(pos, batch, changed, new, tril, [rc])
+    for got, exp in ((added, a), (removed, r)):
+        np.testing.assert_array_equal(got[0], exp[0])
+        np.testing.assert_array_equal(got[1], exp[1])
