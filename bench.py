@@ -986,7 +986,127 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- profiling subcommands
+# ``python bench.py --profile <what> [numbers...]`` runs one kernel's workload in the shape an ncu
+# capture targets (the commands in profiles/*.md); nothing here is part of the JSON line.
+MD_PHASES = ["setup+first build", "integrate", "list/ghosts", "forces", "kick+reduce", "write-back",
+             "build:atoms", "build:ghosts", "thermostat/barostat", "build:list"]
+
+
+def _events_ms(torch, fn):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def profile_md(n_sys=4096, equil=1000, steps=20, integrator="baoab"):
+    """Fused MD on the batched workload: `equil` steps in four launches with the kernel's
+    clock64 phase counters (ms/step, list builds per system, share of time per phase), then
+    one launch of `steps` steps without counters (the launch `-s 4 -c 1` captures).
+    integrator: baoab, velocity_verlet, csvr or csvr_npt (tau_T 100 fs, P0 1 bar, tau_P 1 ps,
+    beta 2e-4 / bar)."""
+    import torch
+
+    from kups_gb300 import md
+    from kups_gb300.units import FEMTO_SECOND
+
+    n_sys, equil, steps = int(n_sys), int(equil), int(steps)
+    W = workload(n_sys, 1)
+    prop = md.FusedLennardJonesMD(integrator)
+    state = state_from_workload(W, torch)
+    if integrator in ("csvr", "csvr_npt"):
+        bar = 6.241509074e-7  # eV / A^3
+        full = lambda v: torch.full((n_sys,), float(v), dtype=torch.float64, device="cuda")
+        state.systems.thermostat_time_constant = full(100 * FEMTO_SECOND)
+        state.systems.target_pressure = full(bar)
+        state.systems.pressure_coupling_time = full(1000 * FEMTO_SECOND)
+        state.systems.compressibility = full(2e-4 / bar)
+        state.systems.minimum_scale_factor = full(0.99)
+    packed = md.pack(state)
+    packed.rebuilds = torch.zeros(n_sys, device="cuda", dtype=torch.int32)
+    packed.profile = torch.zeros(10, device="cuda", dtype=torch.int64)
+    step0 = 0
+    for chunk in [equil // 4] * 4:
+        packed.rebuilds.zero_()
+        packed.profile.zero_()
+        ms = _events_ms(torch, lambda: prop.run_packed(packed, chunk, seed=1, step0=step0))
+        step0 += chunk
+        pr = packed.profile.cpu().double()
+        pr /= pr[:6].sum() + pr[8]
+        rb = packed.rebuilds.double()
+        print(f"{chunk} steps: {ms / chunk:.3f} ms/step, list builds per system {rb.mean():.2f} "
+              f"(max {rb.max():.0f}); " + " ".join(f"{n}={v:.3f}" for n, v in zip(MD_PHASES, pr.tolist())),
+              flush=True)
+    packed.profile = None
+    ms = _events_ms(torch, lambda: prop.run_packed(packed, steps, seed=1, step0=step0))
+    print(f"profiled launch: {steps} steps, {ms / steps:.3f} ms/step")
+
+
+def profile_gcmc(replicas=1024, equil=3000, steps=40):
+    """Plain GCMC of CO2 in the 2x2x1-replicated porous host: one launch of `equil` steps, then
+    one launch of `steps` steps (the launch `-k regex:gcmc_kernel -s 1 -c 1` captures)."""
+    import torch
+
+    from kups_gb300 import gcmc as g
+    from kups_gb300 import workloads
+
+    replicas, equil, steps = int(replicas), int(equil), int(steps)
+    mc = g.GCMC(workloads.gcmc_co2_framework(n_replicas=replicas), seed=1)
+    mc.launch(equil)
+    ms = _events_ms(torch, lambda: mc.launch(steps))
+    mc.check()
+    print(f"gcmc: {replicas} replicas, loading {mc.n_mol.float().mean().item():.2f}, {ms / steps * 1e3:.1f} us/step")
+
+
+def profile_mlp(train_steps=20):
+    """Learned-proposal network: `train_steps` training steps (batch 16384) on seeded points,
+    then five 64^3 grid refreshes (forward of 262144 nodes, normaliser, CDF) and 200 training
+    steps, each timed with CUDA events."""
+    import torch
+
+    from kups_gb300.mlp import LearnedInsertionProposal
+
+    net = LearnedInsertionProposal(seed=0, grid=64)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    data = torch.rand(200000, 3, dtype=torch.float64, device="cuda", generator=gen) * 0.3
+    net.train(data, steps=int(train_steps), batch=16384)
+    net.build_grid()
+    torch.cuda.synchronize()
+    flop_node = 2 * (64 * 256 + 2 * 256 * 256 + 256)
+    ms = _events_ms(torch, lambda: [net.build_grid() for _ in range(5)]) / 5
+    print(f"grid refresh: {ms:.3f} ms, {flop_node * 64**3 / ms / 1e9:.1f} TFLOP/s")
+    ms = _events_ms(torch, lambda: net.train(data, steps=200, batch=16384)) / 200
+    print(f"train step (batch 16384): {ms:.3f} ms, {3 * flop_node * 16384 / ms / 1e9:.1f} TFLOP/s")
+
+
+def profile_ewald(steps=50):
+    """LJ + Ewald NVE of the ionic melt: 20 steps (graph capture and warm-up), then `steps`
+    graph replays (the real-space launch `-k regex:real_packed_kernel -s 30 -c 1` captures)."""
+    import torch
+
+    from kups_gb300 import workloads
+
+    W = workloads.ionic_melt()
+    sim = _melt_sim(W, torch)
+    sim.start(torch.as_tensor(W.momenta).cuda())
+    sim.run(20)
+    torch.cuda.synchronize()
+    ms = _events_ms(torch, lambda: sim.run(int(steps)))
+    sim.check()
+    print(f"{steps} steps: {ms / int(steps):.4f} ms/step, {len(W.charges)} ions, {W.kvec_n.shape[1]} k vectors")
+
+
+PROFILES = {"md": profile_md, "gcmc": profile_gcmc, "mlp": profile_mlp, "ewald": profile_ewald}
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--profile":
+        what = sys.argv[2]
+        PROFILES[what](*sys.argv[3:])
+        return
     a = parse()
     if a.impl == "reference":
         run_reference(a)

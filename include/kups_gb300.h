@@ -10,8 +10,12 @@
  *     and never synchronises the device; every call except
  *     kups_ewald_recip_static is safe to capture in a CUDA graph (it issues
  *     only kernel launches and cudaMemsetAsync);
+ *   - a workspace holds nothing a later call needs, except the fused MD's
+ *     (kups_lj_md_run), whose per-system records let the next call on the
+ *     same workspace resume its Verlet lists (kups_md_args.reuse_lists);
  *   - the return value reports host-side validation and launch errors
- *     (KUPS_OK, KUPS_ERR_INVALID, KUPS_ERR_CUDA); device-side conditions
+ *     (KUPS_OK, KUPS_ERR_INVALID, KUPS_ERR_CUDA; kups_ewald_recip_static also
+ *     returns KUPS_ERR_CAPACITY and KUPS_ERR_UNSUPPORTED, see there); device-side conditions
  *     (capacity overflow, non-finite input) are written to the caller's
  *     device `kups_status`, which the caller reads back with its outputs.
  *     Kernels never trap and never write past a capacity: on overflow they
@@ -129,6 +133,31 @@ int32_t kups_neighborlist_split_changes(const int32_t *edges, const int32_t *shi
                                         int64_t *n_added, int32_t *removed_edges, int32_t *removed_shifts,
                                         int64_t removed_capacity, int64_t *n_removed, void *workspace,
                                         size_t workspace_bytes, kups_status *status, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Edge-set kernels of the local machine-learned potential (message passing
+ * over the neighbour list; local_mliap_energy_full, src/kups/potential/mliap/
+ * local.py:310-356).  Directed edges (i, j, s) as the neighbour list writes
+ * them; rows past n_edges or with an index outside [0, n) are padding.
+ *   kups_edge_vectors     d_e = x_j - x_i + s @ L (Edges.difference_vectors,
+ *                         src/kups/core/neighborlist.py:164-184), float64 [E, 3]
+ *                         (zero for padding rows)
+ *   kups_edge_segment_sum out[i, :] = sum over edges with first index i of
+ *                         values[e, :] (jax.ops.segment_sum), float64 [N, width],
+ *                         written
+ *   kups_edge_gradients   from g_e = dE/dd_e: dE/dx_j += g_e, dE/dx_i -= g_e and
+ *                         dE/dL_ab += s_a g_b (Cartesian positions held fixed,
+ *                         tril order), grad [N, 3] and grad_tril [S, 6] (may be
+ *                         NULL) written
+ * ------------------------------------------------------------------------ */
+int32_t kups_edge_vectors(const double *positions, const int32_t *system, int64_t n, const double *tril,
+                          int32_t n_systems, const int32_t *edges, const int32_t *shifts, int64_t n_edges,
+                          double *d, void *stream);
+int32_t kups_edge_segment_sum(const double *values, int32_t width, const int32_t *edges, int64_t n_edges,
+                              int64_t n, double *out, void *stream);
+int32_t kups_edge_gradients(const double *dE_dd, const int32_t *system, int64_t n, int32_t n_systems,
+                            const int32_t *edges, const int32_t *shifts, int64_t n_edges, double *grad,
+                            double *grad_tril, void *stream);
 
 /* ------------------------------------------------------------------------
  * Lennard-Jones over an edge list — replaces lennard_jones_energy
@@ -329,10 +358,20 @@ int32_t kups_ewald_recip_energy(const double *tril, const int32_t *kvec_n, int32
  *     the array are refused with KUPS_ERR_CAPACITY before anything is
  *     launched (16 MiB holds, e.g., 512 systems x 1000 k vectors).
  *   - The first call on each device looks up the array's address with that
- *     device current; make that first call before any stream capture.
+ *     device current; make that first call before any stream capture.  The
+ *     address is kept per device for the life of the process: after a
+ *     cudaDeviceReset the library must not be called on that device again.
  *   - The array is shared by all calls on a device and keeps the last call's
  *     contents; nothing in it needs to start at zero.  Calls that overlap in
  *     time (other streams or host threads) race on it: order them.
+ *   - The array belongs to the library's Ewald module: every device on which
+ *     any of this module's entry points runs (kups_ewald_recip, _static,
+ *     _energy, kups_ewald_self, kups_pair_edges, kups_lj_ewald_real_forces*)
+ *     holds its 16 MiB until the process exits.
+ *   - Host-side returns, beyond the general KUPS_OK / KUPS_ERR_INVALID /
+ *     KUPS_ERR_CUDA: KUPS_ERR_CAPACITY when the sizes need more than the
+ *     array (nothing launched), KUPS_ERR_UNSUPPORTED for a device ordinal of
+ *     64 or more.
  */
 #define KUPS_EWALD_RECIP_STATIC_SCRATCH_BYTES ((size_t)16 << 20)
 int32_t kups_ewald_recip_static(const double *positions, const double *charges,
@@ -467,6 +506,11 @@ int32_t kups_md_drift(double *positions, const double *momenta, const double *ma
 int32_t kups_md_thermostat(double *momenta, const double *masses, const int32_t *system,
                            const double *dt, const double *kT, const double *friction,
                            uint64_t seed, uint64_t step, int64_t n_particles, void *stream);
+/* kups_md_thermostat with the step (the noise counter) read from device memory when the
+ * kernel runs: a captured CUDA graph that also advances *step replays successive steps. */
+int32_t kups_md_thermostat_counted(double *momenta, const double *masses, const int32_t *system,
+                                   const double *dt, const double *kT, const double *friction,
+                                   uint64_t seed, const uint64_t *step, int64_t n_particles, void *stream);
 
 /* ------------------------------------------------------------------------
  * Virial observables per system — replaces stress_via_virial_theorem,
@@ -613,6 +657,9 @@ typedef struct kups_gcmc_args {
                                    centre (atom mean) from the grid density q and add
                                    -ln(V q) to ln acc, deletions add +ln(V q) */
   kups_gcmc_trace *trace;       /* [n_steps, S] or NULL: per-step record of every system */
+  int32_t block_threads;        /* threads per system's CTA: 64, 128 or 256 (0: 128); the
+                                   launch-shape autotuner picks one per workload */
+  int32_t pad1;
 } kups_gcmc_args;
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);

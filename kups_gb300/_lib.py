@@ -72,7 +72,7 @@ class GcmcArgs(C.Structure):
         ("move_cum", C.c_float * 3), ("pad0", C.c_float), ("coulomb_k", C.c_double), ("seed", C.c_uint64),
         ("step0", C.c_uint64), ("n_systems", C.c_int32), ("max_mol", C.c_int32), ("atoms_per_mol", C.c_int32),
         ("n_species", C.c_int32), ("n_kvecs", C.c_int32), ("n_steps", C.c_int32), ("history_len", C.c_int32),
-        ("proposal_grid", C.c_int32), ("trace", C.c_void_p),
+        ("proposal_grid", C.c_int32), ("trace", C.c_void_p), ("block_threads", C.c_int32), ("pad1", C.c_int32),
     ]
 
 
@@ -100,6 +100,9 @@ SIGNATURES = {
     "kups_neighborlist_split_workspace_bytes": (_SZ, [_I64, _I64]),
     "kups_neighborlist_split_changes": (_I32, [_P, _P, _P, _I64, _I64, _P, _I64, _P, _P, _I64, _P, _P, _P, _I64, _P,
                                                _P, _SZ, _P, _P]),
+    "kups_edge_vectors": (_I32, [_P, _P, _I64, _P, _I32, _P, _P, _I64, _P, _P]),
+    "kups_edge_segment_sum": (_I32, [_P, _I32, _P, _I64, _I64, _P, _P]),
+    "kups_edge_gradients": (_I32, [_P, _P, _I64, _I32, _P, _P, _I64, _P, _P, _P]),
     "kups_lj_edges": (_I32, [_P, _P, _P, _I64, _P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _I32, _P, _P]),
     "kups_lj_md_workspace_bytes": (_SZ, [C.POINTER(MdArgs)]),
     "kups_lj_md_run": (_I32, [C.POINTER(MdArgs), _P, _SZ, _P, _P]),
@@ -117,6 +120,7 @@ SIGNATURES = {
     "kups_md_kick": (_I32, [_P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_drift": (_I32, [_P, _P, _P, _P, _P, _P, C.c_double, _I64, _P]),
     "kups_md_thermostat": (_I32, [_P, _P, _P, _P, _P, _P, C.c_uint64, C.c_uint64, _I64, _P]),
+    "kups_md_thermostat_counted": (_I32, [_P, _P, _P, _P, _P, _P, C.c_uint64, _P, _I64, _P]),
     "kups_virial_stress_workspace_bytes": (C.c_size_t, [_I32, _I32]),
     "kups_virial_stress": (_I32, [_P, _P, _P, _I64, _P, _P, _I32, _P, _I32, _P, _P, _P, _P, _P, _P, _P, _P,
                                   C.c_size_t, _P, _P]),

@@ -99,3 +99,47 @@ def autotune_md(prop, packed, steps: int = 40, cache_file: str | None = None,
         with open(cache_file, "w") as f:
             json.dump(_CACHE, f, indent=1)
     return TunedShape(best[1][0], best[1][1], best[0], table)
+
+
+GCMC_THREADS = (64, 128, 256)
+
+
+def autotune_gcmc(mc, steps: int = 200, candidates=GCMC_THREADS) -> TunedShape:
+    """Threads per system's CTA of the GCMC kernel (64, 128 or 256: more threads share a
+    system's host-atom and k-vector loops, fewer fit more systems per SM), each timed for
+    `steps` steps on a clone of the sampler's state (``GCMC.clone``: `mc` itself does not
+    advance), after one untimed launch of the same length; the fastest is set on `mc` and
+    cached per workload signature (systems, host atoms, k vectors, molecules, proposal)."""
+    st = mc.setup
+    key = json.dumps({"kernel": "gcmc", "systems": int(st.n_systems), "host_atoms": int(max(st.fw_count)),
+                      "kvecs": int(st.kvec_n.shape[1]), "max_mol": int(st.max_mol),
+                      "loading": round(float(mc.n_mol.float().mean()), 0), "learned": mc.proposal is not None},
+                     sort_keys=True)
+    if key in _CACHE:
+        c = _CACHE[key]
+        mc.block_threads = c["block_threads"]
+        return TunedShape(c["block_threads"], 0, c["ms_per_step"], c["table"])
+    table, best = [], (math.inf, None)
+    for t in candidates:
+        trial = mc.clone(seed=mc.seed)
+        trial.block_threads = t
+        trial.launch(steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        trial.launch(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        status = read_status(trial.status)
+        ms = e0.elapsed_time(e1) / steps
+        del trial
+        if status.code != _lib.KUPS_OK:
+            table.append((t, 0, None))
+            continue
+        table.append((t, 0, ms))
+        if ms < best[0]:
+            best = (ms, t)
+    if best[1] is None:
+        raise _lib.KupsError("no GCMC launch shape ran without a device error")
+    mc.block_threads = best[1]
+    _CACHE[key] = {"block_threads": best[1], "min_lanes_per_atom": 0, "ms_per_step": best[0], "table": table}
+    return TunedShape(best[1], 0, best[0], table)

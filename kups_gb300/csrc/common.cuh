@@ -14,6 +14,20 @@
 
 namespace kups {
 
+// Multiprocessor count of the current device, looked up once per device.
+inline int device_sm_count() {
+  constexpr int kDevices = 64;
+  static int sms[kDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  int n = dev >= 0 && dev < kDevices ? sms[dev] : 0;
+  if (n <= 0) {
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    if (dev >= 0 && dev < kDevices) sms[dev] = n;
+  }
+  return n;
+}
+
 // ----------------------------------------------------------------- status word
 // First error wins; capacity errors keep the largest requirement seen.
 __device__ inline void status_capacity(kups_status *st, int32_t which, int64_t required,

@@ -720,21 +720,6 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// SM count of the current device, looked up once per device.
-inline int recip_sm_count() {
-  constexpr int kDevices = 64;
-  static int sms[kDevices] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
-  int n = dev >= 0 && dev < kDevices ? sms[dev] : 0;
-  if (n <= 0) {
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-    if (dev >= 0 && dev < kDevices) sms[dev] = n;
-  }
-  return n;
-}
-
 // The reciprocal-space launch sequence of kups_ewald_recip and
 // kups_ewald_recip_static: setup, structure factor, energy and forces.
 // `base` is 256-byte aligned scratch of at least recip_scratch_bytes().
@@ -765,7 +750,7 @@ int32_t recip_launch(char *base, const double *positions, const double *charges,
   if (chunks > 0 && n_kvecs > 0) {
     // enough k splits that the launch holds about 16 warps per SM
     const int kblocks = (n_kvecs + kKPerBlock - 1) / kKPerBlock;
-    const int want = std::max(1, (16 * recip_sm_count()) / std::max(1, 4 * chunks * n_systems));
+    const int want = std::max(1, (16 * device_sm_count()) / std::max(1, 4 * chunks * n_systems));
     const int splits = std::min(kblocks, want);
     const int per = (kblocks + splits - 1) / splits;
     dim3 g(chunks, n_systems, (kblocks + per - 1) / per);

@@ -30,7 +30,7 @@
 namespace kups {
 namespace {
 
-constexpr int kThreads = 128;
+constexpr int kDefaultThreads = 128;  // threads per CTA unless kups_gcmc_args.block_threads says otherwise
 constexpr int kMaxApm = 8;       // atoms per molecule
 constexpr int kMaxSpeciesMC = 8;
 constexpr int kMaxKVec = 4096;
@@ -247,11 +247,10 @@ __device__ inline double tail_energy(const double *counts, int nsp, const double
   return e;
 }
 
-// 7 resident CTAs per SM (at most 73 registers a thread): 1024 replicas run in one wave
-// on 152 SMs, each CTA keeping its system for all n_steps.
-constexpr int kMinCtasPerSm = 7;
-
-__global__ void __launch_bounds__(kThreads, kMinCtasPerSm) gcmc_kernel(kups_gcmc_args a, kups_status *status) {
+// kThreads per CTA, 896 / kThreads resident CTAs per SM (at most 73 registers a thread): at 128
+// threads 1024 replicas run in one wave on 152 SMs, each CTA keeping its system for all n_steps.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcmc_args a, kups_status *status) {
   __shared__ StepShared sh;
   __shared__ float2 lj[kMaxSpeciesMC * kMaxSpeciesMC];
   // per-axis phase tables of the step's moved atoms: e^{2 pi i n f_a}, |n| <= kMaxM
@@ -799,6 +798,13 @@ extern "C" int32_t kups_gcmc_run(const kups_gcmc_args *a, kups_status *status, v
   if (a->n_systems == 0 || a->n_steps == 0) return KUPS_OK;
   if (a->n_kvecs > 0 && a->workspace == nullptr) return KUPS_ERR_INVALID;
   const size_t smem = sizeof(float2) * 2 * (size_t)a->atoms_per_mol * 3 * kTab;
-  gcmc_kernel<<<a->n_systems, kThreads, smem, (cudaStream_t)stream>>>(*a, status);
+  const int threads = a->block_threads > 0 ? a->block_threads : kDefaultThreads;
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (threads) {
+    case 64: gcmc_kernel<64><<<a->n_systems, 64, smem, st>>>(*a, status); break;
+    case 128: gcmc_kernel<128><<<a->n_systems, 128, smem, st>>>(*a, status); break;
+    case 256: gcmc_kernel<256><<<a->n_systems, 256, smem, st>>>(*a, status); break;
+    default: return KUPS_ERR_INVALID;
+  }
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

@@ -42,9 +42,10 @@ __global__ void drift_kernel(double *pos, const double *mom, const double *mass,
 
 __global__ void thermostat_kernel(double *mom, const double *mass, const int32_t *system,
                                   const double *dt, const double *kT, const double *friction,
-                                  uint64_t seed, uint64_t step, int64_t n) {
+                                  uint64_t seed, uint64_t step, const uint64_t *step_ptr, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (step_ptr != nullptr) step = *step_ptr;
   const int s = system[i];
   const double c1 = exp(-friction[s] * dt[s]);
   const double amp = sqrt(kT[s] * (1.0 - c1 * c1)) * sqrt(mass[i]);
@@ -58,13 +59,7 @@ __global__ void thermostat_kernel(double *mom, const double *mass, const int32_t
 // fill every SM, fewer (down to one warp) below that, so that a small system's atoms
 // spread over all SMs instead of queueing on the float64 units of a few.
 inline unsigned atom_block(int64_t n) {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
+  const int sms = device_sm_count();
   const int64_t per = (n + sms - 1) / sms;
   return (unsigned)std::min<int64_t>(256, std::max<int64_t>(32, (per + 31) / 32 * 32));
 }
@@ -98,6 +93,18 @@ extern "C" int32_t kups_md_thermostat(double *momenta, const double *masses, con
   if (n < 0) return KUPS_ERR_INVALID;
   if (n == 0) return KUPS_OK;
   thermostat_kernel<<<(unsigned)((n + atom_block(n) - 1) / atom_block(n)), atom_block(n), 0, (cudaStream_t)stream>>>(
-      momenta, masses, system, dt, kT, friction, seed, step, n);
+      momenta, masses, system, dt, kT, friction, seed, step, nullptr, n);
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
+// The same with the step read from device memory when the kernel runs, so a captured CUDA
+// graph that also advances the counter replays successive steps.
+extern "C" int32_t kups_md_thermostat_counted(double *momenta, const double *masses, const int32_t *system,
+                                              const double *dt, const double *kT, const double *friction,
+                                              uint64_t seed, const uint64_t *step, int64_t n, void *stream) {
+  if (n < 0 || step == nullptr) return KUPS_ERR_INVALID;
+  if (n == 0) return KUPS_OK;
+  thermostat_kernel<<<(unsigned)((n + atom_block(n) - 1) / atom_block(n)), atom_block(n), 0, (cudaStream_t)stream>>>(
+      momenta, masses, system, dt, kT, friction, seed, 0, step, n);
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }

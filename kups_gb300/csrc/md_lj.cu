@@ -1329,10 +1329,7 @@ static cudaError_t launch_md(const kups_md_args &a, int ctas, int threads, size_
 extern "C" int32_t kups_lj_md_max_atoms(void) { return kMaxAtoms; }
 
 extern "C" size_t kups_lj_md_workspace_bytes(const kups_md_args *a) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int ctas = a->n_ctas > 0 ? a->n_ctas : (sms > 0 ? sms : 1);
+  const int ctas = a->n_ctas > 0 ? a->n_ctas : device_sm_count();
   return md_layout(ctas, a->n_atoms < 0 ? 0 : a->n_atoms, a->n_systems < 0 ? 0 : a->n_systems,
                    a->neighbor_capacity).total + 256;
 }
@@ -1353,10 +1350,7 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
   if (a->integrator == 3 && a->trace_virial != nullptr) return KUPS_ERR_INVALID;
   if (ws_bytes < kups_lj_md_workspace_bytes(a)) return KUPS_ERR_INVALID;
   if (a->n_systems == 0) return KUPS_OK;
-  int dev = 0, sms = 0;
-  KUPS_CUDA_TRY(cudaGetDevice(&dev));
-  KUPS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int ctas = a->n_ctas > 0 ? a->n_ctas : sms;
+  const int ctas = a->n_ctas > 0 ? a->n_ctas : device_sm_count();
   const int threads = a->block_threads > 0 ? a->block_threads : kThreads;
   if (threads % 32 != 0 || threads > kThreads || threads < 64) return KUPS_ERR_INVALID;
   const int lanes = a->min_lanes_per_atom;

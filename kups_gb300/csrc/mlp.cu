@@ -452,12 +452,15 @@ __global__ void features_kernel(const double *x, int64_t row0, int64_t n, int gr
     f[1] = (double)((v / grid) % grid) / grid;
     f[2] = (double)(v % grid) / grid;
   }
+  // coordinates reduced to [-0.5, 0.5) once in float64, phases in float32 (the features are
+  // rounded to bfloat16), as the fused forward pass computes them
+  const float fx = (float)(f[0] - rint(f[0])), fy = (float)(f[1] - rint(f[1])), fz = (float)(f[2] - rint(f[2]));
   __nv_bfloat162 *o = reinterpret_cast<__nv_bfloat162 *>(feat + r * kIn);
   for (int j = 0; j < kFreq; ++j) {
-    double t = freq[3 * j] * f[0] + freq[3 * j + 1] * f[1] + freq[3 * j + 2] * f[2];
-    t -= rint(t);
+    float t = fmaf((float)freq[3 * j], fx, fmaf((float)freq[3 * j + 1], fy, (float)freq[3 * j + 2] * fz));
+    t -= rintf(t);
     float sn, cs;
-    sincospif(2.0f * (float)t, &sn, &cs);
+    sincospif(2.0f * t, &sn, &cs);
     o[j] = __floats2bfloat162_rn(sn, cs);
     if (featT != nullptr) {
       featT[(int64_t)(2 * j) * n + r] = __float2bfloat16(sn);
@@ -777,33 +780,57 @@ __global__ void proposal_density_kernel(const float *node, const double *cdf, in
 
 // ============================================================================
 // Fused forward pass (inference: kups_mlp_fwd and the grid refresh).  A persistent
-// CTA (8 warps) takes tiles of 128 points: the features go straight into shared
-// memory as the first layer's A operand (bfloat16, no-swizzle K-major core
-// matrices); for each layer the weights (bfloat16 [256, K]) are staged with 16-byte
-// cp.async, tcgen05.mma accumulates the 128 x 256 tile in tensor memory, and the
-// epilogue (bias, softplus, bfloat16) writes the next layer's A operand back into
-// shared memory while the next weights stream in; the last epilogue folds in the
-// head (w4 . h3 + b4).  Operands are rounded where the layered path rounds them.
-constexpr int kFwdThreads = 512, kFwdRows = 128;  // 16 warps: 4 TMEM lane groups x 4 column quarters
+// CTA (16 warps, one per SM) takes tiles of 256 points, two 128-row halves that share
+// every weight chunk:
+//   * features: each point's fractional coordinates reduced to [-0.5, 0.5) once in
+//     float64, the 32 phases m_j . f in float32 (the output is bfloat16), written
+//     straight into shared memory as the first layer's A operand (bfloat16,
+//     no-swizzle K-major core matrices);
+//   * weights: K-chunks of 64 columns of W [256, K] (32 KB) stream through a two-stage
+//     ring of 16-byte cp.async copies; the chunk after the current one is in flight
+//     while the tensor cores work on the current one (the copies run ahead across
+//     layer and tile boundaries: they never depend on the activations);
+//   * one thread issues tcgen05.mma (128 x 256 x 16, BF16 in, FP32 accumulate) for both
+//     halves per K step into two accumulators of 256 tensor-memory columns each (all
+//     512 columns) and commits each chunk to its stage's mbarrier;
+//   * the epilogue (all warps: warp w reads TMEM lanes 32 (w % 4) .. + 31 of both halves,
+//     64 columns w / 4 ..) adds the bias and applies softplus through the SFU
+//     (exp2 / log2: the result is rounded to bfloat16), writes the next layer's A operand
+//     into shared memory, and after the last layer folds in the head (w4 . h3 + b4).
+// Every mbarrier wait is bounded; on time-out the kernel records KUPS_ERR_UNSUPPORTED,
+// waits (bounded) for its own copies, frees its tensor memory and returns.
+constexpr int kFwdThreads = 512, kFwdRows = 256, kFwdHalf = 128, kFwdKc = 64;
 
-// softplus(x) = max(x, 0) + log1p(exp(-|x|)) (no overflow, SFU exp, accurate log1p)
-__device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + log1pf(__expf(-fabsf(x))); }
-constexpr size_t kFwdA = (size_t)kFwdRows * kHid * 2, kFwdB = (size_t)kHid * kHid * 2;
-constexpr size_t kFwdSmem = kFwdA + kFwdB + 4 * kFwdRows * 4 + 3 * kFwdRows * 8 + 64;
-
-// weights W [256, K] row-major -> core-matrix layout; chunk e covers row (e / 8K') * 8 + e % 8
-// (K' = K / 8 groups) at group (e / 8) % K' and lands at element 8 e
-__device__ inline void fwd_stage_weights(__nv_bfloat16 *sB, const __nv_bfloat16 *W, int K, int tid) {
-  const int groups = K / 8;
-  const uint32_t s0 = smem_u32(sB);
-  for (int e = tid; e < kHid * groups; e += kFwdThreads) {
-    const int lo = e & 7, kg = (e >> 3) % groups, rb = (e >> 3) / groups;
-    cp_async16(s0 + (uint32_t)e * 16u, W + (size_t)(rb * 8 + lo) * K + kg * 8, 16u);
-  }
-}
+// softplus(x) = max(x, 0) + ln(1 + exp(-|x|)) with SFU exp / log (no overflow; the absolute
+// error, a few 1e-8, is far below the bfloat16 rounding that follows)
+__device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + __logf(1.0f + __expf(-fabsf(x))); }
+constexpr size_t kFwdA = (size_t)kFwdRows * kHid * 2;           // 128 KB: A operand, K up to 256
+constexpr size_t kFwdStage = (size_t)kHid * kFwdKc * 2;          // 32 KB: one weight chunk
+constexpr size_t kFwdSmem = kFwdA + 2 * kFwdStage + 4 * kFwdRows * 4 + 3 * kFwdRows * 4 + 64;
 
 __device__ inline int fwd_core(int r, int kk, int K) {
   return ((r >> 3) * (K / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7);
+}
+
+// Chunk q of the per-tile sequence W1 (1 chunk of 64 columns), W2 (4), W3 (4).
+constexpr int kFwdChunks = 1 + 4 + 4;
+__device__ inline void fwd_chunk_of(int q, int &layer, int &kc) {
+  layer = q == 0 ? 0 : (q <= 4 ? 1 : 2);
+  kc = q == 0 ? 0 : (q <= 4 ? q - 1 : q - 5);
+}
+
+// columns [64 kc, 64 kc + 64) of W [256, K] -> core-matrix layout of 256 rows x 64; copy e
+// takes row (e / 64) * 8 + e % 8, column group (e / 8) % 8 and lands at element 8 e
+__device__ inline void fwd_stage_chunk(__nv_bfloat16 *sB, const __nv_bfloat16 *pb, int q, int tid) {
+  int layer, kc;
+  fwd_chunk_of(q, layer, kc);
+  const __nv_bfloat16 *W = pb + (layer == 0 ? kOffW1 : layer == 1 ? kOffW2 : kOffW3);
+  const int K = layer == 0 ? kIn : kHid;
+  const uint32_t s0 = smem_u32(sB);
+  for (int e = tid; e < kHid * (kFwdKc / 8); e += kFwdThreads) {
+    const int lo = e & 7, kg = (e >> 3) & 7, rb = e >> 6;
+    cp_async16(s0 + (uint32_t)e * 16u, W + (size_t)(rb * 8 + lo) * K + kc * kFwdKc + kg * 8, 16u);
+  }
 }
 
 __global__ void __launch_bounds__(kFwdThreads, 1)
@@ -811,31 +838,41 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
                    int grid, float *g_out, kups_status *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);
-  __nv_bfloat16 *sB = reinterpret_cast<__nv_bfloat16 *>(smem + kFwdA);
-  float *part = reinterpret_cast<float *>(smem + kFwdA + kFwdB);  // [4][128] head partial sums
-  double *fr = reinterpret_cast<double *>(smem + kFwdA + kFwdB + 4 * kFwdRows * 4);  // [3][128] coordinates
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kFwdA + kFwdB + 4 * kFwdRows * 4 + 3 * kFwdRows * 8);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+  auto sB = [&](int st) { return reinterpret_cast<__nv_bfloat16 *>(smem + kFwdA + st * kFwdStage); };
+  float *part = reinterpret_cast<float *>(smem + kFwdA + 2 * kFwdStage);       // [4][256] head partials
+  float *fr = part + 4 * kFwdRows;                                                 // [3][256] coordinates
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(fr + 3 * kFwdRows);               // [2]
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, cq = warp >> 2;  // TMEM lanes 32 quarter .., columns 64 cq ..
+  const int quarter = warp & 3, cq = warp >> 2;  // TMEM lanes 32 quarter .., columns 64 cq .. of each half
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(kHid));
+                 "r"(2 * kHid));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) mbar_init(smem_u32(mbar), 1);
+  if (tid == 0) {
+    mbar_init(smem_u32(&mbar[0]), 1);
+    mbar_init(smem_u32(&mbar[1]), 1);
+  }
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t idesc = make_idesc(kFwdRows, kHid);
-  uint32_t phase = 0;
+  const uint32_t idesc = make_idesc(kFwdHalf, kHid);
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
   bool ok = true;
   const int64_t n_tiles = (n + kFwdRows - 1) / kFwdRows;
-  fwd_stage_weights(sB, pb + kOffW1, kIn, tid);
-  cp_async_commit();
-  for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-    // features of the tile's points (rows past n are zero); coordinates once per row
+  const int64_t my_tiles = blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int64_t total_chunks = my_tiles * kFwdChunks;
+  int64_t qg = 0;  // this CTA's chunk counter; stage qg & 1
+  if (total_chunks > 0) {
+    fwd_stage_chunk(sB(0), pb, 0, tid);
+    cp_async_commit();
+  }
+  for (int64_t t = 0; t < my_tiles && ok; ++t) {
+    const int64_t tile = blockIdx.x + t * gridDim.x;
+    // coordinates of the tile's points reduced to [-0.5, 0.5) in float64, kept in float32
     if (tid < kFwdRows) {
       const int64_t pt = tile * kFwdRows + tid;
       double f[3] = {0.0, 0.0, 0.0};
@@ -849,7 +886,7 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
           f[2] = (double)(pt % grid) / grid;
         }
       }
-      for (int a = 0; a < 3; ++a) fr[a * kFwdRows + tid] = f[a];
+      for (int a = 0; a < 3; ++a) fr[a * kFwdRows + tid] = (float)(f[a] - rint(f[a]));
     }
     __syncthreads();
     for (int e = tid; e < kFwdRows * kFreq; e += kFwdThreads) {
@@ -857,80 +894,106 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
       const int64_t pt = tile * kFwdRows + r;
       float sn = 0.f, cs = 0.f;
       if (pt < n) {
-        const double f[3] = {fr[r], fr[kFwdRows + r], fr[2 * kFwdRows + r]};
-        double t = freq[3 * j] * f[0] + freq[3 * j + 1] * f[1] + freq[3 * j + 2] * f[2];
-        t -= rint(t);
-        sincospif(2.0f * (float)t, &sn, &cs);
+        float ph = fmaf((float)freq[3 * j], fr[r],
+                        fmaf((float)freq[3 * j + 1], fr[kFwdRows + r], (float)freq[3 * j + 2] * fr[2 * kFwdRows + r]));
+        ph -= rintf(ph);
+        sincospif(2.0f * ph, &sn, &cs);
       }
       *reinterpret_cast<__nv_bfloat162 *>(sA + fwd_core(r, 2 * j, kIn)) = __floats2bfloat162_rn(sn, cs);
     }
     for (int layer = 0; layer < 3 && ok; ++layer) {
       const int K = layer == 0 ? kIn : kHid;
-      const float *bias = p + (layer == 0 ? kOffB1 : layer == 1 ? kOffB2 : kOffB3);
-      cp_async_wait<0>();
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        for (int ks = 0; ks < K / 16; ++ks) {
-          const uint64_t ad = make_sdesc(smem_u32(sA) + ks * 256, 128, (K / 8) * 128);
-          const uint64_t bd = make_sdesc(smem_u32(sB) + ks * 256, 128, (K / 8) * 128);
-          const uint32_t accumulate = ks > 0 ? 1u : 0u;
-          asm volatile(
-              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-              "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+      const int nch = K / kFwdKc;
+      for (int c = 0; c < nch && ok; ++c, ++qg) {
+        const int st = (int)(qg & 1), nx = st ^ 1;
+        if (qg + 1 < total_chunks) {
+          if (pending[nx]) {  // the MMAs of chunk qg - 1 read stage nx
+            ok = mbar_wait(smem_u32(&mbar[nx]), phase[nx]);
+            if (ok) {  // after a time-out the clean-up waits for these MMAs again
+              phase[nx] ^= 1u;
+              pending[nx] = false;
+            }
+          }
+          if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+          }
+          fwd_stage_chunk(sB(nx), pb, (int)((qg + 1) % kFwdChunks), tid);
+          cp_async_commit();
+          cp_async_wait<1>();  // chunk qg has landed (this thread's copies)
+        } else {
+          cp_async_wait<0>();
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         smem_u32(mbar))
-                     : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // A written by the generic proxy
+        __syncthreads();
+        if (tid == 0) {
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          for (int ks = 0; ks < kFwdKc / 16; ++ks) {
+            const uint64_t bd = make_sdesc(smem_u32(sB(st)) + ks * 256, 128, (kFwdKc / 8) * 128);
+            const uint32_t accumulate = (c > 0 || ks > 0) ? 1u : 0u;
+            for (int h = 0; h < 2; ++h) {
+              const uint64_t ad = make_sdesc(smem_u32(sA) + (uint32_t)(h * kFwdHalf * K * 2) + (c * 4 + ks) * 256,
+                                             128, (K / 8) * 128);
+              asm volatile(
+                  "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                  " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem + (uint32_t)(h * kHid)),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&mbar[st]))
+                       : "memory");
+        }
+        pending[st] = true;
+        if (c == nch - 1) {  // the layer's accumulators are complete once its last chunk is
+          ok = mbar_wait(smem_u32(&mbar[st]), phase[st]);
+          if (ok) {
+            phase[st] ^= 1u;
+            pending[st] = false;
+          }
+        }
       }
-      ok = mbar_wait(smem_u32(mbar), phase);
-      phase ^= 1u;
       if (!__syncthreads_and(ok)) {
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // the MMAs are done with A and B: stream the next weights while the epilogue runs
-      const bool more = layer < 2 || tile + gridDim.x < n_tiles;
-      if (more) {
-        fwd_stage_weights(sB, pb + (layer == 0 ? kOffW2 : layer == 1 ? kOffW3 : kOffW1), layer == 2 ? kIn : kHid, tid);
-        cp_async_commit();
-      }
-      const int row = quarter * 32 + lane;
-      float head = 0.f;
-      for (int c0 = cq * (kHid / 4); c0 < (cq + 1) * (kHid / 4); c0 += 16) {
-        uint32_t r[16];
-        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-            "%14, %15}, [%16];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (layer < 2) {
-          // next layer's A operand: 2 core-matrix rows of 8 bfloat16 (16 bytes each)
+      const float *bias = p + (layer == 0 ? kOffB1 : layer == 1 ? kOffB2 : kOffB3);
+      const float *w4 = p + kOffW4;
+      for (int h = 0; h < 2; ++h) {
+        const int row = h * kFwdHalf + quarter * 32 + lane;
+        float head = 0.f;
+        for (int c0 = cq * (kHid / 4); c0 < (cq + 1) * (kHid / 4); c0 += 16) {
+          uint32_t r[16];
+          const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * kHid + c0);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+              "%13, %14, %15}, [%16];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (layer < 2) {
+            // next layer's A operand: 2 core-matrix rows of 8 bfloat16 (16 bytes each)
 #pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            __nv_bfloat162 h[4];
+            for (int q = 0; q < 2; ++q) {
+              __nv_bfloat162 hv[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const int i = q * 8 + 2 * u;
-              h[u] = __floats2bfloat162_rn(softplus_fast(__uint_as_float(r[i]) + bias[c0 + i]),
-                                           softplus_fast(__uint_as_float(r[i + 1]) + bias[c0 + i + 1]));
+              for (int u = 0; u < 4; ++u) {
+                const int i = q * 8 + 2 * u;
+                hv[u] = __floats2bfloat162_rn(softplus_fast(__uint_as_float(r[i]) + bias[c0 + i]),
+                                              softplus_fast(__uint_as_float(r[i + 1]) + bias[c0 + i + 1]));
+              }
+              *reinterpret_cast<uint4 *>(sA + fwd_core(row, c0 + q * 8, kHid)) = *reinterpret_cast<uint4 *>(hv);
             }
-            *reinterpret_cast<uint4 *>(sA + fwd_core(row, c0 + q * 8, kHid)) = *reinterpret_cast<uint4 *>(h);
-          }
-        } else {
-          const float *w4 = p + kOffW4;
+          } else {
 #pragma unroll
-          for (int i = 0; i < 16; ++i)
-            head = fmaf(softplus_fast(__uint_as_float(r[i]) + bias[c0 + i]), w4[c0 + i], head);
+            for (int i = 0; i < 16; ++i)
+              head = fmaf(softplus_fast(__uint_as_float(r[i]) + bias[c0 + i]), w4[c0 + i], head);
+          }
         }
+        if (layer == 2) part[cq * kFwdRows + row] = head;
       }
-      if (layer == 2) part[cq * kFwdRows + row] = head;
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       if (layer == 2 && tid < kFwdRows) {
@@ -942,19 +1005,23 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
     }
   }
   cp_async_wait<0>();
+  // a time-out leaves MMAs possibly in flight: wait for them (bounded) before freeing TMEM
+  for (int st = 0; st < 2; ++st)
+    if (pending[st]) {
+      (void)mbar_wait(smem_u32(&mbar[st]), phase[st]);
+      pending[st] = false;
+    }
   if (!ok && tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kHid));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kHid));
 }
 
 int32_t fused_forward(const kups_mlp *net, const double *x, int64_t n, int grid, float *g, kups_status *status,
                       cudaStream_t st) {
   if (n <= 0) return KUPS_OK;
   KUPS_CUDA_TRY(cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem));
-  int dev = 0, sms = 148;
-  KUPS_CUDA_TRY(cudaGetDevice(&dev));
-  KUPS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int sms = device_sm_count();
   const int64_t tiles = (n + kFwdRows - 1) / kFwdRows;
   const unsigned ctas = (unsigned)std::min<int64_t>(tiles, sms);
   mlp_forward_kernel<<<ctas, kFwdThreads, kFwdSmem, st>>>((const __nv_bfloat16 *)net->param_bf16, net->param,

@@ -288,6 +288,7 @@ class GCMC:
         self.step = 0
         self.status = new_status()
         self.proposal = None  # learned insertion density (LearnedInsertionProposal) or None: uniform
+        self.block_threads = 0  # threads per CTA (0: library default); kups_gb300.autotune.autotune_gcmc picks one
 
     def _min_half_width(self):
         out = []
@@ -337,6 +338,7 @@ class GCMC:
         a.fw_group = self.fw_group.data_ptr() if self.fw_group is not None else None
         a.obs_sums = self.obs.data_ptr()
         a.trace = trace.data_ptr() if trace is not None else None
+        a.block_threads = int(self.block_threads)
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid
@@ -403,6 +405,7 @@ class GCMC:
             getattr(other, k).copy_(getattr(self, k))
         other.step = self.step
         other.proposal = self.proposal
+        other.block_threads = self.block_threads
         return other
 
     def use_proposal(self, proposal):

@@ -407,6 +407,8 @@ class LennardJonesMD64:
         self.status = new_status()
         self.seed = int(seed)
         self.step = int(state.step)
+        # the Langevin noise counter lives on the device, so a captured step replays as the next one
+        self.counter = torch.tensor([self.step], dtype=torch.int64, device="cuda")
         self.graph = None
         self._forces()
 
@@ -436,9 +438,10 @@ class LennardJonesMD64:
                          self.n, st)
         if self.integrator == 1:
             lib.kups_md_drift(*args, 0.5, self.n, st)
-            lib.kups_md_thermostat(self.mom.data_ptr(), self.mass.data_ptr(), self.system.data_ptr(),
-                                   self.dt.data_ptr(), self.kT.data_ptr(), self.friction.data_ptr(), self.seed, step,
-                                   self.n, st)
+            lib.kups_md_thermostat_counted(self.mom.data_ptr(), self.mass.data_ptr(), self.system.data_ptr(),
+                                           self.dt.data_ptr(), self.kT.data_ptr(), self.friction.data_ptr(),
+                                           self.seed, self.counter.data_ptr(), self.n, st)
+            self.counter.add_(1)
             lib.kups_md_drift(*args, 0.5, self.n, st)
         else:
             lib.kups_md_drift(*args, 1.0, self.n, st)
@@ -447,8 +450,9 @@ class LennardJonesMD64:
                          self.n, st)
 
     def run(self, n_steps: int, use_graph: bool = True):
-        """n_steps steps (the Langevin noise of step k is keyed by (seed, atom, k))."""
-        if self.integrator == 1 or not use_graph:
+        """n_steps steps (the Langevin noise of step k is keyed by (seed, atom, k)); after a warm-up
+        step the step is captured once as a CUDA graph and replayed."""
+        if not use_graph:
             for _ in range(n_steps):
                 self._step(self.step)
                 self.step += 1

@@ -5,9 +5,11 @@ Mirrors ``LocalMLIAPConfig`` / ``local_mliap_energy_full`` / ``local_mliap_energ
 directed edge m_ij = edge(h_i, h_j, d_ij) with d_ij = x_j - x_i + s @ L, summed onto the
 edge's first atom, per-atom energies readout(h, sum_j m_ij) summed per system.  The three
 functions are the user's model and run as torch callables (the reference's are JAX
-callables); the graph is ``kups_neighborlist_build`` on the device (the reference's full
-directed neighbour list), and forces / cell gradients come from torch autograd through the
-difference vectors (the reference's ``jax.vjp`` of the same expression).
+callables).  Everything around them is native: the graph (``kups_neighborlist_build``, the
+reference's full directed neighbour list), the edge vectors (``kups_edge_vectors``), the
+message sum (``kups_edge_segment_sum``, whose backward is the gather of the node gradient)
+and the forces and cell gradient (``kups_edge_gradients`` from dE/dd_ij, the only gradient the
+model's autograd is asked for: the reference's ``jax.vjp`` of the same expression).
 
 The incremental path keeps the reference's cache (node embeddings and message sums) and
 updates it for a set of changed atoms: messages of every edge touching a changed atom in the
@@ -22,7 +24,8 @@ from typing import Callable
 
 import torch
 
-from .neighborlist import CellListNeighborList, NeighborListPoints
+from . import _lib
+from .neighborlist import CellListNeighborList, NeighborListPoints, _stream
 
 
 @dataclass
@@ -44,6 +47,58 @@ def _segment_sum(values: torch.Tensor, index: torch.Tensor, n: int) -> torch.Ten
     return out.index_add(0, index.long(), values)
 
 
+def edge_vectors(positions, system, tril, edges) -> torch.Tensor:
+    """d_e = x_j - x_i + s_e @ L of the valid edges, float64 [E, 3] (kups_edge_vectors)."""
+    pos = positions.detach().to(torch.float64).contiguous()
+    sysi = system.to(torch.int32).contiguous()
+    tr = tril.detach().to(torch.float64).contiguous()
+    ne = edges.n_edges
+    d = torch.empty((ne, 3), dtype=torch.float64, device=pos.device)
+    rc = _lib.load().kups_edge_vectors(pos.data_ptr(), sysi.data_ptr(), pos.shape[0], tr.data_ptr(), tr.shape[0],
+                                       edges.indices.data_ptr(), edges.shifts.data_ptr(), ne, d.data_ptr(), _stream())
+    _lib.check(rc, "kups_edge_vectors")
+    return d
+
+
+class _EdgeSegmentSum(torch.autograd.Function):
+    """sum of edge rows onto the edge's first atom (kups_edge_segment_sum); backward: the node
+    gradient gathered back to the edges."""
+
+    @staticmethod
+    def forward(ctx, values, edges_idx, n_edges, n):
+        v = values.to(torch.float64).contiguous()
+        w = int(v.shape[1]) if v.dim() > 1 else 1
+        out = torch.empty((n, w), dtype=torch.float64, device=v.device)
+        rc = _lib.load().kups_edge_segment_sum(v.data_ptr(), w, edges_idx.data_ptr(), n_edges, n, out.data_ptr(),
+                                               _stream())
+        _lib.check(rc, "kups_edge_segment_sum")
+        ctx.save_for_backward(edges_idx)
+        ctx.n_edges = n_edges
+        ctx.shape = values.shape
+        out = out.to(values.dtype)  # summed in float64, returned in the model's type
+        return out if values.dim() > 1 else out[:, 0]
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (edges_idx,) = ctx.saved_tensors
+        first = edges_idx[: ctx.n_edges, 0].long()
+        g = grad_out.index_select(0, first)
+        return g.reshape(ctx.shape), None, None, None
+
+
+def edge_gradients(dE_dd, system, n, n_systems, edges):
+    """dE/dx [N, 3] and dE/dtril [S, 6] from dE/dd of the valid edges (kups_edge_gradients)."""
+    g = dE_dd.detach().to(torch.float64).contiguous()
+    sysi = system.to(torch.int32).contiguous()
+    grad = torch.empty((n, 3), dtype=torch.float64, device=g.device)
+    gt = torch.empty((n_systems, 6), dtype=torch.float64, device=g.device)
+    rc = _lib.load().kups_edge_gradients(g.data_ptr(), sysi.data_ptr(), n, n_systems, edges.indices.data_ptr(),
+                                         edges.shifts.data_ptr(), edges.n_edges, grad.data_ptr(), gt.data_ptr(),
+                                         _stream())
+    _lib.check(rc, "kups_edge_gradients")
+    return grad, gt
+
+
 @dataclass
 class LocalMLIAP:
     """init_function(Z [N]) -> [N, F]; edge_function(h_i, h_j, d [E, 3]) -> [E, F'];
@@ -63,9 +118,10 @@ class LocalMLIAP:
             NeighborListPoints(positions.detach(), system), None, tril.detach(), cutoffs)
         return edges
 
-    def _messages(self, h, edges, positions, system, tril):
+    def _messages(self, h, edges, positions, system, tril, d=None):
         idx, _ = edges.valid()
-        d = edges.difference_vectors(positions, system, tril)
+        if d is None:
+            d = edge_vectors(positions, system, tril, edges)
         return self.edge_function(h[idx[:, 0].long()], h[idx[:, 1].long()], d), idx[:, 0]
 
     def energy(self, positions, atomic_numbers, system, tril, cutoffs, gradients: bool = True) -> LocalMLIAPResult:
@@ -75,20 +131,21 @@ class LocalMLIAP:
         sysi = torch.as_tensor(system, device="cuda").to(torch.int64)
         z = torch.as_tensor(atomic_numbers, device="cuda").to(torch.int64)
         edges = self.graph(pos, sysi, tr, cutoffs)
+        n, s = pos.shape[0], tr.shape[0]
+        d = edge_vectors(pos, sysi, tr, edges)
         if gradients:
-            pos = pos.detach().requires_grad_(True)
-            tr = tr.detach().requires_grad_(True)
+            d.requires_grad_(True)
         with torch.set_grad_enabled(gradients):
             h = self.init_function(z)
-            m, first = self._messages(h, edges, pos, sysi, tr)
-            msg = _segment_sum(m, first, pos.shape[0])
+            m, _ = self._messages(h, edges, pos, sysi, tr, d)
+            msg = _EdgeSegmentSum.apply(m, edges.indices, edges.n_edges, n)
             e_atom = self.readout_function(h, msg)
-            energy = _segment_sum(e_atom, sysi, tr.shape[0])
+            energy = _segment_sum(e_atom, sysi, s)
         grad = grad_tril = None
         if gradients:
-            grad, grad_tril = torch.autograd.grad(energy.sum(), (pos, tr), allow_unused=True)
-            grad = torch.zeros_like(pos) if grad is None else grad
-            grad_tril = torch.zeros_like(tr) if grad_tril is None else grad_tril
+            (g_d,) = torch.autograd.grad(energy.sum(), (d,), allow_unused=True)
+            g_d = torch.zeros_like(d) if g_d is None else g_d
+            grad, grad_tril = edge_gradients(g_d, sysi, n, s, edges)
         return LocalMLIAPResult(energy.detach(), LocalMLIAPCache(h.detach(), msg.detach()), grad, grad_tril)
 
     def energy_update(self, cache: LocalMLIAPCache, positions_old, positions_new, atomic_numbers_old,
@@ -114,8 +171,8 @@ class LocalMLIAP:
             touch = mask[idx[:, 0].long()] | mask[idx[:, 1].long()]
             sub = type(edges)(idx[touch].contiguous(), sh[touch].reshape(-1, 1, 3).contiguous(), int(touch.sum()))
             with torch.no_grad():
-                m, first = self._messages(h, sub, pos, sysi, tr)
-                msg = msg + sign * _segment_sum(m, first, n)
+                m, _ = self._messages(h, sub, pos, sysi, tr)
+                msg = msg + sign * _EdgeSegmentSum.apply(m, sub.indices, sub.n_edges, n).to(msg.dtype)
         with torch.no_grad():
             energy = _segment_sum(self.readout_function(h_new, msg), sysi, tr.shape[0])
         return LocalMLIAPResult(energy, LocalMLIAPCache(h_new, msg))

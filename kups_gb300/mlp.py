@@ -227,7 +227,7 @@ def _timed_run(mc, steps, block):
 
 def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, train_steps=3000, batch=16384,
                      equil_steps=10000, prod_steps=5000, block=500, temper=0.5, floor=0.05, grid=64, seed=0,
-                     groups=8):
+                     groups=8, tune=True):
     """Plain GCMC from empty, centres of the molecules it holds as training data, NCE training,
     equilibration with the learned proposal, then plain and learned production runs from copies
     of that state.  Returns rates (accepted insertions / moves per second, device time) and the
@@ -261,6 +261,11 @@ def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, 
     for tag, proposal in (("plain", None), ("learned", net)):
         run = mc.clone(seed=seed + 3)
         run.use_proposal(proposal)
+        shape = None
+        if tune:
+            from .autotune import autotune_gcmc
+
+            shape = autotune_gcmc(run)  # on clones of `run`'s state: `run` does not advance
         ms, att, acc, sums = _timed_run(run, prod_steps, block)
         m = sums / block  # block means of U, N, U N, N^2, U^2 per system
         loads = m[..., 1]
@@ -286,6 +291,9 @@ def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, 
             "loading_all_se": float(loads.mean(1).std(ddof=1) / np.sqrt(len(loads))),
             "heat_of_adsorption_kj_mol": qg.mean(0).tolist(),
             "heat_of_adsorption_se": (qg.std(0, ddof=1) / np.sqrt(len(qg))).tolist(),
+            "launch_shape": ({"block_threads": shape.block_threads, "chosen_by": "kups_gb300.autotune.autotune_gcmc",
+                              "candidates_ms_per_step": [[t, m] for t, _, m in shape.table]}
+                             if shape is not None else {"block_threads": 128, "chosen_by": "library default"}),
         }
     lp, ll = np.array(out["plain"]["loading"]), np.array(out["learned"]["loading"])
     sp, sl = np.array(out["plain"]["loading_se"]), np.array(out["learned"]["loading_se"])

@@ -24,7 +24,7 @@ from test_gpu_gcmc import oracle_energy, random_molecule, small_setup, wrapped
 pytestmark = pytest.mark.gpu
 
 
-def _replay(rc, seed, n_steps, energy_every):
+def _replay(rc, seed, n_steps, energy_every, block_threads=0):
     from kups_gb300 import gcmc
     from oracle import unitcell as ouc
 
@@ -38,6 +38,7 @@ def _replay(rc, seed, n_steps, energy_every):
     guests = [np.concatenate([wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0])
                               for _ in range(4)]) for _ in range(S)]
     mc = gcmc.GCMC(setup, seed=seed)
+    mc.block_threads = block_threads
     mc.set_guests(guests)
     # the device holds float32 positions: the oracle state starts from those
     state = [g.reshape(-1, apm, 3).astype(np.float32).astype(np.float64) for g in guests]
@@ -119,3 +120,10 @@ def test_free_running_steps_replay_exactly(rc):
     # the schedulers moved: 1200 steps give every displacement kind more than 100 moves
     w = mc.width.cpu().numpy()
     assert np.any(np.abs(w[:, :3] - 0.1) > 1e-3)
+
+
+@pytest.mark.parametrize("threads", [64, 256])
+def test_replay_holds_for_every_launch_shape(threads):
+    """The autotuner's other CTA sizes run the same chain (600 steps, minimum image)."""
+    kinds_seen, _, _ = _replay(5.0, seed=29, n_steps=600, energy_every=0, block_threads=threads)
+    assert {k for k, _ in kinds_seen} == {0, 1, 2, 3, 4}

@@ -100,6 +100,21 @@ def test_mlp_forward_matches_oracle():
     assert np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g) < 1e-4
 
 
+def test_mlp_forward_many_tiles_per_cta_matches_oracle():
+    """Ragged point count spanning two to three 256-point tiles per CTA (the weight-chunk ring
+    runs across tile boundaries), against the oracle and against the layered training path."""
+    from oracle import mlp as om
+
+    net = _net(8)
+    rng = np.random.default_rng(9)
+    n = 152 * 256 * 2 + 77
+    x = rng.uniform(-1, 2, (n, 3))  # any periodic image
+    g = net.forward(torch.as_tensor(x, device="cuda")).cpu().numpy()
+    ref_g = om.forward(net.params(), x, net.freq.cpu().numpy())["g"]
+    assert np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g) < 1e-4
+    assert np.isfinite(g).all()
+
+
 def test_mlp_backward_matches_oracle():
     from oracle import mlp as om
 

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 RTOL = 1e-12
 
 
-def _batch(seed, n_systems, kmax):
+def _batch(seed, n_systems, kmax, n_kvecs=None, empty=False):
     from oracle import ewald as oew
     from oracle import unitcell as ouc
 
@@ -25,7 +25,7 @@ def _batch(seed, n_systems, kmax):
     pos, q, counts, trils = [], [], [], []
     for s in range(n_systems):
         L = ouc.lattice_from_lengths_angles(rng.uniform(11, 15, 3), rng.uniform(80, 100, 3))
-        n = int(rng.integers(20, 70))
+        n = 0 if empty else int(rng.integers(20, 70))
         pos.append(rng.uniform(-0.5, 0.5, (n, 3)) @ L)
         qq = rng.normal(0, 1, n)
         q.append(qq - qq.mean())
@@ -33,10 +33,11 @@ def _batch(seed, n_systems, kmax):
         trils.append(ouc.tril_from_lattice(L))
     off = np.zeros(n_systems + 1, np.int32)
     off[1:] = np.cumsum(counts)
-    kn = np.stack([oew.kvecs_cube(kmax)] * n_systems).astype(np.int32)
+    kv = oew.kvecs_cube(kmax)[: n_kvecs]
+    kn = np.stack([kv] * n_systems).astype(np.int32).reshape(n_systems, len(kv), 3)
     alpha = rng.uniform(0.28, 0.36, n_systems)
     dev = lambda x, dt: torch.as_tensor(np.ascontiguousarray(x), dtype=dt).cuda()
-    return dict(pos=dev(np.concatenate(pos), torch.float64), q=dev(np.concatenate(q), torch.float64),
+    return dict(pos=dev(np.concatenate(pos).reshape(-1, 3), torch.float64), q=dev(np.concatenate(q), torch.float64),
                 off=dev(off, torch.int32), max_atoms=max(counts), tril=dev(np.stack(trils), torch.float64),
                 kn=dev(kn, torch.int32), alpha=dev(alpha, torch.float64))
 
@@ -74,7 +75,7 @@ def _call(lib, b, static):
 def _close(a, b):
     for x, y in zip(a, b):
         assert np.isfinite(x).all()
-        np.testing.assert_allclose(x, y, rtol=RTOL, atol=RTOL * np.abs(y).max())
+        np.testing.assert_allclose(x, y, rtol=RTOL, atol=RTOL * (np.abs(y).max() if y.size else 0.0))
 
 
 def test_static_scratch_matches_workspace_entry_point_twice():
@@ -94,3 +95,45 @@ def test_static_scratch_refuses_sizes_beyond_the_array():
     lib = _lib.load()
     assert lib.kups_ewald_recip_static(None, None, None, 600, 10, None, None, 1000, None, 1.0, None, None, None, None,
                                        None, None) == 1  # KUPS_ERR_CAPACITY, nothing launched
+
+
+def _scratch_bytes(n_systems, n_kvecs):
+    """Bytes of the fixed array a call needs: 120 B of cell data per system and 32 B per
+    (system, k vector), each part rounded up to 256 bytes."""
+    up = lambda x: (x + 255) // 256 * 256
+    return up(120 * n_systems) + up(32 * n_systems * n_kvecs)
+
+
+def test_static_scratch_at_and_just_past_its_size():
+    """256 systems x 2044 k vectors fill all but 2 KiB of the 16 MiB array and run; one more k
+    vector per system needs more than the array and is refused before any launch."""
+    from kups_gb300 import _lib
+
+    lib = _lib.load()
+    limit = 16 << 20
+    assert _scratch_bytes(256, 2044) <= limit < _scratch_bytes(256, 2045)
+    fits = _batch(21, 256, 8, n_kvecs=2044)
+    _close(_call(lib, fits, True), _call(lib, fits, False))
+    past = _batch(22, 256, 8, n_kvecs=2045)
+    from kups_gb300.units import TO_STANDARD_UNITS
+
+    e, g, gt, sk = _outputs(past)
+    rc = lib.kups_ewald_recip_static(past["pos"].data_ptr(), past["q"].data_ptr(), past["off"].data_ptr(), 256,
+                                     past["max_atoms"], past["tril"].data_ptr(), past["kn"].data_ptr(), 2045,
+                                     past["alpha"].data_ptr(), TO_STANDARD_UNITS, e.data_ptr(), g.data_ptr(),
+                                     gt.data_ptr(), sk.data_ptr(), None, None)
+    assert rc == _lib.KUPS_ERR_CAPACITY
+    torch.cuda.synchronize()
+    assert torch.isnan(e).all()  # nothing was launched
+
+
+def test_static_scratch_without_k_vectors_or_atoms():
+    """n_kvecs = 0 (no structure-factor or force kernels over k) and systems without atoms
+    (no per-atom kernels) give what the workspace entry point gives."""
+    from kups_gb300 import _lib
+
+    lib = _lib.load()
+    no_k = _batch(31, 6, 3, n_kvecs=0)
+    _close(_call(lib, no_k, True), _call(lib, no_k, False))
+    no_atoms = _batch(32, 4, 3, empty=True)
+    _close(_call(lib, no_atoms, True), _call(lib, no_atoms, False))
