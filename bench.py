@@ -1061,10 +1061,10 @@ def profile_gcmc(replicas=1024, equil=3000, steps=40):
     print(f"gcmc: {replicas} replicas, loading {mc.n_mol.float().mean().item():.2f}, {ms / steps * 1e3:.1f} us/step")
 
 
-def profile_mlp(train_steps=20):
+def profile_mlp(train_steps=20, timed_train=200):
     """Learned-proposal network: `train_steps` training steps (batch 16384) on seeded points,
-    then five 64^3 grid refreshes (forward of 262144 nodes, normaliser, CDF) and 200 training
-    steps, each timed with CUDA events."""
+    then five 64^3 grid refreshes (forward of 262144 nodes, normaliser, CDF), five forward passes
+    over 2^20 points alone and `timed_train` training steps, each timed with CUDA events."""
     import torch
 
     from kups_gb300.mlp import LearnedInsertionProposal
@@ -1074,12 +1074,17 @@ def profile_mlp(train_steps=20):
     data = torch.rand(200000, 3, dtype=torch.float64, device="cuda", generator=gen) * 0.3
     net.train(data, steps=int(train_steps), batch=16384)
     net.build_grid()
+    pts = torch.rand(1 << 20, 3, dtype=torch.float64, device="cuda", generator=gen)
+    net.forward(pts)
     torch.cuda.synchronize()
     flop_node = 2 * (64 * 256 + 2 * 256 * 256 + 256)
     ms = _events_ms(torch, lambda: [net.build_grid() for _ in range(5)]) / 5
     print(f"grid refresh: {ms:.3f} ms, {flop_node * 64**3 / ms / 1e9:.1f} TFLOP/s")
-    ms = _events_ms(torch, lambda: net.train(data, steps=200, batch=16384)) / 200
-    print(f"train step (batch 16384): {ms:.3f} ms, {3 * flop_node * 16384 / ms / 1e9:.1f} TFLOP/s")
+    ms = _events_ms(torch, lambda: [net.forward(pts) for _ in range(5)]) / 5
+    print(f"forward of 2^20 points: {ms:.3f} ms, {flop_node * (1 << 20) / ms / 1e9:.1f} TFLOP/s")
+    if int(timed_train) > 0:
+        ms = _events_ms(torch, lambda: net.train(data, steps=int(timed_train), batch=16384)) / int(timed_train)
+        print(f"train step (batch 16384): {ms:.3f} ms, {3 * flop_node * 16384 / ms / 1e9:.1f} TFLOP/s")
 
 
 def profile_ewald(steps=50):

@@ -437,6 +437,27 @@ __device__ inline float warp_sum(float v) {
 
 __device__ inline float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
 
+// sin and cos of 2 pi (m . f) for a point whose coordinates, reduced to [-0.5, 0.5), are the
+// float pairs fh + fl.  The phase is carried as a float pair (the products' rounding errors
+// recovered by fma, the sums' by two-sum) and reduced modulo one before its single rounding
+// to float, so the phase reaching sincospi is within 3e-8 of a turn of the float64 phase and
+// the features round to the same bfloat16 values as the float64 features almost always.
+__device__ inline void phase_sincos(const int32_t *m, const float fh[3], const float fl[3], float &sn, float &cs) {
+  const float m0 = (float)m[0], m1 = (float)m[1], m2 = (float)m[2];
+  const float p0 = __fmul_rn(m0, fh[0]), p1 = __fmul_rn(m1, fh[1]), p2 = __fmul_rn(m2, fh[2]);
+  float lo = __fadd_rn(__fadd_rn(fmaf(m0, fh[0], -p0), fmaf(m1, fh[1], -p1)), fmaf(m2, fh[2], -p2));
+  lo = fmaf(m0, fl[0], fmaf(m1, fl[1], fmaf(m2, fl[2], lo)));
+  const float s1 = __fadd_rn(p0, p1);
+  float b = __fsub_rn(s1, p0);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(p0, __fsub_rn(s1, b)), __fsub_rn(p1, b)));
+  const float s2 = __fadd_rn(s1, p2);
+  b = __fsub_rn(s2, s1);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, b)), __fsub_rn(p2, b)));
+  float t = __fadd_rn(__fsub_rn(s2, rintf(s2)), lo);
+  t = __fsub_rn(t, rintf(t));
+  sincospif(2.0f * t, &sn, &cs);
+}
+
 // Features of point row0 + r: from x (fractional, f64 [., 3]) or, with x null,
 // of grid node row0 + r of a grid^3 lattice.
 __global__ void features_kernel(const double *x, int64_t row0, int64_t n, int grid, const int32_t *freq,
@@ -452,15 +473,18 @@ __global__ void features_kernel(const double *x, int64_t row0, int64_t n, int gr
     f[1] = (double)((v / grid) % grid) / grid;
     f[2] = (double)(v % grid) / grid;
   }
-  // coordinates reduced to [-0.5, 0.5) once in float64, phases in float32 (the features are
-  // rounded to bfloat16), as the fused forward pass computes them
-  const float fx = (float)(f[0] - rint(f[0])), fy = (float)(f[1] - rint(f[1])), fz = (float)(f[2] - rint(f[2]));
+  // coordinates reduced to [-0.5, 0.5) once in float64 and split into float pairs, phases
+  // as float pairs (phase_sincos), as the fused forward pass computes them
+  float fh[3], fl[3];
+  for (int a = 0; a < 3; ++a) {
+    const double red = f[a] - rint(f[a]);
+    fh[a] = (float)red;
+    fl[a] = (float)(red - (double)fh[a]);
+  }
   __nv_bfloat162 *o = reinterpret_cast<__nv_bfloat162 *>(feat + r * kIn);
   for (int j = 0; j < kFreq; ++j) {
-    float t = fmaf((float)freq[3 * j], fx, fmaf((float)freq[3 * j + 1], fy, (float)freq[3 * j + 2] * fz));
-    t -= rintf(t);
     float sn, cs;
-    sincospif(2.0f * t, &sn, &cs);
+    phase_sincos(freq + 3 * j, fh, fl, sn, cs);
     o[j] = __floats2bfloat162_rn(sn, cs);
     if (featT != nullptr) {
       featT[(int64_t)(2 * j) * n + r] = __float2bfloat16(sn);
@@ -658,32 +682,62 @@ __device__ inline double block_sum_d(double v, double *red) {
 }
 
 // node holds g on entry; on exit d = exp(temper (g - max g)) + floor_frac * mean(exp(temper (g - max g))).
-// One block of 1024 threads.
-__global__ void __launch_bounds__(1024) grid_normalise_kernel(float *node, int64_t n, float temper,
-                                                              float floor_frac, kups_status *status) {
+// Two launches over the whole GPU: each block of grid_partials_kernel reduces a grid-stride
+// share of the nodes to (its max m_b, sum exp(temper (g - m_b)) in float64, a non-finite flag);
+// every block of grid_apply_kernel combines the partials (M = max m_b,
+// Z = sum_b s_b exp(temper (m_b - M))) and rewrites its share of the nodes.
+constexpr int kNormBlocks = 152, kNormThreads = 1024;
+
+__global__ void __launch_bounds__(kNormThreads) grid_partials_kernel(const float *node, int64_t n, float temper,
+                                                                     double *partial, kups_status *status) {
   __shared__ float redf[32];
   __shared__ double redd[32];
   float mx = -INFINITY;
   int bad = 0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const float v = node[i];
     if (!isfinite(v)) bad = 1;
     mx = fmaxf(mx, v);
   }
-  if (__syncthreads_or(bad)) {
-    if (threadIdx.x == 0) status_error(status, KUPS_ERR_NONFINITE, -1);
-    return;
-  }
+  bad = __syncthreads_or(bad);
   mx = block_max1024(mx, redf);
   double s = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const float e = expf(temper * (node[i] - mx));
-    node[i] = e;
-    s += e;
+  if (!bad && mx > -INFINITY)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+      s += expf(temper * (node[i] - mx));
+  s = block_sum_d(s, redd);
+  if (threadIdx.x == 0) {
+    partial[3 * blockIdx.x] = (double)mx;
+    partial[3 * blockIdx.x + 1] = s;
+    partial[3 * blockIdx.x + 2] = bad ? 1.0 : 0.0;
+    if (bad) status_error(status, KUPS_ERR_NONFINITE, -1);
   }
-  const double mean = block_sum_d(s, redd) / (double)n;
-  const float fl = (float)(floor_frac * mean);
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) node[i] += fl;
+}
+
+__global__ void __launch_bounds__(256) grid_apply_kernel(float *node, int64_t n, float temper, float floor_frac,
+                                                         const double *partial, int n_partial) {
+  __shared__ float sh_m, sh_fl;
+  __shared__ int sh_bad;
+  if (threadIdx.x == 0) {
+    double M = -INFINITY;
+    int bad = 0;
+    for (int b = 0; b < n_partial; ++b) {
+      M = fmax(M, partial[3 * b]);
+      bad |= partial[3 * b + 2] != 0.0;
+    }
+    double z = 0.0;
+    for (int b = 0; b < n_partial; ++b)
+      if (partial[3 * b] > -INFINITY) z += partial[3 * b + 1] * exp((double)temper * (partial[3 * b] - M));
+    sh_m = (float)M;
+    sh_fl = (float)(floor_frac * (z / (double)n));
+    sh_bad = bad;
+  }
+  __syncthreads();
+  if (sh_bad) return;
+  const float M = sh_m, fl = sh_fl;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    node[i] = expf(temper * (node[i] - M)) + fl;
 }
 
 // cdf[c] = sum_{c' < c} mass(c'), mass = mean of the cell's 8 corners (float64),
@@ -783,7 +837,8 @@ __global__ void proposal_density_kernel(const float *node, const double *cdf, in
 // CTA (16 warps, one per SM) takes tiles of 256 points, two 128-row halves that share
 // every weight chunk:
 //   * features: each point's fractional coordinates reduced to [-0.5, 0.5) once in
-//     float64, the 32 phases m_j . f in float32 (the output is bfloat16), written
+//     float64 and split into float pairs, the 32 phases m_j . f as float pairs
+//     (phase_sincos), written
 //     straight into shared memory as the first layer's A operand (bfloat16,
 //     no-swizzle K-major core matrices);
 //   * weights: K-chunks of 64 columns of W [256, K] (32 KB) stream through a two-stage
@@ -806,7 +861,7 @@ constexpr int kFwdThreads = 512, kFwdRows = 256, kFwdHalf = 128, kFwdKc = 64;
 __device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + __logf(1.0f + __expf(-fabsf(x))); }
 constexpr size_t kFwdA = (size_t)kFwdRows * kHid * 2;           // 128 KB: A operand, K up to 256
 constexpr size_t kFwdStage = (size_t)kHid * kFwdKc * 2;          // 32 KB: one weight chunk
-constexpr size_t kFwdSmem = kFwdA + 2 * kFwdStage + 4 * kFwdRows * 4 + 3 * kFwdRows * 4 + 64;
+constexpr size_t kFwdSmem = kFwdA + 2 * kFwdStage + 4 * kFwdRows * 4 + 6 * kFwdRows * 4 + 64;
 
 __device__ inline int fwd_core(int r, int kk, int K) {
   return ((r >> 3) * (K / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7);
@@ -840,8 +895,8 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
   __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);
   auto sB = [&](int st) { return reinterpret_cast<__nv_bfloat16 *>(smem + kFwdA + st * kFwdStage); };
   float *part = reinterpret_cast<float *>(smem + kFwdA + 2 * kFwdStage);       // [4][256] head partials
-  float *fr = part + 4 * kFwdRows;                                                 // [3][256] coordinates
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(fr + 3 * kFwdRows);               // [2]
+  float *fr = part + 4 * kFwdRows;                                                 // [6][256] coordinates hi, lo
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(fr + 6 * kFwdRows);               // [2]
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3, cq = warp >> 2;  // TMEM lanes 32 quarter .., columns 64 cq .. of each half
@@ -886,7 +941,12 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
           f[2] = (double)(pt % grid) / grid;
         }
       }
-      for (int a = 0; a < 3; ++a) fr[a * kFwdRows + tid] = (float)(f[a] - rint(f[a]));
+      for (int a = 0; a < 3; ++a) {
+        const double red = f[a] - rint(f[a]);
+        const float hi = (float)red;
+        fr[a * kFwdRows + tid] = hi;
+        fr[(3 + a) * kFwdRows + tid] = (float)(red - (double)hi);
+      }
     }
     __syncthreads();
     for (int e = tid; e < kFwdRows * kFreq; e += kFwdThreads) {
@@ -894,10 +954,9 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
       const int64_t pt = tile * kFwdRows + r;
       float sn = 0.f, cs = 0.f;
       if (pt < n) {
-        float ph = fmaf((float)freq[3 * j], fr[r],
-                        fmaf((float)freq[3 * j + 1], fr[kFwdRows + r], (float)freq[3 * j + 2] * fr[2 * kFwdRows + r]));
-        ph -= rintf(ph);
-        sincospif(2.0f * ph, &sn, &cs);
+        const float fh[3] = {fr[r], fr[kFwdRows + r], fr[2 * kFwdRows + r]};
+        const float fl[3] = {fr[3 * kFwdRows + r], fr[4 * kFwdRows + r], fr[5 * kFwdRows + r]};
+        phase_sincos(freq + 3 * j, fh, fl, sn, cs);
       }
       *reinterpret_cast<__nv_bfloat162 *>(sA + fwd_core(r, 2 * j, kIn)) = __floats2bfloat162_rn(sn, cs);
     }
@@ -1176,8 +1235,12 @@ extern "C" int32_t kups_mlp_grid_norm(const kups_mlp *net, int32_t grid, float t
   const MlpWork w = carve(workspace, std::min<int64_t>(n, kChunk));
   const int32_t rc = fused_forward(net, nullptr, n, grid, node, status, st);
   if (rc) return rc;
-  grid_normalise_kernel<<<1, 1024, 0, st>>>(node, n, temper, floor_frac, status);
-  // three-pass scan; the block totals live in the (no longer needed) activation buffer
+  // the normaliser's partials and the scan's block totals live in the (unused) activation buffers
+  double *partial = reinterpret_cast<double *>(w.h2);
+  const int n_norm = (int)std::min<int64_t>(kNormBlocks, (n + kNormThreads - 1) / kNormThreads);
+  grid_partials_kernel<<<n_norm, kNormThreads, 0, st>>>(node, n, temper, partial, status);
+  grid_apply_kernel<<<4 * kNormBlocks, 256, 0, st>>>(node, n, temper, floor_frac, partial, n_norm);
+  // three-pass scan
   const int n_blocks = (int)((n + kCdfPerBlock - 1) / kCdfPerBlock);
   double *totals = reinterpret_cast<double *>(w.h1);
   grid_cdf_local_kernel<<<n_blocks, kCdfThreads, 0, st>>>(node, grid, cdf, totals);

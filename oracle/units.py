@@ -1,32 +1,24 @@
 """Unit system of the reference (ASE-consistent: Angstrom, eV, amu).
 
-Restates src/kups/core/constants.py:26-76 (CODATA 2014 values as used by ASE).
+The constant table (src/kups/core/constants.py:26-76, CODATA 2014 values as used by ASE) is
+data shared by the library and the oracle; it is kept once, in kups_gb300/units.py, and the
+oracle reads it from there.  Test infrastructure: imported by tests, smoke() and bench.py's
+CPU legs only.
 """
 
-import math
-
-_SPEED_OF_LIGHT = 299792458.0
-_MU_0 = 4e-7 * math.pi
-_PLANCK_CONSTANT = 6.626070040e-34
-_ELECTRON_CHARGE = 1.6021766208e-19
-_ELECTRON_MASS = 9.10938356e-31
-_AVOGADRO_NUMBER = 6.022140857e23
-_BOLTZMANN_CONSTANT = 1.38064852e-23
-_ATOMIC_MASS_UNIT = 1.660539040e-27
-
-EPSILON_0 = 1 / (_MU_0 * _SPEED_OF_LIGHT**2)
-HBAR = _PLANCK_CONSTANT / (2 * math.pi)
-BOHR = 4e10 * math.pi * EPSILON_0 * HBAR**2 / _ELECTRON_MASS / _ELECTRON_CHARGE**2
-HARTREE = _ELECTRON_MASS * _ELECTRON_CHARGE**3 / 16 / math.pi**2 / EPSILON_0**2 / HBAR**2
-KILO_JOULE = 1e3 / _ELECTRON_CHARGE
-KILO_CALORIE = 4.184 * KILO_JOULE
-MOL = _AVOGADRO_NUMBER
-SECOND = 1e10 * (_ELECTRON_CHARGE / _ATOMIC_MASS_UNIT) ** 0.5
-FEMTO_SECOND = 1e-15 * SECOND
-BOLTZMANN_CONSTANT = _BOLTZMANN_CONSTANT / _ELECTRON_CHARGE  # eV/K
-METER = 1e10
-PASCAL = 1 / (METER**3 * _ELECTRON_CHARGE)
-BAR = 1e5 * PASCAL
-
-# Coulomb constant in eV*Angstrom/e^2 (src/kups/potential/classical/ewald.py:82)
-TO_STANDARD_UNITS = HARTREE * BOHR
+from kups_gb300.units import (  # noqa: F401
+    BAR,
+    BOHR,
+    BOLTZMANN_CONSTANT,
+    EPSILON_0,
+    FEMTO_SECOND,
+    HARTREE,
+    HBAR,
+    KILO_CALORIE,
+    KILO_JOULE,
+    METER,
+    MOL,
+    PASCAL,
+    SECOND,
+    TO_STANDARD_UNITS,
+)

@@ -99,7 +99,7 @@ def main(root):
     expected = {
         "md_nvt_lj_argon": {
             "source": "ci/statistical/expected/md_nvt_lj_argon.yaml; inputs ci/statistical/inputs/ci/md_nvt_lj_argon.yaml",
-            "settings": {"temperature_k": 100.0, "time_step_fs": 2.0, "friction_per_ps": 1.0, "cutoff_a": 10.0,
+            "settings": {"temperature_k": 100.0, "time_step_fs": 2.0, "friction_per_fs": 1.0, "cutoff_a": 10.0,
                          "sigma_a": 3.405, "epsilon_ev": 0.01032356174398622, "tail_correction": False,
                          "warmup_steps": 5000, "steps": 5000, "integrator": "baoab_langevin"},
             "expected": read_expected(os.path.join(st, "expected", "md_nvt_lj_argon.yaml"))},

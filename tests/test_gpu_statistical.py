@@ -8,7 +8,8 @@ use this library's own random streams, so the comparison is statistical, with th
 bar |mean - expected| < 10 sigma_expected.
 
 * Argon NVT (md_nvt_lj_argon): 256 Ar from argon_fcc.cif (21.04 A cube), LJ sigma 3.405 A,
-  eps 0.0103236 eV, cutoff 10 A, no tail correction, BAOAB dt 2 fs, friction 1 / ps, 100 K;
+  eps 0.0103236 eV, cutoff 10 A, no tail correction, BAOAB dt 2 fs, friction 1 / fs (the input's
+  friction_coefficient is per fs: application/md/data.py:200-201), 100 K;
   5000 warm-up steps, 20000 production steps on the fused kernel: potential, kinetic and total
   energy, temperature (3N - 3 degrees of freedom) and instantaneous pressure.
 * CO2 GCMC in RUBTAK (gcmc_co2_rubtak): the DDEC-charged host replicated 2 x 2 x 2, TraPPE CO2,
@@ -67,7 +68,7 @@ def test_argon_nvt_matches_the_reference_statistics():
                                            torch.tensor([st["cutoff_a"]], dtype=torch.float64))
     state = md.MDState(md.MDParticles(c(pos), c(mom), c(mass), c(np.zeros(n), torch.int32), c(np.zeros(n), torch.int32)),
                        md.MDSystems(c(tril), c([st["time_step_fs"] * FEMTO_SECOND]), c([T]),
-                                    c([st["friction_per_ps"] / 1000.0 / FEMTO_SECOND])),
+                                    c([st["friction_per_fs"] / FEMTO_SECOND])),
                        prm, skin=1.0)
     prop = md.make_baoab_langevin_step()
     packed = md.pack(state)
