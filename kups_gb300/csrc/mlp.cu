@@ -717,25 +717,17 @@ __global__ void __launch_bounds__(kNormThreads) grid_partials_kernel(const float
 
 __global__ void __launch_bounds__(256) grid_apply_kernel(float *node, int64_t n, float temper, float floor_frac,
                                                          const double *partial, int n_partial) {
-  __shared__ float sh_m, sh_fl;
-  __shared__ int sh_bad;
-  if (threadIdx.x == 0) {
-    double M = -INFINITY;
-    int bad = 0;
-    for (int b = 0; b < n_partial; ++b) {
-      M = fmax(M, partial[3 * b]);
-      bad |= partial[3 * b + 2] != 0.0;
-    }
-    double z = 0.0;
-    for (int b = 0; b < n_partial; ++b)
-      if (partial[3 * b] > -INFINITY) z += partial[3 * b + 1] * exp((double)temper * (partial[3 * b] - M));
-    sh_m = (float)M;
-    sh_fl = (float)(floor_frac * (z / (double)n));
-    sh_bad = bad;
-  }
-  __syncthreads();
-  if (sh_bad) return;
-  const float M = sh_m, fl = sh_fl;
+  // thread b < n_partial (<= 256) holds partial b: block max, then the rescaled sums
+  __shared__ float redf[32];
+  __shared__ double redd[32];
+  const int b = threadIdx.x;
+  const bool has = b < n_partial;
+  const float mb = has ? (float)partial[3 * b] : -INFINITY;
+  const int bad = __syncthreads_or(has && partial[3 * b + 2] != 0.0);
+  if (bad) return;
+  const float M = block_max1024(mb, redf);
+  const double zb = has && mb > -INFINITY ? partial[3 * b + 1] * (double)expf(temper * (mb - M)) : 0.0;
+  const float fl = (float)(floor_frac * (block_sum_d(zb, redd) / (double)n));
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     node[i] = expf(temper * (node[i] - M)) + fl;
 }
@@ -861,7 +853,16 @@ constexpr int kFwdThreads = 512, kFwdRows = 256, kFwdHalf = 128, kFwdKc = 64;
 __device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + __logf(1.0f + __expf(-fabsf(x))); }
 constexpr size_t kFwdA = (size_t)kFwdRows * kHid * 2;           // 128 KB: A operand, K up to 256
 constexpr size_t kFwdStage = (size_t)kHid * kFwdKc * 2;          // 32 KB: one weight chunk
-constexpr size_t kFwdSmem = kFwdA + 2 * kFwdStage + 4 * kFwdRows * 4 + 6 * kFwdRows * 4 + 64;
+// shared memory: A operand | two weight stages | head partials [4][256] | coordinates [6][256] |
+// biases b1 b2 b3 and head weights w4 [4][256] | frequencies [32][3] | b4 | mbarriers, TMEM slot
+constexpr size_t kFwdOffPart = kFwdA + 2 * kFwdStage;
+constexpr size_t kFwdOffFr = kFwdOffPart + 4 * kFwdRows * 4;
+constexpr size_t kFwdOffPar = kFwdOffFr + 6 * kFwdRows * 4;
+constexpr size_t kFwdOffFreq = kFwdOffPar + 4 * kHid * 4;
+constexpr size_t kFwdOffB4 = kFwdOffFreq + 3 * kFreq * 4;
+constexpr size_t kFwdOffBar = kFwdOffB4 + 16;
+constexpr size_t kFwdSmem = kFwdOffBar + 64;
+static_assert(kFwdOffBar % 8 == 0, "mbarriers are 8-byte aligned");
 
 __device__ inline int fwd_core(int r, int kk, int K) {
   return ((r >> 3) * (K / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7);
@@ -894,11 +895,21 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
   extern __shared__ __align__(1024) unsigned char smem[];
   __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);
   auto sB = [&](int st) { return reinterpret_cast<__nv_bfloat16 *>(smem + kFwdA + st * kFwdStage); };
-  float *part = reinterpret_cast<float *>(smem + kFwdA + 2 * kFwdStage);       // [4][256] head partials
-  float *fr = part + 4 * kFwdRows;                                                 // [6][256] coordinates hi, lo
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(fr + 6 * kFwdRows);               // [2]
+  float *part = reinterpret_cast<float *>(smem + kFwdOffPart);  // [4][256] head partials
+  float *fr = reinterpret_cast<float *>(smem + kFwdOffFr);       // [6][256] coordinates hi, lo
+  float *spar = reinterpret_cast<float *>(smem + kFwdOffPar);    // [4][256] b1, b2, b3, w4
+  int32_t *sfreq = reinterpret_cast<int32_t *>(smem + kFwdOffFreq);
+  float *sb4 = reinterpret_cast<float *>(smem + kFwdOffB4);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kFwdOffBar);  // [2]
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < 4 * kHid; e += kFwdThreads) {
+    const int which = e / kHid;
+    const int64_t off = which == 0 ? kOffB1 : which == 1 ? kOffB2 : which == 2 ? kOffB3 : kOffW4;
+    spar[e] = p[off + e % kHid];
+  }
+  for (int e = tid; e < 3 * kFreq; e += kFwdThreads) sfreq[e] = freq[e];
+  if (tid == 0) sb4[0] = p[kOffB4];
   const int quarter = warp & 3, cq = warp >> 2;  // TMEM lanes 32 quarter .., columns 64 cq .. of each half
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -914,8 +925,9 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const uint32_t idesc = make_idesc(kFwdHalf, kHid);
-  uint32_t phase[2] = {0u, 0u};
-  bool pending[2] = {false, false};
+  // per stage (bit st): parity of the next completion to wait for, and whether MMAs reading it are
+  // in flight (bit fields, not arrays: the stage index is dynamic)
+  uint32_t phase = 0u, pending = 0u;
   bool ok = true;
   const int64_t n_tiles = (n + kFwdRows - 1) / kFwdRows;
   const int64_t my_tiles = blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
@@ -956,7 +968,7 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
       if (pt < n) {
         const float fh[3] = {fr[r], fr[kFwdRows + r], fr[2 * kFwdRows + r]};
         const float fl[3] = {fr[3 * kFwdRows + r], fr[4 * kFwdRows + r], fr[5 * kFwdRows + r]};
-        phase_sincos(freq + 3 * j, fh, fl, sn, cs);
+        phase_sincos(sfreq + 3 * j, fh, fl, sn, cs);
       }
       *reinterpret_cast<__nv_bfloat162 *>(sA + fwd_core(r, 2 * j, kIn)) = __floats2bfloat162_rn(sn, cs);
     }
@@ -966,11 +978,11 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
       for (int c = 0; c < nch && ok; ++c, ++qg) {
         const int st = (int)(qg & 1), nx = st ^ 1;
         if (qg + 1 < total_chunks) {
-          if (pending[nx]) {  // the MMAs of chunk qg - 1 read stage nx
-            ok = mbar_wait(smem_u32(&mbar[nx]), phase[nx]);
+          if ((pending >> nx) & 1u) {  // the MMAs of chunk qg - 1 read stage nx
+            ok = mbar_wait(smem_u32(&mbar[nx]), (phase >> nx) & 1u);
             if (ok) {  // after a time-out the clean-up waits for these MMAs again
-              phase[nx] ^= 1u;
-              pending[nx] = false;
+              phase ^= 1u << nx;
+              pending &= ~(1u << nx);
             }
           }
           if (!__syncthreads_and(ok)) {
@@ -1003,12 +1015,12 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
                            smem_u32(&mbar[st]))
                        : "memory");
         }
-        pending[st] = true;
+        pending |= 1u << st;
         if (c == nch - 1) {  // the layer's accumulators are complete once its last chunk is
-          ok = mbar_wait(smem_u32(&mbar[st]), phase[st]);
+          ok = mbar_wait(smem_u32(&mbar[st]), (phase >> st) & 1u);
           if (ok) {
-            phase[st] ^= 1u;
-            pending[st] = false;
+            phase ^= 1u << st;
+            pending &= ~(1u << st);
           }
         }
       }
@@ -1017,25 +1029,27 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const float *bias = p + (layer == 0 ? kOffB1 : layer == 1 ? kOffB2 : kOffB3);
-      const float *w4 = p + kOffW4;
+      const float *bias = spar + layer * kHid;
+      const float *w4 = spar + 3 * kHid;
       for (int h = 0; h < 2; ++h) {
         const int row = h * kFwdHalf + quarter * 32 + lane;
         float head = 0.f;
-        for (int c0 = cq * (kHid / 4); c0 < (cq + 1) * (kHid / 4); c0 += 16) {
-          uint32_t r[16];
+        for (int c0 = cq * (kHid / 4); c0 < (cq + 1) * (kHid / 4); c0 += 32) {
+          uint32_t r[32];
           const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(h * kHid + c0);
           asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-              "%13, %14, %15}, [%16];"
+              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+              "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
               : "r"(taddr));
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
           if (layer < 2) {
-            // next layer's A operand: 2 core-matrix rows of 8 bfloat16 (16 bytes each)
+            // next layer's A operand: 4 core-matrix rows of 8 bfloat16 (16 bytes each)
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
+            for (int q = 0; q < 4; ++q) {
               __nv_bfloat162 hv[4];
 #pragma unroll
               for (int u = 0; u < 4; ++u) {
@@ -1047,7 +1061,7 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
             }
           } else {
 #pragma unroll
-            for (int i = 0; i < 16; ++i)
+            for (int i = 0; i < 32; ++i)
               head = fmaf(softplus_fast(__uint_as_float(r[i]) + bias[c0 + i]), w4[c0 + i], head);
           }
         }
@@ -1059,16 +1073,16 @@ mlp_forward_kernel(const __nv_bfloat16 *pb, const float *p, const int32_t *freq,
         const int64_t pt = tile * kFwdRows + tid;
         if (pt < n)
           g_out[pt] = ((part[tid] + part[kFwdRows + tid]) + (part[2 * kFwdRows + tid] + part[3 * kFwdRows + tid])) +
-                      p[kOffB4];
+                      sb4[0];
       }
     }
   }
   cp_async_wait<0>();
   // a time-out leaves MMAs possibly in flight: wait for them (bounded) before freeing TMEM
   for (int st = 0; st < 2; ++st)
-    if (pending[st]) {
-      (void)mbar_wait(smem_u32(&mbar[st]), phase[st]);
-      pending[st] = false;
+    if ((pending >> st) & 1u) {
+      (void)mbar_wait(smem_u32(&mbar[st]), (phase >> st) & 1u);
+      pending &= ~(1u << st);
     }
   if (!ok && tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -278,6 +278,13 @@ def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, 
         kt = np.asarray(setup.temperature, np.float64).reshape(groups, S // groups).mean(1) * BOLTZMANN_CONSTANT
         with np.errstate(invalid="ignore", divide="ignore"):
             qg = (cov / var - kt[None, :]) * EV_TO_KJ_PER_MOL
+        # a block whose N never changed in any of the group's replicas defines no heat of
+        # adsorption: averaged over the blocks that do; null where fewer than two do
+        q_ok = np.isfinite(qg) & (var > 0)
+        q_n = q_ok.sum(0)
+        q_mean = [float(qg[q_ok[:, j], j].mean()) if q_n[j] >= 2 else None for j in range(groups)]
+        q_se = [float(qg[q_ok[:, j], j].std(ddof=1) / np.sqrt(q_n[j])) if q_n[j] >= 2 else None
+                for j in range(groups)]
         out[tag] = {
             "ms_per_step": ms / prod_steps,
             "accepted_insertions_per_s": float(acc[3] / ms * 1e3),
@@ -289,8 +296,9 @@ def learned_vs_plain(setup, plain_steps=6000, snapshots=40, snapshot_every=100, 
             "loading_se": (g.std(0, ddof=1) / np.sqrt(len(g))).tolist(),
             "loading_all": float(loads.mean()),
             "loading_all_se": float(loads.mean(1).std(ddof=1) / np.sqrt(len(loads))),
-            "heat_of_adsorption_kj_mol": qg.mean(0).tolist(),
-            "heat_of_adsorption_se": (qg.std(0, ddof=1) / np.sqrt(len(qg))).tolist(),
+            "heat_of_adsorption_kj_mol": q_mean,
+            "heat_of_adsorption_se": q_se,
+            "heat_of_adsorption_blocks": q_n.tolist(),
             "launch_shape": ({"block_threads": shape.block_threads, "chosen_by": "kups_gb300.autotune.autotune_gcmc",
                               "candidates_ms_per_step": [[t, m] for t, _, m in shape.table]}
                              if shape is not None else {"block_threads": 128, "chosen_by": "library default"}),

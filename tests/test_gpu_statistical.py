@@ -11,7 +11,8 @@ bar |mean - expected| < 10 sigma_expected.
   eps 0.0103236 eV, cutoff 10 A, no tail correction, BAOAB dt 2 fs, friction 1 / fs (the input's
   friction_coefficient is per fs: application/md/data.py:200-201), 100 K;
   5000 warm-up steps, 20000 production steps on the fused kernel: potential, kinetic and total
-  energy, temperature (3N - 3 degrees of freedom) and instantaneous pressure.
+  energy, temperature (3N - 3 degrees of freedom) and the reference's pressure statistic
+  (-Tr(dE/dL) / 3V, lattice gradient at fixed Cartesian positions).
 * CO2 GCMC in RUBTAK (gcmc_co2_rubtak): the DDEC-charged host replicated 2 x 2 x 2, TraPPE CO2,
   LJ cutoff 12 A with tail correction, Ewald real cutoff 12 A at precision 1e-6, 10 kPa,
   298.15 K (Peng-Robinson fugacity), translate / rotate / reinsert / exchange at 1:1:1:2;
@@ -76,16 +77,24 @@ def test_argon_nvt_matches_the_reference_statistics():
     steps, chunk = 20000, 10
     pe = torch.zeros((steps, 1), dtype=torch.float64, device="cuda")
     ke = torch.zeros_like(pe)
-    prs = torch.zeros(steps // chunk, dtype=torch.float64, device="cuda")
+    vir = torch.zeros((steps, 1, 6), dtype=torch.float64, device="cuda")
+    phys = torch.zeros(steps // chunk, dtype=torch.float64, device="cuda")
     step0 = st["warmup_steps"]
     for k in range(steps // chunk):
-        prop.launch(packed, chunk, seed=42, step0=step0, trace_pe=pe[k * chunk:(k + 1) * chunk],
-                    trace_ke=ke[k * chunk:(k + 1) * chunk])
-        prs[k] = packed.pressure[0]
+        sl = slice(k * chunk, (k + 1) * chunk)
+        prop.launch(packed, chunk, seed=42, step0=step0, trace_pe=pe[sl], trace_ke=ke[sl], trace_virial=vir[sl])
+        phys[k] = packed.pressure[0]
         step0 += chunk
     torch.cuda.synchronize()
-    pe, ke, prs = pe.cpu().numpy()[:, 0], ke.cpu().numpy()[:, 0], prs.cpu().numpy()
+    pe, ke, vir = pe.cpu().numpy()[:, 0], ke.cpu().numpy()[:, 0], vir.cpu().numpy()[:, 0]
     temp = 2.0 * ke / ((3 * n - 3) * BOLTZMANN_CONSTANT)
+    # The reference's logged "pressure" is Tr(stress) / 3 with stress = -dE/dL / V, dE/dL the
+    # potential's lattice gradient at fixed Cartesian positions (application/md/data.py:102-107,
+    # application/md/analysis.py:101): no kinetic part, and the positions wrapped into
+    # [-0.5, 0.5) as both codes wrap them.  The per-step dE/dtril trace is that gradient.
+    vol = abs(np.prod(tril[0, [0, 2, 5]]))
+    prs = -(vir[:, 0] + vir[:, 2] + vir[:, 5]) / (3.0 * vol)
+    print(f"physical pressure (2K - Tr W) / 3V: {phys.mean().item():.4g} eV/A^3 (not a reference statistic)")
     exp = ref["expected"]
     zs = [_check("potential_energy", pe.mean(), exp["potential_energy"], tol),
           _check("kinetic_energy", ke.mean(), exp["kinetic_energy"], tol),
