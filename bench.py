@@ -142,15 +142,20 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def read_traffic():
-    """DRAM bytes per atom-step of the MD kernel from the committed ncu summary, if present."""
+def read_profile_value(key):
+    """A per-atom-step figure of the MD kernel from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "md_lj_batched_uneven_ncu.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_atom_step:"):
-            return float(line.split(":")[1])
+        if line.startswith(key + ":"):
+            return float(line.split(":")[1].split()[0])
     return None
+
+
+def read_traffic():
+    """DRAM bytes per atom-step of the MD kernel from the committed ncu summary, if present."""
+    return read_profile_value("dram_bytes_per_atom_step")
 
 
 def measured_peak():
@@ -348,6 +353,18 @@ def run_ours(a):
     line["fp32_roofline"] = {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                              "frac": fp32_achieved / fp32_peak, "flop_per_atom_step": flop_atom_step,
                              "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x {mhz:.0f} MHz"}
+    # shared memory: the kernel keeps every system on chip, so its on-chip ceiling is the
+    # shared-memory data path (one wavefront per clock per SM); wavefronts per atom-step from the
+    # committed ncu capture of the same kernel and workload
+    wf = read_profile_value("shared_wavefronts_per_atom_step")
+    if wf is not None:
+        smem_peak = sms * mhz * 1e6
+        smem_achieved = value * wf / max(world, 1)
+        line["smem_roofline"] = {"achieved": smem_achieved, "peak": smem_peak, "unit": "wavefronts/s",
+                                 "frac": smem_achieved / smem_peak, "wavefronts_per_atom_step": wf,
+                                 "bank_conflict_share": read_profile_value("shared_bank_conflict_share"),
+                                 "peak_source": f"derived: {sms} SMs x 1 shared-memory wavefront per clock x {mhz:.0f} MHz",
+                                 "source": "profiles/md_lj_batched_uneven_ncu.txt"}
     line["steady_state"] = steady_state(prop, packed, torch, step0, W.n_atoms)
     if not a.no_e2e:
         line["e2e"] = run_e2e(a, W, torch)
@@ -772,6 +789,9 @@ def run_ewald_md(a):
     ref = _melt_sim(W, torch, real_space="edges")
     sim.start(torch.as_tensor(W.momenta).cuda())
     ref.start(torch.as_tensor(W.momenta).cuda())
+    from kups_gb300.autotune import autotune_lj_ewald
+
+    tuned = autotune_lj_ewald(sim)  # untimed; before the step is captured
     acc0 = _against_float64(sim, ref, torch)
     sim.run(20)
     torch.cuda.synchronize()
@@ -793,6 +813,9 @@ def run_ewald_md(a):
            "real_space": ("all pairs (float hi/lo positions, per-warp hit queue), no list" if sim.allpairs
                           else "neighbour list every step"),
            "accuracy_vs_float64_path": {"start": acc0, "after_timed_run": acc1},
+           "launch_shape": {"real_space_partner_shares": tuned.block_threads,
+                            "chosen_by": "kups_gb300.autotune.autotune_lj_ewald",
+                            "candidates_ms_per_force_evaluation": [[sp, ms] for sp, _, ms in tuned.table]},
            "fp32_roofline": ewald_fp32_roofline(W, n * steps / (ms / 1e3))}
     if getattr(a, "nve_check", True):
         from kups_gb300.units import FEMTO_SECOND

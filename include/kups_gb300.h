@@ -402,8 +402,11 @@ int32_t kups_lj_ewald_real_forces(const double *positions, const double *charges
  * relative accuracy with no float64 arithmetic) and the pair terms evaluated only for
  * the partners a lane found inside the cutoff among 32 tested.  terms & 8 adds the
  * energy and gradient onto the caller's (e.g. the reciprocal-space result) instead
- * of writing them.  A system with more than max_atoms_per_system atoms records
- * KUPS_ERR_INVALID and is skipped.
+ * of writing them.  With terms & 8, bits 8-11 of terms give the number of partner
+ * shares per block of 16 atoms (1-15: gridDim.z; the shares add their partial forces
+ * with atomics, so the float summation order varies); 0 means one share.  Without
+ * terms & 8 there is one share.  A system with more than
+ * max_atoms_per_system atoms records KUPS_ERR_INVALID and is skipped.
  * Workspace: kups_lj_ewald_real_forces_workspace_bytes(n_systems, max_atoms). */
 size_t kups_lj_ewald_real_forces_workspace_bytes(int32_t n_systems, int32_t max_atoms_per_system);
 int32_t kups_lj_ewald_real_forces_packed(const double *positions, const double *charges,

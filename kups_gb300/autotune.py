@@ -1,4 +1,5 @@
-"""Launch-shape autotuner of the fused Lennard-Jones MD kernel.
+"""Launch-shape autotuners: the fused Lennard-Jones MD kernel, the GCMC kernel and the
+all-pairs LJ + Ewald real space.
 
 The fused kernel's throughput depends on two launch choices that no formula fixes well
 across workloads: threads per CTA (one CTA per SM owns one system at a time; more threads
@@ -141,5 +142,52 @@ def autotune_gcmc(mc, steps: int = 200, candidates=GCMC_THREADS) -> TunedShape:
     if best[1] is None:
         raise _lib.KupsError("no GCMC launch shape ran without a device error")
     mc.block_threads = best[1]
+    _CACHE[key] = {"block_threads": best[1], "min_lanes_per_atom": 0, "ms_per_step": best[0], "table": table}
+    return TunedShape(best[1], 0, best[0], table)
+
+
+LJ_EWALD_SPLITS = (1, 2, 3, 4)
+
+
+def autotune_lj_ewald(sim, calls: int = 30, candidates=LJ_EWALD_SPLITS) -> TunedShape:
+    """Partner shares per 16-atom block of the all-pairs LJ + Ewald real space
+    (``kups_lj_ewald_real_forces_packed``, terms bits 8-11; 0 is the library default, one share)
+    for an ``ewald.LJEwaldMD`` whose real space runs without a list.
+    Each candidate is timed over `calls` force evaluations at the current positions (a force
+    evaluation does not advance the state), after one untimed call; the fastest is set on `sim`
+    (before its step is captured as a CUDA graph) and cached per workload signature (systems,
+    largest system, cutoffs).  The returned table lists (shares, 0, ms per force evaluation)."""
+    if not sim.allpairs:
+        return TunedShape(0, 0, math.nan, [])
+    key = json.dumps({"kernel": "lj_ewald_real_packed", "systems": int(sim.s), "max_atoms": int(sim.max_atoms),
+                      "rc": round(float(sim.rc_ew.max()), 3), "kvecs": int(sim.kn.shape[1])}, sort_keys=True)
+    if key in _CACHE:
+        c = _CACHE[key]
+        sim.real_splits = c["block_threads"]
+        return TunedShape(c["block_threads"], 0, c["ms_per_step"], c["table"])
+    keep = sim.real_splits
+    table, best = [], (math.inf, None)
+    for sp in candidates:
+        sim.real_splits = sp
+        sim._forces()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(calls):
+            sim._forces()
+        e1.record()
+        torch.cuda.synchronize()
+        status = read_status(sim.status)
+        ms = e0.elapsed_time(e1) / calls
+        if status.code != _lib.KUPS_OK:
+            table.append((sp, 0, None))
+            continue
+        table.append((sp, 0, ms))
+        if ms < best[0]:
+            best = (ms, sp)
+    sim.real_splits = keep if best[1] is None else best[1]
+    sim._forces()  # energy and gradient of the current state with the chosen shape
+    torch.cuda.synchronize()
+    if best[1] is None:
+        raise _lib.KupsError("no LJ + Ewald launch shape ran without a device error")
     _CACHE[key] = {"block_threads": best[1], "min_lanes_per_atom": 0, "ms_per_step": best[0], "table": table}
     return TunedShape(best[1], 0, best[0], table)

@@ -559,6 +559,8 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
     const int32_t *sys_offset, const double *tril, const double *lj_sigma, const double *lj_eps, int nsp,
     const double *rc_lj, const double *alpha, const double *rc_ew, double ke, int terms, int max_atoms,
     const float4 *hi, const float4 *lo, double *energy, double *grad, kups_status *status) {
+  // blockIdx.z of gridDim.z takes an equal share of every atom's partners; with more than one
+  // share the blocks add their partial forces (terms & 8 is then required)
   __shared__ float2 ljt[64];
   __shared__ float part[kRealStreams][kRealAtoms][3];
   __shared__ double red[40];
@@ -625,9 +627,12 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
   for (int k = threadIdx.x; k < kRealStreams * kRealAtoms * 3; k += blockDim.x) (&part[0][0][0])[k] = 0.f;
   __syncthreads();
   float ef = 0.f;
-  const int per = (n + kRealStreams - 1) / kRealStreams;
-  const int j0 = stream_id * per, j1 = min(n, j0 + per);
-  const int j0h[2] = {(warp * 2) * per, (warp * 2 + 1) * per};  // chunk starts of the warp's two streams
+  const int n_streams = kRealStreams * (int)gridDim.z;
+  const int per = (n + n_streams - 1) / n_streams;
+  const int sbase = (int)blockIdx.z * kRealStreams;
+  const int j0 = (sbase + stream_id) * per, j1 = min(n, j0 + per);
+  // chunk starts of the warp's two streams
+  const int j0h[2] = {(sbase + warp * 2) * per, (sbase + warp * 2 + 1) * per};
   uint16_t *wq = queue[warp];
   const int passes = (per + 31) / 32;  // the same for both half-warps of a warp
   for (int pass = 0; pass < passes; ++pass) {
@@ -704,7 +709,11 @@ __global__ void __launch_bounds__(32 * kRealWarps) real_packed_kernel(
       gy += part[k][slot][1];
       gz += part[k][slot][2];
     }
-    if (terms & 8) {  // add onto the caller's gradient (this block owns atom gi)
+    if (gridDim.z > 1) {  // several blocks share atom gi
+      atomicAdd(&grad[3 * gi], (double)gx);
+      atomicAdd(&grad[3 * gi + 1], (double)gy);
+      atomicAdd(&grad[3 * gi + 2], (double)gz);
+    } else if (terms & 8) {  // add onto the caller's gradient (this block owns atom gi)
       grad[3 * gi] += gx;
       grad[3 * gi + 1] += gy;
       grad[3 * gi + 2] += gz;
@@ -946,6 +955,8 @@ extern "C" int32_t kups_lj_ewald_real_forces_packed(const double *positions, con
                                                     double *energy, double *grad, void *workspace,
                                                     size_t workspace_bytes, kups_status *status, void *stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
+  const int splits_req = (terms >> 8) & 15;  // partner shares per atom block; 0: chosen here
+  terms &= 255;
   if (n_systems < 0 || max_atoms_per_system < 0 || (terms & ~11) != 0 || (terms & 3) == 0) return KUPS_ERR_INVALID;
   if ((terms & 1) && (n_species < 1 || n_species > 8 || lj_sigma == nullptr || lj_epsilon == nullptr))
     return KUPS_ERR_INVALID;
@@ -962,7 +973,12 @@ extern "C" int32_t kups_lj_ewald_real_forces_packed(const double *positions, con
   dim3 gp((max_atoms_per_system + 255) / 256, n_systems);
   real_pack_kernel<<<gp, 256, 0, stream>>>(positions, charges, species, sys_offset, terms, max_atoms_per_system, hi,
                                            lo, status);
-  dim3 g((max_atoms_per_system + kRealAtoms - 1) / kRealAtoms, n_systems);
+  // partner shares: the caller's choice (a launch-shape tuner's), else one.  Shares add their
+  // partial forces, so they need terms & 8 (the caller's gradient is the base).  One share
+  // measured fastest on the 4000-ion melt (250 blocks on 152 SMs: 0.152 ms per force
+  // evaluation against 0.164 / 0.166 / 0.171 for 2 / 3 / 4 shares).
+  const int splits = (terms & 8) && splits_req > 0 ? splits_req : 1;
+  dim3 g((max_atoms_per_system + kRealAtoms - 1) / kRealAtoms, n_systems, splits);
   real_packed_kernel<<<g, 32 * kRealWarps, 0, stream>>>(sys_offset, tril, lj_sigma, lj_epsilon, n_species, lj_cutoff,
                                                         alpha, ewald_cutoff, coulomb_k, terms, max_atoms_per_system,
                                                         hi, lo, energy, grad, status);

@@ -187,8 +187,9 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
   const int kc_end = min(nk_all, kc_begin + per_split);
   const bool fa = fast_operand(g.a, g.a_bf16, g.sar, g.sac, g.k);
   const bool fb = fast_operand(g.b, g.b_bf16, g.sbr, g.sbc, g.k);
-  uint32_t phase[2] = {0u, 0u};
-  bool pending[2] = {false, false};
+  // per stage (bit st): parity of the next completion to wait for, and whether MMAs reading it are
+  // in flight (bit fields, not arrays: the stage index is dynamic)
+  uint32_t phase = 0u, pending = 0u;
   bool ok = true;
   if (kc_begin < kc_end) {
     stage_operand<kBM>(sa(0), g.a, g.a_bf16, g.sar, g.sac, fa, m0, g.m, kc_begin * kBK, g.k, tid);
@@ -198,10 +199,12 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
   for (int kc = kc_begin; kc < kc_end; ++kc) {
     const int st = (kc - kc_begin) & 1, nx = st ^ 1;
     if (kc + 1 < kc_end) {
-      if (pending[nx]) {  // the MMAs of chunk kc - 1 read stage nx
-        ok = mbar_wait(smem_u32(&mbar[nx]), phase[nx]);
-        phase[nx] ^= 1u;
-        pending[nx] = false;
+      if ((pending >> nx) & 1u) {  // the MMAs of chunk kc - 1 read stage nx
+        ok = mbar_wait(smem_u32(&mbar[nx]), (phase >> nx) & 1u);
+        if (ok) {  // after a time-out the clean-up below waits for these MMAs again
+          phase ^= 1u << nx;
+          pending &= ~(1u << nx);
+        }
       }
       if (!__syncthreads_and(ok)) {
         ok = false;
@@ -232,14 +235,12 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
                        smem_u32(&mbar[st]))
                    : "memory");
     }
-    pending[st] = true;
+    pending |= 1u << st;
   }
   cp_async_wait<0>();
+  // every MMA in flight completes (bounded waits) before the accumulator is read or freed
   for (int st = 0; st < 2; ++st)
-    if (pending[st] && ok) {
-      ok = mbar_wait(smem_u32(&mbar[st]), phase[st]);
-      phase[st] ^= 1u;
-    }
+    if ((pending >> st) & 1u) ok = mbar_wait(smem_u32(&mbar[st]), (phase >> st) & 1u) && ok;
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (!ok) {
@@ -271,10 +272,11 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
       const int col = n0 + c0 + lane;
       if (col < g.n) {
         const float bias = g.bias ? g.bias[col] : 0.f;
-#pragma unroll 1
+        // unrolled so that the gate loads of several rows are in flight together
+#pragma unroll 8
         for (int rr = 0; rr < 32; ++rr) {
           const int row = rbase + rr;
-          if (row >= g.m) break;
+          if (row >= g.m) continue;
           float v = g.alpha * blk[rr * 33 + lane];
           const int64_t o = (int64_t)row * g.scr + (int64_t)col * g.scc;
           if (g.split_k > 1) {
@@ -304,10 +306,10 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
       if (g.c3 != nullptr && g.split_k == 1) {
         const int row = rbase + lane;
         if (row < g.m) {
-#pragma unroll 1
+#pragma unroll 8
           for (int i = 0; i < 32; ++i) {
             const int cc = n0 + c0 + i;
-            if (cc >= g.n) break;
+            if (cc >= g.n) continue;
             ((__nv_bfloat16 *)g.c3)[(int64_t)row * g.sc3r + (int64_t)cc * g.sc3c] =
                 __float2bfloat16(blk[lane * 33 + i]);
           }

@@ -433,6 +433,11 @@ class LJEwaldMD:
         self.excl = torch.arange(self.n, dtype=torch.int32, device="cuda")
         self.seed = seed
         self.step_counter = torch.zeros(1, dtype=torch.int64)
+        # the Langevin noise counter of the captured BAOAB step lives on the device
+        self.counter = torch.zeros(1, dtype=torch.int64, device="cuda")
+        # partner shares per 16-atom block of the all-pairs real space (0: the library default of
+        # one; autotune.autotune_lj_ewald picks one per workload)
+        self.real_splits = 0
         self.graph = None
 
     def _forces(self):
@@ -448,7 +453,8 @@ class LJEwaldMD:
                 pos.data_ptr(), self.q.data_ptr(), self.species.data_ptr(), self.off.data_ptr(), self.s,
                 self.max_atoms, self.tril.data_ptr(), self.sig.data_ptr() if self.lj else None,
                 self.eps.data_ptr() if self.lj else None, nsp, self.rc_lj.data_ptr() if self.lj else None,
-                self.alpha.data_ptr(), self.rc_ew.data_ptr(), TO_STANDARD_UNITS, terms | TERM_ACCUMULATE,
+                self.alpha.data_ptr(), self.rc_ew.data_ptr(), TO_STANDARD_UNITS,
+                terms | TERM_ACCUMULATE | (self.real_splits << 8),
                 self.energy.data_ptr(), self.grad.data_ptr(), self.real_ws.data_ptr(), self.real_ws.numel(),
                 self.status.data_ptr(), _stream())
             _lib.check(rc, "kups_lj_ewald_real_forces_packed")
@@ -479,8 +485,10 @@ class LJEwaldMD:
         if self.integrator == "baoab":
             lib.kups_md_drift(p.positions.data_ptr(), p_mom, self.masses.data_ptr(), self.system.data_ptr(),
                               self.dt.data_ptr(), self.tril.data_ptr(), 0.5, self.n, st)
-            lib.kups_md_thermostat(p_mom, self.masses.data_ptr(), self.system.data_ptr(), self.dt.data_ptr(),
-                                   self.kT.data_ptr(), self.friction.data_ptr(), self.seed, step, self.n, st)
+            lib.kups_md_thermostat_counted(p_mom, self.masses.data_ptr(), self.system.data_ptr(),
+                                           self.dt.data_ptr(), self.kT.data_ptr(), self.friction.data_ptr(),
+                                           self.seed, self.counter.data_ptr(), self.n, st)
+            self.counter.add_(1)
             lib.kups_md_drift(p.positions.data_ptr(), p_mom, self.masses.data_ptr(), self.system.data_ptr(),
                               self.dt.data_ptr(), self.tril.data_ptr(), 0.5, self.n, st)
         else:
@@ -496,9 +504,9 @@ class LJEwaldMD:
         torch.cuda.synchronize()
 
     def run(self, n_steps: int, use_graph: bool = True):
-        """n_steps steps; the Langevin counter advances by one per step."""
-        if not use_graph or self.integrator == "baoab":
-            # the thermostat's step counter is a launch argument: replay would freeze it
+        """n_steps steps; the Langevin counter (on the device, so that a replayed graph advances
+        it) goes up by one per step."""
+        if not use_graph:
             for _ in range(n_steps):
                 self._step(int(self.step_counter.item()))
                 self.step_counter += 1

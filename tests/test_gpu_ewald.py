@@ -246,3 +246,44 @@ def test_pair_term_erfc_accuracy():
     bound = torch.where(xs <= 4.0, torch.full_like(xs, 2e-6), (xs * xs + 2.0) * 2.0**-23 + 1e-6)
     keep = ref > 1e-15
     assert bool((rel[keep] < bound[keep]).all()), float((rel / bound)[keep].max())
+
+
+def test_lj_ewald_md_baoab_graph_replays_the_eager_steps():
+    """The captured BAOAB step of LJEwaldMD reads its Langevin counter from the device, so graph
+    replays continue the eager trajectory's noise sequence (with a frozen counter the replayed
+    steps would repeat one noise draw and leave it at once)."""
+    from kups_gb300 import ewald
+    from kups_gb300.autotune import autotune_lj_ewald
+    from kups_gb300.units import FEMTO_SECOND
+
+    rng = np.random.default_rng(5)
+    n = 400
+    L = ouc.lattice_from_lengths_angles([26.0, 27.0, 25.0], [90, 90, 90])
+    g = np.stack(np.meshgrid(*[np.arange(8)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    pos = (g + 0.5 + rng.uniform(-0.1, 0.1, g.shape)) / 8.0 @ L
+    q = np.where(np.arange(n) % 2 == 0, 1.0, -1.0)
+    sp = (np.arange(n) % 2).astype(np.int32)
+    masses = np.where(sp == 0, 22.99, 35.45)
+    kn = oew.kvecs_cube(4)[None].astype(np.int32)
+    prm = ewald.EwaldParameters(torch.tensor([0.3]), torch.tensor([9.0]), torch.as_tensor(kn))
+    sig = np.array([[2.35, 2.6], [2.6, 2.9]])  # below the 3.2 A lattice spacing: a gentle start
+    eps = np.array([[0.0043, 0.0053], [0.0053, 0.0065]])
+
+    def make():
+        parts = ewald.EwaldParticles(cuda(pos), cuda(q), cuda(np.zeros(n), torch.int32), cuda(sp, torch.int32))
+        sim = ewald.LJEwaldMD(parts, cuda(masses), cuda(ouc.tril_from_lattice(L)[None]), prm, 1.0 * FEMTO_SECOND,
+                              sig, eps, [9.0], integrator="baoab", temperature=1000.0, friction=0.01 / FEMTO_SECOND,
+                              seed=3)
+        sim.start(torch.zeros((n, 3), dtype=torch.float64, device="cuda"))
+        return sim
+
+    eager, graph = make(), make()
+    assert eager.allpairs
+    autotune_lj_ewald(graph, calls=3)
+    eager.real_splits = graph.real_splits
+    eager.run(6, use_graph=False)
+    graph.run(6)
+    torch.cuda.synchronize()
+    assert int(graph.counter.item()) == 6 and int(eager.counter.item()) == 6
+    np.testing.assert_allclose(graph.mom.cpu().numpy(), eager.mom.cpu().numpy(), rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(graph.p.positions.cpu().numpy(), eager.p.positions.cpu().numpy(), atol=1e-8)
