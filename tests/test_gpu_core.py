@@ -7,6 +7,8 @@ arithmetic within force RMS relative error 1e-5 and energy relative error
 positions.
 """
 
+from dataclasses import replace
+
 import numpy as np
 import pytest
 import torch
@@ -414,3 +416,24 @@ def test_fused_md_per_step_virial_trace():
         np.testing.assert_allclose(tv[-1].cpu().numpy(), dt, rtol=1e-4, atol=1e-4 * np.abs(dt).max())
         rows.append(tv[0].cpu().numpy())
     assert all(np.isfinite(r).all() for r in rows)
+
+
+def test_pack_reuses_the_layout_of_unchanged_inputs():
+    """md.pack(state, reuse=previous) takes the sort by system, offsets, queue order and
+    per-system parameters from `previous` while the state's static objects are the same and
+    unmodified, and packs the same arrays as a fresh pack; a modified input forces a fresh one."""
+    from kups_gb300 import md, workloads
+
+    W = workloads.batched_uneven_lj(n_systems=24, seed=3)
+    state = md_state(W)
+    first = md.pack(state)
+    moved = replace(state, particles=replace(state.particles, positions=state.particles.positions + 0.01))
+    again = md.pack(moved, reuse=first)
+    fresh = md.pack(moved)
+    assert again.perm is first.perm and again.order is first.order
+    for f in ("pos4", "mom4", "perm", "sys_offset", "order", "tril32", "cutoff", "skin", "dt", "kT", "friction"):
+        assert torch.equal(getattr(again, f), getattr(fresh, f)), f
+    assert (again.max_atoms, again.max_density) == (fresh.max_atoms, fresh.max_density)
+    state.particles.masses.mul_(1.0)  # an in-place write bumps the version: no reuse
+    third = md.pack(moved, reuse=again)
+    assert third.perm is not again.perm
