@@ -36,7 +36,8 @@ struct NLWork {
   int *cell_start;      // [n_cells_cap + 1]
   int *cell_fill;       // [n_cells_cap]
   int *cell_items;      // [N]
-  int64_t *edge_off;    // [N + 1]
+  int64_t *edge_off;    // [N + 1], or [27 N + 1] for the split pair search
+  bool split;           // one thread per (particle, neighbour cell): N <= kNLSplitMax
   int64_t *scan_tmp;    // scan block sums (int64)
   int *scan_tmp32;      // scan block sums (int32)
   int64_t *n_cells;     // [1]
@@ -44,6 +45,12 @@ struct NLWork {
 };
 
 inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Neighbour cells per particle, and the batch size up to which the pair search runs one
+// thread per (particle, neighbour cell) instead of one per particle (a single system of a
+// few thousand particles otherwise occupies a few SMs).
+constexpr int kNLCells = 27;
+constexpr int64_t kNLSplitMax = 32768;
 
 // Cells allotted: never more than max(1, 2 * atoms) per system, so the total
 // is bounded by n_systems + 2 * n_particles.
@@ -64,8 +71,10 @@ size_t layout(NLWork *w, char *base, int64_t n, int32_t s) {
   t.cell_start = (int *)take(sizeof(int) * (size_t)(cc + 1));
   t.cell_fill = (int *)take(sizeof(int) * (size_t)cc);
   t.cell_items = (int *)take(sizeof(int) * (size_t)n);
-  t.edge_off = (int64_t *)take(sizeof(int64_t) * (size_t)(n + 1));
-  const int64_t nb = scan_blocks_needed(std::max<int64_t>(n + 1, cc + 1));
+  t.split = n <= kNLSplitMax;
+  const int64_t n_off = t.split ? kNLCells * n : n;
+  t.edge_off = (int64_t *)take(sizeof(int64_t) * (size_t)(n_off + 1));
+  const int64_t nb = scan_blocks_needed(std::max<int64_t>(n_off + 1, cc + 1));
   t.scan_tmp = (int64_t *)take(sizeof(int64_t) * (size_t)nb);
   t.scan_tmp32 = (int *)take(sizeof(int) * (size_t)nb);
   t.n_cells = (int64_t *)take(sizeof(int64_t));
@@ -223,18 +232,27 @@ __device__ inline bool edge_test(const SysNL &p, const double fi[3], const doubl
   return true;
 }
 
-template <bool WRITE>
+// One thread per particle, or with SPLIT one thread per (particle, neighbour cell): thread
+// a n + i scans cell a = (az * 3 + ay) * 3 + ax of particle i's (up to) 3 x 3 x 3 cells, so
+// that a batch of few particles still fills the GPU, and the lanes of a warp (consecutive,
+// cell-sorted particles) scan the same relative cell in step.  Offsets are kept at 27 i + a,
+// the (particle, az, ay, ax) order of the per-particle form's loops, so both forms write the
+// same edges in the same order.
+template <bool WRITE, bool SPLIT>
 __global__ void pairs_kernel(const int32_t *system, const int32_t *inclusion,
                              const int32_t *exclusion, int64_t n, int32_t n_incl, int32_t s,
                              const SysNL *sys, const double *frac, const int *cell_of,
                              const int *cell_start, const int *cell_items, int64_t *edge_off,
                              int32_t *edges, int32_t *shifts, int64_t cap) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (SPLIT ? kNLCells * n : n)) return;
+  const int a_only = SPLIT ? (int)(t / n) : -1;
+  const int64_t i = SPLIT ? t - (int64_t)a_only * n : t;
+  const int64_t slot = SPLIT ? i * kNLCells + a_only : i;  // this thread's offset entry
   const int32_t si = system[i];
   const int32_t inc = inclusion[i];
   int64_t count = 0;
-  int64_t out = WRITE ? edge_off[i] : 0;
+  int64_t out = WRITE ? edge_off[slot] : 0;
   if (si >= 0 && si < s && inc >= 0 && inc < n_incl) {
     const SysNL p = sys[si];
     const double fi[3] = {frac[3 * i], frac[3 * i + 1], frac[3 * i + 2]};
@@ -265,6 +283,7 @@ __global__ void pairs_kernel(const int32_t *system, const int32_t *inclusion,
     for (int az = 0; az < nz; ++az)
       for (int ay = 0; ay < ny; ++ay)
         for (int ax = 0; ax < nx; ++ax) {
+          if (SPLIT && (az * 3 + ay) * 3 + ax != a_only) continue;
           const int c = (int)p.cell_base + (lz[az] * p.nc[1] + ly[ay]) * p.nc[0] + lx[ax];
           const int b = cell_start[c], e = cell_start[c + 1];
           for (int k = b; k < e; ++k) {
@@ -307,7 +326,7 @@ __global__ void pairs_kernel(const int32_t *system, const int32_t *inclusion,
           }
         }
   }
-  if (!WRITE) edge_off[i] = count;
+  if (!WRITE) edge_off[slot] = count;
 }
 
 __global__ void check_capacity_kernel(const int64_t *n_edges, int64_t cap, kups_status *st) {
@@ -363,13 +382,25 @@ extern "C" int32_t kups_neighborlist_build(const double *positions, const int32_
   scatter_kernel<<<gb, 256, 0, stream>>>(w.cell_of, n, w.cell_start, w.cell_fill, w.cell_items);
   sort_cells_kernel<<<(unsigned)((w.n_cells_cap + 255) / 256), 256, 0, stream>>>(
       w.cell_start, w.n_cells, w.cell_items);
-  pairs_kernel<false><<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys,
-                                              w.frac, w.cell_of, w.cell_start, w.cell_items,
-                                              w.edge_off, edges, shifts, cap);
-  KUPS_CUDA_TRY(exclusive_scan<int64_t>(w.edge_off, n, w.scan_tmp, n_edges, stream));
-  pairs_kernel<true><<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys,
-                                             w.frac, w.cell_of, w.cell_start, w.cell_items,
-                                             w.edge_off, edges, shifts, cap);
+  const int64_t n_thr = w.split ? kNLCells * n : n;
+  const unsigned gp = (unsigned)((n_thr + 127) / 128);
+  if (w.split)
+    pairs_kernel<false, true><<<gp, 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys, w.frac,
+                                                      w.cell_of, w.cell_start, w.cell_items, w.edge_off, edges,
+                                                      shifts, cap);
+  else
+    pairs_kernel<false, false><<<gp, 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys, w.frac,
+                                                       w.cell_of, w.cell_start, w.cell_items, w.edge_off, edges,
+                                                       shifts, cap);
+  KUPS_CUDA_TRY(exclusive_scan<int64_t>(w.edge_off, n_thr, w.scan_tmp, n_edges, stream));
+  if (w.split)
+    pairs_kernel<true, true><<<gp, 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys, w.frac,
+                                                     w.cell_of, w.cell_start, w.cell_items, w.edge_off, edges,
+                                                     shifts, cap);
+  else
+    pairs_kernel<true, false><<<gp, 128, 0, stream>>>(system, inclusion, exclusion, n, n_incl, s, w.sys, w.frac,
+                                                      w.cell_of, w.cell_start, w.cell_items, w.edge_off, edges,
+                                                      shifts, cap);
   check_capacity_kernel<<<1, 1, 0, stream>>>(n_edges, cap, status);
   if (cap > 0)
     pad_kernel<<<(unsigned)((cap + 255) / 256), 256, 0, stream>>>(n_edges, cap, n, edges, shifts);
