@@ -76,6 +76,9 @@ const char *kups_error_string(int32_t code);
  * and the minimum-image-only exclusion rule (:731-735).  Edges are grouped by
  * i (lh) in increasing order; entries [n_edges, edge_capacity) are padded
  * with i = j = n_particles and a zero shift, as _compact_edges pads (:651-689).
+ * A system whose cutoff needs more than 1331 image offsets per pair (a cutoff
+ * of about five cell widths) gets no edges and KUPS_ERR_UNSUPPORTED is recorded
+ * with its index; an infinite cutoff means the minimum image only.
  *
  *   positions  f64 [n_particles, 3]   Cartesian
  *   system     i32 [n_particles]      values outside [0, n_systems) = empty slot

@@ -27,7 +27,13 @@ struct SysNL {
   int image_mode;  // prod(nimg) > 1: explicit image offsets, all system pairs are candidates
   int n_atoms;
   int64_t cell_base;
+  int refused;     // more than kMaxNLImages image offsets: no edges, KUPS_ERR_UNSUPPORTED recorded
 };
+
+// Image offsets per candidate pair beyond which a system is refused instead of searched (a
+// cutoff of many cell widths: 11^3 offsets is a cutoff of about five widths; the
+// reference's own image replication would materialise that many copies of every pair).
+constexpr double kMaxNLImages = 1331.0;
 
 struct NLWork {
   SysNL *sys;
@@ -91,8 +97,8 @@ __global__ void count_atoms_kernel(const int32_t *system, int64_t n, int32_t s, 
 }
 
 // One block: per-system parameters and the exclusive scan of cells per system.
-__global__ void setup_systems_kernel(const double *tril, const double *cutoffs, int32_t s,
-                                     SysNL *sys, int64_t *n_cells) {
+__global__ void __launch_bounds__(1024) setup_systems_kernel(const double *tril, const double *cutoffs, int32_t s,
+                                     SysNL *sys, int64_t *n_cells, kups_status *status) {
   __shared__ int64_t scratch[32];
   int64_t carry = 0;
   for (int base = 0; base < s; base += blockDim.x) {
@@ -107,7 +113,7 @@ __global__ void setup_systems_kernel(const double *tril, const double *cutoffs, 
       double w[3];
       perpendicular_widths64(p.L, w);
       const bool finite = isfinite(rc);
-      int prod = 1;
+      double prod = 1.0;
       for (int a = 0; a < 3; ++a) {
         int n = 1;
         if (finite) {
@@ -117,9 +123,15 @@ __global__ void setup_systems_kernel(const double *tril, const double *cutoffs, 
           if (n % 2 == 0) n += 1;
         }
         p.nimg[a] = n;
-        prod *= (n > 1 ? n : 1);
+        prod *= (double)n;
       }
-      p.image_mode = prod > 1;
+      p.refused = prod > kMaxNLImages;
+      if (p.refused) {
+        status_error(status, KUPS_ERR_UNSUPPORTED, k);
+        p.nimg[0] = p.nimg[1] = p.nimg[2] = 1;
+        prod = 1.0;
+      }
+      p.image_mode = prod > 1.0;
       int64_t budget = 2 * (int64_t)p.n_atoms;
       if (budget < 1) budget = 1;
       for (int a = 0; a < 3; ++a) {
@@ -253,7 +265,7 @@ __global__ void pairs_kernel(const int32_t *system, const int32_t *inclusion,
   const int32_t inc = inclusion[i];
   int64_t count = 0;
   int64_t out = WRITE ? edge_off[slot] : 0;
-  if (si >= 0 && si < s && inc >= 0 && inc < n_incl) {
+  if (si >= 0 && si < s && inc >= 0 && inc < n_incl && !sys[si].refused) {
     const SysNL p = sys[si];
     const double fi[3] = {frac[3 * i], frac[3 * i + 1], frac[3 * i + 2]};
     const int32_t exi = exclusion[i];
@@ -375,7 +387,7 @@ extern "C" int32_t kups_neighborlist_build(const double *positions, const int32_
   KUPS_CUDA_TRY(cudaMemsetAsync(w.cell_start, 0, sizeof(int) * (w.n_cells_cap + 1), stream));
   KUPS_CUDA_TRY(cudaMemsetAsync(w.cell_fill, 0, sizeof(int) * w.n_cells_cap, stream));
   count_atoms_kernel<<<gb, 256, 0, stream>>>(system, n, s, w.sys);
-  setup_systems_kernel<<<1, 1024, 0, stream>>>(tril, cutoffs, s, w.sys, w.n_cells);
+  setup_systems_kernel<<<1, 1024, 0, stream>>>(tril, cutoffs, s, w.sys, w.n_cells, status);
   bin_kernel<<<gb, 256, 0, stream>>>(positions, system, n, s, w.sys, w.frac, w.cell_of,
                                      w.cell_start);
   KUPS_CUDA_TRY(exclusive_scan<int>(w.cell_start, w.n_cells_cap + 1, w.scan_tmp32, nullptr, stream));
@@ -472,7 +484,7 @@ __global__ void pairs_rh_kernel(const int32_t *lh_incl, const int32_t *lh_excl, 
   const int32_t inc = rh_incl[j];
   int64_t count = 0;
   int64_t out = WRITE ? rh_off[j] : 0;
-  if (sj >= 0 && sj < s && inc >= 0 && inc < n_incl) {
+  if (sj >= 0 && sj < s && inc >= 0 && inc < n_incl && !sys[sj].refused) {
     const SysNL p = sys[sj];
     const double r[3] = {rh_pos[3 * j], rh_pos[3 * j + 1], rh_pos[3 * j + 2]};
     double fj[3];
@@ -644,7 +656,7 @@ extern "C" int32_t kups_neighborlist_build_rh(
   KUPS_CUDA_TRY(cudaMemsetAsync(l.cell_fill, 0, sizeof(int) * l.n_cells_cap, stream));
   KUPS_CUDA_TRY(cudaMemsetAsync(w.in_remap, 0, (size_t)std::max<int64_t>(n, 1), stream));
   count_atoms_kernel<<<gb, 256, 0, stream>>>(lh_system, n, s, l.sys);
-  setup_systems_kernel<<<1, 1024, 0, stream>>>(tril, cutoffs, s, l.sys, l.n_cells);
+  setup_systems_kernel<<<1, 1024, 0, stream>>>(tril, cutoffs, s, l.sys, l.n_cells, status);
   bin_kernel<<<gb, 256, 0, stream>>>(lh_positions, lh_system, n, s, l.sys, l.frac, l.cell_of, l.cell_start);
   KUPS_CUDA_TRY(exclusive_scan<int>(l.cell_start, l.n_cells_cap + 1, l.scan_tmp32, nullptr, stream));
   scatter_kernel<<<gb, 256, 0, stream>>>(l.cell_of, n, l.cell_start, l.cell_fill, l.cell_items);
