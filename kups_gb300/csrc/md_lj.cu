@@ -550,6 +550,10 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return r;
 }
 
+// Per-atom pair energies of the last force evaluation with ENERGY, kept in the counting-sort
+// scratch: no phase between a force evaluation and the sum of its energies sorts anything.
+__device__ inline float *atom_energy(Smem &sm) { return reinterpret_cast<float *>(sm.bin_a); }
+
 // Accumulators of one lane for one atom.
 struct PairAcc {
   float fx, fy, fz, e;
@@ -590,8 +594,8 @@ __device__ __forceinline__ void lj_pair(const Smem &sm, const float4 &xi, int ti
   }
 }
 
-// Forces into sm.frc[i].xyz.  With ENERGY, adds this thread's share of the
-// potential energy (sum over its pairs / 2) to *pe; with VIRIAL, adds the
+// Forces into sm.frc[i].xyz.  With ENERGY, each atom's potential energy (sum over its
+// pairs / 2) into atom_energy(sm)[i]; with VIRIAL, adds the
 // Cartesian pair virial W_cb = 1/2 sum d_c g_b ([xx, yx, yy, zx, zy, zz]) to wv.
 // Warps take 32 / tpa atoms at a time from a shared counter (sm.work, zeroed
 // by the caller before the preceding barrier), so uneven neighbour counts do
@@ -599,8 +603,7 @@ __device__ __forceinline__ void lj_pair(const Smem &sm, const float4 &xi, int ti
 // (8 bytes) per iteration, fetched one iteration ahead.
 template <bool ENERGY, bool VIRIAL, bool SINGLE>
 __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa, const uint2 *nl,
-                                               float rc2, float sig2, float a4, double *pe,
-                                               float wv[6]) {
+                                               float rc2, float sig2, float a4, float wv[6]) {
   const int lane = threadIdx.x & 31;
   const int lane_g = lane & (tpa - 1);
   const int per_warp = 32 / tpa;
@@ -649,7 +652,11 @@ __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa
       f.z = acc.fz;
       sm.frc[i] = f;
     }
-    if (ENERGY) *pe += 0.5 * (double)acc.e;
+    if (ENERGY) {  // the atom's pair energy / 2, lanes summed in a fixed order
+      float e = acc.e;
+      for (int o = tpa >> 1; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+      if (active && lane_g == 0) atom_energy(sm)[i] = 0.5f * e;
+    }
     if (VIRIAL) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) wv[k] += acc.w[k];
@@ -659,15 +666,15 @@ __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa
 
 template <bool ENERGY, bool VIRIAL>
 __device__ __forceinline__ void forces_dispatch(Smem &sm, int n, int nsp, int tpa, const uint2 *nl,
-                                                float rc2, float sig2, float a4, double *pe,
-                                                float wv[6]) {
+                                                float rc2, float sig2, float a4, float wv[6]) {
   if (nsp == 1)
-    compute_forces<ENERGY, VIRIAL, true>(sm, n, nsp, tpa, nl, rc2, sig2, a4, pe, wv);
+    compute_forces<ENERGY, VIRIAL, true>(sm, n, nsp, tpa, nl, rc2, sig2, a4, wv);
   else
-    compute_forces<ENERGY, VIRIAL, false>(sm, n, nsp, tpa, nl, rc2, sig2, a4, pe, wv);
+    compute_forces<ENERGY, VIRIAL, false>(sm, n, nsp, tpa, nl, rc2, sig2, a4, wv);
 }
 
 static_assert(sizeof(Smem) <= 227 * 1024, "fused MD shared memory above the per-CTA limit");
+static_assert(sizeof(Smem::bin_a) >= kMaxAtoms * sizeof(float), "per-atom energies fit the sort scratch");
 
 // Key offsets that separate the system-level draws (CSVR R1, the barostat's R)
 // and the chi-squared normals from the per-atom Langevin noise.
@@ -701,6 +708,18 @@ __device__ inline void block_sums(const float (&v)[N], Smem &sm, double (&out)[N
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < N; ++k) out[k] = sm.red_d[k];
+}
+
+// Sum of the per-atom energies of the last ENERGY force evaluation (thread k takes atoms
+// k, k + blockDim.x, ...: a fixed order, so the result does not depend on which warp took
+// which atom in the force phase), returned to every thread.
+__device__ inline double atom_energy_sum(Smem &sm, int n) {
+  float e = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) e += atom_energy(sm)[i];
+  const float v[1] = {e};
+  double r[1];
+  block_sums<1>(v, sm, r);
+  return r[0];
 }
 
 // One standard normal (Box-Muller on two words) and one uniform in (0, 1] from
@@ -879,27 +898,29 @@ __device__ void save_record(const Smem &sm, const kups_md_args &a, const MdWork 
 // sum_i f_i,a F_i,b over atoms (f fractional, wrapped; F the force), written by thread 0:
 // X_ab = sum_c (L^-1)_ca W_cb + sum_i f_i,a F_i,b.  Returns Tr W (every thread).
 __device__ double virial_from_sums(const SysParams &p, const double r[12], double *out) {
-  double W[3][3];
-  W[0][0] = r[0];
-  W[1][0] = W[0][1] = r[1];
-  W[1][1] = r[2];
-  W[2][0] = W[0][2] = r[3];
-  W[2][1] = W[1][2] = r[4];
-  W[2][2] = r[5];
-  const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
-  double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
-  Li[1][0] = -(B * Li[0][0]) / C;
-  Li[2][1] = -(E * Li[1][1]) / F;
-  Li[2][0] = -((D * Li[0][0]) + (E * Li[1][0])) / F;
-  const int ia[6] = {0, 1, 1, 2, 2, 2}, ib[6] = {0, 0, 1, 0, 1, 2};
+  // only thread 0 forms the cell inverse (float64 divisions: a handful of FP64 operations per
+  // thread of a 1024-thread block would cost the whole block tens of microseconds per call)
   if (threadIdx.x == 0) {
+    double W[3][3];
+    W[0][0] = r[0];
+    W[1][0] = W[0][1] = r[1];
+    W[1][1] = r[2];
+    W[2][0] = W[0][2] = r[3];
+    W[2][1] = W[1][2] = r[4];
+    W[2][2] = r[5];
+    const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
+    double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
+    Li[1][0] = -(B * Li[0][0]) / C;
+    Li[2][1] = -(E * Li[1][1]) / F;
+    Li[2][0] = -((D * Li[0][0]) + (E * Li[1][0])) / F;
+    const int ia[6] = {0, 1, 1, 2, 2, 2}, ib[6] = {0, 0, 1, 0, 1, 2};
     for (int k = 0; k < 6; ++k) {
       double x = 0.0;
       for (int c = 0; c < 3; ++c) x += Li[c][ia[k]] * W[c][ib[k]];
       out[k] = x + r[6 + k];
     }
   }
-  return W[0][0] + W[1][1] + W[2][2];
+  return r[0] + r[2] + r[5];
 }
 
 template <int INTEGRATOR>
@@ -1016,13 +1037,14 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
     float thr = half_skin, inv_mcum = 1.0f;
     double mcum = 1.0;
     float wv[6] = {0, 0, 0, 0, 0, 0};
-    double pe = 0.0;
+    bool energy_valid = false;  // atom_energy holds the current forces' energies
     if (!a.forces_valid) {
       if (a.n_steps == 0 && a.virial != nullptr)
-        forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
       else
-        forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
       __syncthreads();
+      energy_valid = true;
     }
     if (INTEGRATOR >= 2 && a.n_steps > 0) {
       float ke = 0.f;
@@ -1105,22 +1127,21 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
       }
       prof_add(prof, 2, t0);
       // ---- forces
-      pe = 0.0;
       if (INTEGRATOR == 3) {
         // the barostat needs the pair virial at every step
 #pragma unroll
         for (int k = 0; k < 6; ++k) wv[k] = 0.f;
-        forces_dispatch<false, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        forces_dispatch<false, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
       } else if ((last && a.virial != nullptr) || trace_v) {
         if (trace_v) {
 #pragma unroll
           for (int k = 0; k < 6; ++k) wv[k] = 0.f;
         }
-        forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
       } else if (want_e) {
-        forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
       } else {
-        forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+        forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
       }
       __syncthreads();
       prof_add(prof, 3, t0);
@@ -1227,21 +1248,20 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
         }
         prof_add(prof, 2, t0);
         // ---- forces at the rescaled positions (the next step's first kick)
-        pe = 0.0;
         if (last && a.virial != nullptr) {
 #pragma unroll
           for (int k = 0; k < 6; ++k) wv[k] = 0.f;
-          forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+          forces_dispatch<true, true>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
         } else if (want_e) {
-          forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+          forces_dispatch<true, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
         } else {
-          forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, &pe, wv);
+          forces_dispatch<false, false>(sm, n, nsp, tpa, nl, rc2, sig2_0, a4_0, wv);
         }
         __syncthreads();
         prof_add(prof, 3, t0);
       }
       if (want_e) {
-        const double pe_tot = block_sum(pe, sm.red);
+        const double pe_tot = atom_energy_sum(sm, n);
         if (tid == 0) {
           if (a.trace_pe) a.trace_pe[(int64_t)step * a.n_systems + s] = pe_tot;
           if (a.trace_ke) a.trace_ke[(int64_t)step * a.n_systems + s] = ke_tot;
@@ -1264,7 +1284,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
         const float4 m = sm.mom[i];
         ke += 0.5f * fmaf(m.z, m.z, fmaf(m.y, m.y, m.x * m.x)) / m.w;
       }
-      const double pe_tot = block_sum(pe, sm.red);
+      const double pe_tot = energy_valid ? atom_energy_sum(sm, n) : 0.0;
       const double ke_tot = block_sum((double)ke, sm.red + 36);
       if (tid == 0) {
         a.energy[s] = pe_tot;
