@@ -118,6 +118,7 @@ struct SysParams {
   float dt, c1, c2;
   float rc, rl;
   double Ld[6];   // the cell in float64 (the barostat scales it)
+  double Lid[9];  // its inverse, row-major 3 x 3, formed by set_inverse64 when Ld changes
   // CSVR (integrators 2, 3) and stochastic cell rescaling (integrator 3), set
   // up in float64 once per system and used in float32 per step
   float csvr_c1, csvr_omc1;  // exp(-dt / tau_T), 1 - exp(-dt / tau_T)
@@ -155,16 +156,19 @@ struct Smem {
 };
 
 
+// Explicit fused multiply-adds: every inlined copy rounds the same way (the compiler would
+// otherwise contract each copy as its context suggests), so wraps, cell indices and the virial
+// sums agree bit for bit wherever they are formed.
 __device__ inline void frac_of(const SysParams &p, float x, float y, float z, float f[3]) {
-  f[0] = (x * p.inv[0] + y * p.inv[1]) + z * p.inv[3];
-  f[1] = y * p.inv[2] + z * p.inv[4];
-  f[2] = z * p.inv[5];
+  f[0] = __fmaf_rn(z, p.inv[3], __fmaf_rn(y, p.inv[1], __fmul_rn(x, p.inv[0])));
+  f[1] = __fmaf_rn(z, p.inv[4], __fmul_rn(y, p.inv[2]));
+  f[2] = __fmul_rn(z, p.inv[5]);
 }
 
 __device__ inline void cart_of(const SysParams &p, const float f[3], float &x, float &y, float &z) {
-  x = (f[0] * p.L[0] + f[1] * p.L[1]) + f[2] * p.L[3];
-  y = f[1] * p.L[2] + f[2] * p.L[4];
-  z = f[2] * p.L[5];
+  x = __fmaf_rn(f[2], p.L[3], __fmaf_rn(f[1], p.L[1], __fmul_rn(f[0], p.L[0])));
+  y = __fmaf_rn(f[2], p.L[4], __fmul_rn(f[1], p.L[2]));
+  z = __fmul_rn(f[2], p.L[5]);
 }
 
 // Wrap into fractional [-0.5, 0.5) by subtracting whole lattice vectors; an
@@ -682,9 +686,9 @@ constexpr uint64_t kSysSeed = 0x6a09e667f3bcc909ull;
 constexpr uint64_t kChiSeed = 0xbb67ae8584caa73bull;
 
 // Block-wide sums of N floats, returned to every thread in float64: each warp
-// adds in float, then warp 0 adds the warp partials in float64 (FP64 issue is
-// scarce on this part, so only 32 x N double additions are made).  Contains
-// two __syncthreads().
+// adds in float, then warp k adds the warp partials of value k in float64 (FP64
+// issue is scarce on this part, so only 32 x N double additions are made, the N
+// sums side by side).  Contains two __syncthreads().
 template <int N>
 __device__ inline void block_sums(const float (&v)[N], Smem &sm, double (&out)[N]) {
   static_assert(N <= 12, "block_sums scratch holds 12 values");
@@ -698,12 +702,10 @@ __device__ inline void block_sums(const float (&v)[N], Smem &sm, double (&out)[N
     if (lane == 0) sm.red_f[k * 32 + wid] = x;
   }
   __syncthreads();
-  if (wid == 0) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      const double x = warp_sum(lane < nw ? (double)sm.red_f[k * 32 + lane] : 0.0);
-      if (lane == 0) sm.red_d[k] = x;
-    }
+  // warp k adds the warp partials of value k in float64 (the N sums run side by side)
+  for (int k = wid; k < N; k += nw) {
+    const double x = warp_sum(lane < nw ? (double)sm.red_f[k * 32 + lane] : 0.0);
+    if (lane == 0) sm.red_d[k] = x;
   }
   __syncthreads();
 #pragma unroll
@@ -893,6 +895,27 @@ __device__ void save_record(const Smem &sm, const kups_md_args &a, const MdWork 
   }
 }
 
+// fw += f (x) F in tril order [xx, yx, yy, zx, zy, zz] (f fractional, F a force), with explicit
+// fused multiply-adds so the per-step record and the launch's final virial round identically
+__device__ __forceinline__ void add_fw(float fw[6], const float f[3], const float4 &F) {
+  fw[0] = __fmaf_rn(f[0], F.x, fw[0]);
+  fw[1] = __fmaf_rn(f[1], F.x, fw[1]);
+  fw[2] = __fmaf_rn(f[1], F.y, fw[2]);
+  fw[3] = __fmaf_rn(f[2], F.x, fw[3]);
+  fw[4] = __fmaf_rn(f[2], F.y, fw[4]);
+  fw[5] = __fmaf_rn(f[2], F.z, fw[5]);
+}
+
+// The float64 inverse of the lower-triangular cell p.Ld (one thread; float64 divisions are slow
+// on this part, so it is formed once per cell, not per step).
+__device__ inline void set_inverse64(SysParams &p) {
+  const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
+  const double i00 = 1.0 / A, i11 = 1.0 / C, i22 = 1.0 / F;
+  const double i10 = -(B * i00) / C, i21 = -(E * i11) / F, i20 = -((D * i00) + (E * i10)) / F;
+  const double Li[9] = {i00, 0.0, 0.0, i10, i11, 0.0, i20, i21, i22};
+  for (int k = 0; k < 9; ++k) p.Lid[k] = Li[k];
+}
+
 // dE/dtril [xx, yx, yy, zx, zy, zz] of a system from block sums r[0..5] of the pair virial
 // W_cb = 1/2 sum d_c g_b (Cartesian, [xx, yx, yy, zx, zy, zz]) and r[6..11] of
 // sum_i f_i,a F_i,b over atoms (f fractional, wrapped; F the force), written by thread 0:
@@ -908,15 +931,10 @@ __device__ double virial_from_sums(const SysParams &p, const double r[12], doubl
     W[2][0] = W[0][2] = r[3];
     W[2][1] = W[1][2] = r[4];
     W[2][2] = r[5];
-    const double A = p.Ld[0], B = p.Ld[1], C = p.Ld[2], D = p.Ld[3], E = p.Ld[4], F = p.Ld[5];
-    double Li[3][3] = {{1.0 / A, 0, 0}, {0, 1.0 / C, 0}, {0, 0, 1.0 / F}};
-    Li[1][0] = -(B * Li[0][0]) / C;
-    Li[2][1] = -(E * Li[1][1]) / F;
-    Li[2][0] = -((D * Li[0][0]) + (E * Li[1][0])) / F;
     const int ia[6] = {0, 1, 1, 2, 2, 2}, ib[6] = {0, 0, 1, 0, 1, 2};
     for (int k = 0; k < 6; ++k) {
       double x = 0.0;
-      for (int c = 0; c < 3; ++c) x += Li[c][ia[k]] * W[c][ib[k]];
+      for (int c = 0; c < 3; ++c) x += p.Lid[3 * c + ia[k]] * W[c][ib[k]];
       out[k] = x + r[6 + k];
     }
   }
@@ -968,6 +986,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
         for (int k = 0; k < 6; ++k) p.Ld[k] = (double)a.tril[6 * (int64_t)s + k];
       }
       for (int k = 0; k < 6; ++k) p.L[k] = (float)p.Ld[k];
+      set_inverse64(p);
       const float rc = a.cutoff[s], skin = a.skin[s], rl = rc + skin;
       p.rc = rc;
       p.rl = rl;
@@ -1161,12 +1180,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
           float4 x = sm.pos[i];
           float fr[3];
           wrap_position(p, x, fr);
-          fwt[0] += fr[0] * f.x;
-          fwt[1] += fr[1] * f.x;
-          fwt[2] += fr[1] * f.y;
-          fwt[3] += fr[2] * f.x;
-          fwt[4] += fr[2] * f.y;
-          fwt[5] += fr[2] * f.z;
+          add_fw(fwt, fr, f);
         }
       }
       if (INTEGRATOR != 3 && trace_v) {
@@ -1208,6 +1222,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
             p.Ld[k] *= mu;
             p.L[k] = (float)p.Ld[k];
           }
+          set_inverse64(p);
           set_cell(p);
           sm.mu = (float)mu;
           sm.work = 0;
@@ -1304,12 +1319,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
       float4 F = sm.frc[i];
       F.w = 0.f;
       gfrc[o] = F;
-      fw[0] += f[0] * F.x;
-      fw[1] += f[1] * F.x;
-      fw[2] += f[1] * F.y;
-      fw[3] += f[2] * F.x;
-      fw[4] += f[2] * F.y;
-      fw[5] += f[2] * F.z;
+      add_fw(fw, f, F);
     }
     if (a.virial != nullptr) {
       const float v[12] = {wv[0], wv[1], wv[2], wv[3], wv[4], wv[5], fw[0], fw[1], fw[2], fw[3], fw[4], fw[5]};
