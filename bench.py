@@ -1087,6 +1087,14 @@ def profile_gcmc(replicas=1024, equil=3000, steps=40):
     ms = _events_ms(torch, lambda: mc.launch(steps))
     mc.check()
     print(f"gcmc: {replicas} replicas, loading {mc.n_mol.float().mean().item():.2f}, {ms / steps * 1e3:.1f} us/step")
+    # phase shares from the kernel's clock counters (a separate launch: the counters add barriers)
+    mc.profile = torch.zeros(6, dtype=torch.int64, device="cuda")
+    mc.launch(steps)
+    mc.check()
+    pr = mc.profile.cpu().double()
+    names = ["proposal", "host atoms", "guests + moved molecule", "phase tables", "k sum", "acceptance + commit"]
+    print("phases: " + " ".join(f"{n}={v / pr.sum():.3f}" for n, v in zip(names, pr.tolist())))
+    mc.profile = None
 
 
 def profile_mlp(train_steps=20, timed_train=200):

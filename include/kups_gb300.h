@@ -666,6 +666,9 @@ typedef struct kups_gcmc_args {
   int32_t block_threads;        /* threads per system's CTA: 64, 128 or 256 (0: 128); the
                                    launch-shape autotuner picks one per workload */
   int32_t pad1;
+  unsigned long long *profile;  /* [6] or NULL: clock cycles of thread 0 summed over all systems
+                                   and steps per phase (proposal, host atoms, guests and the
+                                   moved molecule, phase tables, k sum, acceptance and commit) */
 } kups_gcmc_args;
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);

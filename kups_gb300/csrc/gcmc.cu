@@ -239,6 +239,19 @@ __device__ inline float pair_images(const float L[6], const float fa[3], const f
   return e;
 }
 
+// Optional phase timing (kups_gcmc_args::profile): thread 0 adds the clock cycles since the
+// last mark to counter k; with profiling on, a barrier closes the phase first so a span covers
+// every thread's share of it.
+__device__ __forceinline__ void gcmc_mark(unsigned long long *prof, int k, long long &t0) {
+  if (prof == nullptr) return;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const long long t = clock64();
+    atomicAdd(&prof[k], (unsigned long long)(t - t0));
+    t0 = t;
+  }
+}
+
 __device__ inline double tail_energy(const double *counts, int nsp, const double *coef) {
   // sum_ab coef_ab N_a N_b   (coef = (8/3) pi eps sigma^3 [(sigma/rc)^9/3 - (sigma/rc)^3] / V, masked)
   double e = 0.0;
@@ -345,6 +358,8 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
   }
   const bool learned = a.proposal_node != nullptr;
   double ob[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // thread 0: this launch's U, N, U N, N^2, U^2 sums
+  unsigned long long *prof = a.profile;
+  long long t0 = clock64();
   for (int step = 0; step < a.n_steps; ++step) {
     const uint64_t ctr = a.step0 + (uint64_t)step;
     // ---------------------------------------------------------------- proposal (thread 0)
@@ -496,6 +511,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       mon[tid] = st == 0 ? has_old : has_new;
     }
     __syncthreads();
+    gcmc_mark(prof, 0, t0);
     const int nm = 2 * apm;
     if (min_image) {
       // every axis has one image: the pair is taken at its minimum image, one rounding
@@ -544,6 +560,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
           e_acc += sg * pair_u(r2, __float_as_int(fa.w), tj, mq[m] * qj, lj, nsp, li, ei, alpha, ke, true, true);
         }
       }
+      gcmc_mark(prof, 1, t0);
       // guest atoms (not grouped)
       for (int j = fwn + tid; j < n_other; j += kThreads) {
         float4 pj;
@@ -613,6 +630,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
                                   nsp, li, ei, alpha, ke, true);
     }
     const double de_real = block_sum_f(e_acc, red);
+    gcmc_mark(prof, 2, t0);
     // ---------------------------------------------------------------- reciprocal space
     // per-k terms in float32 (|term| <~ 15 eV: ~1e-6 eV rounding each), the k sum of a
     // thread in float32, the block sum and S(k) itself in float64
@@ -629,6 +647,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       ph[e] = make_float2(cs, sn);
     }
     __syncthreads();
+    gcmc_mark(prof, 3, t0);
     for (int k = tid; k < nk; k += kThreads) {
       const float2 pkk = pk32[k];
       const uint32_t packed = __float_as_uint(pkk.y);
@@ -650,6 +669,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     }
     __syncthreads();
     const double de_rec = block_sum_f(de_rec_f, red) * a.coulomb_k;
+    gcmc_mark(prof, 4, t0);
     // ---------------------------------------------------------------- acceptance (thread 0)
     if (tid == 0) {
       double de = de_real + de_rec;
@@ -777,6 +797,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       }
     }
     __syncthreads();
+    gcmc_mark(prof, 5, t0);
   }
   if (tid == 0 && a.obs_sums != nullptr)
     for (int k = 0; k < 5; ++k) a.obs_sums[5 * (int64_t)s + k] += ob[k];

@@ -339,6 +339,7 @@ class GCMC:
         a.obs_sums = self.obs.data_ptr()
         a.trace = trace.data_ptr() if trace is not None else None
         a.block_threads = int(self.block_threads)
+        a.profile = self.profile.data_ptr() if getattr(self, "profile", None) is not None else None
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid
