@@ -535,6 +535,9 @@ __global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n
                                                        float *loss) {
   __shared__ float red_w[8][kHid];
   __shared__ float red_b[8], red_l[8];
+  // a tile of 32 rows of dz in bfloat16, written out transposed (dzT[col, row]) with consecutive
+  // threads on consecutive rows, so the transposed copy's stores coalesce
+  __shared__ __nv_bfloat16 tile[32][kHid + 8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float wl[8], dw[8];
   for (int j = 0; j < 8; ++j) {
@@ -543,28 +546,41 @@ __global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n
   }
   float db = 0.f, ls = 0.f;
   const float inv_n = 1.f / (float)n;
-  for (int64_t row = (int64_t)blockIdx.x * 8 + warp; row < n; row += (int64_t)gridDim.x * 8) {
-    const float *hr = h + row * kHid;
-    float hv[8], acc = 0.f;
-    for (int j = 0; j < 8; ++j) {
-      hv[j] = hr[lane + 32 * j];
-      acc = fmaf(hv[j], wl[j], acc);
+  for (int64_t r0 = (int64_t)blockIdx.x * 32; r0 < n; r0 += (int64_t)gridDim.x * 32) {
+    for (int k = 0; k < 4; ++k) {  // warp w takes rows r0 + 4 w .. r0 + 4 w + 3
+      const int rl = warp * 4 + k;
+      const int64_t row = r0 + rl;
+      if (row >= n) break;
+      const float *hr = h + row * kHid;
+      float hv[8], acc = 0.f;
+      for (int j = 0; j < 8; ++j) {
+        hv[j] = hr[lane + 32 * j];
+        acc = fmaf(hv[j], wl[j], acc);
+      }
+      const float gg = warp_sum(acc) + b4[0];
+      const float y = label[row];
+      const float dg = (1.f / (1.f + expf(-gg)) - y) * inv_n;
+      if (lane == 0) {
+        ls += y > 0.5f ? softplus(-gg) : softplus(gg);
+        db += dg;
+      }
+      for (int j = 0; j < 8; ++j) {
+        dw[j] = fmaf(dg, hv[j], dw[j]);
+        const float d = dg * wl[j] * -expm1f(-hv[j]);
+        const int col = lane + 32 * j;
+        dz[row * kHid + col] = d;
+        const __nv_bfloat16 db16 = __float2bfloat16(d);
+        dzb[row * kHid + col] = db16;
+        tile[rl][col] = db16;
+      }
     }
-    const float gg = warp_sum(acc) + b4[0];
-    const float y = label[row];
-    const float dg = (1.f / (1.f + expf(-gg)) - y) * inv_n;
-    if (lane == 0) {
-      ls += y > 0.5f ? softplus(-gg) : softplus(gg);
-      db += dg;
+    __syncthreads();
+    const int nr = n - r0 < 32 ? (int)(n - r0) : 32;
+    for (int e = threadIdx.x; e < 32 * kHid; e += blockDim.x) {
+      const int col = e >> 5, rl = e & 31;
+      if (rl < nr) dzT[(int64_t)col * n + r0 + rl] = tile[rl][col];
     }
-    for (int j = 0; j < 8; ++j) {
-      dw[j] = fmaf(dg, hv[j], dw[j]);
-      const float d = dg * wl[j] * -expm1f(-hv[j]);
-      const int col = lane + 32 * j;
-      dz[row * kHid + col] = d;
-      dzb[row * kHid + col] = __float2bfloat16(d);
-      dzT[(int64_t)col * n + row] = __float2bfloat16(d);
-    }
+    __syncthreads();
   }
   for (int j = 0; j < 8; ++j) red_w[warp][lane + 32 * j] = dw[j];
   if (lane == 0) {
@@ -1200,7 +1216,7 @@ extern "C" int32_t kups_mlp_bwd(const kups_mlp *net, const double *x, const floa
   const float *p = net->param;
   float *gr = net->grad;
   const int sms = 148;
-  head_nce_kernel<<<std::min<int64_t>(blocks(n, 8), 4 * sms), 256, 0, st>>>(
+  head_nce_kernel<<<std::min<int64_t>(blocks(n, 32), 4 * sms), 256, 0, st>>>(
       w.h3, n, p + kOffW4, p + kOffB4, label, w.dza, w.dzab, w.dzaT, gr + kOffW4, gr + kOffB4, loss);
   const int split = split_for(n);
   const unsigned cs_blocks = (unsigned)std::min<int64_t>(blocks(n, 64), 2 * sms);
