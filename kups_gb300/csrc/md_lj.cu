@@ -320,10 +320,11 @@ __device__ void sort_by_cell(Smem &sm, int count, int ncell, int *start) {
 // Verlet list.  Returns false (and records the requirement) if a capacity is
 // exceeded.  `scratch` is this CTA's slice of global workspace (permutation
 // staging, 48 bytes per atom).
-// Verlet-list layout: 8-byte units of four uint16 item indices (entries
-// 4u .. 4u + 3 of atom i); unit u of atom i sits at ((u / tpa) * n + i) * tpa
-// + u % tpa, so the tpa lanes serving atom i, and the atoms of a warp, read
-// consecutive units.  The last unit is padded with the far-away sentinel item.
+// Verlet-list layout: 8-byte units of four uint16 item indices; unit u of atom i
+// sits at ((u / tpa) * n + i) * tpa + u % tpa, so the tpa lanes serving atom i, and
+// the atoms of a warp, read consecutive units.  Entry e of atom i is slot (e / tpa) % 4
+// of unit (e / (4 tpa)) * tpa + e % tpa: at each slot the atom's lanes hold consecutive
+// entries.  The last row of 4 tpa entries is padded with the far-away sentinel item.
 __device__ __noinline__ bool rebuild(Smem &sm, const SysParams &p, int n, int tpa, uint2 *nl,
                                      int nb_cap, kups_status *status, int sys_index,
                                      unsigned long long *prof, float4 *scratch) {
@@ -480,15 +481,16 @@ __device__ __noinline__ bool rebuild(Smem &sm, const SysParams &p, int n, int tp
       const int i = mine ? a0 + lane : ab;
       const float4 q = sm.pos[i];
       int cnt = 0;
-      uint32_t buf0 = 0, buf1 = 0;
+      // entry e of atom i: row t = e / (4 tpa) of its list, lane g = e % tpa, slot k of
+      // the lane's 4-entry unit = (e / tpa) % 4, so at each slot the atom's tpa lanes read
+      // tpa consecutive entries (consecutive candidates in cell order: mostly distinct banks)
+      uint16_t *nl16 = reinterpret_cast<uint16_t *>(nl);
+      auto put = [&](int e, uint32_t j) {
+        const int t = e >> (ltpa + 2), g = e & (tpa - 1), k = (e >> ltpa) & 3;
+        nl16[((((size_t)t * n + i) << ltpa) + g) * 4 + k] = (uint16_t)j;
+      };
       auto push = [&](uint32_t j) {
-        const uint32_t sh = (cnt & 1) << 4;
-        if (cnt & 2) buf1 |= j << sh; else buf0 |= j << sh;
-        if ((cnt & 3) == 3) {
-          const int u = cnt >> 2;
-          if (cnt < nb_cap) nl[(((size_t)(u >> ltpa) * n + i) << ltpa) + (u & (tpa - 1))] = make_uint2(buf0, buf1);
-          buf0 = buf1 = 0;
-        }
+        if (cnt < nb_cap) put(cnt, j);
         ++cnt;
       };
       auto scan_range = [&](int kb, int ke) {
@@ -519,7 +521,10 @@ __device__ __noinline__ bool rebuild(Smem &sm, const SysParams &p, int n, int tp
         }
       if (mine) {
         const int total_cnt = cnt;
-        while (cnt & 3) push(sent);  // pad the last unit with the sentinel item
+        // pad the last row with the sentinel item (whole rows of at most nb_cap entries stay
+        // below n * md_units_per_atom units, which rounds nb_cap / 4 up to 16 units)
+        if (cnt <= nb_cap)
+          for (; cnt & (4 * tpa - 1); ++cnt) put(cnt, sent);
         sm.nbr_count[i] = (uint16_t)min(total_cnt, nb_cap);
         my_max = max(my_max, total_cnt);
       }
@@ -626,7 +631,7 @@ __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa
     if (active) {
       const float4 xi = sm.pos[i];
       const int ti = __float_as_int(xi.w);
-      const int nu = (sm.nbr_count[i] + 3) >> 2;  // 4-entry units
+      const int nu = ((sm.nbr_count[i] + 4 * tpa - 1) >> (2 + __ffs(tpa) - 1)) * tpa;  // whole rows of units
       const uint2 *row = nl + (size_t)i * tpa + lane_g;
       int u = lane_g;
       uint2 v0 = make_uint2(0u, 0u), v1 = make_uint2(0u, 0u);
@@ -1384,10 +1389,9 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
   const int threads = a->block_threads > 0 ? a->block_threads : kThreads;
   if (threads % 32 != 0 || threads > kThreads || threads < 64) return KUPS_ERR_INVALID;
   const int lanes = a->min_lanes_per_atom;
-  // at most 4: the list layout strides groups of `tpa` units and neighbor_capacity / 4 is only
-  // guaranteed to be a multiple of 4 (8 or 16 lanes arise only for systems below 256 atoms,
-  // whose lists stay inside the CTA's slice for any capacity)
-  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4) return KUPS_ERR_INVALID;
+  // a power of two up to 16: md_units_per_atom keeps whole rows of tpa units inside the lists
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16)
+    return KUPS_ERR_INVALID;
   kups_md_args args = *a;
   if (args.min_lanes_per_atom == 0) args.min_lanes_per_atom = 2;
   if (a->n_atoms < 0) return KUPS_ERR_INVALID;
