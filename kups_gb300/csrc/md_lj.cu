@@ -563,43 +563,69 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // scratch: no phase between a force evaluation and the sum of its energies sorts anything.
 __device__ inline float *atom_energy(Smem &sm) { return reinterpret_cast<float *>(sm.bin_a); }
 
-// Accumulators of one lane for one atom.
+// 1.0f where a < b, else 0.0f, in one instruction.
+__device__ __forceinline__ float lt_mask(float a, float b) {
+  float m;
+  asm("set.lt.f32.f32 %0, %1, %2;" : "=f"(m) : "f"(a), "f"(b));
+  return m;
+}
+
+// Accumulators of one lane for one atom: forces and energy as pairs (the two list entries a
+// lane evaluates together, added at the end), the virial scalar.
 struct PairAcc {
-  float fx, fy, fz, e;
+  float2 fx, fy, fz, e;
   float w[6];
 };
 
+// Pair constants of one species pair, each held twice for the packed float32x2 arithmetic:
+// sigma^2, -12 (4 eps), 6 (4 eps) and 4 eps.
+struct PairConst {
+  float2 s2, a12n, a6, a;
+};
+
+// Two neighbours j0, j1 of atom i at once with packed float32x2 operations (each lane of a
+// packed operation rounds exactly as the scalar operation).  Per pair: d = x_j - x_i,
+// r2 = |d|^2, c6 = (sigma^2 / r2)^3, and with nfs = c6 (6 a - 12 a c6) / r2 (a = 4 eps):
+// F_i += nfs d, e_i += a (c6^2 - c6) (half of it is the atom's share), W += -(1/2) fs d d.
+// Pairs at r2 >= rc2 contribute exactly zero (their 1 / r2 is masked to zero).
 template <bool ENERGY, bool VIRIAL, bool SINGLE>
-__device__ __forceinline__ void lj_pair(const Smem &sm, const float4 &xi, int ti, int nsp, uint32_t j,
-                                        float rc2, float sig2, float a4, PairAcc &acc) {
-  const float4 xj = sm.pos[j];
-  const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-  float s2c = sig2, ac = a4;
+__device__ __forceinline__ void lj_pair2(const Smem &sm, const float4 &xi, int ti, int nsp, uint32_t j0,
+                                         uint32_t j1, float rc2, const PairConst &pc, PairAcc &acc) {
+  const float4 p0 = sm.pos[j0], p1 = sm.pos[j1];
+  const float2 dx = make_float2(p0.x - xi.x, p1.x - xi.x);
+  const float2 dy = make_float2(p0.y - xi.y, p1.y - xi.y);
+  const float2 dz = make_float2(p0.z - xi.z, p1.z - xi.z);
+  const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+  PairConst c = pc;
   if (!SINGLE) {
-    const float2 c = sm.lj[ti * nsp + __float_as_int(xj.w)];
-    s2c = c.x;
-    ac = c.y;
+    const float2 c0 = sm.lj[ti * nsp + __float_as_int(p0.w)];
+    const float2 c1 = sm.lj[ti * nsp + __float_as_int(p1.w)];
+    c.s2 = make_float2(c0.x, c1.x);
+    c.a12n = make_float2(-12.0f * c0.y, -12.0f * c1.y);
+    c.a6 = make_float2(6.0f * c0.y, 6.0f * c1.y);
+    c.a = make_float2(c0.y, c1.y);
   }
-  const float inv = rcp_approx(r2);
-  const float s2 = s2c * inv;
-  const float c6 = s2 * s2 * s2;
-  // g = dE/dd = -6 (4 eps) c6 (2 c6 - 1) / r2 * d ; F_i = sum_j g
-  float fs = c6 * fmaf(12.0f * ac, c6, -6.0f * ac) * inv;
-  const bool in = r2 < rc2;
-  fs = in ? fs : 0.0f;
-  acc.fx = fmaf(-fs, dx, acc.fx);
-  acc.fy = fmaf(-fs, dy, acc.fy);
-  acc.fz = fmaf(-fs, dz, acc.fz);
-  if (ENERGY) acc.e += in ? ac * fmaf(c6, c6, -c6) : 0.0f;
+  const float2 inv = __fmul2_rn(make_float2(rcp_approx(r2.x), rcp_approx(r2.y)),
+                                make_float2(lt_mask(r2.x, rc2), lt_mask(r2.y, rc2)));
+  const float2 s2 = __fmul2_rn(c.s2, inv);
+  const float2 c6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
+  const float2 nfs = __fmul2_rn(__fmul2_rn(c6, __ffma2_rn(c.a12n, c6, c.a6)), inv);
+  acc.fx = __ffma2_rn(nfs, dx, acc.fx);
+  acc.fy = __ffma2_rn(nfs, dy, acc.fy);
+  acc.fz = __ffma2_rn(nfs, dz, acc.fz);
+  if (ENERGY) acc.e = __fadd2_rn(acc.e, __fmul2_rn(c.a, __ffma2_rn(c6, c6, make_float2(-c6.x, -c6.y))));
   if (VIRIAL) {
-    const float h = -0.5f * fs;  // (1/2) d_c g_b = -(1/2) fs d_c d_b
-    acc.w[0] = fmaf(h * dx, dx, acc.w[0]);
-    acc.w[1] = fmaf(h * dy, dx, acc.w[1]);
-    acc.w[2] = fmaf(h * dy, dy, acc.w[2]);
-    acc.w[3] = fmaf(h * dz, dx, acc.w[3]);
-    acc.w[4] = fmaf(h * dz, dy, acc.w[4]);
-    acc.w[5] = fmaf(h * dz, dz, acc.w[5]);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const float h = 0.5f * (q ? nfs.y : nfs.x);  // (1/2) d_c g_b = -(1/2) fs d_c d_b
+      const float ex = q ? dx.y : dx.x, ey = q ? dy.y : dy.x, ez = q ? dz.y : dz.x;
+      acc.w[0] = fmaf(h * ex, ex, acc.w[0]);
+      acc.w[1] = fmaf(h * ey, ex, acc.w[1]);
+      acc.w[2] = fmaf(h * ey, ey, acc.w[2]);
+      acc.w[3] = fmaf(h * ez, ex, acc.w[3]);
+      acc.w[4] = fmaf(h * ez, ey, acc.w[4]);
+      acc.w[5] = fmaf(h * ez, ez, acc.w[5]);
+    }
   }
 }
 
@@ -609,7 +635,7 @@ __device__ __forceinline__ void lj_pair(const Smem &sm, const float4 &xi, int ti
 // Warps take 32 / tpa atoms at a time from a shared counter (sm.work, zeroed
 // by the caller before the preceding barrier), so uneven neighbour counts do
 // not leave warps idle at the barrier; each lane loads a 4-entry list unit
-// (8 bytes) per iteration, fetched one iteration ahead.
+// (8 bytes) per iteration, fetched one iteration ahead, and evaluates its entries two at a time.
 template <bool ENERGY, bool VIRIAL, bool SINGLE>
 __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa, const uint2 *nl,
                                                float rc2, float sig2, float a4, float wv[6]) {
@@ -617,6 +643,11 @@ __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa
   const int lane_g = lane & (tpa - 1);
   const int per_warp = 32 / tpa;
   const size_t stride = (size_t)n * tpa;
+  PairConst pc;
+  pc.s2 = make_float2(sig2, sig2);
+  pc.a12n = make_float2(-12.0f * a4, -12.0f * a4);
+  pc.a6 = make_float2(6.0f * a4, 6.0f * a4);
+  pc.a = make_float2(a4, a4);
   while (true) {
     int wb = 0;
     if (lane == 0) wb = atomicAdd(&sm.work, per_warp);
@@ -625,7 +656,7 @@ __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa
     const int i = wb + lane / tpa;
     const bool active = i < n;
     PairAcc acc;
-    acc.fx = acc.fy = acc.fz = acc.e = 0.f;
+    acc.fx = acc.fy = acc.fz = acc.e = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 6; ++k) acc.w[k] = 0.f;
     if (active) {
@@ -643,26 +674,25 @@ __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa
         row += stride;
         u += tpa;
         if (u + tpa < nu) v1 = row[stride];
-        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.x & 0xffffu, rc2, sig2, a4, acc);
-        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.x >> 16, rc2, sig2, a4, acc);
-        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.y & 0xffffu, rc2, sig2, a4, acc);
-        lj_pair<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.y >> 16, rc2, sig2, a4, acc);
+        lj_pair2<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.x & 0xffffu, cur.x >> 16, rc2, pc, acc);
+        lj_pair2<ENERGY, VIRIAL, SINGLE>(sm, xi, ti, nsp, cur.y & 0xffffu, cur.y >> 16, rc2, pc, acc);
       }
     }
+    float fx = acc.fx.x + acc.fx.y, fy = acc.fy.x + acc.fy.y, fz = acc.fz.x + acc.fz.y;
     for (int o = tpa >> 1; o > 0; o >>= 1) {
-      acc.fx += __shfl_xor_sync(0xffffffffu, acc.fx, o);
-      acc.fy += __shfl_xor_sync(0xffffffffu, acc.fy, o);
-      acc.fz += __shfl_xor_sync(0xffffffffu, acc.fz, o);
+      fx += __shfl_xor_sync(0xffffffffu, fx, o);
+      fy += __shfl_xor_sync(0xffffffffu, fy, o);
+      fz += __shfl_xor_sync(0xffffffffu, fz, o);
     }
     if (active && lane_g == 0) {
       float4 f = sm.frc[i];
-      f.x = acc.fx;
-      f.y = acc.fy;
-      f.z = acc.fz;
+      f.x = fx;
+      f.y = fy;
+      f.z = fz;
       sm.frc[i] = f;
     }
     if (ENERGY) {  // the atom's pair energy / 2, lanes summed in a fixed order
-      float e = acc.e;
+      float e = acc.e.x + acc.e.y;
       for (int o = tpa >> 1; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
       if (active && lane_g == 0) atom_energy(sm)[i] = 0.5f * e;
     }
