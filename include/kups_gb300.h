@@ -285,6 +285,13 @@ typedef struct kups_md_args {
   double *trace_virial;           /* [n_steps, n_systems, 6] out (may be NULL; integrators 0-2):
                                      dE/dtril after every step, as `virial` holds it after the
                                      last (the reference's potential returns it every step) */
+  int64_t atom_base;              /* added to an atom's packed index where it keys the Langevin
+                                     noise, and */
+  int32_t system_base;            /* to the system index where it keys the thermostat and
+                                     barostat draws: a call on systems [b, b + n_systems) of a
+                                     larger batch (atoms from atom_base) draws the same numbers
+                                     as the whole batch's call (0 for a whole batch) */
+  int32_t pad_base;
 } kups_md_args;
 
 size_t kups_lj_md_workspace_bytes(const kups_md_args *args);

@@ -47,7 +47,8 @@ class MdArgs(C.Structure):
         ("min_lanes_per_atom", C.c_int32), ("reuse_lists", C.c_int32),
         ("thermostat_tau", C.c_void_p), ("target_pressure", C.c_void_p), ("barostat_tau", C.c_void_p),
         ("compressibility", C.c_void_p), ("min_scale", C.c_void_p), ("cell", C.c_void_p),
-        ("trace_virial", C.c_void_p),
+        ("trace_virial", C.c_void_p), ("atom_base", C.c_int64), ("system_base", C.c_int32),
+        ("pad_base", C.c_int32),
     ]
 
 

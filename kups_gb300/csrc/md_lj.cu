@@ -634,8 +634,10 @@ __device__ __forceinline__ void lj_pair2(const Smem &sm, const float4 &xi, int t
 // Cartesian pair virial W_cb = 1/2 sum d_c g_b ([xx, yx, yy, zx, zy, zz]) to wv.
 // Warps take 32 / tpa atoms at a time from a shared counter (sm.work, zeroed
 // by the caller before the preceding barrier), so uneven neighbour counts do
-// not leave warps idle at the barrier; each lane loads a 4-entry list unit
-// (8 bytes) per iteration, fetched one iteration ahead, and evaluates its entries two at a time.
+// not leave warps idle at the barrier; with VIRIAL, warp w takes groups w, w + warps, ... in
+// order instead, so that each thread's virial partial sums (and hence the block's sum) are the
+// same on every run.  Each lane loads a 4-entry list unit (8 bytes) per iteration, fetched
+// one iteration ahead, and evaluates its entries two at a time.
 template <bool ENERGY, bool VIRIAL, bool SINGLE>
 __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa, const uint2 *nl,
                                                float rc2, float sig2, float a4, float wv[6]) {
@@ -648,10 +650,17 @@ __device__ __forceinline__ void compute_forces(Smem &sm, int n, int nsp, int tpa
   pc.a12n = make_float2(-12.0f * a4, -12.0f * a4);
   pc.a6 = make_float2(6.0f * a4, 6.0f * a4);
   pc.a = make_float2(a4, a4);
+  const int n_warps = blockDim.x >> 5;
+  int next = threadIdx.x >> 5;  // static schedule (VIRIAL)
   while (true) {
     int wb = 0;
-    if (lane == 0) wb = atomicAdd(&sm.work, per_warp);
-    wb = __shfl_sync(0xffffffffu, wb, 0);
+    if (VIRIAL) {
+      wb = next * per_warp;
+      next += n_warps;
+    } else {
+      if (lane == 0) wb = atomicAdd(&sm.work, per_warp);
+      wb = __shfl_sync(0xffffffffu, wb, 0);
+    }
     if (wb >= n) break;
     const int i = wb + lane / tpa;
     const bool active = i < n;
@@ -1109,7 +1118,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
       const float kv[1] = {ke};
       double kt[1];
       block_sums<1>(kv, sm, kt);
-      csvr_alpha(sm, kt[0], a.seed, s, a.step0);
+      csvr_alpha(sm, kt[0], a.seed, a.system_base + s, a.step0);
     }
     const bool trace_v = INTEGRATOR != 3 && a.trace_virial != nullptr;
     for (int step = 0; step < a.n_steps && ok; ++step) {
@@ -1142,7 +1151,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
           dy = m.y * sc;
           dz = m.z * sc;
           float eta[4];
-          normal4(a.seed, (uint64_t)(a0 + sm.gid[i]), a.step0 + (uint64_t)step, eta);
+          normal4(a.seed, (uint64_t)(a.atom_base + a0 + sm.gid[i]), a.step0 + (uint64_t)step, eta);
           const float amp = c2 * sqrtf(m.w);
           m.x = fmaf(c1, m.x, amp * eta[0]);
           m.y = fmaf(c1, m.y, amp * eta[1]);
@@ -1250,7 +1259,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
           const float vol = fabsf(p.L[0] * p.L[2] * p.L[5]);
           const float prs = (float)(2.0 * ke_tot - (w6[0] + w6[2] + w6[5])) / (3.0f * vol);
           float z[4];
-          normal4(a.seed ^ kSysSeed, (uint64_t)s, a.step0 + (uint64_t)step, z);
+          normal4(a.seed ^ kSysSeed, (uint64_t)(a.system_base + s), a.step0 + (uint64_t)step, z);
           const float deps = p.scr_a * (prs - p.p0f) + sqrtf(p.scr_b / vol) * z[1];
           const double mu = fmin(fmax(1.0 + (double)expm1f(deps * (1.0f / 3.0f)), p.mumin), p.mumax);
           for (int k = 0; k < 6; ++k) {
@@ -1323,7 +1332,7 @@ md_lj_kernel(kups_md_args a, MdWork w, int *queue, kups_status *status) {
       }
       prof_add(prof, 4, t0);
       if (INTEGRATOR >= 2 && !last) {
-        csvr_alpha(sm, ke_tot, a.seed, s, a.step0 + (uint64_t)step + 1);
+        csvr_alpha(sm, ke_tot, a.seed, a.system_base + s, a.step0 + (uint64_t)step + 1);
         prof_add(prof, 8, t0);
       }
     }
@@ -1424,7 +1433,7 @@ extern "C" int32_t kups_lj_md_run(const kups_md_args *a, void *workspace, size_t
     return KUPS_ERR_INVALID;
   kups_md_args args = *a;
   if (args.min_lanes_per_atom == 0) args.min_lanes_per_atom = 2;
-  if (a->n_atoms < 0) return KUPS_ERR_INVALID;
+  if (a->n_atoms < 0 || a->atom_base < 0 || a->system_base < 0) return KUPS_ERR_INVALID;
   char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~uintptr_t(255));
   int *queue = reinterpret_cast<int *>(base);
   const MdLayout l = md_layout(ctas, a->n_atoms, a->n_systems, a->neighbor_capacity);

@@ -70,6 +70,15 @@ __device__ inline bool mbar_wait(uint32_t addr, uint32_t phase) {
   return false;
 }
 
+// softplus(x) = max(x, 0) + ln(1 + exp(-|x|)) with SFU exp / log (no overflow; the absolute
+// error, a few 1e-8, is far below the bfloat16 rounding that follows)
+__device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + __logf(1.0f + __expf(-fabsf(x))); }
+
+__device__ inline void red_add_v4(float *p, float a, float b, float c, float d) {
+  asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
+               : "memory");
+}
+
 __device__ inline float act_fn(float x, int act) {
   if (act == 1) return fmaxf(x, 0.f);                      // ReLU
   if (act == 2) return x > 20.f ? x : log1pf(__expf(x));  // softplus (SFU exp)
@@ -103,6 +112,8 @@ struct GemmArgs {
   int split_k;        // > 1: blockIdx.z takes a slice of K and atomically adds alpha * partial to C
   void *c3;           // optional third output, bfloat16, its own strides (a transposed copy)
   int64_t sc3r, sc3c;
+  int row_epi;        // set by dispatch_gemm: the register (lane = row) epilogue applies
+  int fast_math;      // softplus and the gates through SFU exp / log (the network's own calls)
 };
 
 __device__ inline void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
@@ -157,7 +168,7 @@ __device__ inline bool fast_operand(const void *p, int is_bf16, int64_t sr, int6
 // the tensor cores work on chunk c; a stage is refilled only after the
 // mbarrier of the MMAs that read it has completed.
 template <int BN>
-__global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, kups_status *status) {
+__global__ void __launch_bounds__(kGemmThreads, 4) gemm_tcgen05_kernel(GemmArgs g, kups_status *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   constexpr int kStageBytes = (kBM + BN) * kBK * 2;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * kStageBytes);  // [2]
@@ -245,6 +256,113 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_tcgen05_kernel(GemmArgs g, 
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (!ok) {
     if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
+  } else if (kc_begin < kc_end && g.row_epi) {
+    // register epilogue (row-major float32 C with 16-byte aligned rows, N a multiple of 32,
+    // beta = 0): warp w reads TMEM lanes 32 (w % 4) .. + 31, so lane l holds row
+    // m0 + 32 (w % 4) + l, 32 columns at a time of the column half w / 4, and applies every
+    // term in registers: 16-byte loads of bias and gate, 16-byte stores of C and of the
+    // bfloat16 copy (c2), vector reductions for split K, and the transposed bfloat16 copy
+    // (c3, element (row, col) at col * sc3c + row) written with lane = row (64 contiguous
+    // bytes per warp instruction).
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = m0 + quarter * 32 + lane;
+    const bool rin = row < g.m;
+    for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
+      uint32_t r[32];
+      const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+          "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const int col0 = n0 + c0;
+      if (col0 >= g.n) continue;  // N is a multiple of 32: the chunk is wholly in or out
+      float v[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = g.alpha * __uint_as_float(r[i]);
+      if (g.split_k > 1) {
+        if (rin) {
+          float *dst = (float *)g.c + (int64_t)row * g.scr + col0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) red_add_v4(dst + 4 * q, v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        }
+        continue;
+      }
+      if (g.bias != nullptr) {
+        const float4 *b4 = reinterpret_cast<const float4 *>(g.bias + col0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float4 b = __ldg(b4 + q);
+          v[4 * q] += b.x;
+          v[4 * q + 1] += b.y;
+          v[4 * q + 2] += b.z;
+          v[4 * q + 3] += b.w;
+        }
+      }
+      if (g.gate_kind != 0 && rin) {
+        const float4 *g4 = reinterpret_cast<const float4 *>(g.gate + (int64_t)row * g.sgr + col0);
+        const int kind = g.gate_kind + (g.fast_math ? 3 : 0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float4 t = g4[q];
+          const float pre[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float x = pre[e];
+            float f;
+            if (kind == 1 || kind == 4) f = x > 0.f ? 1.f : 0.f;
+            else if (kind == 2) f = 1.f / (1.f + expf(-x));
+            else if (kind == 5) f = __frcp_rn(1.f + __expf(-x));
+            else if (kind == 3) f = -expm1f(-x);
+            else f = 1.f - __expf(-x);
+            v[4 * q + e] *= f;
+          }
+        }
+      }
+      if (g.act == 1) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.f);
+      } else if (g.act == 2) {
+        if (g.fast_math) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = softplus_fast(v[i]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = act_fn(v[i], 2);
+        }
+      }
+      if (rin) {
+        float4 *cp = reinterpret_cast<float4 *>((float *)g.c + (int64_t)row * g.scr + col0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) cp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        if (g.c2 != nullptr) {
+          uint4 *c2p = reinterpret_cast<uint4 *>((__nv_bfloat16 *)g.c2 + (int64_t)row * g.sc2r + col0);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            uint4 u;
+            uint32_t *w = reinterpret_cast<uint32_t *>(&u);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 h = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
+              w[e] = *reinterpret_cast<const uint32_t *>(&h);
+            }
+            c2p[q] = u;
+          }
+        }
+        if (g.c3 != nullptr) {
+          __nv_bfloat16 *c3p = (__nv_bfloat16 *)g.c3 + (int64_t)col0 * g.sc3c + row;
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            *c3p = __float2bfloat16(v[i]);
+            c3p += g.sc3c;
+          }
+        }
+      }
+    }
   } else if (kc_begin < kc_end) {  // an empty K slice holds no accumulator
     // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) and the column half
     // w / 4, 32 columns at a time, into a padded 32 x 33 shared-memory block.  The
@@ -338,7 +456,24 @@ int32_t launch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t stream)
 // Tile width: 128 (64 for N <= 64), narrowed to 64 while the grid would leave SMs idle
 // (fewer than two CTAs per SM of 148).  128-wide tiles (64 KB of pipeline buffers, three
 // CTAs per SM) beat 256-wide ones (two CTAs per SM) on the network's K <= 256 GEMMs.
-int32_t dispatch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t st) {
+// Whether the register epilogue of gemm_tcgen05_kernel applies: float32 C (and the optional
+// bias, gate and bfloat16 copy) row-major with unit column stride and 16-byte aligned rows,
+// N a multiple of 32, no beta term; the transposed copy (c3) with unit row stride.
+bool row_epilogue(const GemmArgs &g) {
+  auto al16 = [](const void *q) { return (((uintptr_t)q) & 15) == 0; };
+  if (g.c_bf16 || g.scc != 1 || g.scr % 4 != 0 || !al16(g.c) || g.n % 32 != 0) return false;
+  if (g.split_k > 1) return true;  // alpha * partial added into C
+  if (g.beta != 0.f) return false;
+  if (g.bias != nullptr && !al16(g.bias)) return false;
+  if (g.gate_kind != 0 && (g.sgc != 1 || g.sgr % 4 != 0 || !al16(g.gate))) return false;
+  if (g.c2 != nullptr && (!g.c2_bf16 || g.sc2c != 1 || g.sc2r % 8 != 0 || !al16(g.c2))) return false;
+  if (g.c3 != nullptr && g.sc3r != 1) return false;
+  return true;
+}
+
+int32_t dispatch_gemm(const GemmArgs &g0, kups_status *status, cudaStream_t st) {
+  GemmArgs g = g0;
+  g.row_epi = row_epilogue(g) ? 1 : 0;
   const int64_t rows = ((int64_t)g.m + kBM - 1) / kBM * g.split_k;
   int bn = g.n <= 64 ? 64 : 128;
   while (bn > 64 && rows * ((g.n + bn - 1) / bn) < 2 * 148) bn >>= 1;
@@ -367,6 +502,7 @@ int32_t gemm_call(Op a, Op b, void *c, int64_t scr, int64_t scc, void *c2, const
   g.m = m; g.n = n; g.k = k; g.alpha = 1.f; g.beta = beta; g.act = act;
   g.a_bf16 = a.bf16; g.b_bf16 = b.bf16; g.c_bf16 = 0; g.c2_bf16 = 1; g.gate_kind = gate_kind;
   g.split_k = split;
+  g.fast_math = 1;
   return dispatch_gemm(g, status, st);
 }
 
@@ -866,9 +1002,6 @@ __global__ void proposal_density_kernel(const float *node, const double *cdf, in
 // waits (bounded) for its own copies, frees its tensor memory and returns.
 constexpr int kFwdThreads = 512, kFwdRows = 256, kFwdHalf = 128, kFwdKc = 64;
 
-// softplus(x) = max(x, 0) + ln(1 + exp(-|x|)) with SFU exp / log (no overflow; the absolute
-// error, a few 1e-8, is far below the bfloat16 rounding that follows)
-__device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + __logf(1.0f + __expf(-fabsf(x))); }
 constexpr size_t kFwdA = (size_t)kFwdRows * kHid * 2;           // 128 KB: A operand, K up to 256
 constexpr size_t kFwdStage = (size_t)kHid * kFwdKc * 2;          // 32 KB: one weight chunk
 // shared memory: A operand | two weight stages | head partials [4][256] | coordinates [6][256] |
@@ -1174,6 +1307,7 @@ extern "C" int32_t kups_gemm_bf16(const void *a, int32_t a_bf16, int64_t sa_row,
   g.split_k = split_k;
   g.c3 = nullptr;
   g.sc3r = g.sc3c = 0;
+  g.fast_math = 0;
   return dispatch_gemm(g, status, (cudaStream_t)stream);
 }
 

@@ -97,6 +97,7 @@ class PackedMD:
     n_species: int
     max_atoms: int
     max_density: float
+    max_range: float = 0.0  # largest cutoff + skin of the batch (host copy: no device read per launch)
     forces_valid: bool = False
     energy: torch.Tensor | None = None
     kinetic: torch.Tensor | None = None
@@ -207,13 +208,15 @@ def pack(state: MDState, reuse: PackedMD | None = None) -> PackedMD:
     dens = float((counts.to(torch.float64) / vol).max()) if s > 0 else 0.0
     kT = torch.as_tensor(sy.temperature, dtype=torch.float64).to(dev) * BOLTZMANN_CONSTANT
     f64 = lambda x: None if x is None else torch.as_tensor(x, dtype=torch.float64).to(dev).reshape(-1).expand(s).contiguous()
+    cutoff32, skin32 = f32(state.lj_parameters.cutoff), f32(state.skin)
+    rmax = float((cutoff32 + skin32).max()) if s > 0 else 0.0
     return PackedMD(
         pos4=pos4, mom4=mom4, frc4=frc4, perm=perm32, sys_offset=sys_offset.to(torch.int32).contiguous(),
         order=order.to(torch.int32).contiguous(), tril32=tril.to(torch.float32).contiguous(),
-        cutoff=f32(state.lj_parameters.cutoff), skin=f32(state.skin), dt=f32(sy.time_step), kT=f32(kT),
+        cutoff=cutoff32, skin=skin32, dt=f32(sy.time_step), kT=f32(kT),
         friction=f32(sy.friction_coefficient), lj_table=lj_table(state.lj_parameters),
         n_species=int(state.lj_parameters.sigma.shape[0]), max_atoms=int(counts.max()) if s > 0 else 0,
-        max_density=dens, forces_valid=p.forces is not None, cell=tril.clone().contiguous(),
+        max_density=dens, max_range=rmax, forces_valid=p.forces is not None, cell=tril.clone().contiguous(),
         thermostat_tau=f64(sy.thermostat_time_constant), target_pressure=f64(sy.target_pressure),
         barostat_tau=f64(sy.pressure_coupling_time), compressibility=f64(sy.compressibility),
         min_scale=f64(sy.minimum_scale_factor), layout_key=key,
@@ -251,6 +254,26 @@ def key_to_seed(key) -> int:
 
 
 @dataclass
+class _HostRun:
+    """What ``FusedLennardJonesMD.propagate_host`` keeps between calls on one layout: the runs
+    of whole systems (atom range, system range), a propagator per run, the runs' static
+    device arrays (the same objects every call, so each run's packed layout is reused), the
+    device buffers the host arrays are copied through, the copy stream and a second compute
+    stream."""
+
+    key: tuple
+    chunks: int
+    n: int
+    bounds: list
+    props: list
+    static: list
+    dev: list
+    forces_host: torch.Tensor | None
+    stream: torch.cuda.Stream  # host <-> device copies
+    side: torch.cuda.Stream  # the second compute stream (odd runs)
+
+
+@dataclass
 class FusedLennardJonesMD:
     """Propagator: ``steps_per_call`` VV or BAOAB steps of LJ dynamics per call."""
 
@@ -261,8 +284,11 @@ class FusedLennardJonesMD:
     block_threads: int = 0
     min_lanes_per_atom: int = 0  # 0: library default; kups_gb300.autotune picks one per workload
     reuse_lists: bool = True  # resume systems whose workspace record matches the input (kups_md_args.reuse_lists)
+    atom_base: int = 0  # global index of the first atom / system of this batch: the random streams
+    system_base: int = 0  # are keyed by global indices (kups_md_args.atom_base / system_base)
     _ws: torch.Tensor | None = field(default=None, repr=False)
     _last: PackedMD | None = field(default=None, repr=False)
+    _host: "_HostRun | None" = field(default=None, repr=False)
 
     def __call__(self, key, state: MDState) -> MDState:
         # the previous call's layout is reused while the state's system, cell and parameter
@@ -273,10 +299,155 @@ class FusedLennardJonesMD:
         out = unpack(packed, state, INTEGRATORS[self.integrator])
         return replace(out, step=state.step + self.steps_per_call)
 
+    def propagate_host(self, key, state: MDState, chunks: int = 4) -> MDState:
+        """``__call__`` for a state whose positions, momenta and forces live in host memory
+        (pinned, for the copies to overlap): those arrays are updated in place and returned in
+        the new state, with the per-system outputs (energies, virial, pressure, the NPT cell)
+        on the device.  When the particle table is grouped by system (non-decreasing
+        ``system``), the batch is cut into ``chunks`` runs of whole systems of about equal atom
+        counts, each with its own propagator, packed layout and workspace; the host-to-device
+        copies of every run are queued at once on a copy stream, each run's launch waits only
+        for its own inputs, and its results go back to the host while the next run computes.
+        The random streams are keyed by the global atom and system index (``atom_base``,
+        ``system_base``), so the result equals ``__call__`` on the same state bit for bit.
+        Consecutive runs alternate between two compute streams, so a run's launch fills the SMs
+        that the previous run's last systems leave idle.
+        Static arrays (masses, species, system index, the system table) may live on the host
+        or the device; keeping the same objects between calls keeps the packed layouts and the
+        resumable Verlet lists.  Returns after the results are in host memory and every run's
+        status is checked (capacity overflows are retried run by run, as ``run_packed`` does)."""
+        p = state.particles
+        if p.positions.is_cuda or p.momenta.is_cuda or (p.forces is not None and p.forces.is_cuda):
+            raise ValueError("propagate_host takes positions, momenta and forces in host memory")
+        run = self._host_run(state, int(chunks))
+        seed, step0, integ = key_to_seed(key), state.step, INTEGRATORS[self.integrator]
+        comp, copy = torch.cuda.current_stream(), run.stream
+        have_f = p.forces is not None
+        if not have_f and (run.forces_host is None or run.forces_host.shape != p.positions.shape):
+            run.forces_host = torch.zeros(p.positions.shape, dtype=torch.float64).pin_memory()
+        frc_h = p.forces if have_f else run.forces_host
+        ev_in = []
+        with torch.cuda.stream(copy):
+            copy.wait_stream(comp)  # the device buffers of the previous call are free
+            for (a0, a1, _, _), (dp, dm, df) in zip(run.bounds, run.dev):
+                dp.copy_(p.positions[a0:a1], non_blocking=True)
+                dm.copy_(p.momenta[a0:a1], non_blocking=True)
+                if have_f:
+                    df.copy_(p.forces[a0:a1], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(copy)
+                ev_in.append(ev)
+        done = []
+        # consecutive runs alternate between two compute streams: the next run's CTAs take the
+        # SMs the previous run's last systems leave idle (each run is one persistent launch)
+        streams = (comp, run.side)
+        run.side.wait_stream(comp)
+        for k, ((a0, a1, _, _), (dp, dm, df), sub, stat) in enumerate(zip(run.bounds, run.dev, run.props, run.static)):
+            self._sync_settings(sub)
+            with torch.cuda.stream(streams[k % 2]):
+                torch.cuda.current_stream().wait_event(ev_in[k])
+                st_k = MDState(MDParticles(dp, dm, stat[0], stat[1], stat[2], df if have_f else None), stat[3],
+                               state.lj_parameters, skin=state.skin, step=step0)
+                packed = pack(st_k, reuse=sub._last)
+                sub._last = packed
+                backup, valid0 = packed.clone_dynamic(), packed.forces_valid
+                status = sub.launch(packed, self.steps_per_call, seed, step0)
+                out = unpack(packed, st_k, integ)
+                self._to_host(run, out, p.positions, p.momenta, frc_h, a0, a1)
+            done.append([packed, backup, valid0, status, st_k, out])
+        comp.wait_stream(run.side)
+        comp.wait_stream(copy)
+        comp.synchronize()
+        for k, (packed, backup, valid0, status, st_k, out) in enumerate(done):
+            code = read_status(status)
+            if code.code == _lib.KUPS_OK:
+                continue
+            if code.code != _lib.KUPS_ERR_CAPACITY or code.detail != _lib.KUPS_CAP_NEIGHBORS:
+                _lib.raise_status(code)
+            sub, (a0, a1, _, _) = run.props[k], run.bounds[k]
+            packed.restore_dynamic(backup)
+            packed.forces_valid = valid0
+            sub.neighbor_capacity = int(math.ceil(code.required * 1.25 / 16.0) * 16)
+            sub.run_packed(packed, self.steps_per_call, seed, step0)
+            out = unpack(packed, st_k, integ)
+            self._to_host(run, out, p.positions, p.momenta, frc_h, a0, a1)
+            comp.wait_stream(copy)
+            comp.synchronize()
+            done[k][5] = out
+        cat = lambda xs: None if any(x is None for x in xs) else torch.cat(xs)
+        outs = [d[5].systems for d in done]
+        systems = replace(state.systems, potential_energy=cat([o.potential_energy for o in outs]),
+                          kinetic_energy=cat([o.kinetic_energy for o in outs]),
+                          unitcell_gradients=cat([o.unitcell_gradients for o in outs]),
+                          pressure=cat([o.pressure for o in outs]))
+        if integ == INTEGRATORS["csvr_npt"]:
+            systems = replace(systems, tril=torch.cat([o.tril for o in outs]))
+        return replace(state, particles=replace(p, forces=frc_h), systems=systems,
+                       step=step0 + self.steps_per_call)
+
+    @staticmethod
+    def _to_host(run, out: MDState, pos_h, mom_h, frc_h, a0: int, a1: int) -> None:
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream())
+        with torch.cuda.stream(run.stream):
+            run.stream.wait_event(ev)
+            for t, h in ((out.particles.positions, pos_h), (out.particles.momenta, mom_h),
+                         (out.particles.forces, frc_h)):
+                t.record_stream(run.stream)
+                h[a0:a1].copy_(t, non_blocking=True)
+
+    def _sync_settings(self, sub: "FusedLennardJonesMD") -> None:
+        sub.integrator, sub.steps_per_call = self.integrator, self.steps_per_call
+        sub.n_ctas, sub.block_threads = self.n_ctas, self.block_threads
+        sub.min_lanes_per_atom, sub.reuse_lists = self.min_lanes_per_atom, self.reuse_lists
+        if self.neighbor_capacity is not None:
+            sub.neighbor_capacity = self.neighbor_capacity
+
+    def _host_run(self, state: MDState, chunks: int) -> "_HostRun":
+        key = _layout_key(state)
+        p, sy = state.particles, state.systems
+        n, s = int(p.positions.shape[0]), int(sy.tril.shape[0])
+        run = self._host
+        if run is not None and run.chunks == chunks and run.n == n and _same_key(run.key, key):
+            return run
+        system = p.system.to("cpu", torch.int64)
+        counts = torch.bincount(system, minlength=s) if n else torch.zeros(s, dtype=torch.int64)
+        offs = [0] + torch.cumsum(counts, 0).tolist()
+        grouped = n == 0 or bool((system[1:] >= system[:-1]).all())
+        cuts = [0]
+        if grouped and chunks > 1:
+            for k in range(1, chunks):
+                target = k * n / chunks
+                c = min(range(cuts[-1] + 1, s), key=lambda j: abs(offs[j] - target), default=s)
+                if c > cuts[-1] and c < s:
+                    cuts.append(c)
+        cuts.append(s)
+        bounds = [(offs[s0], offs[s1], s0, s1) for s0, s1 in zip(cuts[:-1], cuts[1:])]
+        dev = "cuda"
+        masses, species = p.masses.to(dev), p.species.to(dev)
+        system_d = p.system.to(dev)
+        old = {(b[0], b[2]): q for b, q in zip(run.bounds, run.props)} if run is not None else {}
+        props, static, bufs = [], [], []
+        for a0, a1, s0, s1 in bounds:
+            sub = old.get((a0, s0)) or FusedLennardJonesMD(atom_base=a0, system_base=s0)
+            sub.atom_base, sub.system_base = a0, s0
+            props.append(sub)
+            cut = lambda x: x[s0:s1] if isinstance(x, torch.Tensor) and x.dim() > 0 and x.shape[0] == s else x
+            sys_k = MDSystems(**{f: (cut(getattr(sy, f)).to(dev) if isinstance(getattr(sy, f), torch.Tensor)
+                                     else getattr(sy, f)) for f in sy.__dataclass_fields__})
+            static.append((masses[a0:a1], species[a0:a1], (system_d[a0:a1] - s0), sys_k))
+            bufs.append(tuple(torch.empty((a1 - a0, 3), device=dev, dtype=torch.float64) for _ in range(3)))
+        stream = run.stream if run is not None else torch.cuda.Stream()
+        side = run.side if run is not None else torch.cuda.Stream()
+        fh = run.forces_host if run is not None else None
+        self._host = _HostRun(key=key, chunks=chunks, n=n, bounds=bounds, props=props, static=static, dev=bufs,
+                              forces_host=fh, stream=stream, side=side)
+        return self._host
+
     def capacity_for(self, packed: PackedMD) -> int:
         if self.neighbor_capacity is not None:
             return self.neighbor_capacity
-        rl = float((packed.cutoff + packed.skin).max())
+        rl = packed.max_range if packed.max_range > 0 else float((packed.cutoff + packed.skin).max())
         est = 4.0 / 3.0 * math.pi * rl**3 * packed.max_density * 1.35 + 16
         return int(math.ceil(est / 16.0) * 16)
 
@@ -310,6 +481,7 @@ class FusedLennardJonesMD:
         a.n_ctas, a.block_threads = self.n_ctas, self.block_threads
         a.min_lanes_per_atom = self.min_lanes_per_atom
         a.reuse_lists = int(bool(self.reuse_lists))
+        a.atom_base, a.system_base = int(self.atom_base), int(self.system_base)
         if a.integrator >= 2:
             need = ["thermostat_tau"] + (["target_pressure", "barostat_tau", "compressibility", "min_scale"]
                                          if a.integrator == 3 else [])

@@ -165,3 +165,22 @@ def test_csvr_ideal_gas_kinetic_energy_is_canonical():
     # Var(K) / <K>^2 = 2 / N_dof for a Gamma(N_dof / 2) law
     z = (tke.cpu().numpy()[50::10] / (0.5 * dof * kt) - 1) / np.sqrt(2.0 / dof)
     assert abs(z.reshape(-1).var() - 1) < 0.1, z.var()
+
+
+def test_npt_cell_and_virial_are_the_same_on_every_run():
+    """The barostat reads the pair virial every step; the force pass that forms it takes its atom
+    groups in a fixed order, so cells, positions and dE/dtril repeat bit for bit."""
+    from kups_gb300 import md
+
+    W = workload(n_systems=8, n_max=900, seed=12)
+    dt = W.time_step[0]
+    runs = []
+    for _ in range(2):
+        prop = md.make_csvr_npt_step(steps_per_call=20)
+        out = prop(3, state_of(W, tau_t=20 * dt, p0=np.zeros(W.n_systems), tau_p=10 * dt, beta=1e-4))
+        runs.append([out.systems.tril.cpu().numpy(), out.particles.positions.cpu().numpy(),
+                     out.systems.unitcell_gradients.cpu().numpy()])
+    diag = [0, 2, 5]
+    assert np.abs(runs[0][0][:, diag] / W.tril[:, diag] - 1).max() > 1e-7  # the cells moved
+    for x, y in zip(*runs):
+        np.testing.assert_array_equal(x, y)
