@@ -15,7 +15,9 @@
 // the accumulator back with tcgen05.ld.32x32b.  Every mbarrier wait is
 // bounded; on time-out the kernel records KUPS_ERR_UNSUPPORTED, frees its
 // tensor memory and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 
@@ -164,6 +166,116 @@ __device__ inline bool fast_operand(const void *p, int is_bf16, int64_t sr, int6
   return is_bf16 && sc == 1 && (sr % 8) == 0 && (k % 8) == 0 && (((uintptr_t)p) & 15) == 0;
 }
 
+// Register epilogue of a 128 x BN accumulator tile in tensor memory (row-major float32 C with
+// 16-byte aligned rows, N a multiple of 32, beta = 0 or split K): warp w reads TMEM lanes
+// 32 (w % 4) .. + 31, so lane l holds row m0 + 32 (w % 4) + l, 32 columns at a time of the
+// column half w / 4, and applies every term in registers: 16-byte loads of bias and gate,
+// 16-byte stores of C and of the bfloat16 copy (c2), vector reductions for split K, and the
+// transposed bfloat16 copy (c3, element (row, col) at col * sc3c + row) written with
+// lane = row (64 contiguous bytes per warp instruction).
+template <int BN>
+__device__ inline void register_epilogue(const GemmArgs &g, uint32_t tmem, int m0, int n0, int warp, int lane) {
+  const int quarter = warp & 3, half = warp >> 2;
+  const int row = m0 + quarter * 32 + lane;
+  const bool rin = row < g.m;
+  for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
+    uint32_t r[32];
+    const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const int col0 = n0 + c0;
+    if (col0 >= g.n) continue;  // N is a multiple of 32: the chunk is wholly in or out
+    float v[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = g.alpha * __uint_as_float(r[i]);
+    if (g.split_k > 1) {
+      if (rin) {
+        float *dst = (float *)g.c + (int64_t)row * g.scr + col0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) red_add_v4(dst + 4 * q, v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
+      continue;
+    }
+    if (g.bias != nullptr) {
+      const float4 *b4 = reinterpret_cast<const float4 *>(g.bias + col0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float4 b = __ldg(b4 + q);
+        v[4 * q] += b.x;
+        v[4 * q + 1] += b.y;
+        v[4 * q + 2] += b.z;
+        v[4 * q + 3] += b.w;
+      }
+    }
+    if (g.gate_kind != 0 && rin) {
+      const float4 *g4 = reinterpret_cast<const float4 *>(g.gate + (int64_t)row * g.sgr + col0);
+      const int kind = g.gate_kind + (g.fast_math ? 3 : 0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float4 t = g4[q];
+        const float pre[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float x = pre[e];
+          float f;
+          if (kind == 1 || kind == 4) f = x > 0.f ? 1.f : 0.f;
+          else if (kind == 2) f = 1.f / (1.f + expf(-x));
+          else if (kind == 5) f = __frcp_rn(1.f + __expf(-x));
+          else if (kind == 3) f = -expm1f(-x);
+          else f = 1.f - __expf(-x);
+          v[4 * q + e] *= f;
+        }
+      }
+    }
+    if (g.act == 1) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.f);
+    } else if (g.act == 2) {
+      if (g.fast_math) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = softplus_fast(v[i]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = act_fn(v[i], 2);
+      }
+    }
+    if (rin) {
+      float4 *cp = reinterpret_cast<float4 *>((float *)g.c + (int64_t)row * g.scr + col0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) cp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      if (g.c2 != nullptr) {
+        uint4 *c2p = reinterpret_cast<uint4 *>((__nv_bfloat16 *)g.c2 + (int64_t)row * g.sc2r + col0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          uint4 u;
+          uint32_t *w = reinterpret_cast<uint32_t *>(&u);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
+            w[e] = *reinterpret_cast<const uint32_t *>(&h);
+          }
+          c2p[q] = u;
+        }
+      }
+      if (g.c3 != nullptr) {
+        __nv_bfloat16 *c3p = (__nv_bfloat16 *)g.c3 + (int64_t)col0 * g.sc3c + row;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          *c3p = __float2bfloat16(v[i]);
+          c3p += g.sc3c;
+        }
+      }
+    }
+  }
+}
+
 // Two-stage pipeline: the 16-byte copies of K chunk c + 1 are in flight while
 // the tensor cores work on chunk c; a stage is refilled only after the
 // mbarrier of the MMAs that read it has completed.
@@ -257,112 +369,7 @@ __global__ void __launch_bounds__(kGemmThreads, 4) gemm_tcgen05_kernel(GemmArgs 
   if (!ok) {
     if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
   } else if (kc_begin < kc_end && g.row_epi) {
-    // register epilogue (row-major float32 C with 16-byte aligned rows, N a multiple of 32,
-    // beta = 0): warp w reads TMEM lanes 32 (w % 4) .. + 31, so lane l holds row
-    // m0 + 32 (w % 4) + l, 32 columns at a time of the column half w / 4, and applies every
-    // term in registers: 16-byte loads of bias and gate, 16-byte stores of C and of the
-    // bfloat16 copy (c2), vector reductions for split K, and the transposed bfloat16 copy
-    // (c3, element (row, col) at col * sc3c + row) written with lane = row (64 contiguous
-    // bytes per warp instruction).
-    const int quarter = warp & 3, half = warp >> 2;
-    const int row = m0 + quarter * 32 + lane;
-    const bool rin = row < g.m;
-    for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
-      uint32_t r[32];
-      const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-          "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      const int col0 = n0 + c0;
-      if (col0 >= g.n) continue;  // N is a multiple of 32: the chunk is wholly in or out
-      float v[32];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = g.alpha * __uint_as_float(r[i]);
-      if (g.split_k > 1) {
-        if (rin) {
-          float *dst = (float *)g.c + (int64_t)row * g.scr + col0;
-#pragma unroll
-          for (int q = 0; q < 8; ++q) red_add_v4(dst + 4 * q, v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-        }
-        continue;
-      }
-      if (g.bias != nullptr) {
-        const float4 *b4 = reinterpret_cast<const float4 *>(g.bias + col0);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float4 b = __ldg(b4 + q);
-          v[4 * q] += b.x;
-          v[4 * q + 1] += b.y;
-          v[4 * q + 2] += b.z;
-          v[4 * q + 3] += b.w;
-        }
-      }
-      if (g.gate_kind != 0 && rin) {
-        const float4 *g4 = reinterpret_cast<const float4 *>(g.gate + (int64_t)row * g.sgr + col0);
-        const int kind = g.gate_kind + (g.fast_math ? 3 : 0);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float4 t = g4[q];
-          const float pre[4] = {t.x, t.y, t.z, t.w};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float x = pre[e];
-            float f;
-            if (kind == 1 || kind == 4) f = x > 0.f ? 1.f : 0.f;
-            else if (kind == 2) f = 1.f / (1.f + expf(-x));
-            else if (kind == 5) f = __frcp_rn(1.f + __expf(-x));
-            else if (kind == 3) f = -expm1f(-x);
-            else f = 1.f - __expf(-x);
-            v[4 * q + e] *= f;
-          }
-        }
-      }
-      if (g.act == 1) {
-#pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.f);
-      } else if (g.act == 2) {
-        if (g.fast_math) {
-#pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] = softplus_fast(v[i]);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] = act_fn(v[i], 2);
-        }
-      }
-      if (rin) {
-        float4 *cp = reinterpret_cast<float4 *>((float *)g.c + (int64_t)row * g.scr + col0);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) cp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-        if (g.c2 != nullptr) {
-          uint4 *c2p = reinterpret_cast<uint4 *>((__nv_bfloat16 *)g.c2 + (int64_t)row * g.sc2r + col0);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            uint4 u;
-            uint32_t *w = reinterpret_cast<uint32_t *>(&u);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const __nv_bfloat162 h = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
-              w[e] = *reinterpret_cast<const uint32_t *>(&h);
-            }
-            c2p[q] = u;
-          }
-        }
-        if (g.c3 != nullptr) {
-          __nv_bfloat16 *c3p = (__nv_bfloat16 *)g.c3 + (int64_t)col0 * g.sc3c + row;
-#pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            *c3p = __float2bfloat16(v[i]);
-            c3p += g.sc3c;
-          }
-        }
-      }
-    }
+    register_epilogue<BN>(g, tmem, m0, n0, warp, lane);
   } else if (kc_begin < kc_end) {  // an empty K slice holds no accumulator
     // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) and the column half
     // w / 4, 32 columns at a time, into a padded 32 x 33 shared-memory block.  The
@@ -453,6 +460,191 @@ int32_t launch_gemm(const GemmArgs &g, kups_status *status, cudaStream_t stream)
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------------------
+// TMA-fed variant for bfloat16 operands with K contiguous (every GEMM of the network's
+// training step): one thread issues cp.async.bulk.tensor loads of 64-wide K chunks (128-byte
+// rows, 128-byte swizzle) into a ring of STAGES stages, each completing on its mbarrier, and
+// the MMAs of a chunk as soon as it has landed; the ring holds the whole K extent of the
+// network's GEMMs (K <= 256), so every load of a tile is in flight at once.  A stage is
+// refilled only after the commit of the MMAs that read it.  The other threads wait at the
+// block barrier, then all run the register epilogue.  Every wait is bounded; on time-out the
+// thread waits (bounded) for the loads and MMAs it issued, records KUPS_ERR_UNSUPPORTED, and
+// the tile frees its tensor memory without writing C.
+
+// Shared-memory matrix descriptor, K-major with 128-byte swizzle: 8-row groups of 128-byte
+// rows 1024 bytes apart (stride byte offset), leading byte offset unused (1), version 1,
+// layout type 2 (128-byte swizzle) in [61, 64).  The tile base is 1024-byte aligned; a K step
+// of 16 elements advances the start address by 32 bytes.
+__device__ inline uint64_t make_sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+__device__ inline void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// 2-D tiled load of the box at (x = c0 along K, y = c1 along rows) into shared memory.
+__device__ inline void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(mbar)
+      : "memory");
+}
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    gemm_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmArgs g,
+                    kups_status *status) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                          ~uintptr_t(1023));
+  constexpr uint32_t kABytes = kBM * kBK * 2, kBBytes = BN * kBK * 2, kStage = kABytes + kBBytes;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * kStage);  // [STAGES]: chunk landed
+  uint64_t *freed = full + STAGES;                                        // [STAGES]: its MMAs done
+  uint64_t *done = freed + STAGES;                                        // every MMA of the tile done
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  int *ok_flag = reinterpret_cast<int *>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"((uint32_t)BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int st = 0; st < STAGES; ++st) {
+      mbar_init(smem_u32(&full[st]), 1);
+      mbar_init(smem_u32(&freed[st]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    *ok_flag = 1;
+  }
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const int nk_all = (g.k + kBK - 1) / kBK;
+  const int per_split = (nk_all + g.split_k - 1) / g.split_k;
+  const int kc_begin = blockIdx.z * per_split;
+  const int kc_end = min(nk_all, kc_begin + per_split);
+  const int nk = max(0, kc_end - kc_begin);
+  if (tid == 0) {
+    const uint32_t idesc = make_idesc(kBM, BN);
+    auto sa = [&](int st) { return smem_u32(smem + st * kStage); };
+    auto sb = [&](int st) { return smem_u32(smem + st * kStage + kABytes); };
+    auto load = [&](int j) {  // chunk j of this tile's K range into stage j % STAGES
+      const int st = j % STAGES, k0 = (kc_begin + j) * kBK;
+      mbar_expect_tx(smem_u32(&full[st]), kStage);
+      tma_load_2d(sa(st), &ta, k0, m0, smem_u32(&full[st]));
+      tma_load_2d(sb(st), &tb, k0, n0, smem_u32(&full[st]));
+    };
+    bool ok = true;
+    int issued = 0, consumed = 0;
+    for (; issued < min(STAGES, nk); ++issued) load(issued);
+    for (int i = 0; i < nk && ok; ++i) {
+      const int st = i % STAGES;
+      const uint32_t par = (uint32_t)(i / STAGES) & 1u;
+      ok = mbar_wait(smem_u32(&full[st]), par);
+      if (!ok) break;
+      consumed = i + 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int ks = 0; ks < kBK / 16; ++ks) {
+        const uint64_t ad = make_sdesc_sw128(sa(st) + ks * 32);
+        const uint64_t bd = make_sdesc_sw128(sb(st) + ks * 32);
+        const uint32_t accumulate = (i > 0 || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&freed[st]))
+                   : "memory");
+      if (issued < nk) {  // refill this stage once its MMAs are done
+        ok = mbar_wait(smem_u32(&freed[st]), par);
+        if (!ok) break;
+        load(issued++);
+      }
+    }
+    // every MMA issued so far completes before the accumulator is read or freed
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(done))
+                 : "memory");
+    const bool mma_done = mbar_wait(smem_u32(done), 0u);
+    if (!ok) {  // loads still in flight land before the tile exits
+      for (int j = consumed; j < issued; ++j)
+        mbar_wait(smem_u32(&full[j % STAGES]), (uint32_t)(j / STAGES) & 1u);
+    }
+    *ok_flag = (ok && mma_done) ? 1 : 0;
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (!*ok_flag) {
+    if (tid == 0) status_error(status, KUPS_ERR_UNSUPPORTED, blockIdx.x);
+  } else if (nk > 0) {
+    register_epilogue<BN>(g, tmem, m0, n0, warp, lane);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN));
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of a bfloat16 [rows, k] operand with row stride sr elements (K contiguous), boxes
+// of 64 x box_rows, 128-byte swizzle; out-of-range elements read as zero.
+bool operand_map(CUtensorMap *m, const void *p, int64_t rows, int64_t k, int64_t sr, int box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (enc == nullptr) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)sr * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(p), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Whether the TMA-fed kernel applies: both operands bfloat16 with K contiguous, 16-byte aligned
+// bases and row strides of at least K elements that are multiples of 8, and the register epilogue.
+bool tma_operands(const GemmArgs &g) {
+  auto al16 = [](const void *q) { return (((uintptr_t)q) & 15) == 0; };
+  return g.a_bf16 && g.b_bf16 && g.sac == 1 && g.sbc == 1 && g.sar % 8 == 0 && g.sbr % 8 == 0 && g.sar >= g.k &&
+         g.sbr >= g.k && al16(g.a) && al16(g.b) && g.row_epi;
+}
+
+template <int BN>
+int32_t launch_gemm_tma(const GemmArgs &g, kups_status *status, cudaStream_t stream, bool &launched) {
+  constexpr int kStages = 4;
+  launched = false;
+  CUtensorMap ta, tb;
+  if (!operand_map(&ta, g.a, g.m, g.k, g.sar, kBM) || !operand_map(&tb, g.b, g.n, g.k, g.sbr, BN)) return KUPS_OK;
+  const size_t smem = (size_t)kStages * (kBM + BN) * kBK * 2 + 1024 + 256;
+  KUPS_CUDA_TRY(cudaFuncSetAttribute(gemm_tma_kernel<BN, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+  dim3 grid((g.m + kBM - 1) / kBM, (g.n + BN - 1) / BN, g.split_k);
+  gemm_tma_kernel<BN, kStages><<<grid, kGemmThreads, smem, stream>>>(ta, tb, g, status);
+  launched = true;
+  return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
+}
+
 // Tile width: 128 (64 for N <= 64), narrowed to 64 while the grid would leave SMs idle
 // (fewer than two CTAs per SM of 148).  128-wide tiles (64 KB of pipeline buffers, three
 // CTAs per SM) beat 256-wide ones (two CTAs per SM) on the network's K <= 256 GEMMs.
@@ -474,6 +666,13 @@ bool row_epilogue(const GemmArgs &g) {
 int32_t dispatch_gemm(const GemmArgs &g0, kups_status *status, cudaStream_t st) {
   GemmArgs g = g0;
   g.row_epi = row_epilogue(g) ? 1 : 0;
+  if (tma_operands(g)) {  // one tile column per 256 of N; the tile ring holds K <= 256 whole
+    bool launched = false;
+    int32_t rc = g.n <= 64    ? launch_gemm_tma<64>(g, status, st, launched)
+                 : g.n <= 128 ? launch_gemm_tma<128>(g, status, st, launched)
+                              : launch_gemm_tma<256>(g, status, st, launched);
+    if (launched || rc != KUPS_OK) return rc;
+  }
   const int64_t rows = ((int64_t)g.m + kBM - 1) / kBM * g.split_k;
   int bn = g.n <= 64 ? 64 : 128;
   while (bn > 64 && rows * ((g.n + bn - 1) / bn) < 2 * 148) bn >>= 1;

@@ -238,3 +238,19 @@ def test_gemm_bf16_row_major_operands(m, n, k):
     b = torch.randn(n, k, device="cuda", generator=g).bfloat16()
     c = gemm(a, b)
     assert rel(c, a.float() @ b.float().T) < 1e-5
+
+
+@pytest.mark.parametrize("m,n,k,split", [(256, 64, 3000, 2), (256, 64, 3000, 12), (300, 256, 1024, 1),
+                                         (130, 128, 200, 1)])
+def test_gemm_bf16_tma_ring_split_k_and_ragged(m, n, k, split):
+    """bfloat16 operands with K contiguous take the TMA-fed kernel: K beyond the four-stage ring
+    (stages refilled), split K (vector reductions into C), ragged M, K not a multiple of 64
+    (zero-filled boxes), 64-, 128- and 256-wide tiles."""
+    from kups_gb300.mlp import gemm
+
+    g = torch.Generator(device="cuda").manual_seed(m + n + k + split)
+    a = torch.randn(m, k, device="cuda", generator=g).bfloat16()
+    b = torch.randn(n, k, device="cuda", generator=g).bfloat16()
+    c = torch.zeros(m, n, device="cuda")
+    gemm(a, b, c, beta=1.0 if split > 1 else 0.0, split_k=split)
+    assert rel(c, a.float() @ b.float().T) < 1e-5
