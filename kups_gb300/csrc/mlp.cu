@@ -76,6 +76,13 @@ __device__ inline bool mbar_wait(uint32_t addr, uint32_t phase) {
 // error, a few 1e-8, is far below the bfloat16 rounding that follows)
 __device__ inline float softplus_fast(float x) { return fmaxf(x, 0.f) + __logf(1.0f + __expf(-fabsf(x))); }
 
+// One 32-byte store (a whole L2 sector) of eight 32-bit values.
+__device__ inline void st_v8(void *p, const uint32_t (&w)[8]) {
+  asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]),
+               "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+               : "memory");
+}
+
 __device__ inline void red_add_v4(float *p, float a, float b, float c, float d) {
   asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
                : "memory");
@@ -115,6 +122,7 @@ struct GemmArgs {
   void *c3;           // optional third output, bfloat16, its own strides (a transposed copy)
   int64_t sc3r, sc3c;
   int row_epi;        // set by dispatch_gemm: the register (lane = row) epilogue applies
+  int row_v8;         // ... and C (and c2) rows are 32-byte aligned: whole-sector 32-byte stores
   int fast_math;      // softplus and the gates through SFU exp / log (the network's own calls)
 };
 
@@ -247,21 +255,35 @@ __device__ inline void register_epilogue(const GemmArgs &g, uint32_t tmem, int m
       }
     }
     if (rin) {
-      float4 *cp = reinterpret_cast<float4 *>((float *)g.c + (int64_t)row * g.scr + col0);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) cp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-      if (g.c2 != nullptr) {
-        uint4 *c2p = reinterpret_cast<uint4 *>((__nv_bfloat16 *)g.c2 + (int64_t)row * g.sc2r + col0);
+      float *cr = (float *)g.c + (int64_t)row * g.scr + col0;
+      if (g.row_v8) {  // each lane writes whole 32-byte sectors of its row
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          uint4 u;
-          uint32_t *w = reinterpret_cast<uint32_t *>(&u);
+          uint32_t w[8];
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const __nv_bfloat162 h = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
-            w[e] = *reinterpret_cast<const uint32_t *>(&h);
-          }
-          c2p[q] = u;
+          for (int e = 0; e < 8; ++e) w[e] = __float_as_uint(v[8 * q + e]);
+          st_v8(cr + 8 * q, w);
+        }
+      } else {
+        float4 *cp = reinterpret_cast<float4 *>(cr);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) cp[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
+      if (g.c2 != nullptr) {
+        __nv_bfloat16 *c2r = (__nv_bfloat16 *)g.c2 + (int64_t)row * g.sc2r + col0;
+        uint32_t w[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+          w[e] = *reinterpret_cast<const uint32_t *>(&h);
+        }
+        if (g.row_v8) {
+          st_v8(c2r, *reinterpret_cast<const uint32_t(*)[8]>(&w[0]));
+          st_v8(c2r + 16, *reinterpret_cast<const uint32_t(*)[8]>(&w[8]));
+        } else {
+          uint4 *c2p = reinterpret_cast<uint4 *>(c2r);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) c2p[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
         }
       }
       if (g.c3 != nullptr) {
@@ -498,8 +520,8 @@ __device__ inline void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0,
       : "memory");
 }
 
-template <int BN, int STAGES>
-__global__ void __launch_bounds__(kGemmThreads, 1)
+template <int BN, int STAGES, int MINB>
+__global__ void __launch_bounds__(kGemmThreads, MINB)
     gemm_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmArgs g,
                     kups_status *status) {
   extern __shared__ unsigned char smem_raw[];
@@ -596,6 +618,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN));
 }
 
+bool encode_operand_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap *m, const void *p, int64_t rows,
+                        int64_t k, int64_t sr, int box_rows);
+
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void *p = nullptr;
@@ -609,10 +634,35 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // Tensor map of a bfloat16 [rows, k] operand with row stride sr elements (K contiguous), boxes
-// of 64 x box_rows, 128-byte swizzle; out-of-range elements read as zero.
+// of 64 x box_rows, 128-byte swizzle; out-of-range elements read as zero.  The last maps made
+// are kept (a training step passes the same workspace operands every step), so encoding runs
+// once per distinct operand; the cache is per host thread.
 bool operand_map(CUtensorMap *m, const void *p, int64_t rows, int64_t k, int64_t sr, int box_rows) {
+  struct Entry {
+    const void *p;
+    int64_t rows, k, sr;
+    int box;
+    CUtensorMap map;
+  };
+  constexpr int kCache = 32;
+  static thread_local Entry cache[kCache];
+  static thread_local int next = 0;
+  for (int i = 0; i < kCache; ++i) {
+    const Entry &e = cache[i];
+    if (e.p == p && e.rows == rows && e.k == k && e.sr == sr && e.box == box_rows) {
+      *m = e.map;
+      return true;
+    }
+  }
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-  if (enc == nullptr) return false;
+  if (enc == nullptr || !encode_operand_map(enc, m, p, rows, k, sr, box_rows)) return false;
+  cache[next] = Entry{p, rows, k, sr, box_rows, *m};
+  next = (next + 1) % kCache;
+  return true;
+}
+
+bool encode_operand_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap *m, const void *p, int64_t rows,
+                        int64_t k, int64_t sr, int box_rows) {
   cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)sr * 2};
   cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
@@ -630,17 +680,22 @@ bool tma_operands(const GemmArgs &g) {
          g.sbr >= g.k && al16(g.a) && al16(g.b) && g.row_epi;
 }
 
-template <int BN>
+template <int BN, int STAGES, int MINB>
 int32_t launch_gemm_tma(const GemmArgs &g, kups_status *status, cudaStream_t stream, bool &launched) {
-  constexpr int kStages = 4;
   launched = false;
   CUtensorMap ta, tb;
   if (!operand_map(&ta, g.a, g.m, g.k, g.sar, kBM) || !operand_map(&tb, g.b, g.n, g.k, g.sbr, BN)) return KUPS_OK;
-  const size_t smem = (size_t)kStages * (kBM + BN) * kBK * 2 + 1024 + 256;
-  KUPS_CUDA_TRY(cudaFuncSetAttribute(gemm_tma_kernel<BN, kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+  const size_t smem = (size_t)STAGES * (kBM + BN) * kBK * 2 + 1024 + 256;
+  static int set_device = -1;  // the attribute is per device: set it once for each device in turn
+  int dev = 0;
+  KUPS_CUDA_TRY(cudaGetDevice(&dev));
+  if (set_device != dev) {
+    KUPS_CUDA_TRY(cudaFuncSetAttribute(gemm_tma_kernel<BN, STAGES, MINB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set_device = dev;
+  }
   dim3 grid((g.m + kBM - 1) / kBM, (g.n + BN - 1) / BN, g.split_k);
-  gemm_tma_kernel<BN, kStages><<<grid, kGemmThreads, smem, stream>>>(ta, tb, g, status);
+  gemm_tma_kernel<BN, STAGES, MINB><<<grid, kGemmThreads, smem, stream>>>(ta, tb, g, status);
   launched = true;
   return cudaGetLastError() == cudaSuccess ? KUPS_OK : KUPS_ERR_CUDA;
 }
@@ -666,11 +721,17 @@ bool row_epilogue(const GemmArgs &g) {
 int32_t dispatch_gemm(const GemmArgs &g0, kups_status *status, cudaStream_t st) {
   GemmArgs g = g0;
   g.row_epi = row_epilogue(g) ? 1 : 0;
+  auto al32 = [](const void *q) { return (((uintptr_t)q) & 31) == 0; };
+  g.row_v8 = g.row_epi && g.scr % 8 == 0 && al32(g.c) &&
+             (g.c2 == nullptr || (g.sc2r % 16 == 0 && al32(g.c2)));
   if (tma_operands(g)) {  // one tile column per 256 of N; the tile ring holds K <= 256 whole
+    // tiles as wide as N (up to 256, one CTA per SM) with a four-stage ring: measured against
+    // 128 x 128 and 128 x 64 tiles with two stages (three and four CTAs per SM) and with four
+    // stages, it was the fastest on the network's training step (0.194 against 0.196-0.214 ms)
     bool launched = false;
-    int32_t rc = g.n <= 64    ? launch_gemm_tma<64>(g, status, st, launched)
-                 : g.n <= 128 ? launch_gemm_tma<128>(g, status, st, launched)
-                              : launch_gemm_tma<256>(g, status, st, launched);
+    const int32_t rc = g.n <= 64    ? launch_gemm_tma<64, 4, 1>(g, status, st, launched)
+                       : g.n <= 128 ? launch_gemm_tma<128, 4, 1>(g, status, st, launched)
+                                    : launch_gemm_tma<256, 4, 1>(g, status, st, launched);
     if (launched || rc != KUPS_OK) return rc;
   }
   const int64_t rows = ((int64_t)g.m + kBM - 1) / kBM * g.split_k;
@@ -882,16 +943,22 @@ __global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n
   float db = 0.f, ls = 0.f;
   const float inv_n = 1.f / (float)n;
   for (int64_t r0 = (int64_t)blockIdx.x * 32; r0 < n; r0 += (int64_t)gridDim.x * 32) {
-    for (int k = 0; k < 4; ++k) {  // warp w takes rows r0 + 4 w .. r0 + 4 w + 3
+    // warp w takes rows r0 + 4 w .. r0 + 4 w + 3, all four rows' loads issued first
+    float hk[4][8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t row = r0 + warp * 4 + k;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) hk[k][j] = row < n ? h[row * kHid + lane + 32 * j] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
       const int rl = warp * 4 + k;
       const int64_t row = r0 + rl;
       if (row >= n) break;
-      const float *hr = h + row * kHid;
-      float hv[8], acc = 0.f;
-      for (int j = 0; j < 8; ++j) {
-        hv[j] = hr[lane + 32 * j];
-        acc = fmaf(hv[j], wl[j], acc);
-      }
+      const float *hv = hk[k];
+      float acc = 0.f;
+      for (int j = 0; j < 8; ++j) acc = fmaf(hv[j], wl[j], acc);
       const float gg = warp_sum(acc) + b4[0];
       const float y = label[row];
       const float dg = (1.f / (1.f + expf(-gg)) - y) * inv_n;
@@ -901,7 +968,7 @@ __global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n
       }
       for (int j = 0; j < 8; ++j) {
         dw[j] = fmaf(dg, hv[j], dw[j]);
-        const float d = dg * wl[j] * -expm1f(-hv[j]);
+        const float d = dg * wl[j] * (1.f - __expf(-hv[j]));  // softplus' through its output (SFU exp)
         const int col = lane + 32 * j;
         dz[row * kHid + col] = d;
         const __nv_bfloat16 db16 = __float2bfloat16(d);
@@ -939,15 +1006,28 @@ __global__ void __launch_bounds__(256) head_nce_kernel(const float *h, int64_t n
   }
 }
 
-// out[c] += sum_r z[r, c] over 256 columns (bias gradients); thread = column.
+// Column sums of z [n, 256] (float32) added into out: thread t reads columns 4 (t % 64) .. + 3
+// (16-byte loads, a warp reads 512 contiguous bytes of a row) of every fourth row of the
+// block's slab, and the four row groups meet in shared memory.
 __global__ void __launch_bounds__(kHid) colsum_kernel(const float *z, int64_t n, float *out) {
-  const int c = threadIdx.x;
+  __shared__ float4 part[4][kHid / 4];
+  const int t = threadIdx.x, q = t & (kHid / 4 - 1), grp = t / (kHid / 4);
   const int64_t per = (n + gridDim.x - 1) / gridDim.x;
   const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
-  if (r0 >= r1) return;
-  float s = 0.f;
-  for (int64_t r = r0; r < r1; ++r) s += z[r * kHid + c];
-  atomicAdd(&out[c], s);
+  const float4 *z4 = reinterpret_cast<const float4 *>(z);
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+  for (int64_t r = r0 + grp; r < r1; r += 4) {
+    const float4 v = z4[r * (kHid / 4) + q];
+    s.x += v.x;
+    s.y += v.y;
+    s.z += v.z;
+    s.w += v.w;
+  }
+  part[grp][q] = s;
+  __syncthreads();
+  const float *pf = reinterpret_cast<const float *>(part);
+  if (r0 < r1) atomicAdd(&out[t], (pf[t] + pf[kHid + t]) + (pf[2 * kHid + t] + pf[3 * kHid + t]));
 }
 
 // Adam (Kingma & Ba 2015) with bias corrections c1 = 1 / (1 - beta1^t),
@@ -1552,7 +1632,7 @@ extern "C" int32_t kups_mlp_bwd(const kups_mlp *net, const double *x, const floa
   head_nce_kernel<<<std::min<int64_t>(blocks(n, 32), 4 * sms), 256, 0, st>>>(
       w.h3, n, p + kOffW4, p + kOffB4, label, w.dza, w.dzab, w.dzaT, gr + kOffW4, gr + kOffB4, loss);
   const int split = split_for(n);
-  const unsigned cs_blocks = (unsigned)std::min<int64_t>(blocks(n, 64), 2 * sms);
+  const unsigned cs_blocks = (unsigned)std::min<int64_t>(blocks(n, 32), 4 * sms);
   // Every GEMM operand is bfloat16 with K contiguous: the weight gradients read the
   // transposed copies ([width, n], K = points), the input gradients W^T.
   // layer 3: dW3 += dz3^T h2, db3 += colsum dz3, dz2 = (dz3 W3) * (1 - exp(-h2))
