@@ -415,11 +415,13 @@ class FusedLennardJonesMD:
         offs = [0] + torch.cumsum(counts, 0).tolist()
         grouped = n == 0 or bool((system[1:] >= system[:-1]).all())
         cuts = [0]
-        if grouped and chunks > 1:
+        if grouped and chunks > 1 and n > 0:
             for k in range(1, chunks):
                 target = k * n / chunks
-                c = min(range(cuts[-1] + 1, s), key=lambda j: abs(offs[j] - target), default=s)
-                if c > cuts[-1] and c < s:
+                # the system boundary nearest the target that leaves atoms on both sides
+                c = min((j for j in range(cuts[-1] + 1, s) if offs[cuts[-1]] < offs[j] < n),
+                        key=lambda j: abs(offs[j] - target), default=None)
+                if c is not None:
                     cuts.append(c)
         cuts.append(s)
         bounds = [(offs[s0], offs[s1], s0, s1) for s0, s1 in zip(cuts[:-1], cuts[1:])]
