@@ -676,6 +676,17 @@ typedef struct kups_gcmc_args {
   unsigned long long *profile;  /* [6] or NULL: clock cycles of thread 0 summed over all systems
                                    and steps per phase (proposal, host atoms, guests and the
                                    moved molecule, phase tables, k sum, acceptance and commit) */
+  double *host_cache;           /* [S, max_mol, 2] in/out or NULL: per guest molecule its real-space
+                                   energy with the (rigid) host and a 64-bit key of the atom
+                                   positions it belongs to (bits in the second double; zeros =
+                                   no entry).  With every cell width at least twice the cutoffs,
+                                   a move reads the old molecule's host energy from its entry
+                                   when the key matches the molecule's positions, and computes
+                                   only the new positions against the host; entries follow
+                                   their molecules (written on acceptance, moved on deletion,
+                                   filled on a miss).  A hit equals the recomputed value bit for
+                                   bit; stale or foreign entries only miss.  NULL: both ends
+                                   are computed every move */
 } kups_gcmc_args;
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);

@@ -57,7 +57,23 @@ struct StepShared {
   double log_p;
   double de_total;
   double ln_ratio;  // log proposal ratio of the learned insertion density (0 when uniform)
+  // host energy cache (kups_gcmc_args.host_cache): keys of the old and new positions, whether
+  // the old molecule's entry matched, and its energy
+  unsigned long long old_key, new_key;
+  int cache_hit;
+  double e_host_old;
 };
+
+// 64-bit key of a molecule's atom positions (FNV-1a over the float bits; never 0, which marks
+// an empty cache entry).
+__device__ inline unsigned long long position_key(const float4 *p, int apm) {
+  unsigned long long h = 0xcbf29ce484222325ull;
+  for (int i = 0; i < apm; ++i) {
+    const uint32_t w[3] = {__float_as_uint(p[i].x), __float_as_uint(p[i].y), __float_as_uint(p[i].z)};
+    for (int k = 0; k < 3; ++k) h = (h ^ w[k]) * 0x100000001b3ull;
+  }
+  return h | 1ull;
+}
 
 __device__ inline void frac32(const float inv[6], float x, float y, float z, float f[3]) {
   f[0] = (x * inv[0] + y * inv[1]) + z * inv[3];
@@ -357,6 +373,9 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     }
   }
   const bool learned = a.proposal_node != nullptr;
+  // the host energy cache serves the minimum-image path, where a molecule's host energy is a
+  // function of its positions alone
+  const bool use_cache = a.host_cache != nullptr && min_image;
   double ob[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // thread 0: this launch's U, N, U N, N^2, U^2 sums
   unsigned long long *prof = a.profile;
   long long t0 = clock64();
@@ -493,6 +512,19 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       if (learned && kind == 4 && sh.has_old)
         sh.ln_ratio = grid_log_q(a.proposal_node, a.proposal_cdf, a.proposal_grid,
                                  anchor_frac(sh.old_pos, apm, Lf, If).v);
+      sh.cache_hit = 0;
+      sh.e_host_old = 0.0;
+      if (use_cache) {
+        sh.old_key = sh.has_old ? position_key(sh.old_pos, apm) : 0ull;
+        sh.new_key = sh.has_new ? position_key(sh.new_pos, apm) : 0ull;
+        if (sh.has_old) {
+          const double *ent = a.host_cache + ((int64_t)s * a.max_mol + mol) * 2;
+          if (__double_as_longlong(ent[1]) == (long long)sh.old_key) {
+            sh.cache_hit = 1;
+            sh.e_host_old = ent[0];
+          }
+        }
+      }
     }
     __syncthreads();
     const int has_old = sh.has_old, has_new = sh.has_new, mol = sh.mol, kind = sh.kind;
@@ -513,6 +545,8 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     __syncthreads();
     gcmc_mark(prof, 0, t0);
     const int nm = 2 * apm;
+    float e_host_new = 0.f, e_host_old = 0.f;  // minimum-image path: host terms, by end
+    const int cache_hit = sh.cache_hit;
     if (min_image) {
       // every axis has one image: the pair is taken at its minimum image, one rounding
       // per moved atom and partner.  Host atoms go by warp in aligned groups of 32; a
@@ -520,8 +554,8 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       // of the atom's fractional coordinate to the group's centre minus the group's half
       // extent, times the width w_a, reaches the cutoff (|cart(d)| >= |d_a| w_a, and the
       // rounded image's d_a is the circular distance, so no pair within it is dropped).
-      unsigned on_mask = 0u;
-      for (int m = 0; m < nm; ++m) on_mask |= mon[m] ? (1u << m) : 0u;
+      unsigned on_mask = 0u;  // moved atoms to take against the host (old ones unless cached)
+      for (int m = 0; m < nm; ++m) on_mask |= (mon[m] && !(m < apm && cache_hit)) ? (1u << m) : 0u;
       for (int base = (tid & ~31); base < fwn; base += kThreads) {
         unsigned near = on_mask;
         if (grp != nullptr) {
@@ -556,8 +590,9 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
           cart32(Lf, d, c);
           const float r2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
           if (r2 >= rc2_any) continue;
-          const float sg = m < apm ? -1.f : 1.f;
-          e_acc += sg * pair_u(r2, __float_as_int(fa.w), tj, mq[m] * qj, lj, nsp, li, ei, alpha, ke, true, true);
+          const float u = pair_u(r2, __float_as_int(fa.w), tj, mq[m] * qj, lj, nsp, li, ei, alpha, ke, true, true);
+          if (m < apm) e_host_old += u;
+          else e_host_new += u;
         }
       }
       gcmc_mark(prof, 1, t0);
@@ -629,7 +664,13 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       e_acc += sign * pair_images(Lf, fa, fb, __float_as_int(pa.w), __float_as_int(pb.w), sh.q[ia] * sh.q[ib], lj,
                                   nsp, li, ei, alpha, ke, true);
     }
-    const double de_real = block_sum_f(e_acc, red);
+    double de_real = block_sum_f(e_acc, red);
+    double e_host_new_tot = 0.0, e_host_old_tot = 0.0;
+    if (min_image) {  // host terms: new minus old end, the old one from the cache on a hit
+      e_host_new_tot = block_sum_f(e_host_new, red);
+      e_host_old_tot = cache_hit ? sh.e_host_old : block_sum_f(e_host_old, red);
+      de_real += e_host_new_tot - e_host_old_tot;
+    }
     gcmc_mark(prof, 2, t0);
     // ---------------------------------------------------------------- reciprocal space
     // per-k terms in float32 (|term| <~ 15 eV: ~1e-6 eV rounding each), the k sum of a
@@ -748,6 +789,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       }
       if (tid == 0) {
         a.energy[s] += sh.de_total;
+        double *cache = use_cache ? a.host_cache + (int64_t)s * a.max_mol * 2 : nullptr;
         if (kind == 3 && has_new) {
           for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = sh.new_pos[i];
           a.n_mol[s] = nmol + 1;
@@ -755,10 +797,22 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
           const int last = nmol - 1;
           for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = gpos[last * apm + i];
           a.n_mol[s] = last;
+          if (cache != nullptr) {  // the entry follows the molecule moved into the slot
+            cache[2 * mol] = cache[2 * last];
+            cache[2 * mol + 1] = cache[2 * last + 1];
+          }
         } else if (has_new) {
           for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = sh.new_pos[i];
         }
+        if (cache != nullptr && has_new) {
+          cache[2 * mol] = e_host_new_tot;
+          cache[2 * mol + 1] = __longlong_as_double((long long)sh.new_key);
+        }
       }
+    } else if (tid == 0 && use_cache && has_old && !cache_hit) {  // rejected: keep what the miss computed
+      double *ent = a.host_cache + ((int64_t)s * a.max_mol + mol) * 2;
+      ent[0] = e_host_old_tot;
+      ent[1] = __longlong_as_double((long long)sh.old_key);
     }
     // ---------------------------------------------------------------- statistics and step widths
     if (tid == 0) {

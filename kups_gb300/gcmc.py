@@ -244,6 +244,10 @@ class GCMC:
         self.fw_count = i32(setup.fw_count)
         self.guest = torch.zeros((s, setup.max_mol, apm, 4), dtype=torch.float32, device=dev)
         self.n_mol = torch.zeros(s, dtype=torch.int32, device=dev)
+        # per guest molecule: its real-space energy with the rigid host and the key of the
+        # positions it belongs to (kups_gcmc_args.host_cache); entries are keyed by positions,
+        # so edits of the guests need no invalidation
+        self.host_cache = torch.zeros((s, max(setup.max_mol, 1), 2), dtype=torch.float64, device=dev)
         # per-step U, N, U N, N^2, U^2 sums the kernel adds to (kups_gcmc_args.obs_sums)
         self.obs = torch.zeros((s, 5), dtype=torch.float64, device=dev)
         self.motif = f32(np.concatenate([setup.motif_positions, sp_bits(setup.motif_species)[:, None]], 1))
@@ -289,6 +293,7 @@ class GCMC:
         self.status = new_status()
         self.proposal = None  # learned insertion density (LearnedInsertionProposal) or None: uniform
         self.block_threads = 0  # threads per CTA (0: library default); kups_gb300.autotune.autotune_gcmc picks one
+        self.use_host_cache = True  # False: both ends of every move against the host, every step
 
     def _min_half_width(self):
         out = []
@@ -340,6 +345,7 @@ class GCMC:
         a.trace = trace.data_ptr() if trace is not None else None
         a.block_threads = int(self.block_threads)
         a.profile = self.profile.data_ptr() if getattr(self, "profile", None) is not None else None
+        a.host_cache = self.host_cache.data_ptr() if self.use_host_cache else None
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid
@@ -396,7 +402,7 @@ class GCMC:
         self.launch(1, proposals=buf, out_delta=out)
         return out.cpu().numpy()
 
-    _STATE = ("guest", "n_mol", "sk", "energy", "width", "history", "history_index")
+    _STATE = ("guest", "n_mol", "sk", "energy", "width", "history", "history_index", "host_cache")
 
     def clone(self, seed: int | None = None) -> "GCMC":
         """A sampler on the same setup starting from this one's state (positions, counts,
@@ -407,6 +413,7 @@ class GCMC:
         other.step = self.step
         other.proposal = self.proposal
         other.block_threads = self.block_threads
+        other.use_host_cache = self.use_host_cache
         return other
 
     def use_proposal(self, proposal):

@@ -131,6 +131,7 @@ def test_ideal_gas_loading_is_poisson():
 
     setup = small_setup(n_sys=64, tail=False, charges=False)
     setup.epsilon = np.zeros_like(setup.epsilon)
+    setup.max_mol = 40  # Poisson(3) reaches 16 molecules about once in 10^7 system-steps
     vol = abs(np.prod(setup.tril[0, [0, 2, 5]]))
     target = 3.0
     setup.log_activity = np.full(64, np.log(target / vol))
@@ -220,6 +221,7 @@ def test_ideal_gas_with_learned_proposal_stays_uniform_and_poisson():
     net = _blob_proposal(3)
     setup = small_setup(n_sys=64, tail=False, charges=False)
     setup.epsilon = np.zeros_like(setup.epsilon)
+    setup.max_mol = 40  # Poisson(3) reaches 16 molecules about once in 10^7 system-steps
     vol = abs(np.prod(setup.tril[0, [0, 2, 5]]))
     target = 3.0
     setup.log_activity = np.full(64, np.log(target / vol))
@@ -451,3 +453,55 @@ def test_guest_stress_is_the_volume_derivative_of_the_guest_energy():
     np.testing.assert_allclose(res["tail_correction"], pt[:, None, None] * np.eye(3), rtol=1e-10, atol=1e-300)
     pi = oobs.ideal_gas_pressure([7, 5], setup.temperature, setup.tril)
     np.testing.assert_allclose(res["ideal_gas"], pi[:, None, None] * np.eye(3), rtol=1e-12, atol=1e-300)
+
+
+def test_host_energy_cache_hit_equals_the_recomputed_value():
+    """Minimum-image path with the host energy cache (kups_gcmc_args.host_cache): a move whose
+    old molecule misses computes both ends against the host and stores the old one; the same
+    move again reads it back and gives the same energy change bit for bit; the uncached kernel
+    agrees within the float32 pair sums' rounding.  Entries follow their molecules on deletion."""
+    from kups_gb300 import gcmc
+    from oracle import unitcell as ouc
+
+    S = 3
+    setup = small_setup(n_sys=S, rc=5.0)
+    L = ouc.lattice_from_tril(setup.tril[0])
+    rng = np.random.default_rng(4)
+    guests = [np.concatenate([wrapped(random_molecule(rng, L, setup.motif_positions), setup.tril[0])
+                              for _ in range(5)]) for _ in range(S)]
+    mc = gcmc.GCMC(setup, seed=2)
+    mc.set_guests(guests)
+    off = mc.clone()
+    off.use_host_cache = False
+    kinds, mols = np.full(S, 4), np.full(S, 1)  # delete molecule 1 (rejected: nothing changes)
+    assert float(mc.host_cache[:, 1, 1].abs().max()) == 0.0
+    first = mc.evaluate(kinds, mols, [None] * S)
+    assert bool((mc.host_cache[:, 1, 1] != 0).all())  # the miss stored the old end
+    second = mc.evaluate(kinds, mols, [None] * S)
+    np.testing.assert_array_equal(first, second)
+    plain = off.evaluate(kinds, mols, [None] * S)
+    np.testing.assert_allclose(first[:, :3], plain[:, :3], rtol=1e-6, atol=1e-6)
+    # a translation of molecule 2: the old end from a filled entry, the new end computed
+    apm = len(setup.motif_charges)
+    moved = [wrapped(guests[s].reshape(-1, apm, 3)[2] + 0.3, setup.tril[0]) for s in range(S)]
+    mc.evaluate(np.full(S, 4), np.full(S, 2), [None] * S)  # fill molecule 2's entry
+    a = mc.evaluate(np.zeros(S, int), np.full(S, 2), moved)
+    b = off.evaluate(np.zeros(S, int), np.full(S, 2), moved)
+    np.testing.assert_allclose(a[:, :3], b[:, :3], rtol=1e-6, atol=1e-6)
+    # free-running steps from a relaxed state (the random start overlaps): the sum of the
+    # accepted changes against E(after) - E(before); a wrong cached host energy would be off by
+    # a molecule's host energy (tenths of an eV)
+    mc.launch(400)
+    mc.check()
+    start = mc.guest_positions()
+    mc.energy.zero_()
+    mc.launch(400)
+    mc.check()
+    got = mc.energy.cpu().numpy()
+    state = mc.guest_positions()
+    for s in range(S):
+        e0 = oracle_energy(setup, start[s].astype(np.float64).reshape(-1, 3))
+        e1 = oracle_energy(setup, state[s].astype(np.float64).reshape(-1, 3))
+        assert abs(e0) < 1e3, e0  # relaxed
+        assert abs((e1 - e0) - got[s]) < 2e-3, (s, e0, e1 - e0, got[s])
+    assert int(mc.accepted.sum()) > 50
