@@ -268,14 +268,6 @@ __device__ __forceinline__ void gcmc_mark(unsigned long long *prof, int k, long 
   }
 }
 
-__device__ inline double tail_energy(const double *counts, int nsp, const double *coef) {
-  // sum_ab coef_ab N_a N_b   (coef = (8/3) pi eps sigma^3 [(sigma/rc)^9/3 - (sigma/rc)^3] / V, masked)
-  double e = 0.0;
-  for (int a = 0; a < nsp; ++a)
-    for (int b = 0; b < nsp; ++b) e += coef[a * nsp + b] * counts[a] * counts[b];
-  return e;
-}
-
 // kThreads per CTA, 896 / kThreads resident CTAs per SM (at most 73 registers a thread): at 128
 // threads 1024 replicas run in one wave on 152 SMs, each CTA keeping its system for all n_steps.
 template <int kThreads>
@@ -294,6 +286,19 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
   const int apm = a.atoms_per_mol;
   const int nsp = a.n_species;
   const int nk = a.n_kvecs;
+  // the system's mutable scalars live in shared memory for the launch (read once, written back
+  // at the end), so no step waits on a global round trip for them; ss.tail_b / ss.tail_c give
+  // the tail correction as a function of the molecule count N (coef_ab = (8/3) pi eps sigma^3
+  // [(sigma/rc)^9 / 3 - (sigma/rc)^3] / V, masked):
+  //   E_tail(N) = sum_ab coef_ab c_a c_b, c = fw + N motif  =>  E_tail(N) - E_tail(0) = b N + c N^2
+  __shared__ struct {
+    double energy, tail_b, tail_c, self_excl;
+    int n_mol;
+    float width[4], width_max[4];
+    uint32_t hist[4][4];
+    int hist_idx[4];
+    int attempted[5], accepted[5];  // this launch's counts
+  } ss;
   for (int k = tid; k < nsp * nsp; k += kThreads)
     lj[k] = make_float2(a.lj_table[2 * k], a.lj_table[2 * k + 1]);
   if (tid == 0) {
@@ -303,6 +308,29 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       Lf[k] = (float)L.t[k];
       If[k] = (float)inv.t[k];
     }
+    ss.energy = a.energy[s];
+    ss.n_mol = a.n_mol[s];
+    for (int k = 0; k < 4; ++k) {
+      ss.width[k] = a.width[s * 4 + k];
+      ss.width_max[k] = a.width_max[s * 4 + k];
+      ss.hist_idx[k] = a.history_index[s * 4 + k];
+      for (int w = 0; w < 4; ++w) ss.hist[k][w] = a.history[((int64_t)s * 4 + k) * 4 + w];
+    }
+    for (int k = 0; k < 5; ++k) ss.attempted[k] = ss.accepted[k] = 0;
+    ss.self_excl = a.self_energy_mol[s] + a.exclusion_energy_mol[s];
+    double tb = 0.0, tcq = 0.0;
+    if (a.tail_coef != nullptr) {
+      const double *tc = a.tail_coef + (int64_t)s * nsp * nsp;
+      for (int p = 0; p < nsp; ++p)
+        for (int q = 0; q < nsp; ++q) {
+          const double fp = a.fw_species_count[s * nsp + p], fq = a.fw_species_count[s * nsp + q];
+          const double mp = a.motif_species_count[p], mq_ = a.motif_species_count[q];
+          tb += tc[p * nsp + q] * (fp * mq_ + mp * fq);
+          tcq += tc[p * nsp + q] * (mp * mq_);
+        }
+    }
+    ss.tail_b = tb;
+    ss.tail_c = tcq;
   }
   __syncthreads();
   // image configurations of the two terms (neighborlist.py:461-466)
@@ -383,7 +411,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     const uint64_t ctr = a.step0 + (uint64_t)step;
     // ---------------------------------------------------------------- proposal (thread 0)
     if (tid == 0) {
-      const int nmol = a.n_mol[s];
+      const int nmol = ss.n_mol;
       int kind;
       if (a.proposals != nullptr) {
         kind = a.proposals[s].kind;
@@ -427,7 +455,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
         } else if (kind == 0) {  // translation: N(0, 1) * width per axis, wrap
           float eta[4];
           normal4(a.seed, 1 + (uint64_t)s, 8 * ctr + 3, eta);
-          const float w = a.width[s * 4 + 0];
+          const float w = ss.width[0];
           for (int i = 0; i < apm; ++i) {
             const float4 p = sh.old_pos[i];
             float c[3] = {p.x + eta[0] * w, p.y + eta[1] * w, p.z + eta[2] * w};
@@ -455,7 +483,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
           }
           float q0[4], q[4];
           shoemake(u01(r2.x), u01(r2.y), u01(r2.z), q0);
-          if (kind == 1) qpow(q0, a.width[s * 4 + 1], q);
+          if (kind == 1) qpow(q0, ss.width[1], q);
           else for (int c = 0; c < 4; ++c) q[c] = q0[c];
           float shift[3] = {0.f, 0.f, 0.f};
           if (kind == 2) {
@@ -530,7 +558,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     const int has_old = sh.has_old, has_new = sh.has_new, mol = sh.mol, kind = sh.kind;
     // ---------------------------------------------------------------- real space: moved vs others
     float e_acc = 0.f;
-    const int nmol = a.n_mol[s];
+    const int nmol = ss.n_mol;
     const int n_other = fwn + nmol * apm;
     // moved atoms (old state, then new) in fractional coordinates, staged once per step
     if (tid < 2 * apm) {
@@ -720,17 +748,10 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       if (kind == 4 && has_old) n_new = n_old - 1;
       if (n_new != n_old) {
         const double sgn = n_new > n_old ? 1.0 : -1.0;
-        de += sgn * (a.self_energy_mol[s] + a.exclusion_energy_mol[s]);
-        // tail correction with species counts before / after
-        double c0[kMaxSpeciesMC], c1[kMaxSpeciesMC];
-        for (int t = 0; t < nsp; ++t) {
-          c0[t] = a.fw_species_count[s * nsp + t] + (double)n_old * a.motif_species_count[t];
-          c1[t] = a.fw_species_count[s * nsp + t] + (double)n_new * a.motif_species_count[t];
-        }
-        if (a.tail_coef != nullptr) {
-          const double *tc = a.tail_coef + (int64_t)s * nsp * nsp;
-          de += tail_energy(c1, nsp, tc) - tail_energy(c0, nsp, tc);
-        }
+        de += sgn * ss.self_excl;
+        // tail correction with the molecule counts before / after
+        const double dn = (double)(n_new - n_old), dn2 = (double)n_new * n_new - (double)n_old * n_old;
+        de += ss.tail_b * dn + ss.tail_c * dn2;
       }
       double logp = -de * inv_kT + sh.ln_ratio;
       if (n_new != n_old) {
@@ -753,7 +774,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
         t.n_mol = n_old;
         t.has_old = has_old;
         t.has_new = has_new;
-        t.width = a.width[s * 4 + (kind >= 3 ? 3 : kind)];
+        t.width = ss.width[kind >= 3 ? 3 : kind];
         t.pad = 0;
         t.de = de;
         t.log_p = logp;
@@ -788,15 +809,15 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
         sk32[k] = make_float2((float)c, (float)sn);
       }
       if (tid == 0) {
-        a.energy[s] += sh.de_total;
+        ss.energy += sh.de_total;
         double *cache = use_cache ? a.host_cache + (int64_t)s * a.max_mol * 2 : nullptr;
         if (kind == 3 && has_new) {
           for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = sh.new_pos[i];
-          a.n_mol[s] = nmol + 1;
+          ss.n_mol = nmol + 1;
         } else if (kind == 4 && has_old) {
           const int last = nmol - 1;
           for (int i = 0; i < apm; ++i) gpos[mol * apm + i] = gpos[last * apm + i];
-          a.n_mol[s] = last;
+          ss.n_mol = last;
           if (cache != nullptr) {  // the entry follows the molecule moved into the slot
             cache[2 * mol] = cache[2 * last];
             cache[2 * mol + 1] = cache[2 * last + 1];
@@ -816,16 +837,16 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     }
     // ---------------------------------------------------------------- statistics and step widths
     if (tid == 0) {
-      a.attempted[5 * (int64_t)s + kind] += 1;
-      a.accepted[5 * (int64_t)s + kind] += accept;
+      ss.attempted[kind] += 1;
+      ss.accepted[kind] += accept;
       const int sched = kind >= 3 ? 3 : kind;  // insert / delete share the exchange scheduler
       const int hs = a.history_len;
-      uint32_t *hist = a.history + ((int64_t)s * 4 + sched) * 4;
-      int idx = a.history_index[s * 4 + sched];
+      uint32_t *hist = ss.hist[sched];
+      int idx = ss.hist_idx[sched];
       const uint32_t bit = 1u << (idx & 31);
       hist[idx >> 5] = accept ? (hist[idx >> 5] | bit) : (hist[idx >> 5] & ~bit);
       idx = (idx + 1) % hs;
-      a.history_index[s * 4 + sched] = idx;
+      ss.hist_idx[sched] = idx;
       if (idx == 0) {
         int acc = 0;
         for (int w = 0; w < 4; ++w) {
@@ -834,15 +855,15 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
         }
         const float avg = (float)acc / hs;
         const float target = 0.5f, tol = 0.05f, mult = 1.1f;
-        float v = a.width[s * 4 + sched];
+        float v = ss.width[sched];
         float nv = avg < target ? v / mult : v * mult;  // step widths correlate negatively
         nv = fmaxf(nv, 0.0f);
-        const float ub = a.width_max[s * 4 + sched];
+        const float ub = ss.width_max[sched];
         if (ub > 0.f) nv = fminf(nv, ub);
-        if (fabsf(avg - target) > tol) a.width[s * 4 + sched] = nv;
+        if (fabsf(avg - target) > tol) ss.width[sched] = nv;
       }
       if (a.obs_sums != nullptr) {
-        const double u = a.energy[s], nm = (double)a.n_mol[s];
+        const double u = ss.energy, nm = (double)ss.n_mol;
         ob[0] += u;
         ob[1] += nm;
         ob[2] += __dmul_rn(u, nm);  // rounded products, as the reference's float64 series hold them
@@ -853,8 +874,21 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     __syncthreads();
     gcmc_mark(prof, 5, t0);
   }
-  if (tid == 0 && a.obs_sums != nullptr)
-    for (int k = 0; k < 5; ++k) a.obs_sums[5 * (int64_t)s + k] += ob[k];
+  if (tid == 0) {  // the launch's state back to the caller's arrays
+    if (a.obs_sums != nullptr)
+      for (int k = 0; k < 5; ++k) a.obs_sums[5 * (int64_t)s + k] += ob[k];
+    a.energy[s] = ss.energy;
+    a.n_mol[s] = ss.n_mol;
+    for (int k = 0; k < 4; ++k) {
+      a.width[s * 4 + k] = ss.width[k];
+      a.history_index[s * 4 + k] = ss.hist_idx[k];
+      for (int w = 0; w < 4; ++w) a.history[((int64_t)s * 4 + k) * 4 + w] = ss.hist[k][w];
+    }
+    for (int k = 0; k < 5; ++k) {
+      a.attempted[5 * (int64_t)s + k] += ss.attempted[k];
+      a.accepted[5 * (int64_t)s + k] += ss.accepted[k];
+    }
+  }
 }
 
 }  // namespace
