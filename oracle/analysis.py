@@ -50,7 +50,8 @@ def analyze_single_system(energy, counts, temperature: float, n_blocks: int) -> 
     except np.linalg.LinAlgError:  # singular count covariance: the reference's inverse gives inf / nan
         inv = np.full_like(cov, np.nan)
     hoa = np.einsum("bi,bij->bj", diff, inv) - temperature * BOLTZMANN_CONSTANT
-    w = n / n.sum(axis=1, keepdims=True)
+    with np.errstate(invalid="ignore", divide="ignore"):  # a block without molecules: nan, as in the reference
+        w = n / n.sum(axis=1, keepdims=True)
     return {
         "energy": block_average(energy, n_blocks),
         "loading": block_average(counts, n_blocks),
