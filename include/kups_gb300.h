@@ -716,6 +716,11 @@ int32_t kups_lj_tail_correction(const int32_t *species, const int32_t *sys_offse
  * split_k > 1 splits K over CTAs that atomically add alpha * partial into a
  * float32 C (beta must be 1, no act / bias / gate / c2); zero C first to get
  * the plain product.
+ * Bfloat16 operands with K contiguous (16-byte aligned, row strides multiples of
+ * 8 elements) and a row-major float32 C with N a multiple of 32 (and beta = 0
+ * unless split) are loaded by TMA into 128-byte swizzled tiles; every other
+ * layout is staged element-wise.  Results agree to the float32 accumulation
+ * order either way.
  * ------------------------------------------------------------------------ */
 int32_t kups_gemm_bf16(const void *a, int32_t a_bf16, int64_t sa_row, int64_t sa_col,
                        const void *b, int32_t b_bf16, int64_t sb_row, int64_t sb_col,
