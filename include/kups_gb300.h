@@ -260,7 +260,7 @@ typedef struct kups_md_args {
   int32_t n_ctas;            /* 0 = one per SM */
   int32_t block_threads;     /* 0 = library default */
   int32_t min_lanes_per_atom; /* lanes sharing one atom's Verlet list in the force phase:
-                                 at least this many (1, 2 or 4; 0 = library default 2),
+                                 at least this many (1, 2, 4, 8 or 16; 0 = library default 2),
                                  more for small systems so every thread has work */
   int32_t reuse_lists;       /* 1: a system whose record in the workspace (written by the
                                 previous call on the same workspace) matches this call's inputs
