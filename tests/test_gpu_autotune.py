@@ -9,7 +9,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("block_threads,lanes", [(512, 1), (640, 4), (896, 2), (1024, 4)])
+@pytest.mark.parametrize("block_threads,lanes", [(512, 1), (640, 4), (896, 2), (1024, 4), (1024, 8), (256, 16)])
 def test_every_launch_shape_matches_oracle(block_threads, lanes):
     from kups_gb300 import md
     from test_gpu_core import md_state, oracle_forces, small_batch
