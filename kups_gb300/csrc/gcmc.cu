@@ -37,6 +37,7 @@ constexpr int kMaxKVec = 4096;
 constexpr int kMaxImg = 5;       // odd image count per axis
 constexpr int kMaxM = 16;        // |n_a| of a k vector
 constexpr int kTab = 2 * kMaxM + 1;
+constexpr int kMaxNearGroups = 512;  // host groups of 32 atoms a system's near lists can hold
 
 struct ImgCfg {
   int n[3];
@@ -281,6 +282,12 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
   __shared__ float4 mfa[2 * kMaxApm];  // moved atoms (old, then new): fractional xyz, species bits
   __shared__ float mq[2 * kMaxApm];
   __shared__ int mon[2 * kMaxApm];
+  // near-group lists of the step (minimum-image path with group bounds): for the new end and
+  // for the old end of the move, the host groups within reach of any of its atoms and, per
+  // group, which moved atoms reach it
+  __shared__ uint16_t near_g[2][kMaxNearGroups], near_m[2][kMaxNearGroups];
+  __shared__ float gsum[2][kMaxNearGroups];  // per end and host group: its pair energy (0 if skipped)
+  __shared__ int near_n[2], iscan[32];
   const int s = blockIdx.x;
   const int tid = threadIdx.x;
   const int apm = a.atoms_per_mol;
@@ -584,6 +591,102 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
       // rounded image's d_a is the circular distance, so no pair within it is dropped).
       unsigned on_mask = 0u;  // moved atoms to take against the host (old ones unless cached)
       for (int m = 0; m < nm; ++m) on_mask |= (mon[m] && !(m < apm && cache_hit)) ? (1u << m) : 0u;
+      const int n_groups = (fwn + 31) >> 5;
+      if (n_groups <= kMaxNearGroups) {
+        // 1. every (group, moved atom) bound at once (without group bounds every group is near),
+        //    then the near groups of each end compacted in a fixed order (a thread's groups t,
+        //    t + threads, ... after those of lower threads)
+        unsigned gm[kMaxNearGroups / 64 + 1];
+        int cnt_new = 0, cnt_old = 0, slot = 0;
+        for (int g = tid; g < n_groups; g += kThreads, ++slot) {
+          gsum[0][g] = 0.f;
+          gsum[1][g] = 0.f;
+          if (grp == nullptr) {
+            gm[slot] = on_mask;
+            const unsigned old_bits = (1u << apm) - 1u;
+            cnt_old += (on_mask & old_bits) != 0u;
+            cnt_new += (on_mask & ~old_bits) != 0u;
+            continue;
+          }
+          const int gi = (fw0 >> 5) + g;
+          const float4 c = grp[2 * gi], h = grp[2 * gi + 1];
+          unsigned mk = 0u;
+          for (unsigned mm = on_mask; mm != 0u; mm &= mm - 1u) {
+            const int m = __ffs(mm) - 1;
+            const float4 fa = mfa[m];
+            float dx = fa.x - c.x, dy = fa.y - c.y, dz = fa.z - c.z;
+            dx = fabsf(dx - rintf(dx));
+            dy = fabsf(dy - rintf(dy));
+            dz = fabsf(dz - rintf(dz));
+            const float sep = fmaxf(fmaxf(fmaxf(dx - h.x, 0.f) * wdt[0], fmaxf(dy - h.y, 0.f) * wdt[1]),
+                                    fmaxf(dz - h.z, 0.f) * wdt[2]);
+            if (sep < rc_any) mk |= 1u << m;
+          }
+          gm[slot] = mk;
+          const unsigned old_bits = (1u << apm) - 1u;
+          cnt_old += (mk & old_bits) != 0u;
+          cnt_new += (mk & ~old_bits) != 0u;
+        }
+        int tot;
+        const int off = block_exclusive_scan<int>(cnt_new | (cnt_old << 16), iscan, &tot);
+        int on = off & 0xffff, oo = off >> 16;
+        slot = 0;
+        for (int g = tid; g < n_groups; g += kThreads, ++slot) {
+          const unsigned mk = gm[slot], old_bits = (1u << apm) - 1u;
+          if (mk & ~old_bits) {
+            near_g[0][on] = (uint16_t)g;
+            near_m[0][on++] = (uint16_t)(mk & ~old_bits);
+          }
+          if (mk & old_bits) {
+            near_g[1][oo] = (uint16_t)g;
+            near_m[1][oo++] = (uint16_t)(mk & old_bits);
+          }
+        }
+        if (tid == 0) {
+          near_n[0] = tot & 0xffff;
+          near_n[1] = tot >> 16;
+        }
+        __syncthreads();
+        // 2. the near groups of each end dealt to the warps in turn (balanced), lanes on atoms;
+        //    each group's energy is reduced in the warp and kept per group, so the end's total
+        //    (summed over groups in group order) depends neither on which warp took a group nor
+        //    on which groups were skipped: the same positions give the same bits
+        const int warp = tid >> 5, n_warps = kThreads >> 5;
+        for (int end = 0; end < 2; ++end) {
+          for (int q = warp; q < near_n[end]; q += n_warps) {
+            const int g = near_g[end][q], j = g * 32 + lane;
+            float v = 0.f;
+            if (j < fwn) {
+              const float4 pj = fwp[fw0 + j];
+              const float qj = a.fw_charge[fw0 + j];
+              float fj[3];
+              frac32(If, pj.x, pj.y, pj.z, fj);
+              const int tj = __float_as_int(pj.w);
+              for (unsigned mm = near_m[end][q]; mm != 0u; mm &= mm - 1u) {
+                const int m = __ffs(mm) - 1;
+                const float4 fa = mfa[m];
+                float d[3] = {fa.x - fj[0], fa.y - fj[1], fa.z - fj[2]}, c[3];
+                d[0] -= rintf(d[0]);
+                d[1] -= rintf(d[1]);
+                d[2] -= rintf(d[2]);
+                cart32(Lf, d, c);
+                const float r2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+                if (r2 >= rc2_any) continue;
+                v += pair_u(r2, __float_as_int(fa.w), tj, mq[m] * qj, lj, nsp, li, ei, alpha, ke, true, true);
+              }
+            }
+            v = warp_sum(v);
+            if (lane == 0) gsum[end][g] = v;
+          }
+        }
+        __syncthreads();
+        if (tid < 32) {  // group order: lane l sums groups l, l + 32, ...; block_sum_f adds the lanes
+          for (int g = tid; g < n_groups; g += 32) {
+            e_host_new += gsum[0][g];
+            e_host_old += gsum[1][g];
+          }
+        }
+      } else
       for (int base = (tid & ~31); base < fwn; base += kThreads) {
         unsigned near = on_mask;
         if (grp != nullptr) {
