@@ -644,7 +644,7 @@ typedef struct kups_gcmc_args {
   double *out_delta;            /* [S, 4] or NULL */
   const float *proposal_node;   /* [G^3] learned insertion density (kups_mlp_grid_norm) or NULL */
   const double *proposal_cdf;   /* [G^3 + 1] */
-  void *workspace;              /* float2 [3, S, n_kvecs] scratch (the step's S(k) change, float32
+  void *workspace;              /* float2 [3, S, n_kvecs] scratch (a reserved slab, then float32
                                    mirrors of S(k) and of P(k) with the packed k vector) */
   const void *fw_group;         /* float4 [host atoms / 32][2] or NULL: per 32 host atoms
                                    (blocks start on multiples of 32) the fractional centre and

@@ -384,12 +384,11 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
   double *sk = a.structure_factor + (int64_t)s * nk * 2;
   const double *pk = a.prefactor + (int64_t)s * nk;
   const int32_t *kn = a.kvec_n + (int64_t)s * nk * 3;
-  // scratch per system (three arrays of S x n_k): the step's S(k) change, float32 mirrors of
-  // S(k) (re-derived from the float64 value at every commit) and of P(k), and the packed
+  // scratch per system (arrays of S x n_k after a reserved first one): float32 mirrors of
+  // S(k) (re-derived from the float64 value at every commit) and of P(k) with the packed
   // table offsets of the k vectors.  Reading the mirrors keeps float64<->float32
   // conversions (float64-pipe work) off the per-step path.
   const int64_t snk = (int64_t)a.n_systems * nk;
-  float2 *dS = reinterpret_cast<float2 *>(a.workspace) + (int64_t)s * nk;
   float2 *sk32 = reinterpret_cast<float2 *>(a.workspace) + snk + (int64_t)s * nk;
   float2 *pk32 = reinterpret_cast<float2 *>(a.workspace) + 2 * snk + (int64_t)s * nk;  // (P, packed k)
   // the phase tables hold |n_a| <= kMaxM: a system with a larger k vector is refused
@@ -820,11 +819,13 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     }
     __syncthreads();
     gcmc_mark(prof, 3, t0);
-    for (int k = tid; k < nk; k += kThreads) {
-      const float2 pkk = pk32[k];
+    // the step's change of S(k) (cos and sin parts) at the k vector of table entry pkk, from the
+    // phase tables; the commit forms it again on acceptance instead of storing it every step
+    auto delta_sk = [&](float2 pkk, float &dc, float &ds) {
       const uint32_t packed = __float_as_uint(pkk.y);
       const int n0 = packed & 0xffu, n1 = (packed >> 8) & 0xffu, n2 = (packed >> 16) & 0xffu;
-      float dc = 0.f, ds = 0.f;
+      dc = 0.f;
+      ds = 0.f;
       for (int m = 0; m < nm; ++m) {
         if (!mon[m]) continue;
         const float2 *t = ph + m * 3 * kTab;
@@ -835,7 +836,11 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
         dc += w * cs;
         ds += w * sn;
       }
-      dS[k] = make_float2(dc, ds);
+    };
+    for (int k = tid; k < nk; k += kThreads) {
+      const float2 pkk = pk32[k];
+      float dc, ds;
+      delta_sk(pkk, dc, ds);
       const float2 sck = sk32[k];
       de_rec_f = fmaf(pkk.x, fmaf(2.f, fmaf(sck.x, dc, sck.y * ds), fmaf(dc, dc, ds * ds)), de_rec_f);
     }
@@ -905,7 +910,8 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
     // ---------------------------------------------------------------- commit
     if (accept) {
       for (int k = tid; k < nk; k += kThreads) {
-        const float2 d = dS[k];
+        float2 d;
+        delta_sk(pk32[k], d.x, d.y);
         const double c = sk[2 * k] + (double)d.x, sn = sk[2 * k + 1] + (double)d.y;
         sk[2 * k] = c;
         sk[2 * k + 1] = sn;

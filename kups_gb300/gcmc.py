@@ -263,7 +263,7 @@ class GCMC:
         nk = setup.kvec_n.shape[1]
         self.pk = f64(np.stack([prefactor(setup.tril[i], setup.kvec_n[i], setup.alpha[i]) for i in range(s)]))
         self.sk = torch.zeros((s, nk, 2), dtype=torch.float64, device=dev)
-        # kernel scratch: the step's S(k) change, float32 mirrors of S(k) and of (P(k), packed k)
+        # kernel scratch: a reserved slab, float32 mirrors of S(k) and of (P(k), packed k)
         self.ws = torch.empty((3, s, max(nk, 1), 2), dtype=torch.float32, device=dev)
         self.lj_table = f32(np.stack([setup.sigma**2, 4 * setup.epsilon], -1).reshape(-1))
         vol = np.abs(setup.tril[:, 0] * setup.tril[:, 2] * setup.tril[:, 5])
