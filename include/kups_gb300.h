@@ -687,6 +687,10 @@ typedef struct kups_gcmc_args {
                                    filled on a miss).  A hit equals the recomputed value bit for
                                    bit; stale or foreign entries only miss.  NULL: both ends
                                    are computed every move */
+  int32_t k_shared;             /* 1: every system has the same k vectors and P(k) (replicas of
+                                   one cell): the float32 (P(k), packed k) mirror in the workspace
+                                   is kept once, in system 0's slot, and read by every system */
+  int32_t pad2;
 } kups_gcmc_args;
 
 int32_t kups_gcmc_run(const kups_gcmc_args *args, kups_status *status, void *stream);

@@ -74,7 +74,7 @@ class GcmcArgs(C.Structure):
         ("step0", C.c_uint64), ("n_systems", C.c_int32), ("max_mol", C.c_int32), ("atoms_per_mol", C.c_int32),
         ("n_species", C.c_int32), ("n_kvecs", C.c_int32), ("n_steps", C.c_int32), ("history_len", C.c_int32),
         ("proposal_grid", C.c_int32), ("trace", C.c_void_p), ("block_threads", C.c_int32), ("pad1", C.c_int32),
-        ("profile", C.c_void_p), ("host_cache", C.c_void_p),
+        ("profile", C.c_void_p), ("host_cache", C.c_void_p), ("k_shared", C.c_int32), ("pad2", C.c_int32),
     ]
 
 

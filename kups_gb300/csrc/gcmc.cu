@@ -390,7 +390,8 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) gcmc_kernel(kups_gcm
   // conversions (float64-pipe work) off the per-step path.
   const int64_t snk = (int64_t)a.n_systems * nk;
   float2 *sk32 = reinterpret_cast<float2 *>(a.workspace) + snk + (int64_t)s * nk;
-  float2 *pk32 = reinterpret_cast<float2 *>(a.workspace) + 2 * snk + (int64_t)s * nk;  // (P, packed k)
+  // (P, packed k); one table for all systems with k_shared (every CTA writes the same values)
+  float2 *pk32 = reinterpret_cast<float2 *>(a.workspace) + 2 * snk + (a.k_shared ? 0 : (int64_t)s * nk);
   // the phase tables hold |n_a| <= kMaxM: a system with a larger k vector is refused
   {
     int bad = 0;

@@ -263,6 +263,8 @@ class GCMC:
         nk = setup.kvec_n.shape[1]
         self.pk = f64(np.stack([prefactor(setup.tril[i], setup.kvec_n[i], setup.alpha[i]) for i in range(s)]))
         self.sk = torch.zeros((s, nk, 2), dtype=torch.float64, device=dev)
+        # replicas of one cell share k vectors and P(k): the kernel then keeps one table for all
+        self.k_shared = bool(s > 0 and (self.kn == self.kn[:1]).all().item() and (self.pk == self.pk[:1]).all().item())
         # kernel scratch: a reserved slab, float32 mirrors of S(k) and of (P(k), packed k)
         self.ws = torch.empty((3, s, max(nk, 1), 2), dtype=torch.float32, device=dev)
         self.lj_table = f32(np.stack([setup.sigma**2, 4 * setup.epsilon], -1).reshape(-1))
@@ -346,6 +348,7 @@ class GCMC:
         a.block_threads = int(self.block_threads)
         a.profile = self.profile.data_ptr() if getattr(self, "profile", None) is not None else None
         a.host_cache = self.host_cache.data_ptr() if self.use_host_cache else None
+        a.k_shared = int(self.k_shared)
         if self.proposal is not None:
             a.proposal_node, a.proposal_cdf = self.proposal.node.data_ptr(), self.proposal.cdf.data_ptr()
             a.proposal_grid = self.proposal.grid
