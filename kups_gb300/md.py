@@ -253,6 +253,28 @@ def key_to_seed(key) -> int:
     return h
 
 
+def run_bounds(system: torch.Tensor, n_systems: int, chunks: int) -> list[tuple[int, int, int, int]]:
+    """Runs of whole systems for ``FusedLennardJonesMD.propagate_host``: (first atom, end atom,
+    first system, end system) of each run.  A particle table grouped by system (non-decreasing
+    ``system``) is cut at the system boundaries nearest to equal atom counts, each run keeping
+    at least one atom; any other table is one run."""
+    n = int(system.shape[0])
+    counts = torch.bincount(system, minlength=n_systems) if n else torch.zeros(n_systems, dtype=torch.int64)
+    offs = [0] + torch.cumsum(counts, 0).tolist()
+    grouped = n == 0 or bool((system[1:] >= system[:-1]).all())
+    cuts = [0]
+    if grouped and chunks > 1 and n > 0:
+        for k in range(1, chunks):
+            target = k * n / chunks
+            # the system boundary nearest the target that leaves atoms on both sides
+            c = min((j for j in range(cuts[-1] + 1, n_systems) if offs[cuts[-1]] < offs[j] < n),
+                    key=lambda j: abs(offs[j] - target), default=None)
+            if c is not None:
+                cuts.append(c)
+    cuts.append(n_systems)
+    return [(offs[s0], offs[s1], s0, s1) for s0, s1 in zip(cuts[:-1], cuts[1:])]
+
+
 @dataclass
 class _HostRun:
     """What ``FusedLennardJonesMD.propagate_host`` keeps between calls on one layout: the runs
@@ -410,21 +432,7 @@ class FusedLennardJonesMD:
         run = self._host
         if run is not None and run.chunks == chunks and run.n == n and _same_key(run.key, key):
             return run
-        system = p.system.to("cpu", torch.int64)
-        counts = torch.bincount(system, minlength=s) if n else torch.zeros(s, dtype=torch.int64)
-        offs = [0] + torch.cumsum(counts, 0).tolist()
-        grouped = n == 0 or bool((system[1:] >= system[:-1]).all())
-        cuts = [0]
-        if grouped and chunks > 1 and n > 0:
-            for k in range(1, chunks):
-                target = k * n / chunks
-                # the system boundary nearest the target that leaves atoms on both sides
-                c = min((j for j in range(cuts[-1] + 1, s) if offs[cuts[-1]] < offs[j] < n),
-                        key=lambda j: abs(offs[j] - target), default=None)
-                if c is not None:
-                    cuts.append(c)
-        cuts.append(s)
-        bounds = [(offs[s0], offs[s1], s0, s1) for s0, s1 in zip(cuts[:-1], cuts[1:])]
+        bounds = run_bounds(p.system.to("cpu", torch.int64), s, chunks)
         dev = "cuda"
         masses, species = p.masses.to(dev), p.species.to(dev)
         system_d = p.system.to(dev)
