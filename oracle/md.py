@@ -127,7 +127,8 @@ def cell_rescale_factor(pressure, tril, dt, temperature, target_pressure, tau_p,
     beta, tau_p, dt = (np.asarray(x, np.float64) for x in (compressibility, tau_p, dt))
     deps = dt / tau_p * beta * (pressure - np.asarray(target_pressure)) + np.sqrt(
         2.0 * kt * beta * dt / (tau_p * vol)) * np.asarray(rp)
-    return np.clip(np.exp(deps / 3.0), min_scale, 1.0 / np.asarray(min_scale, np.float64))
+    with np.errstate(over="ignore"):  # an overflowing exp is clipped like any other large mu
+        return np.clip(np.exp(deps / 3.0), min_scale, 1.0 / np.asarray(min_scale, np.float64))
 
 
 def csvr_npt(pos, mom, forces, masses, system, species, tril, sigma, epsilon, cutoffs, dt, temperature, tau,
