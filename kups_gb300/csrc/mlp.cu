@@ -7,9 +7,11 @@
 // GEMM: C[M, N] = act(alpha * A[M, K] . B[N, K]^T + bias[N]) with arbitrary
 // element strides for A, B and C (so transposed operands need no copies);
 // split-K (grid z) for the weight gradients, whose K is the batch.
-// One CTA computes a 128 x BN tile: four warps stage K-chunks of 64 from
-// global memory into shared memory in the canonical no-swizzle K-major
-// layout (8-row x 16-byte core matrices), one thread issues
+// One CTA computes a 128 x BN tile.  Bfloat16 operands with K contiguous are
+// loaded by TMA (cp.async.bulk.tensor, 128-byte swizzle) into a ring of
+// stages (gemm_tma_kernel); other layouts are staged by the threads with
+// 16-byte copies or element-wise into the canonical no-swizzle K-major layout
+// (8-row x 16-byte core matrices, gemm_tcgen05_kernel).  One thread issues
 // tcgen05.mma.cta_group::1.kind::f16 (BF16 inputs, FP32 accumulation in
 // tensor memory) and tcgen05.commit to an mbarrier, and the epilogue reads
 // the accumulator back with tcgen05.ld.32x32b.  Every mbarrier wait is
