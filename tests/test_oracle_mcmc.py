@@ -272,3 +272,21 @@ def test_proposals_keep_molecule_geometry():
             fd = d @ np.linalg.inv(L)
             d = (fd - np.round(fd)) @ L
             np.testing.assert_allclose(np.linalg.norm(d), d0, atol=1e-9)
+
+
+def test_log_factorial_ratio_known_answers():
+    """test/core/test_math.py:21-86: ln(N! / M!) of scalars, equal and swapped arguments, zeros,
+    large counts, vectors and broadcasting."""
+    lfr = om.log_factorial_ratio
+    np.testing.assert_allclose(lfr(np.array([5]), np.array([3])), np.log(5 * 4), rtol=1e-10)
+    np.testing.assert_allclose(lfr(np.array([4]), np.array([4])), [0.0], atol=1e-15)
+    np.testing.assert_allclose(lfr(np.array([3]), np.array([5])), -np.log(5 * 4), rtol=1e-10)
+    np.testing.assert_allclose(lfr(np.array([0]), np.array([0])), [0.0], atol=1e-15)
+    np.testing.assert_allclose(lfr(np.array([3]), np.array([0])), np.log(6), rtol=1e-10)
+    np.testing.assert_allclose(lfr(np.array([100]), np.array([95])), np.sum(np.log(np.arange(96, 101))), rtol=1e-10)
+    np.testing.assert_allclose(lfr(np.array([5, 4, 10]), np.array([3, 4, 7])),
+                               [np.log(5 * 4), 0.0, np.log(10 * 9 * 8)], rtol=1e-10, atol=1e-15)
+    np.testing.assert_allclose(lfr(np.array([[5, 6], [7, 8]]), np.array([3, 4])),
+                               [[np.log(5 * 4), np.log(6 * 5)], [np.log(7 * 6 * 5 * 4), np.log(8 * 7 * 6 * 5)]],
+                               rtol=1e-10)
+    np.testing.assert_allclose(lfr(np.array([7]), np.array([4])), -lfr(np.array([4]), np.array([7])), rtol=1e-10)
