@@ -6,6 +6,7 @@ Peng-Robinson fugacity, pinned to the reference's own known-answer tests:
 * test/mcmc/test_fugacity.py (ideal limit, numpy-roots cross-check at 50 bar, binary mixtures);
 * test/core/test_parameter_scheduler.py:177-360 (history, cycle, bounds, correlation);
 * test/core/test_quaternion.py (identity, inverse, power, matrix, rotation of a vector);
+* test/core/test_math.py:21-86 (ln(N! / M!) of the muVT ratio);
 * test/potential/test_lennard_jones.py:388-450 (global tail correction energy and pressure);
 * Philox4x32-10 against the published known-answer vectors of the Random123 distribution.
 """
