@@ -7,6 +7,7 @@ Peng-Robinson fugacity, pinned to the reference's own known-answer tests:
 * test/core/test_parameter_scheduler.py:177-360 (history, cycle, bounds, correlation);
 * test/core/test_quaternion.py (identity, inverse, power, matrix, rotation of a vector);
 * test/core/test_math.py:21-86 (ln(N! / M!) of the muVT ratio);
+* test/core/test_position.py:77-109 (the unweighted centre the rotation move turns about);
 * test/potential/test_lennard_jones.py:388-450 (global tail correction energy and pressure);
 * Philox4x32-10 against the published known-answer vectors of the Random123 distribution.
 """
@@ -291,3 +292,17 @@ def test_log_factorial_ratio_known_answers():
                                [[np.log(5 * 4), np.log(6 * 5)], [np.log(7 * 6 * 5 * 4), np.log(8 * 7 * 6 * 5)]],
                                rtol=1e-10)
     np.testing.assert_allclose(lfr(np.array([7]), np.array([4])), -lfr(np.array([4]), np.array([7])), rtol=1e-10)
+
+
+def test_atom_mean_known_answers():
+    """The rotation centre: ``center_of_mass`` with equal weights (test/core/test_position.py:77-109):
+    plain means, a pair across the cell boundary, and a single atom (its wrapped position)."""
+    def mean(pos, side):
+        L = np.eye(3) * side
+        return om.atom_mean(np.asarray(pos, np.float64), L, np.linalg.inv(L))
+
+    np.testing.assert_allclose(mean([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], 4.0), [0.5, 0.0, 0.0], atol=1e-10)
+    np.testing.assert_allclose(mean([[0.0, 1.0, 0.0], [1.0, 1.0, 0.0]], 6.0), [0.5, 1.0, 0.0], atol=1e-10)
+    np.testing.assert_allclose(mean([[0.1, 0.0, 0.0], [1.9, 0.0, 0.0]], 2.0), [0.0, 0.0, 0.0], atol=1e-10)
+    np.testing.assert_allclose(mean([[1.0, 2.0, 3.0]], 4.0), [1.0, -2.0, -1.0], atol=1e-10)
+    np.testing.assert_allclose(mean([[4.0, 5.0, 6.0]], 6.0), [-2.0, -1.0, 0.0], atol=1e-10)
