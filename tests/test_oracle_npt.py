@@ -55,3 +55,10 @@ def test_cell_rescale_factor_deterministic_and_clipped():
                                  [5.0, 5.0], [0.9, 0.9], [0.3, 0.3])
     np.testing.assert_allclose(mu[0], np.exp(1.0 / 10.0 * 5.0 * 1e-3 / 3.0), rtol=1e-14)
     assert mu[1] == 1.0 / 0.9
+
+
+def test_kinetic_energy_known_answers():
+    """test_integrators.py:678-686: KE = p^2 / 2m per particle, summed per system here."""
+    ke = omd.kinetic_energy(np.array([[1.0, 0.0, 0.0], [3.0, 4.0, 0.0]]), np.array([1.0, 2.0]),
+                            np.array([0, 1]), 2)
+    np.testing.assert_allclose(ke, [0.5, 6.25], rtol=1e-15)
