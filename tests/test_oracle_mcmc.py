@@ -306,3 +306,32 @@ def test_atom_mean_known_answers():
     np.testing.assert_allclose(mean([[0.1, 0.0, 0.0], [1.9, 0.0, 0.0]], 2.0), [0.0, 0.0, 0.0], atol=1e-10)
     np.testing.assert_allclose(mean([[1.0, 2.0, 3.0]], 4.0), [1.0, -2.0, -1.0], atol=1e-10)
     np.testing.assert_allclose(mean([[4.0, 5.0, 6.0]], 6.0), [-2.0, -1.0, 0.0], atol=1e-10)
+
+
+def test_tail_change_as_a_quadratic_in_the_molecule_count():
+    """The GCMC kernel adds the tail correction's change of an exchange as b dN + c d(N^2), with
+    b = sum_ab coef_ab (f_a m_b + m_a f_b) and c = sum_ab coef_ab m_a m_b (f: host species
+    counts, m: one molecule's); this equals the oracle's tail energy before and after."""
+    from kups_gb300.gcmc import tail_coefficients
+    from oracle import lennard_jones as olj
+    from oracle import unitcell as ouc
+
+    rng = np.random.default_rng(0)
+    T = 6
+    sig_i, eps_i = rng.uniform(2.5, 3.5, T), rng.uniform(0.0, 0.01, T)
+    eps_i[2] = 0.0  # a species without dispersion (masked)
+    sigma = 0.5 * (sig_i[:, None] + sig_i[None, :])
+    epsilon = np.sqrt(eps_i[:, None] * eps_i[None, :])
+    tril = ouc.tril_from_lattice(ouc.lattice_from_lengths_angles([25.0, 25.0, 25.0], [90, 90, 120]))
+    vol = float(ouc.volume(tril))
+    rc = 12.0
+    coef = tail_coefficients(sigma, epsilon, rc, vol)
+    f = np.array([500.0, 700.0, 300.0, 500.0, 0.0, 0.0])
+    m = np.array([0.0, 0.0, 0.0, 0.0, 1.0, 2.0])
+    b = float(np.sum(coef * (f[:, None] * m[None, :] + m[:, None] * f[None, :])))
+    c = float(np.sum(coef * (m[:, None] * m[None, :])))
+    for n_old, n_new in ((0, 1), (7, 8), (8, 7), (120, 121)):
+        e = [olj.tail_correction_energy((f + n * m)[None], tril[None], sigma, epsilon, np.array([rc]))[0]
+             for n in (n_old, n_new)]
+        quad = b * (n_new - n_old) + c * (n_new * n_new - n_old * n_old)
+        np.testing.assert_allclose(quad, e[1] - e[0], rtol=1e-9, atol=1e-12)
